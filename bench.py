@@ -1,0 +1,386 @@
+#!/usr/bin/env python3
+"""Benchmark of the batched hydrodynamic wrench step on GB300.
+
+Workload (default ``batch``): 4096 rigid bodies with distinct meshes drawn
+from icospheres (320-20480 faces), subdivided boxes (12-49152 faces) and
+capped cylinders 1.6 m x 0.2 m (500-50000 faces), about 37M faces in total;
+CG depth U(-1.0,+0.3) m, uniform random orientation, v ~ U(-1,1)^3 m/s,
+omega ~ U(-0.5,0.5)^3 rad/s, flat surface, uniform current (0.2,0,0) m/s,
+rho = 1025 kg/m^3.  Synthetic, seeded data.
+
+One step = one evaluation of every body's wrench (the per-body loop of the
+hydrodynamics block of Stonefish's SimulationManager::SimulationTickCallback)
+with the inputs resident in HBM (``value``), and through the host-buffer C ABI
+call with the host<->device copies inside the timed region (``e2e``).  The
+mesh data (~0.5 GB) is larger than L2, so no flush is needed between steps.
+
+``--impl reference`` times the CPU restatement of the reference's routine
+(the oracle's REF32 variant: FP32 glm-order face arithmetic, one task per
+body on all host threads) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "hydro wrench evals/s & faces/s, 1 GB300: exact FP32 vs surrogate at stated error"
+UNIT = "wrench evals/s"
+BYTES_PER_FACE = 18.0      # indexed mesh: 12 B of indices + 0.5 x 12 B of positions
+BYTES_PER_BODY = 200.0     # FP64 pose/velocity/coefficients in, 6 vec3 + 2 scalars out
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.lines: list[str] = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "50", "-i", str(self.device)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, power, reasons = [], [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+                power.append(float(parts[3]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)),
+                "power_w_max": float(max(power)), "samples": len(sm), "reasons": sorted(reasons)}
+
+
+# ----------------------------------------------------------------- helpers
+def measured_peaks() -> tuple[float, str]:
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(workload: str):
+    """DRAM bytes per launch of the chunk kernel from the committed ncu summary."""
+    p = os.path.join(HERE, "profiles", f"chunk_kernel_{workload}.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("dram_bytes_per_full_launch:"):
+            return float(line.split(":")[1].split()[0])
+    return None
+
+
+def build_workload(name: str, n_bodies: int | None):
+    from stonefish_gb300 import scenarios
+    if name == "batch":
+        return scenarios.mixed_batch(n_bodies=n_bodies or 4096)
+    if name == "waves":
+        return scenarios.torpedo_waves(n_bodies=n_bodies or 1024)
+    if name == "sphere":
+        return scenarios.single_sphere(steps=n_bodies or 1000)
+    raise SystemExit(f"unknown workload {name}")
+
+
+def workload_config(name: str, sc) -> dict:
+    nf = int(sum(len(f) for _, f in sc["meshes"]))
+    per_body_faces = np.array([len(sc["meshes"][m][1]) for m in sc["bodies"]["mesh"]])
+    cfg = {"workload": {"batch": "mixed_batch_4096_bodies_distinct_meshes",
+                        "waves": "torpedo_hulls_on_1024x1024_wave_grid",
+                        "sphere": "single_icosphere_1280_faces_1000_states"}[name],
+           "bodies": int(len(sc["bodies"])), "faces_per_step": int(per_body_faces.sum()),
+           "distinct_mesh_faces": nf, "surface": "waves" if sc["ocean"].waves else "flat",
+           "current_mps": [0.2, 0.0, 0.0], "density": 1025.0,
+           "l2_policy": "inputs larger than L2 (mesh data > 129 MB)" if nf * 13 > 2e8
+           else "inputs L2-resident (shared mesh)"}
+    return cfg, per_body_faces
+
+
+def cpu_baseline(sc, threads: int, budget_s: float = 12.0, max_steps: int = 20):
+    """REF32 (the reference's arithmetic, one task per body) on host threads."""
+    from oracle import REF32, Oracle
+    from stonefish_gb300 import scenarios
+    o = Oracle()
+    io = scenarios.new_wrenches(len(sc["bodies"]))
+    st = scenarios.settings()
+    times = []
+    t_start = time.perf_counter()
+    while len(times) < max_steps and (time.perf_counter() - t_start) < budget_s:
+        times.append(o.batch(REF32, threads, sc["bodies"], sc["meshes"], sc["ocean"], st, io,
+                             waves=sc.get("waves")))
+    return float(np.median(times)), len(times)
+
+
+def fp64_error_sample(sc, gpu_io, n: int = 128) -> dict:
+    """Pair-scaled error of the GPU result against the all-FP64 oracle on a
+    seeded sample of active bodies."""
+    from oracle import REF64, Oracle
+    from stonefish_gb300 import abi, scenarios
+    act = np.flatnonzero((gpu_io["position"] == abi.CROSSING_SURFACE) | (gpu_io["position"] == abi.INSIDE))
+    if act.size == 0:
+        return {}
+    rng = np.random.default_rng(0)
+    pick = np.sort(rng.choice(act, size=min(n, act.size), replace=False))
+    bodies = sc["bodies"][pick].copy()
+    ref = scenarios.new_wrenches(len(pick))
+    Oracle().batch(REF64, os.cpu_count() or 1, bodies, sc["meshes"], sc["ocean"],
+                   scenarios.settings(), ref, waves=sc.get("waves"))
+    g = gpu_io[pick]
+    S = np.maximum(np.max(np.stack([np.linalg.norm(ref[k], axis=1) for k in ("Fb", "Fdq", "Fdf")]), axis=0), 1e-300)
+    L = 0.5 * np.linalg.norm(bodies["aabb_max"] - bodies["aabb_min"], axis=1)
+    errs = []
+    for k in ("Fb", "Fdq", "Fdf"):
+        errs.append(np.linalg.norm(g[k] - ref[k], axis=1) / S)
+    for k in ("Tb", "Tdq", "Tdf"):
+        errs.append(np.linalg.norm(g[k] - ref[k], axis=1) / (S * L))
+    e = np.max(np.stack(errs), axis=0)
+    return {"metric": "pair-scaled |x-x64| / force scale (torques / force scale x size)",
+            "median": float(np.median(e)), "p99": float(np.percentile(e, 99)),
+            "max": float(e.max()), "frac_le_1e-5": float(np.mean(e <= 1e-5)),
+            "sample_bodies": int(len(pick))}
+
+
+# ---------------------------------------------------------------- GPU arm
+def run_gpu(args, rank: int, world: int, local_rank: int, dist):
+    import torch
+
+    from stonefish_gb300 import abi, scenarios
+    from stonefish_gb300.hydro import HydroContext
+
+    torch.cuda.set_device(local_rank)
+    t0 = time.perf_counter()
+    sc = build_workload(args.workload, args.n_bodies)
+    cfg, per_body_faces = workload_config(args.workload, sc)
+    log(f"[rank {rank}] workload built in {time.perf_counter() - t0:.1f}s: {cfg}")
+    h = HydroContext(device=local_rank)
+    t0 = time.perf_counter()
+    if sc.get("waves") is not None:
+        h.set_wave_grid(sc["waves"])
+    ids = np.array([h.upload_mesh(x, f) for x, f in sc["meshes"]], dtype=np.uint32)
+    log(f"[rank {rank}] meshes uploaded in {time.perf_counter() - t0:.1f}s")
+    bodies = sc["bodies"].copy()
+    bodies["mesh"] = ids[sc["bodies"]["mesh"]]
+    batch = h.batch(bodies["mesh"])
+    settings = scenarios.settings()
+    ocean = sc["ocean"]
+    nb = len(bodies)
+
+    d_bodies = torch.from_numpy(bodies.view(np.uint8).copy()).cuda()
+    d_io = torch.zeros(nb * abi.WRENCH_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.Stream()
+    sptr = stream.cuda_stream
+
+    def step():
+        batch.compute_device(d_bodies.data_ptr(), ocean, settings, d_io.data_ptr(), sptr)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+    torch.cuda.synchronize()
+    gpu_io = d_io.cpu().numpy().view(abi.WRENCH_DTYPE).copy()
+    active = (gpu_io["position"] == abi.CROSSING_SURFACE) | (gpu_io["position"] == abi.INSIDE)
+    processed_faces = int(per_body_faces[active].sum())
+
+    sampler = ClockSampler(local_rank)
+    sampler.start()
+    time.sleep(0.2)
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    clocks = sampler.stop()
+    ms = ev0.elapsed_time(ev1)
+    if dist is not None:
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = world * nb * args.steps / (ms / 1e3)
+    faces_per_s = world * int(per_body_faces.sum()) * args.steps / (ms / 1e3)
+
+    # end to end through the host-buffer call, pinned host memory
+    h_bodies = torch.from_numpy(bodies.view(np.uint8).copy()).pin_memory()
+    h_io = torch.zeros(nb * abi.WRENCH_DTYPE.itemsize, dtype=torch.uint8).pin_memory()
+    for _ in range(args.warmup):
+        batch.compute_ptr(h_bodies.data_ptr(), ocean, settings, h_io.data_ptr())
+    if dist is not None:
+        dist.barrier()
+    e2e_steps = max(1, args.steps // 4)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        batch.compute_ptr(h_bodies.data_ptr(), ocean, settings, h_io.data_ptr())
+    e2e_s = time.perf_counter() - t0
+    if dist is not None:
+        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * nb * e2e_steps / e2e_s
+    host_io = h_io.numpy().view(abi.WRENCH_DTYPE)
+    assert host_io.tobytes() == gpu_io.tobytes(), "host-buffer and device-buffer results differ"
+
+    if rank != 0:
+        return None
+    peak, peak_kind = measured_peaks()
+    alg_bytes = BYTES_PER_FACE * processed_faces + BYTES_PER_BODY * nb
+    achieved = alg_bytes / (ms_per_step / 1e3) / 1e9
+    result = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 faces, f64 sums",
+        "data": "synthetic (seeded meshes, poses and velocities)",
+        "config": dict(cfg, processed_faces_per_step=processed_faces,
+                       parallelism=f"replicas x{world}" if world > 1 else "single GPU"),
+        "faces_per_s": faces_per_s,
+        "e2e": {"value": e2e_value, "unit": UNIT,
+                "h2d_bytes_per_step": int(nb * (abi.BODY_DTYPE.itemsize + abi.WRENCH_DTYPE.itemsize)),
+                "d2h_bytes_per_step": int(nb * abi.WRENCH_DTYPE.itemsize), "steps": e2e_steps},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_kind,
+                     "traffic": profile_traffic(args.workload),
+                     "algorithmic_bytes_per_launch": alg_bytes,
+                     "bytes_rule": "18 B per processed face + 200 B per body"},
+        "gpu_launches": args.steps * batch.last_launches(),
+        "clocks": clocks,
+    }
+    if not args.no_error:
+        result["error_vs_fp64"] = fp64_error_sample(sc, gpu_io)
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        cpu_s, n = cpu_baseline(sc, threads)
+        result["cpu_baseline"] = {"value": nb / cpu_s, "unit": UNIT, "cores": threads, "kind": "port",
+                                  "sample": f"median of {n} full steps of the same workload "
+                                            f"(REF32 oracle, one task per body)",
+                                  "faces_per_s": int(per_body_faces.sum()) / cpu_s}
+    batch.close()
+    h.close()
+    return result
+
+
+def run_reference(args, rank: int):
+    if rank != 0:
+        return None
+    sc = build_workload(args.workload, args.n_bodies)
+    cfg, per_body_faces = workload_config(args.workload, sc)
+    threads = os.cpu_count() or 1
+    from oracle import REF32, Oracle
+    from stonefish_gb300 import scenarios
+    o = Oracle()
+    io = scenarios.new_wrenches(len(sc["bodies"]))
+    st = scenarios.settings()
+    for _ in range(min(args.warmup, 1)):
+        o.batch(REF32, threads, sc["bodies"], sc["meshes"], sc["ocean"], st, io, waves=sc.get("waves"))
+    steps = max(1, min(args.steps, 10))
+    total = 0.0
+    for _ in range(steps):
+        total += o.batch(REF32, threads, sc["bodies"], sc["meshes"], sc["ocean"], st, io,
+                         waves=sc.get("waves"))
+    nb = len(sc["bodies"])
+    value = nb * steps / total
+    return {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": 1,
+            "steps": steps, "warmup": min(args.warmup, 1), "ms_per_step": 1e3 * total / steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 faces (reference arithmetic)", "data": "synthetic", "config": cfg,
+            "faces_per_s": int(per_body_faces.sum()) * steps / total,
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{steps} full steps of the workload, capped at 10"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="batch", choices=["batch", "waves", "sphere"])
+    ap.add_argument("--n-bodies", type=int, default=None)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-error", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if args.impl == "reference":
+        res = run_reference(args, rank)
+    else:
+        if world > 1:
+            import torch.distributed as dist_mod
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            import torch
+            torch.cuda.set_device(local_rank)
+            dist_mod.init_process_group("nccl")
+            dist = dist_mod
+        res = run_gpu(args, rank, world, local_rank, dist)
+        if dist is not None:
+            dist.destroy_process_group()
+    if res is not None:
+        print(json.dumps(res), flush=True)
+
+
+if __name__ == "__main__":
+    main()

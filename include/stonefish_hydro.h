@@ -1,0 +1,313 @@
+/*
+ * stonefish_hydro.h -- C ABI of the GB300 geometry-based hydrodynamics path.
+ *
+ * The path replaced here is Stonefish's per-triangle hydrodynamic force
+ * integration (Library/src/entities/SolidEntity.cpp:1239-1850): every face of
+ * a body's physics mesh is clipped against the ocean surface, buoyancy,
+ * pressure (form) drag and skin friction are integrated over the submerged
+ * part, and the result is reduced to force/torque pairs at the body's centre
+ * of gravity.  All entry points compute on the GPU (sm_103a); none falls back
+ * to the CPU.
+ *
+ * Conventions (same as the reference):
+ *   - world frame is NED: z points down, the flat ocean surface is z = 0 and
+ *     depth = z (Ocean.cpp:149-168);
+ *   - transforms are rigid: basis is row-major R[r][c] (btMatrix3x3 rows),
+ *     origin is the translation; a point p maps to R*p + origin
+ *     (btTransform::operator*, 3rdparty/LinearMath/btTransform.h:91-100);
+ *   - every double is a btScalar (BT_USE_DOUBLE_PRECISION, CMakeLists.txt:53);
+ *     face arithmetic runs in FP32 like the reference's glm code.
+ *
+ * Outputs follow the reference's in-out rules exactly: an OUTSIDE body gets
+ * zeros, a CROSSING body whose submerged volume is tiny keeps its previous
+ * Fb/Tb/Vsub, an INSIDE body keeps its previous Vsub, and a body whose physics
+ * mode is neither FLOATING nor SUBMERGED is left untouched.
+ *
+ * Thread safety: one hydro_ctx may be used from several host threads; calls
+ * on the same context are serialised internally.  No call aborts the process
+ * and no C++ exception crosses this boundary.
+ */
+#ifndef STONEFISH_HYDRO_H
+#define STONEFISH_HYDRO_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HYDRO_ABI_VERSION 1
+
+/* ---------------------------------------------------------------- status */
+typedef enum hydro_status {
+    HYDRO_OK = 0,
+    HYDRO_ERR_INVALID_ARG = 1,  /* null pointer, zero/oversized count, bad enum */
+    HYDRO_ERR_OOM = 2,          /* device or host allocation failed */
+    HYDRO_ERR_TIMEOUT = 3,      /* a bounded device-side wait ran out */
+    HYDRO_ERR_DEVICE = 4,       /* CUDA runtime error (see hydro_last_error) */
+    HYDRO_ERR_NOT_FOUND = 5,    /* unknown mesh / batch handle */
+    HYDRO_ERR_INDEX_RANGE = 6,  /* a face index >= vertex count */
+    HYDRO_ERR_UNSUPPORTED = 7,  /* feature not available in this build */
+    HYDRO_ERR_MISMATCH = 8      /* body table does not match its batch */
+} hydro_status;
+
+/* ------------------------------------------------------------ enumerations */
+/* PhysicsMode, Library/include/entities/Entity.h:57 */
+enum {
+    HYDRO_MODE_DISABLED = 0,
+    HYDRO_MODE_SURFACE = 1,
+    HYDRO_MODE_FLOATING = 2,
+    HYDRO_MODE_SUBMERGED = 3,
+    HYDRO_MODE_AERODYNAMIC = 4
+};
+
+/* BodyFluidPosition, Library/include/entities/SolidEntity.h:41 */
+enum {
+    HYDRO_INSIDE = 0,
+    HYDRO_OUTSIDE = 1,
+    HYDRO_CROSSING_SURFACE = 2,
+    HYDRO_SKIPPED = -1          /* mode gate: outputs untouched */
+};
+
+/* VelocityFieldType (Uniform.cpp, Jet.cpp, Pipe.cpp) */
+enum {
+    HYDRO_CURRENT_UNIFORM = 0,
+    HYDRO_CURRENT_JET = 1,
+    HYDRO_CURRENT_PIPE = 2
+};
+
+/* Precision of the waterline cut points (faces that straddle the surface). */
+enum {
+    HYDRO_CUT_FP64 = 0,         /* cut point interpolated in FP64, rounded once */
+    HYDRO_CUT_FP32 = 1          /* FP32 in the reference's own operation order */
+};
+
+#define HYDRO_MAX_CURRENTS 8
+#define HYDRO_MAX_WAVE_LAYERS 4
+#define HYDRO_NO_MESH 0xFFFFFFFFu   /* stands for the reference's mesh == nullptr */
+
+typedef uint32_t hydro_mesh_id;
+typedef struct hydro_ctx hydro_ctx;
+typedef struct hydro_batch hydro_batch;
+
+/* ------------------------------------------------------------------ types */
+/* btTransform: basis rows then origin. */
+typedef struct hydro_transform {
+    double basis[9];
+    double origin[3];
+} hydro_transform;
+
+/* HydrodynamicsSettings, Library/include/entities/forcefields/Ocean.h:36-40 */
+typedef struct hydro_settings {
+    int32_t damping_forces;      /* dampingForces */
+    int32_t realistic_buoyancy;  /* reallisticBuoyancy */
+} hydro_settings;
+
+/* One VelocityField.  Fields used per type:
+ *   UNIFORM: vel                         (Uniform.cpp:56-59)
+ *   JET:     point=c, dir=n, radius=r, speed=vout              (Jet.cpp:59-80)
+ *   PIPE:    point=p1, dir=n, radius=r1, radius2=r2, length=l,
+ *            speed=vin, gamma                                  (Pipe.cpp:57-79) */
+typedef struct hydro_current {
+    int32_t type;
+    int32_t enabled;             /* VelocityField::isEnabled() */
+    double vel[3];
+    double point[3];
+    double dir[3];
+    double radius;
+    double radius2;
+    double length;
+    double speed;
+    double gamma;
+} hydro_current;
+
+/* The Ocean as seen by the hydrodynamics path. */
+typedef struct hydro_ocean {
+    double density;              /* Fluid::density (MaterialManager.h:44) */
+    double gravity;              /* SimulationManager::getGravity().z, 9.81 */
+    int32_t waves;               /* Ocean::hasWaves(): depth = z - wave height */
+    int32_t currents_enabled;    /* Ocean::EnableCurrents() was called */
+    uint32_t n_currents;
+    uint32_t reserved;
+    hydro_current currents[HYDRO_MAX_CURRENTS];
+} hydro_ocean;
+
+/* Per-body state read by SolidEntity::ComputeHydrodynamicForces
+ * (SolidEntity.cpp:1799-1850) and its accessors (:215-226, :410-459). */
+typedef struct hydro_body {
+    hydro_transform T_CG;        /* getCGTransform() */
+    hydro_transform T_C;         /* getCTransform(): physics-mesh frame */
+    double R_O[9];               /* getOTransform().getBasis(), for the drag correction */
+    double v[3];                 /* getLinearVelocity() */
+    double omega[3];             /* getAngularVelocity() */
+    double Cd[3];                /* fdCd */
+    double Cf[3];                /* fdCf */
+    double P_CB[3];              /* centre of buoyancy in the CG frame */
+    double volume;               /* analytic volume (INSIDE buoyancy) */
+    double surface;              /* analytic surface (INSIDE wetted area) */
+    double aabb_min[3];          /* getAABB(): collision-shape AABB, world frame */
+    double aabb_max[3];
+    hydro_mesh_id mesh;          /* getPhysicsMesh(); HYDRO_NO_MESH = nullptr */
+    int32_t mode;                /* PhysicsMode */
+    int32_t buoyancy;            /* PhysicsSettings::buoyancy */
+    int32_t reserved;
+} hydro_body;
+
+/* In-out results: the SolidEntity members Fb..Vsub (SolidEntity.h:400-437). */
+typedef struct hydro_wrench {
+    double Fb[3], Tb[3];         /* buoyancy force / torque */
+    double Fdq[3], Tdq[3];       /* form (quadratic) drag force / torque */
+    double Fdf[3], Tdf[3];       /* skin friction force / torque */
+    double Swet;                 /* wetted surface */
+    double Vsub;                 /* submerged volume */
+    int32_t position;            /* BodyFluidPosition of this evaluation */
+    int32_t status;              /* per-body error word, 0 = ok */
+} hydro_wrench;
+
+typedef struct hydro_config {
+    int32_t device;              /* CUDA device ordinal */
+    int32_t cut_precision;       /* HYDRO_CUT_FP64 (default) or HYDRO_CUT_FP32 */
+    uint32_t tile_faces;         /* faces per work tile; 0 = autotune */
+    uint32_t ctas_per_sm;        /* resident CTAs per SM; 0 = autotune */
+    const char* tune_cache_path; /* autotuner cache file, NULL = none */
+} hydro_config;
+
+/* -------------------------------------------------------------- lifecycle */
+/* Fills *cfg with defaults (device 0, FP64 cut points, autotuned tiles). */
+void hydro_config_default(hydro_config* cfg);
+
+hydro_status hydro_create(hydro_ctx** ctx, const hydro_config* cfg);
+void hydro_destroy(hydro_ctx* ctx);
+
+/* Message of the last failing call on this context (never NULL). */
+const char* hydro_last_error(const hydro_ctx* ctx);
+const char* hydro_status_string(hydro_status s);
+int hydro_abi_version(void);
+
+/* ----------------------------------------------------------------- meshes */
+/* Uploads one physics mesh.  vertex_data/vertex_stride accept the
+ * reference's own interleaved vertex arrays directly: the position is the
+ * first three floats of each vertex, as in Vertex (24 B) and
+ * TexturableVertex (44 B) of OpenGLDataStructs.h:120-155, i.e. what
+ * Mesh::getVertexDataPointer() / getVertexSize() return; face_indices is
+ * Mesh::faces (3 uint32 per face, getFaceDataPointer()).  The device keeps
+ * a tiled copy; every index is range-checked here (HYDRO_ERR_INDEX_RANGE). */
+hydro_status hydro_mesh_upload(hydro_ctx* ctx, const void* vertex_data,
+                               size_t vertex_stride, uint32_t n_vertices,
+                               const uint32_t* face_indices, uint32_t n_faces,
+                               hydro_mesh_id* out_id);
+hydro_status hydro_mesh_info(hydro_ctx* ctx, hydro_mesh_id id,
+                             uint32_t* n_vertices, uint32_t* n_faces,
+                             uint32_t* n_tiles);
+
+/* ------------------------------------------------------------------ waves */
+/* Sets the wave height data read by Ocean::GetDepth when ocean.waves != 0
+ * (OpenGLRealOcean::ComputeWaveHeight, OpenGLRealOcean.cpp:282-331):
+ * data is an N x N grid of `channels` interleaved floats (row j, column i at
+ * (j*N+i)*channels); each of the n_layers layers reads channel
+ * layer_channel[l] over a square of layer_grid_size[l] metres, and
+ * wave height = -sum_l bilinear(layer l) (periodic, texel-centred). */
+hydro_status hydro_wave_grid_set(hydro_ctx* ctx, const float* data,
+                                 uint32_t size, uint32_t channels,
+                                 uint32_t n_layers,
+                                 const uint32_t* layer_channel,
+                                 const float* layer_grid_size);
+
+/* Ocean::GetDepth for n points (xyz interleaved, host memory). */
+hydro_status hydro_depth(hydro_ctx* ctx, const hydro_ocean* ocean,
+                         const float* xyz, uint32_t n, float* depth);
+
+/* ---------------------------------------------------------- batched path */
+/* A batch fixes which mesh each body uses (bodies[i].mesh must equal
+ * mesh_of_body[i] at compute time) and owns the device work list and the
+ * per-tile scratch.  It replaces the per-body loop of the hydrodynamics
+ * block of SimulationManager::SimulationTickCallback
+ * (SimulationManager.cpp:1620-1655) and Ocean::ApplyFluidForces
+ * (Ocean.cpp:219-268). */
+hydro_status hydro_batch_create(hydro_ctx* ctx, const hydro_mesh_id* mesh_of_body,
+                                uint32_t n_bodies, hydro_batch** out);
+void hydro_batch_destroy(hydro_batch* batch);
+
+/* Device-resident step: d_bodies and d_inout are device pointers; the call
+ * enqueues on `stream` (a cudaStream_t, NULL = legacy default) and returns
+ * without synchronising.  One launch per step (captured in a CUDA graph by
+ * the library after its first call). */
+hydro_status hydro_batch_compute_device(hydro_batch* batch, const hydro_body* d_bodies,
+                                        const hydro_ocean* ocean,
+                                        const hydro_settings* settings,
+                                        hydro_wrench* d_inout, void* stream);
+
+/* Host-buffer step: copies bodies and in-out wrenches host->device, runs the
+ * step, copies the wrenches back and synchronises.  With pinned host memory
+ * the copies are asynchronous on the batch's own stream. */
+hydro_status hydro_batch_compute(hydro_batch* batch, const hydro_body* bodies,
+                                 const hydro_ocean* ocean,
+                                 const hydro_settings* settings,
+                                 hydro_wrench* inout);
+
+/* Number of kernel launches the last compute call enqueued. */
+uint32_t hydro_batch_last_launches(const hydro_batch* batch);
+
+/* --------------------------------------------- reference call surface */
+/* SolidEntity::ComputeHydrodynamicForces (SolidEntity.cpp:1799-1850) for
+ * one body: mode gate, CheckBodyFluidPosition, INSIDE/CROSSING branch and
+ * CorrectHydrodynamicForces.  io holds the previous values on entry. */
+hydro_status hydro_body_forces(hydro_ctx* ctx, const hydro_body* body,
+                               const hydro_ocean* ocean,
+                               const hydro_settings* settings,
+                               hydro_wrench* io);
+
+/* SolidEntity::ComputeHydrodynamicForcesSurface (SolidEntity.cpp:1289-1721).
+ * mesh == HYDRO_NO_MESH behaves like mesh == nullptr.  Outputs are in-out:
+ * Fb/Tb/Vsub keep their values when buoyancy is off or the submerged volume
+ * is tiny; Fdq..Tdf are written only with damping_forces. */
+hydro_status hydro_surface_forces(hydro_ctx* ctx, const hydro_settings* settings,
+                                  hydro_mesh_id mesh, const hydro_ocean* ocean,
+                                  const hydro_transform* T_CG,
+                                  const hydro_transform* T_C,
+                                  const double v[3], const double omega[3],
+                                  double Fb[3], double Tb[3],
+                                  double Fdq[3], double Tdq[3],
+                                  double Fdf[3], double Tdf[3],
+                                  double* Swet, double* Vsub);
+
+/* SolidEntity::ComputeHydrodynamicForcesSubmerged (SolidEntity.cpp:1723-1797). */
+hydro_status hydro_submerged_forces(hydro_ctx* ctx, hydro_mesh_id mesh,
+                                    const hydro_ocean* ocean,
+                                    const hydro_transform* T_CG,
+                                    const hydro_transform* T_C,
+                                    const double v[3], const double omega[3],
+                                    double Fdq[3], double Tdq[3],
+                                    double Fdf[3], double Tdf[3]);
+
+/* SolidEntity::CorrectHydrodynamicForces (SolidEntity.cpp:1263-1287);
+ * R_O is the basis of T_O (the body-origin transform). */
+hydro_status hydro_correct_forces(hydro_ctx* ctx, const hydro_ocean* ocean,
+                                  double Fdq[3], double Tdq[3],
+                                  double Fdf[3], double Tdf[3],
+                                  const double Cd[3], const double Cf[3],
+                                  const double R_O[9]);
+
+/* SolidEntity::CheckBodyFluidPosition (SolidEntity.cpp:1239-1261) from the
+ * world AABB; writes HYDRO_INSIDE / HYDRO_OUTSIDE / HYDRO_CROSSING_SURFACE. */
+hydro_status hydro_fluid_position(hydro_ctx* ctx, const hydro_ocean* ocean,
+                                  const double aabb_min[3],
+                                  const double aabb_max[3], int32_t* position);
+
+/* ------------------------------------------------------------ diagnostics */
+/* Per-face contributions of the surface loop (ComputeHydrodynamicForcesSurface,
+ * SolidEntity.cpp:1337-1687) for one body, computed by the same device code
+ * as the batched kernel: out receives n_faces * 23 floats in uploaded face
+ * order, laid out Fb[3] Tb[3] Fdq[3] Tdq[3] Fdf[3] Tdf[3] Swet V6 CB6[3]
+ * (V6 = 6 x the face's fan-tetra volume, CB6 = V6-weighted centroid).  For
+ * validating the face arithmetic against a CPU restatement bit for bit. */
+hydro_status hydro_debug_face_terms(hydro_ctx* ctx, const hydro_body* body,
+                                    const hydro_ocean* ocean,
+                                    const hydro_settings* settings, float* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* STONEFISH_HYDRO_H */

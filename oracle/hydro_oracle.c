@@ -1,0 +1,503 @@
+/*
+ * hydro_oracle.c -- CPU oracle of the hydrodynamic wrench path.
+ *
+ * TEST INFRASTRUCTURE ONLY (tests, smoke check, CPU-baseline leg of the
+ * benchmark); the GPU library neither links nor calls this code.  See
+ * hydro_oracle.h for the variants and for why parity is unpinned.
+ *
+ * Build (see oracle/Makefile): gcc -O3 -std=c11 -ffp-contract=off, no -march,
+ * like the reference's -O3 build without FMA contraction (CMakeLists.txt:18).
+ */
+#define _GNU_SOURCE
+#include "hydro_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <pthread.h>
+#include <stdatomic.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+#include <unistd.h>
+
+/* ----------------------------------------------------- FP64 helpers */
+typedef struct { double Fb[3], Tb[3], Fdq[3], Tdq[3], Fdf[3], Tdf[3], CB[3]; double Swet, V6; } dacc;
+
+static inline void dacc_add3(double* a, double x, double y, double z) { a[0] += x; a[1] += y; a[2] += z; }
+
+/* btVector3::dot / cross (3rdparty/LinearMath/btVector3.h), FP64 */
+static inline double bdot(const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+static inline void bcross(const double* a, const double* b, double* r)
+{
+    double x = a[1] * b[2] - a[2] * b[1];
+    double y = a[2] * b[0] - a[0] * b[2];
+    double z = a[0] * b[1] - a[1] * b[0];
+    r[0] = x; r[1] = y; r[2] = z;
+}
+
+/* Jet::GetVelocityAtPoint (Library/src/entities/forcefields/Jet.cpp:59-80) */
+static void jet_velocity(const hydro_current* c, const double* p, double* out)
+{
+    double cp[3] = {p[0] - c->point[0], p[1] - c->point[1], p[2] - c->point[2]};
+    double x[3];
+    bcross(cp, c->dir, x);
+    double d = sqrt(bdot(x, x));
+    double t = bdot(cp, c->dir);
+    out[0] = out[1] = out[2] = 0.0;
+    if (t < 0.0) return;
+    double r_ = 1.0 / 5.0 * (t + 5.0 * c->radius);
+    if (d >= r_) return;
+    double s = 10.0 * c->radius / (t + 5.0 * c->radius) * c->speed;
+    double vmax[3] = {c->dir[0] * s, c->dir[1] * s, c->dir[2] * s};
+    double f = exp(-50.0 * d * d / (t * t));
+    out[0] = vmax[0] * f; out[1] = vmax[1] * f; out[2] = vmax[2] * f;
+}
+
+/* Pipe::GetVelocityAtPoint (Library/src/entities/forcefields/Pipe.cpp:57-79) */
+static void pipe_velocity(const hydro_current* c, const double* p, double* out)
+{
+    double pp[3] = {p[0] - c->point[0], p[1] - c->point[1], p[2] - c->point[2]};
+    double x[3];
+    bcross(pp, c->dir, x);
+    double d = sqrt(bdot(x, x));
+    double t = bdot(pp, c->dir);
+    out[0] = out[1] = out[2] = 0.0;
+    if (t < 0.0 || t > c->length) return;
+    double r = c->radius + (c->radius2 - c->radius) * t / c->length;
+    if (d >= r) return;
+    double s = c->radius / r * c->speed;
+    double v[3] = {c->dir[0] * s, c->dir[1] * s, c->dir[2] * s};
+    double f = pow(1.0 - d / r, c->gamma);
+    out[0] = v[0] * f; out[1] = v[1] * f; out[2] = v[2] * f;
+}
+
+/* Ocean::GetFluidVelocity(const Vector3&) (Ocean.cpp:183-196): V0() plus
+ * every enabled current, only when currents are enabled. */
+static void current_velocity(const hydro_ocean* o, double x, double y, double z, double* fv)
+{
+    fv[0] = fv[1] = fv[2] = 0.0;
+    if (!o->currents_enabled) return;
+    double p[3] = {x, y, z};
+    uint32_t n = o->n_currents < HYDRO_MAX_CURRENTS ? o->n_currents : HYDRO_MAX_CURRENTS;
+    for (uint32_t i = 0; i < n; ++i) {
+        const hydro_current* c = &o->currents[i];
+        if (!c->enabled) continue;
+        double u[3] = {0.0, 0.0, 0.0};
+        if (c->type == HYDRO_CURRENT_UNIFORM) { u[0] = c->vel[0]; u[1] = c->vel[1]; u[2] = c->vel[2]; }
+        else if (c->type == HYDRO_CURRENT_JET) jet_velocity(c, p, u);
+        else if (c->type == HYDRO_CURRENT_PIPE) pipe_velocity(c, p, u);
+        fv[0] += u[0]; fv[1] += u[1]; fv[2] += u[2];
+    }
+}
+
+/* ------------------------------------------- core instantiations */
+#define T float
+#define SFX _f32
+#define CUT64 0
+#include "hydro_oracle_core.inc"
+#undef T
+#undef SFX
+#undef CUT64
+
+#define T float
+#define SFX _f32c64
+#define CUT64 1
+#include "hydro_oracle_core.inc"
+#undef T
+#undef SFX
+#undef CUT64
+
+#define T double
+#define SFX _f64
+#define CUT64 0
+#include "hydro_oracle_core.inc"
+#undef T
+#undef SFX
+#undef CUT64
+
+/* ------------------------------------------------------- depth queries */
+float oracle_depth(int variant, const hydro_ocean* ocean, const oracle_waves* waves,
+                   float x, float y, float z)
+{
+    (void)variant;
+    return depth_f32(ocean, waves, x, y, z);
+}
+
+double oracle_depth64(const hydro_ocean* ocean, const oracle_waves* waves,
+                      double x, double y, double z)
+{
+    return depth_f64(ocean, waves, x, y, z);
+}
+
+/* SolidEntity::CheckBodyFluidPosition (SolidEntity.cpp:1239-1261) with
+ * Ocean::GetDepth(const Vector3&) (Ocean.cpp:170-173): each corner is cast
+ * to float, queried, and compared > 0 in double.  Every variant classifies
+ * the same way so that they take the same branch. */
+int oracle_fluid_position(const hydro_ocean* ocean, const oracle_waves* waves,
+                          const double mn[3], const double mx[3])
+{
+    double d[3] = {mx[0] - mn[0], mx[1] - mn[1], mx[2] - mn[2]};
+    double c[8][3] = {
+        {mn[0], mn[1], mn[2]},
+        {mx[0], mx[1], mx[2]},
+        {mn[0] + d[0], mn[1] + 0.0, mn[2] + 0.0},
+        {mn[0] + 0.0, mn[1] + d[1], mn[2] + 0.0},
+        {mn[0] + d[0], mn[1] + d[1], mn[2] + 0.0},
+        {mn[0] + 0.0, mn[1] + 0.0, mn[2] + d[2]},
+        {mn[0] + d[0], mn[1] + 0.0, mn[2] + d[2]},
+        {mn[0] + 0.0, mn[1] + d[1], mn[2] + d[2]},
+    };
+    unsigned under = 0;
+    for (int k = 0; k < 8; ++k) {
+        float dep = depth_f32(ocean, waves, (float)c[k][0], (float)c[k][1], (float)c[k][2]);
+        if ((double)dep > 0.0) ++under;
+    }
+    if (under == 0) return HYDRO_OUTSIDE;
+    if (under == 8) return HYDRO_INSIDE;
+    return HYDRO_CROSSING_SURFACE;
+}
+
+/* ------------------------------------------------------------ drivers */
+static void set3(double* d, double x, double y, double z) { d[0] = x; d[1] = y; d[2] = z; }
+static void zero3(double* d) { d[0] = d[1] = d[2] = 0.0; }
+
+/* Finalisation of the surface loop on FP64 sums (SolidEntity.cpp:1689-1720
+ * with the float steps carried out in FP64): REF64 and the MIRROR variants. */
+static void finalize_fp64(const hydro_settings* s, const hydro_ocean* ocean,
+                          const hydro_transform* T_CG, double p0x, double p0y,
+                          const dacc* a, double Fb[3], double Tb[3], double Fdq[3],
+                          double Tdq[3], double Fdf[3], double Tdf[3], double* Swet,
+                          double* Vsub)
+{
+    if (s->realistic_buoyancy && a->V6 > (double)1e-9f) {
+        *Vsub = a->V6 / 6.0;
+        if (ocean->waves) {
+            double k = ocean->density * ocean->gravity;
+            set3(Fb, a->Fb[0] * k, a->Fb[1] * k, a->Fb[2] * k);
+            set3(Tb, a->Tb[0] * k, a->Tb[1] * k, a->Tb[2] * k);
+        } else {
+            double cb[3] = {a->CB[0] / a->V6 + p0x, a->CB[1] / a->V6 + p0y, a->CB[2] / a->V6 + 0.0};
+            double k = -(*Vsub) * ocean->density;
+            double f[3] = {0.0 * k, 0.0 * k, ocean->gravity * k};
+            double r[3] = {cb[0] - T_CG->origin[0], cb[1] - T_CG->origin[1], cb[2] - T_CG->origin[2]};
+            set3(Fb, f[0], f[1], f[2]);
+            bcross(r, f, Tb);
+        }
+    }
+    if (s->damping_forces) {
+        memcpy(Fdq, a->Fdq, sizeof(double) * 3);
+        memcpy(Tdq, a->Tdq, sizeof(double) * 3);
+        memcpy(Fdf, a->Fdf, sizeof(double) * 3);
+        memcpy(Tdf, a->Tdf, sizeof(double) * 3);
+    }
+    *Swet = a->Swet;
+}
+
+static void acc64_to_dacc(const acc_f64* x, dacc* a)
+{
+    set3(a->Fb, x->Fb.x, x->Fb.y, x->Fb.z);
+    set3(a->Tb, x->Tb.x, x->Tb.y, x->Tb.z);
+    set3(a->Fdq, x->Fdq.x, x->Fdq.y, x->Fdq.z);
+    set3(a->Tdq, x->Tdq.x, x->Tdq.y, x->Tdq.z);
+    set3(a->Fdf, x->Fdf.x, x->Fdf.y, x->Fdf.z);
+    set3(a->Tdf, x->Tdf.x, x->Tdf.y, x->Tdf.z);
+    set3(a->CB, x->CB.x, x->CB.y, x->CB.z);
+    a->Swet = x->Swet;
+    a->V6 = x->V6;
+}
+
+void oracle_surface_forces(int variant, const hydro_settings* settings,
+                           const oracle_mesh* mesh, const hydro_ocean* ocean,
+                           const oracle_waves* waves, const hydro_transform* T_CG,
+                           const hydro_transform* T_C, const double v[3],
+                           const double omega[3], double Fb[3], double Tb[3],
+                           double Fdq[3], double Tdq[3], double Fdf[3], double Tdf[3],
+                           double* Swet, double* Vsub)
+{
+    /* mesh == nullptr (:1293-1312) */
+    if (mesh == NULL) {
+        if (settings->realistic_buoyancy) { zero3(Fb); zero3(Tb); }
+        if (settings->damping_forces) { zero3(Fdq); zero3(Tdq); zero3(Fdf); zero3(Tdf); }
+        *Swet = 0.0;
+        *Vsub = 0.0;
+        return;
+    }
+    if (variant == ORACLE_REF32) {
+        job_f32 J;
+        acc_f32 a;
+        job_init_f32(&J, mesh, ocean, waves, T_CG, T_C, v, omega,
+                     settings->realistic_buoyancy, settings->damping_forces);
+        loop_serial_f32(&J, 1, &a);
+        /* :1689-1720 in the reference's own precision */
+        if (settings->realistic_buoyancy && a.V6 > 1e-9f) {
+            *Vsub = (double)(a.V6 / 6.f);
+            if (ocean->waves) {
+                float k = (float)(ocean->density * ocean->gravity);
+                set3(Fb, a.Fb.x * k, a.Fb.y * k, a.Fb.z * k);
+                set3(Tb, a.Tb.x * k, a.Tb.y * k, a.Tb.z * k);
+            } else {
+                float cbx = a.CB.x / a.V6 + J.p0.x;
+                float cby = a.CB.y / a.V6 + J.p0.y;
+                float cbz = a.CB.z / a.V6 + J.p0.z;
+                double k = -(*Vsub) * ocean->density;
+                double f[3] = {0.0 * k, 0.0 * k, ocean->gravity * k};
+                double r[3] = {(double)cbx - T_CG->origin[0], (double)cby - T_CG->origin[1],
+                               (double)cbz - T_CG->origin[2]};
+                set3(Fb, f[0], f[1], f[2]);
+                bcross(r, f, Tb);
+            }
+        }
+        if (settings->damping_forces) {
+            set3(Fdq, a.Fdq.x, a.Fdq.y, a.Fdq.z);
+            set3(Tdq, a.Tdq.x, a.Tdq.y, a.Tdq.z);
+            set3(Fdf, a.Fdf.x, a.Fdf.y, a.Fdf.z);
+            set3(Tdf, a.Tdf.x, a.Tdf.y, a.Tdf.z);
+        }
+        *Swet = (double)a.Swet;
+        return;
+    }
+    dacc d;
+    double p0x, p0y;
+    if (variant == ORACLE_REF64) {
+        job_f64 J;
+        acc_f64 a;
+        job_init_f64(&J, mesh, ocean, waves, T_CG, T_C, v, omega,
+                     settings->realistic_buoyancy, settings->damping_forces);
+        loop_serial_f64(&J, 1, &a);
+        acc64_to_dacc(&a, &d);
+        p0x = J.p0.x; p0y = J.p0.y;
+    } else if (variant == ORACLE_MIRROR64) {
+        job_f32c64 J;
+        job_init_f32c64(&J, mesh, ocean, waves, T_CG, T_C, v, omega,
+                        settings->realistic_buoyancy, settings->damping_forces);
+        loop_exact_f32c64(&J, 1, &d);
+        p0x = J.p0.x; p0y = J.p0.y;
+    } else {
+        job_f32 J;
+        job_init_f32(&J, mesh, ocean, waves, T_CG, T_C, v, omega,
+                     settings->realistic_buoyancy, settings->damping_forces);
+        loop_exact_f32(&J, 1, &d);
+        p0x = J.p0.x; p0y = J.p0.y;
+    }
+    finalize_fp64(settings, ocean, T_CG, p0x, p0y, &d, Fb, Tb, Fdq, Tdq, Fdf, Tdf, Swet, Vsub);
+}
+
+void oracle_submerged_forces(int variant, const oracle_mesh* mesh,
+                             const hydro_ocean* ocean, const hydro_transform* T_CG,
+                             const hydro_transform* T_C, const double v[3],
+                             const double omega[3], double Fdq[3], double Tdq[3],
+                             double Fdf[3], double Tdf[3])
+{
+    if (mesh == NULL) { zero3(Fdq); zero3(Tdq); zero3(Fdf); zero3(Tdf); return; }  /* :1726-1733 */
+    dacc d;
+    if (variant == ORACLE_REF32) {
+        job_f32 J;
+        acc_f32 a;
+        job_init_f32(&J, mesh, ocean, NULL, T_CG, T_C, v, omega, 0, 1);
+        loop_serial_f32(&J, 0, &a);
+        set3(Fdq, a.Fdq.x, a.Fdq.y, a.Fdq.z);
+        set3(Tdq, a.Tdq.x, a.Tdq.y, a.Tdq.z);
+        set3(Fdf, a.Fdf.x, a.Fdf.y, a.Fdf.z);
+        set3(Tdf, a.Tdf.x, a.Tdf.y, a.Tdf.z);
+        return;
+    }
+    if (variant == ORACLE_REF64) {
+        job_f64 J;
+        acc_f64 a;
+        job_init_f64(&J, mesh, ocean, NULL, T_CG, T_C, v, omega, 0, 1);
+        loop_serial_f64(&J, 0, &a);
+        acc64_to_dacc(&a, &d);
+    } else {
+        /* the submerged loop has no cut points: both mirrors coincide */
+        job_f32 J;
+        job_init_f32(&J, mesh, ocean, NULL, T_CG, T_C, v, omega, 0, 1);
+        loop_exact_f32(&J, 0, &d);
+    }
+    memcpy(Fdq, d.Fdq, sizeof(double) * 3);
+    memcpy(Tdq, d.Tdq, sizeof(double) * 3);
+    memcpy(Fdf, d.Fdf, sizeof(double) * 3);
+    memcpy(Tdf, d.Tdf, sizeof(double) * 3);
+}
+
+/* btMatrix3x3::inverse (3rdparty/LinearMath/btMatrix3x3.h:1093-1103) */
+static void binverse(const double* m, double* r)
+{
+#define M(i, j) m[3 * (i) + (j)]
+#define COF(r1, c1, r2, c2) (M(r1, c1) * M(r2, c2) - M(r1, c2) * M(r2, c1))
+    double co[3] = {COF(1, 1, 2, 2), COF(1, 2, 2, 0), COF(1, 0, 2, 1)};
+    double det = M(0, 0) * co[0] + M(0, 1) * co[1] + M(0, 2) * co[2];
+    double s = 1.0 / det;
+    r[0] = co[0] * s; r[1] = COF(0, 2, 2, 1) * s; r[2] = COF(0, 1, 1, 2) * s;
+    r[3] = co[1] * s; r[4] = COF(0, 0, 2, 2) * s; r[5] = COF(0, 2, 1, 0) * s;
+    r[6] = co[2] * s; r[7] = COF(0, 1, 2, 0) * s; r[8] = COF(0, 0, 1, 1) * s;
+#undef COF
+#undef M
+}
+
+/* One vector of CorrectHydrodynamicForces (SolidEntity.cpp:1266-1286). */
+static void correct_one(const double* inv, double* vec, const double* C, double k)
+{
+    double w[3] = {inv[0] * vec[0] + inv[1] * vec[1] + inv[2] * vec[2],
+                   inv[3] * vec[0] + inv[4] * vec[1] + inv[5] * vec[2],
+                   inv[6] * vec[0] + inv[7] * vec[1] + inv[8] * vec[2]};
+    /* btVector3::safeNormalize (btVector3.h:286-299) */
+    double l2 = bdot(w, w);
+    if (l2 >= DBL_EPSILON * DBL_EPSILON) {
+        double s = 1.0 / sqrt(l2);
+        w[0] *= s; w[1] *= s; w[2] *= s;
+    } else {
+        w[0] = 1.0; w[1] = 0.0; w[2] = 0.0;
+    }
+    double c = fabs(w[0]) * C[0] + fabs(w[1]) * C[1] + fabs(w[2]) * C[2];
+    double f = k * c;
+    vec[0] = f * vec[0]; vec[1] = f * vec[1]; vec[2] = f * vec[2];
+}
+
+void oracle_correct_forces(const hydro_ocean* ocean, double Fdq[3], double Tdq[3],
+                           double Fdf[3], double Tdf[3], const double Cd[3],
+                           const double Cf[3], const double R_O[9])
+{
+    double inv[9];
+    binverse(R_O, inv);
+    correct_one(inv, Fdq, Cd, 0.5 * ocean->density);
+    correct_one(inv, Tdq, Cd, 0.5 * ocean->density);
+    correct_one(inv, Fdf, Cf, ocean->density);
+    correct_one(inv, Tdf, Cf, ocean->density);
+}
+
+/* SolidEntity::ComputeHydrodynamicForces (SolidEntity.cpp:1799-1850). */
+void oracle_body_forces(int variant, const hydro_body* b, const oracle_mesh* mesh,
+                        const hydro_ocean* ocean, const oracle_waves* waves,
+                        const hydro_settings* settings, hydro_wrench* io)
+{
+    if (b->mode != HYDRO_MODE_FLOATING && b->mode != HYDRO_MODE_SUBMERGED) {
+        io->position = HYDRO_SKIPPED;
+        return;
+    }
+    int bf = oracle_fluid_position(ocean, waves, b->aabb_min, b->aabb_max);
+    io->position = bf;
+    if (bf == HYDRO_OUTSIDE) {
+        zero3(io->Fb); zero3(io->Tb); zero3(io->Fdq); zero3(io->Tdq);
+        zero3(io->Fdf); zero3(io->Tdf);
+        io->Swet = 0.0;
+        io->Vsub = 0.0;
+        return;
+    }
+    int buoyant = b->buoyancy != 0;  /* isBuoyant(), :205-208 */
+    if (bf == HYDRO_INSIDE) {
+        if (buoyant) {
+            double k = -b->volume * ocean->density;
+            double f[3] = {0.0 * k, 0.0 * k, ocean->gravity * k};
+            const double* R = b->T_CG.basis;
+            const double* o = b->T_CG.origin;
+            double cb[3] = {(R[0] * b->P_CB[0] + R[1] * b->P_CB[1] + R[2] * b->P_CB[2]) + o[0],
+                            (R[3] * b->P_CB[0] + R[4] * b->P_CB[1] + R[5] * b->P_CB[2]) + o[1],
+                            (R[6] * b->P_CB[0] + R[7] * b->P_CB[1] + R[8] * b->P_CB[2]) + o[2]};
+            double r[3] = {cb[0] - o[0], cb[1] - o[1], cb[2] - o[2]};
+            set3(io->Fb, f[0], f[1], f[2]);
+            bcross(r, f, io->Tb);
+        }
+        if (settings->damping_forces)
+            oracle_submerged_forces(variant, mesh, ocean, &b->T_CG, &b->T_C, b->v, b->omega,
+                                    io->Fdq, io->Tdq, io->Fdf, io->Tdf);
+        io->Swet = b->surface;
+    } else {
+        hydro_settings s = *settings;
+        if (!buoyant) s.realistic_buoyancy = 0;
+        oracle_surface_forces(variant, &s, mesh, ocean, waves, &b->T_CG, &b->T_C, b->v,
+                              b->omega, io->Fb, io->Tb, io->Fdq, io->Tdq, io->Fdf, io->Tdf,
+                              &io->Swet, &io->Vsub);
+    }
+    if (settings->damping_forces)
+        oracle_correct_forces(ocean, io->Fdq, io->Tdq, io->Fdf, io->Tdf, b->Cd, b->Cf, b->R_O);
+}
+
+void oracle_surface_face_terms(int variant, const hydro_settings* settings,
+                               const oracle_mesh* mesh, const hydro_ocean* ocean,
+                               const oracle_waves* waves, const hydro_transform* T_CG,
+                               const hydro_transform* T_C, const double v[3],
+                               const double omega[3], float* out)
+{
+    if (variant == ORACLE_MIRROR64) {
+        job_f32c64 J;
+        job_init_f32c64(&J, mesh, ocean, waves, T_CG, T_C, v, omega,
+                        settings->realistic_buoyancy, settings->damping_forces);
+        face_terms_f32c64(&J, out);
+    } else {
+        job_f32 J;
+        job_init_f32(&J, mesh, ocean, waves, T_CG, T_C, v, omega,
+                     settings->realistic_buoyancy, settings->damping_forces);
+        face_terms_f32(&J, out);
+    }
+}
+
+/* --------------------------------------------------------- batch */
+typedef struct {
+    int variant;
+    const hydro_body* bodies;
+    uint32_t n;
+    const oracle_mesh* meshes;
+    uint32_t n_meshes;
+    const hydro_ocean* ocean;
+    const oracle_waves* waves;
+    const hydro_settings* settings;
+    hydro_wrench* io;
+    atomic_uint next;
+    pthread_barrier_t start;
+} batch_job;
+
+static void* batch_worker(void* arg)
+{
+    batch_job* B = (batch_job*)arg;
+    pthread_barrier_wait(&B->start);
+    for (;;) {
+        unsigned i = atomic_fetch_add_explicit(&B->next, 1u, memory_order_relaxed);
+        if (i >= B->n) break;
+        const hydro_body* b = &B->bodies[i];
+        const oracle_mesh* m = (b->mesh < B->n_meshes) ? &B->meshes[b->mesh] : NULL;
+        oracle_body_forces(B->variant, b, m, B->ocean, B->waves, B->settings, &B->io[i]);
+    }
+    return NULL;
+}
+
+static double now_s(void)
+{
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
+double oracle_batch(int variant, int threads, const hydro_body* bodies, uint32_t n_bodies,
+                    const oracle_mesh* meshes, uint32_t n_meshes, const hydro_ocean* ocean,
+                    const oracle_waves* waves, const hydro_settings* settings,
+                    hydro_wrench* io)
+{
+    if (threads < 1) threads = 1;
+    batch_job B;
+    B.variant = variant;
+    B.bodies = bodies;
+    B.n = n_bodies;
+    B.meshes = meshes;
+    B.n_meshes = n_meshes;
+    B.ocean = ocean;
+    B.waves = waves;
+    B.settings = settings;
+    B.io = io;
+    atomic_init(&B.next, 0u);
+    pthread_barrier_init(&B.start, NULL, (unsigned)threads + 1u);
+    pthread_t* tid = (pthread_t*)calloc((size_t)threads, sizeof(pthread_t));
+    for (int t = 0; t < threads; ++t) pthread_create(&tid[t], NULL, batch_worker, &B);
+    double t0 = now_s();
+    pthread_barrier_wait(&B.start);
+    for (int t = 0; t < threads; ++t) pthread_join(tid[t], NULL);
+    double t1 = now_s();
+    pthread_barrier_destroy(&B.start);
+    free(tid);
+    return t1 - t0;
+}
+
+int oracle_hardware_threads(void)
+{
+    long n = sysconf(_SC_NPROCESSORS_ONLN);
+    return n > 0 ? (int)n : 1;
+}

@@ -1,0 +1,184 @@
+"""ctypes/numpy mirror of include/stonefish_hydro.h.
+
+The numpy structured dtypes have exactly the C layout, so arrays of bodies
+and wrenches can be handed to the C ABI (host pointers) or copied into
+device buffers as raw bytes.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
+LIB_DIR = os.path.join(HERE, "lib")
+LIB_PATH = os.path.join(LIB_DIR, "libstonefish_hydro.so")
+INCLUDE_DIR = os.path.join(REPO, "include")
+
+# status codes
+HYDRO_OK = 0
+HYDRO_ERR_INVALID_ARG = 1
+HYDRO_ERR_OOM = 2
+HYDRO_ERR_TIMEOUT = 3
+HYDRO_ERR_DEVICE = 4
+HYDRO_ERR_NOT_FOUND = 5
+HYDRO_ERR_INDEX_RANGE = 6
+HYDRO_ERR_UNSUPPORTED = 7
+HYDRO_ERR_MISMATCH = 8
+
+# PhysicsMode
+MODE_DISABLED, MODE_SURFACE, MODE_FLOATING, MODE_SUBMERGED, MODE_AERODYNAMIC = range(5)
+# BodyFluidPosition
+INSIDE, OUTSIDE, CROSSING_SURFACE, SKIPPED = 0, 1, 2, -1
+# VelocityFieldType
+CURRENT_UNIFORM, CURRENT_JET, CURRENT_PIPE = 0, 1, 2
+CUT_FP64, CUT_FP32 = 0, 1
+MAX_CURRENTS = 8
+MAX_WAVE_LAYERS = 4
+NO_MESH = 0xFFFFFFFF
+
+_d3 = C.c_double * 3
+
+
+class Transform(C.Structure):
+    _fields_ = [("basis", C.c_double * 9), ("origin", _d3)]
+
+
+class Settings(C.Structure):
+    _fields_ = [("damping_forces", C.c_int32), ("realistic_buoyancy", C.c_int32)]
+
+
+class Current(C.Structure):
+    _fields_ = [("type", C.c_int32), ("enabled", C.c_int32), ("vel", _d3),
+                ("point", _d3), ("dir", _d3), ("radius", C.c_double),
+                ("radius2", C.c_double), ("length", C.c_double),
+                ("speed", C.c_double), ("gamma", C.c_double)]
+
+
+class Ocean(C.Structure):
+    _fields_ = [("density", C.c_double), ("gravity", C.c_double),
+                ("waves", C.c_int32), ("currents_enabled", C.c_int32),
+                ("n_currents", C.c_uint32), ("reserved", C.c_uint32),
+                ("currents", Current * MAX_CURRENTS)]
+
+
+class Body(C.Structure):
+    _fields_ = [("T_CG", Transform), ("T_C", Transform), ("R_O", C.c_double * 9),
+                ("v", _d3), ("omega", _d3), ("Cd", _d3), ("Cf", _d3), ("P_CB", _d3),
+                ("volume", C.c_double), ("surface", C.c_double),
+                ("aabb_min", _d3), ("aabb_max", _d3), ("mesh", C.c_uint32),
+                ("mode", C.c_int32), ("buoyancy", C.c_int32), ("reserved", C.c_int32)]
+
+
+class Wrench(C.Structure):
+    _fields_ = [("Fb", _d3), ("Tb", _d3), ("Fdq", _d3), ("Tdq", _d3), ("Fdf", _d3),
+                ("Tdf", _d3), ("Swet", C.c_double), ("Vsub", C.c_double),
+                ("position", C.c_int32), ("status", C.c_int32)]
+
+
+class Config(C.Structure):
+    _fields_ = [("device", C.c_int32), ("cut_precision", C.c_int32),
+                ("tile_faces", C.c_uint32), ("ctas_per_sm", C.c_uint32),
+                ("tune_cache_path", C.c_char_p)]
+
+
+def _dtype_of(struct) -> np.dtype:
+    names, formats, offsets = [], [], []
+    for name, ctype in struct._fields_:
+        field = getattr(struct, name)
+        names.append(name)
+        offsets.append(field.offset)
+        if issubclass(ctype, C.Structure):
+            formats.append(_dtype_of(ctype))
+        elif issubclass(ctype, C.Array):
+            base = ctype._type_
+            if issubclass(base, C.Structure):
+                formats.append((_dtype_of(base), (ctype._length_,)))
+            else:
+                formats.append((np.dtype(base), (ctype._length_,)))
+        else:
+            formats.append(np.dtype(ctype))
+    return np.dtype({"names": names, "formats": formats, "offsets": offsets,
+                     "itemsize": C.sizeof(struct)})
+
+
+TRANSFORM_DTYPE = _dtype_of(Transform)
+BODY_DTYPE = _dtype_of(Body)
+WRENCH_DTYPE = _dtype_of(Wrench)
+OCEAN_DTYPE = _dtype_of(Ocean)
+CURRENT_DTYPE = _dtype_of(Current)
+
+WRENCH_VECTORS = ("Fb", "Tb", "Fdq", "Tdq", "Fdf", "Tdf")
+
+
+def ptr(a: np.ndarray, ctype=C.c_void_p):
+    return C.cast(a.ctypes.data, ctype)
+
+
+class HydroError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"hydro status {status}: {msg}")
+        self.status = status
+
+
+_lib = None
+
+
+def load_library(path: str | None = None) -> C.CDLL:
+    """Loads the CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise ImportError(f"{p} is missing: build it with stonefish_gb300.build.build()")
+    lib = C.CDLL(p)
+    _declare(lib)
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _declare(lib: C.CDLL) -> None:
+    vp, u32, i32 = C.c_void_p, C.c_uint32, C.c_int32
+    d = C.POINTER(C.c_double)
+    sig = {
+        "hydro_config_default": (None, [C.POINTER(Config)]),
+        "hydro_create": (i32, [C.POINTER(vp), C.POINTER(Config)]),
+        "hydro_destroy": (None, [vp]),
+        "hydro_last_error": (C.c_char_p, [vp]),
+        "hydro_status_string": (C.c_char_p, [i32]),
+        "hydro_abi_version": (i32, []),
+        "hydro_mesh_upload": (i32, [vp, vp, C.c_size_t, u32, vp, u32, C.POINTER(u32)]),
+        "hydro_mesh_info": (i32, [vp, u32, C.POINTER(u32), C.POINTER(u32), C.POINTER(u32)]),
+        "hydro_wave_grid_set": (i32, [vp, vp, u32, u32, u32, vp, vp]),
+        "hydro_depth": (i32, [vp, C.POINTER(Ocean), vp, u32, vp]),
+        "hydro_batch_create": (i32, [vp, vp, u32, C.POINTER(vp)]),
+        "hydro_batch_destroy": (None, [vp]),
+        "hydro_batch_compute_device": (i32, [vp, vp, C.POINTER(Ocean), C.POINTER(Settings), vp, vp]),
+        "hydro_batch_compute": (i32, [vp, vp, C.POINTER(Ocean), C.POINTER(Settings), vp]),
+        "hydro_batch_last_launches": (u32, [vp]),
+        "hydro_body_forces": (i32, [vp, vp, C.POINTER(Ocean), C.POINTER(Settings), vp]),
+        "hydro_surface_forces": (i32, [vp, C.POINTER(Settings), u32, C.POINTER(Ocean),
+                                       C.POINTER(Transform), C.POINTER(Transform), d, d,
+                                       d, d, d, d, d, d, d, d]),
+        "hydro_submerged_forces": (i32, [vp, u32, C.POINTER(Ocean), C.POINTER(Transform),
+                                         C.POINTER(Transform), d, d, d, d, d, d]),
+        "hydro_correct_forces": (i32, [vp, C.POINTER(Ocean), d, d, d, d, d, d, d]),
+        "hydro_fluid_position": (i32, [vp, C.POINTER(Ocean), d, d, C.POINTER(i32)]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+
+
+def exported_symbols_from_header(header: str | None = None) -> list[str]:
+    """Function names declared in include/stonefish_hydro.h."""
+    import re
+    path = header or os.path.join(INCLUDE_DIR, "stonefish_hydro.h")
+    text = open(path).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(hydro_[a-z0-9_]+)\s*\(", text)))

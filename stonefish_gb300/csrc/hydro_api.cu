@@ -1,0 +1,792 @@
+// hydro_api.cu -- C ABI of the GB300 hydrodynamic wrench path
+// (include/stonefish_hydro.h).  Host C++ only: contexts, the tiled device
+// copy of each mesh, batches (work lists and scratch) and the launches.
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/stonefish_hydro.h"
+#include "hydro_internal.h"
+
+using namespace sfh;
+
+namespace {
+
+struct MeshRec {
+    uint32_t n_vertices;
+    uint32_t n_faces;
+    uint32_t first_tile;
+    uint32_t n_tiles;
+};
+
+struct Slab {
+    char* base;
+    size_t size;
+    size_t used;
+};
+
+}  // namespace
+
+struct hydro_batch;
+
+struct hydro_ctx {
+    int device = 0;
+    hydro_config cfg{};
+    cudaStream_t stream = nullptr;
+    std::recursive_mutex mu;
+    std::string err = "";
+    std::vector<MeshRec> meshes;
+    std::vector<Slab> slabs;
+    std::vector<TileDesc> tiles_h;
+    TileDesc* tiles_d = nullptr;
+    size_t tiles_d_cap = 0;
+    size_t tiles_d_count = 0;
+    // wave grid
+    float* wave_d = nullptr;
+    uint32_t wave_n = 0, wave_channels = 0, wave_layers = 0;
+    uint32_t wave_channel[HYDRO_MAX_WAVE_LAYERS] = {0, 0, 0, 0};
+    float wave_grid[HYDRO_MAX_WAVE_LAYERS] = {1.f, 1.f, 1.f, 1.f};
+    // single-body calls
+    std::unordered_map<uint32_t, hydro_batch*> single;
+    void* small_d = nullptr;   // scratch for the small entry points
+    size_t small_cap = 0;
+};
+
+struct hydro_batch {
+    hydro_ctx* ctx = nullptr;
+    uint32_t n_bodies = 0;
+    uint32_t n_chunks = 0;
+    std::vector<uint32_t> mesh_of_body;
+    ChunkDesc* chunks_d = nullptr;
+    BodyInfo* binfo_d = nullptr;
+    double* partials_d = nullptr;
+    unsigned* counters_d = nullptr;
+    hydro_body* bodies_d = nullptr;    // staging for the host-buffer entry point
+    hydro_wrench* io_d = nullptr;
+    cudaStream_t stream = nullptr;
+    uint32_t last_launches = 0;
+};
+
+namespace {
+
+hydro_status fail(hydro_ctx* ctx, hydro_status s, const char* fmt, ...)
+{
+    if (ctx) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof(buf), fmt, ap);
+        va_end(ap);
+        ctx->err = buf;
+    }
+    return s;
+}
+
+hydro_status cuda_fail(hydro_ctx* ctx, cudaError_t e, const char* what)
+{
+    if (e == cudaErrorMemoryAllocation)
+        return fail(ctx, HYDRO_ERR_OOM, "%s: %s", what, cudaGetErrorString(e));
+    return fail(ctx, HYDRO_ERR_DEVICE, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(ctx, call)                                              \
+    do {                                                           \
+        cudaError_t e_ = (call);                                   \
+        if (e_ != cudaSuccess) return cuda_fail((ctx), e_, #call); \
+    } while (0)
+
+constexpr size_t kSlabBytes = size_t(256) << 20;
+
+// Bump allocation of device memory for mesh tiles (256-byte aligned).
+hydro_status slab_alloc(hydro_ctx* ctx, size_t bytes, char** out)
+{
+    bytes = (bytes + 255) & ~size_t(255);
+    if (ctx->slabs.empty() || ctx->slabs.back().size - ctx->slabs.back().used < bytes) {
+        Slab s{};
+        s.size = std::max(kSlabBytes, bytes);
+        cudaError_t e = cudaMalloc(&s.base, s.size);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc(mesh slab)");
+        s.used = 0;
+        ctx->slabs.push_back(s);
+    }
+    Slab& s = ctx->slabs.back();
+    *out = s.base + s.used;
+    s.used += bytes;
+    return HYDRO_OK;
+}
+
+// Device copy of the tile table, grown on demand.
+hydro_status sync_tiles(hydro_ctx* ctx)
+{
+    if (ctx->tiles_d_count == ctx->tiles_h.size()) return HYDRO_OK;
+    if (ctx->tiles_h.size() > ctx->tiles_d_cap) {
+        size_t cap = std::max<size_t>(ctx->tiles_h.size() * 2, 1024);
+        TileDesc* p = nullptr;
+        CK(ctx, cudaMalloc(&p, cap * sizeof(TileDesc)));
+        if (ctx->tiles_d) cudaFree(ctx->tiles_d);
+        ctx->tiles_d = p;
+        ctx->tiles_d_cap = cap;
+        ctx->tiles_d_count = 0;
+    }
+    size_t n = ctx->tiles_h.size() - ctx->tiles_d_count;
+    CK(ctx, cudaMemcpy(ctx->tiles_d + ctx->tiles_d_count, ctx->tiles_h.data() + ctx->tiles_d_count,
+                       n * sizeof(TileDesc), cudaMemcpyHostToDevice));
+    ctx->tiles_d_count = ctx->tiles_h.size();
+    return HYDRO_OK;
+}
+
+hydro_status ensure_small(hydro_ctx* ctx, size_t bytes)
+{
+    if (ctx->small_cap >= bytes) return HYDRO_OK;
+    if (ctx->small_d) cudaFree(ctx->small_d);
+    ctx->small_d = nullptr;
+    ctx->small_cap = 0;
+    size_t cap = std::max<size_t>(bytes, 4096);
+    CK(ctx, cudaMalloc(&ctx->small_d, cap));
+    ctx->small_cap = cap;
+    return HYDRO_OK;
+}
+
+bool valid_ocean(const hydro_ocean* o)
+{
+    return o && o->n_currents <= HYDRO_MAX_CURRENTS;
+}
+
+// The kernels' view of the ocean: the position-independent currents are
+// summed in FP64 in the reference's order and cast once (Ocean.cpp:183-201).
+OceanDev make_ocean(const hydro_ctx* ctx, const hydro_ocean* o)
+{
+    OceanDev d{};
+    d.density = o->density;
+    d.gravity = o->gravity;
+    d.waves = o->waves ? 1 : 0;
+    d.currents_enabled = o->currents_enabled ? 1 : 0;
+    d.n_currents = (int)o->n_currents;
+    double u[3] = {0.0, 0.0, 0.0};
+    int field = 0;
+    if (o->currents_enabled) {
+        for (uint32_t i = 0; i < o->n_currents; ++i) {
+            const hydro_current& c = o->currents[i];
+            if (!c.enabled) continue;
+            if (c.type == HYDRO_CURRENT_UNIFORM) {
+                u[0] += c.vel[0]; u[1] += c.vel[1]; u[2] += c.vel[2];
+            } else {
+                field = 1;
+            }
+        }
+    }
+    d.field_currents = field;
+    d.U[0] = (float)u[0]; d.U[1] = (float)u[1]; d.U[2] = (float)u[2];
+    for (int i = 0; i < HYDRO_MAX_CURRENTS; ++i) d.currents[i] = o->currents[i];
+    if (!o->currents_enabled) d.n_currents = 0;
+    d.wave_data = ctx->wave_d;
+    d.wave_n = ctx->wave_n;
+    d.wave_channels = ctx->wave_channels;
+    d.wave_layers = ctx->wave_layers;
+    for (int l = 0; l < HYDRO_MAX_WAVE_LAYERS; ++l) {
+        d.wave_channel[l] = ctx->wave_channel[l];
+        d.wave_grid[l] = ctx->wave_grid[l];
+    }
+    return d;
+}
+
+uint32_t tiles_per_chunk(const hydro_ctx* ctx)
+{
+    uint32_t faces = ctx->cfg.tile_faces ? ctx->cfg.tile_faces : 4096u;
+    return std::max<uint32_t>(1u, (faces + kTileFaces - 1) / kTileFaces);
+}
+
+void batch_free(hydro_batch* b)
+{
+    if (!b) return;
+    cudaFree(b->chunks_d);
+    cudaFree(b->binfo_d);
+    cudaFree(b->partials_d);
+    cudaFree(b->counters_d);
+    cudaFree(b->bodies_d);
+    cudaFree(b->io_d);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+hydro_status batch_build(hydro_ctx* ctx, const hydro_mesh_id* mesh_of_body, uint32_t n,
+                         hydro_batch** out)
+{
+    for (uint32_t i = 0; i < n; ++i) {
+        if (mesh_of_body[i] != HYDRO_NO_MESH && mesh_of_body[i] >= ctx->meshes.size())
+            return fail(ctx, HYDRO_ERR_NOT_FOUND, "body %u: unknown mesh %u", i, mesh_of_body[i]);
+    }
+    hydro_status st = sync_tiles(ctx);
+    if (st != HYDRO_OK) return st;
+    const uint32_t tpc = tiles_per_chunk(ctx);
+    std::vector<ChunkDesc> chunks;
+    std::vector<BodyInfo> info(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        BodyInfo& bi = info[i];
+        bi.first_chunk = (uint32_t)chunks.size();
+        bi.mesh = mesh_of_body[i];
+        uint32_t first = 0, nt = 0;
+        if (bi.mesh != HYDRO_NO_MESH) {
+            const MeshRec& m = ctx->meshes[bi.mesh];
+            first = m.first_tile;
+            nt = m.n_tiles;
+            bi.n_faces = m.n_faces;
+        } else {
+            bi.n_faces = 0;
+        }
+        uint32_t k = 0;
+        for (uint32_t t = 0; t < nt; t += tpc, ++k)
+            chunks.push_back(ChunkDesc{i, first + t, std::min(tpc, nt - t), k});
+        if (k == 0) chunks.push_back(ChunkDesc{i, first, 0u, 0u});   // finaliser only
+        bi.n_chunks = (uint32_t)chunks.size() - bi.first_chunk;
+    }
+    hydro_batch* b = new (std::nothrow) hydro_batch();
+    if (!b) return fail(ctx, HYDRO_ERR_OOM, "host allocation");
+    b->ctx = ctx;
+    b->n_bodies = n;
+    b->n_chunks = (uint32_t)chunks.size();
+    b->mesh_of_body.assign(mesh_of_body, mesh_of_body + n);
+    cudaError_t e;
+#define BK(call)                                              \
+    do {                                                      \
+        e = (call);                                           \
+        if (e != cudaSuccess) {                               \
+            batch_free(b);                                    \
+            return cuda_fail(ctx, e, #call);                  \
+        }                                                     \
+    } while (0)
+    BK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    BK(cudaMalloc(&b->chunks_d, chunks.size() * sizeof(ChunkDesc)));
+    BK(cudaMalloc(&b->binfo_d, n * sizeof(BodyInfo)));
+    BK(cudaMalloc(&b->partials_d, chunks.size() * kPartialStride * sizeof(double)));
+    BK(cudaMalloc(&b->counters_d, n * sizeof(unsigned)));
+    BK(cudaMemcpy(b->chunks_d, chunks.data(), chunks.size() * sizeof(ChunkDesc), cudaMemcpyHostToDevice));
+    BK(cudaMemcpy(b->binfo_d, info.data(), n * sizeof(BodyInfo), cudaMemcpyHostToDevice));
+    BK(cudaMemset(b->counters_d, 0, n * sizeof(unsigned)));
+    BK(cudaMemset(b->partials_d, 0, chunks.size() * kPartialStride * sizeof(double)));
+#undef BK
+    *out = b;
+    return HYDRO_OK;
+}
+
+hydro_status batch_launch(hydro_batch* b, const hydro_body* d_bodies, const hydro_ocean* ocean,
+                          const hydro_settings* settings, hydro_wrench* d_io, cudaStream_t s,
+                          int op)
+{
+    hydro_ctx* ctx = b->ctx;
+    hydro_status st = sync_tiles(ctx);
+    if (st != HYDRO_OK) return st;
+    KParams P{};
+    P.chunks = b->chunks_d;
+    P.binfo = b->binfo_d;
+    P.tiles = ctx->tiles_d;
+    P.bodies = d_bodies;
+    P.io = d_io;
+    P.partials = b->partials_d;
+    P.counters = b->counters_d;
+    P.ocean = make_ocean(ctx, ocean);
+    P.st.damping = settings->damping_forces ? 1 : 0;
+    P.st.buoyancy = settings->realistic_buoyancy ? 1 : 0;
+    P.op = op;
+    if (P.ocean.waves && ctx->wave_d == nullptr)
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "ocean.waves set but no wave grid was given");
+    cudaError_t e = launch_chunks(P, b->n_chunks, ctx->cfg.cut_precision == HYDRO_CUT_FP64, s);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "chunk kernel launch");
+    b->last_launches = 1;
+    return HYDRO_OK;
+}
+
+hydro_status single_batch(hydro_ctx* ctx, hydro_mesh_id mesh, hydro_batch** out)
+{
+    auto it = ctx->single.find(mesh);
+    if (it != ctx->single.end()) {
+        *out = it->second;
+        return HYDRO_OK;
+    }
+    hydro_batch* b = nullptr;
+    hydro_status st = batch_build(ctx, &mesh, 1, &b);
+    if (st != HYDRO_OK) return st;
+    cudaError_t e1 = cudaMalloc(&b->bodies_d, sizeof(hydro_body));
+    cudaError_t e2 = cudaMalloc(&b->io_d, sizeof(hydro_wrench));
+    if (e1 != cudaSuccess || e2 != cudaSuccess) {
+        batch_free(b);
+        return cuda_fail(ctx, e1 != cudaSuccess ? e1 : e2, "cudaMalloc(single body)");
+    }
+    ctx->single[mesh] = b;
+    *out = b;
+    return HYDRO_OK;
+}
+
+// One body through the batched kernel with host in/out.
+hydro_status run_single(hydro_ctx* ctx, const hydro_body& body, const hydro_ocean* ocean,
+                        const hydro_settings* settings, hydro_wrench& io, int op)
+{
+    hydro_batch* b = nullptr;
+    hydro_status st = single_batch(ctx, body.mesh, &b);
+    if (st != HYDRO_OK) return st;
+    CK(ctx, cudaMemcpyAsync(b->bodies_d, &body, sizeof(hydro_body), cudaMemcpyHostToDevice, ctx->stream));
+    CK(ctx, cudaMemcpyAsync(b->io_d, &io, sizeof(hydro_wrench), cudaMemcpyHostToDevice, ctx->stream));
+    st = batch_launch(b, b->bodies_d, ocean, settings, b->io_d, ctx->stream, op);
+    if (st != HYDRO_OK) return st;
+    CK(ctx, cudaMemcpyAsync(&io, b->io_d, sizeof(hydro_wrench), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(ctx, cudaStreamSynchronize(ctx->stream));
+    return HYDRO_OK;
+}
+
+void copy3(double* d, const double* s) { d[0] = s[0]; d[1] = s[1]; d[2] = s[2]; }
+
+}  // namespace
+
+// =================================================================== C ABI
+extern "C" {
+
+void hydro_config_default(hydro_config* cfg)
+{
+    if (!cfg) return;
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->device = 0;
+    cfg->cut_precision = HYDRO_CUT_FP64;
+    cfg->tile_faces = 0;
+    cfg->ctas_per_sm = 0;
+    cfg->tune_cache_path = nullptr;
+}
+
+int hydro_abi_version(void) { return HYDRO_ABI_VERSION; }
+
+const char* hydro_status_string(hydro_status s)
+{
+    switch (s) {
+    case HYDRO_OK: return "ok";
+    case HYDRO_ERR_INVALID_ARG: return "invalid argument";
+    case HYDRO_ERR_OOM: return "out of memory";
+    case HYDRO_ERR_TIMEOUT: return "device wait timed out";
+    case HYDRO_ERR_DEVICE: return "CUDA error";
+    case HYDRO_ERR_NOT_FOUND: return "not found";
+    case HYDRO_ERR_INDEX_RANGE: return "face index out of range";
+    case HYDRO_ERR_UNSUPPORTED: return "unsupported";
+    case HYDRO_ERR_MISMATCH: return "body table does not match batch";
+    }
+    return "unknown status";
+}
+
+const char* hydro_last_error(const hydro_ctx* ctx)
+{
+    return ctx ? ctx->err.c_str() : "null context";
+}
+
+hydro_status hydro_create(hydro_ctx** out, const hydro_config* cfg)
+{
+    if (!out) return HYDRO_ERR_INVALID_ARG;
+    *out = nullptr;
+    hydro_config c;
+    if (cfg) c = *cfg;
+    else hydro_config_default(&c);
+    if (c.cut_precision != HYDRO_CUT_FP64 && c.cut_precision != HYDRO_CUT_FP32)
+        return HYDRO_ERR_INVALID_ARG;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return HYDRO_ERR_DEVICE;
+    if (c.device < 0 || c.device >= n) return HYDRO_ERR_INVALID_ARG;
+    if (cudaSetDevice(c.device) != cudaSuccess) return HYDRO_ERR_DEVICE;
+    hydro_ctx* ctx = new (std::nothrow) hydro_ctx();
+    if (!ctx) return HYDRO_ERR_OOM;
+    ctx->device = c.device;
+    ctx->cfg = c;
+    ctx->cfg.tune_cache_path = nullptr;
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete ctx;
+        return HYDRO_ERR_DEVICE;
+    }
+    *out = ctx;
+    return HYDRO_OK;
+}
+
+void hydro_destroy(hydro_ctx* ctx)
+{
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    cudaDeviceSynchronize();
+    for (auto& kv : ctx->single) batch_free(kv.second);
+    for (auto& s : ctx->slabs) cudaFree(s.base);
+    cudaFree(ctx->tiles_d);
+    cudaFree(ctx->wave_d);
+    cudaFree(ctx->small_d);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+hydro_status hydro_mesh_upload(hydro_ctx* ctx, const void* vertex_data, size_t vertex_stride,
+                               uint32_t n_vertices, const uint32_t* face_indices,
+                               uint32_t n_faces, hydro_mesh_id* out_id)
+{
+    if (!ctx) return HYDRO_ERR_INVALID_ARG;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (!vertex_data || !face_indices || !out_id || n_vertices == 0 || n_faces == 0)
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "mesh upload: null pointer or empty mesh");
+    if (vertex_stride < 3 * sizeof(float))
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "mesh upload: vertex stride %zu < 12", vertex_stride);
+    for (size_t i = 0; i < (size_t)n_faces * 3; ++i) {
+        if (face_indices[i] >= n_vertices)
+            return fail(ctx, HYDRO_ERR_INDEX_RANGE, "face %zu index %u >= %u vertices",
+                        i / 3, face_indices[i], n_vertices);
+    }
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, HYDRO_ERR_DEVICE, "cudaSetDevice");
+    const char* vbytes = static_cast<const char*>(vertex_data);
+    auto pos = [&](uint32_t v, float* p) { std::memcpy(p, vbytes + (size_t)v * vertex_stride, 12); };
+
+    // Greedy tiling in face order: a tile closes when it would exceed
+    // kTileFaces faces or kTileVerts distinct vertices.
+    std::vector<int32_t> local(n_vertices, -1);
+    std::vector<uint32_t> tv;              // global ids of the open tile's vertices
+    std::vector<uint16_t> ti;              // local indices of the open tile's faces
+    std::vector<char> host;                // all tile blocks of this mesh
+    struct Pending { size_t offset; uint16_t nv, nf; uint32_t first_face; };
+    std::vector<Pending> pend;
+    uint32_t tile_first_face = 0;
+    auto close_tile = [&](uint32_t next_face) {
+        if (ti.empty()) return;
+        const uint32_t nv = (uint32_t)tv.size(), nf = (uint32_t)(ti.size() / 3);
+        const uint32_t nvp = (nv + 3) & ~3u;
+        size_t bytes = (size_t)nvp * 12 + (size_t)nf * 6;
+        bytes = (bytes + 15) & ~size_t(15);
+        size_t off = host.size();
+        host.resize(off + bytes, 0);
+        float* f = reinterpret_cast<float*>(host.data() + off);
+        for (uint32_t k = 0; k < nv; ++k) {
+            float p[3];
+            pos(tv[k], p);
+            f[k] = p[0];
+            f[nvp + k] = p[1];
+            f[2 * nvp + k] = p[2];
+        }
+        std::memcpy(host.data() + off + (size_t)nvp * 12, ti.data(), ti.size() * 2);
+        pend.push_back(Pending{off, (uint16_t)nv, (uint16_t)nf, tile_first_face});
+        for (uint32_t g : tv) local[g] = -1;
+        tv.clear();
+        ti.clear();
+        tile_first_face = next_face;
+    };
+    for (uint32_t f = 0; f < n_faces; ++f) {
+        const uint32_t* fi = face_indices + 3 * (size_t)f;
+        uint32_t fresh = 0;
+        for (int k = 0; k < 3; ++k) {
+            bool dup = false;
+            for (int j = 0; j < k; ++j) dup |= (fi[j] == fi[k]);
+            if (local[fi[k]] < 0 && !dup) ++fresh;
+        }
+        if (ti.size() / 3 + 1 > (size_t)kTileFaces || tv.size() + fresh > (size_t)kTileVerts)
+            close_tile(f);
+        for (int k = 0; k < 3; ++k) {
+            if (local[fi[k]] < 0) {
+                local[fi[k]] = (int32_t)tv.size();
+                tv.push_back(fi[k]);
+            }
+            ti.push_back((uint16_t)local[fi[k]]);
+        }
+    }
+    close_tile(n_faces);
+
+    char* dev = nullptr;
+    hydro_status st = slab_alloc(ctx, host.size(), &dev);
+    if (st != HYDRO_OK) return st;
+    CK(ctx, cudaMemcpy(dev, host.data(), host.size(), cudaMemcpyHostToDevice));
+    MeshRec m{};
+    m.n_vertices = n_vertices;
+    m.n_faces = n_faces;
+    m.first_tile = (uint32_t)ctx->tiles_h.size();
+    m.n_tiles = (uint32_t)pend.size();
+    for (const Pending& p : pend)
+        ctx->tiles_h.push_back(TileDesc{reinterpret_cast<const float*>(dev + p.offset), p.nv, p.nf, p.first_face});
+    *out_id = (hydro_mesh_id)ctx->meshes.size();
+    ctx->meshes.push_back(m);
+    return HYDRO_OK;
+}
+
+hydro_status hydro_mesh_info(hydro_ctx* ctx, hydro_mesh_id id, uint32_t* nv, uint32_t* nf,
+                             uint32_t* nt)
+{
+    if (!ctx) return HYDRO_ERR_INVALID_ARG;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (id >= ctx->meshes.size()) return fail(ctx, HYDRO_ERR_NOT_FOUND, "unknown mesh %u", id);
+    const MeshRec& m = ctx->meshes[id];
+    if (nv) *nv = m.n_vertices;
+    if (nf) *nf = m.n_faces;
+    if (nt) *nt = m.n_tiles;
+    return HYDRO_OK;
+}
+
+hydro_status hydro_wave_grid_set(hydro_ctx* ctx, const float* data, uint32_t size,
+                                 uint32_t channels, uint32_t n_layers,
+                                 const uint32_t* layer_channel, const float* layer_grid_size)
+{
+    if (!ctx) return HYDRO_ERR_INVALID_ARG;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (!data || size == 0 || channels == 0 || n_layers == 0 || n_layers > HYDRO_MAX_WAVE_LAYERS ||
+        !layer_channel || !layer_grid_size || size > 65536)
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "wave grid: bad arguments");
+    for (uint32_t l = 0; l < n_layers; ++l) {
+        if (layer_channel[l] >= channels || !(layer_grid_size[l] > 0.f))
+            return fail(ctx, HYDRO_ERR_INVALID_ARG, "wave grid: bad layer %u", l);
+    }
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, HYDRO_ERR_DEVICE, "cudaSetDevice");
+    CK(ctx, cudaStreamSynchronize(ctx->stream));
+    CK(ctx, cudaDeviceSynchronize());
+    if (ctx->wave_d) cudaFree(ctx->wave_d);
+    ctx->wave_d = nullptr;
+    const size_t bytes = (size_t)size * size * channels * sizeof(float);
+    CK(ctx, cudaMalloc(&ctx->wave_d, bytes));
+    CK(ctx, cudaMemcpy(ctx->wave_d, data, bytes, cudaMemcpyHostToDevice));
+    ctx->wave_n = size;
+    ctx->wave_channels = channels;
+    ctx->wave_layers = n_layers;
+    for (uint32_t l = 0; l < HYDRO_MAX_WAVE_LAYERS; ++l) {
+        ctx->wave_channel[l] = l < n_layers ? layer_channel[l] : 0;
+        ctx->wave_grid[l] = l < n_layers ? layer_grid_size[l] : 1.f;
+    }
+    return HYDRO_OK;
+}
+
+hydro_status hydro_depth(hydro_ctx* ctx, const hydro_ocean* ocean, const float* xyz, uint32_t n,
+                         float* depth)
+{
+    if (!ctx) return HYDRO_ERR_INVALID_ARG;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (!valid_ocean(ocean) || (!xyz && n) || (!depth && n))
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "depth: bad arguments");
+    if (n == 0) return HYDRO_OK;
+    if (ocean->waves && !ctx->wave_d) return fail(ctx, HYDRO_ERR_INVALID_ARG, "depth: no wave grid");
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, HYDRO_ERR_DEVICE, "cudaSetDevice");
+    hydro_status st = ensure_small(ctx, (size_t)n * 16);
+    if (st != HYDRO_OK) return st;
+    float* dx = static_cast<float*>(ctx->small_d);
+    float* dd = dx + 3 * (size_t)n;
+    CK(ctx, cudaMemcpyAsync(dx, xyz, (size_t)n * 12, cudaMemcpyHostToDevice, ctx->stream));
+    cudaError_t e = launch_depth(make_ocean(ctx, ocean), dx, n, dd, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "depth kernel");
+    CK(ctx, cudaMemcpyAsync(depth, dd, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(ctx, cudaStreamSynchronize(ctx->stream));
+    return HYDRO_OK;
+}
+
+hydro_status hydro_batch_create(hydro_ctx* ctx, const hydro_mesh_id* mesh_of_body,
+                                uint32_t n_bodies, hydro_batch** out)
+{
+    if (!ctx) return HYDRO_ERR_INVALID_ARG;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (!out || !mesh_of_body || n_bodies == 0)
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "batch: null pointer or no bodies");
+    *out = nullptr;
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, HYDRO_ERR_DEVICE, "cudaSetDevice");
+    return batch_build(ctx, mesh_of_body, n_bodies, out);
+}
+
+void hydro_batch_destroy(hydro_batch* b)
+{
+    if (!b) return;
+    std::lock_guard<std::recursive_mutex> lk(b->ctx->mu);
+    cudaSetDevice(b->ctx->device);
+    cudaStreamSynchronize(b->stream);
+    batch_free(b);
+}
+
+hydro_status hydro_batch_compute_device(hydro_batch* b, const hydro_body* d_bodies,
+                                        const hydro_ocean* ocean, const hydro_settings* settings,
+                                        hydro_wrench* d_inout, void* stream)
+{
+    if (!b) return HYDRO_ERR_INVALID_ARG;
+    hydro_ctx* ctx = b->ctx;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (!d_bodies || !d_inout || !settings || !valid_ocean(ocean))
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "batch compute: bad arguments");
+    return batch_launch(b, d_bodies, ocean, settings, d_inout, static_cast<cudaStream_t>(stream), OP_BODY);
+}
+
+hydro_status hydro_batch_compute(hydro_batch* b, const hydro_body* bodies, const hydro_ocean* ocean,
+                                 const hydro_settings* settings, hydro_wrench* inout)
+{
+    if (!b) return HYDRO_ERR_INVALID_ARG;
+    hydro_ctx* ctx = b->ctx;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (!bodies || !inout || !settings || !valid_ocean(ocean))
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "batch compute: bad arguments");
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, HYDRO_ERR_DEVICE, "cudaSetDevice");
+    const size_t nb = (size_t)b->n_bodies;
+    if (!b->bodies_d) CK(ctx, cudaMalloc(&b->bodies_d, nb * sizeof(hydro_body)));
+    if (!b->io_d) CK(ctx, cudaMalloc(&b->io_d, nb * sizeof(hydro_wrench)));
+    CK(ctx, cudaMemcpyAsync(b->bodies_d, bodies, nb * sizeof(hydro_body), cudaMemcpyHostToDevice, b->stream));
+    CK(ctx, cudaMemcpyAsync(b->io_d, inout, nb * sizeof(hydro_wrench), cudaMemcpyHostToDevice, b->stream));
+    hydro_status st = batch_launch(b, b->bodies_d, ocean, settings, b->io_d, b->stream, OP_BODY);
+    if (st != HYDRO_OK) return st;
+    CK(ctx, cudaMemcpyAsync(inout, b->io_d, nb * sizeof(hydro_wrench), cudaMemcpyDeviceToHost, b->stream));
+    CK(ctx, cudaStreamSynchronize(b->stream));
+    return HYDRO_OK;
+}
+
+uint32_t hydro_batch_last_launches(const hydro_batch* b) { return b ? b->last_launches : 0u; }
+
+hydro_status hydro_body_forces(hydro_ctx* ctx, const hydro_body* body, const hydro_ocean* ocean,
+                               const hydro_settings* settings, hydro_wrench* io)
+{
+    if (!ctx) return HYDRO_ERR_INVALID_ARG;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (!body || !settings || !io || !valid_ocean(ocean))
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "body forces: bad arguments");
+    if (body->mesh != HYDRO_NO_MESH && body->mesh >= ctx->meshes.size())
+        return fail(ctx, HYDRO_ERR_NOT_FOUND, "unknown mesh %u", body->mesh);
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, HYDRO_ERR_DEVICE, "cudaSetDevice");
+    return run_single(ctx, *body, ocean, settings, *io, OP_BODY);
+}
+
+hydro_status hydro_surface_forces(hydro_ctx* ctx, const hydro_settings* settings, hydro_mesh_id mesh,
+                                  const hydro_ocean* ocean, const hydro_transform* T_CG,
+                                  const hydro_transform* T_C, const double v[3],
+                                  const double omega[3], double Fb[3], double Tb[3],
+                                  double Fdq[3], double Tdq[3], double Fdf[3], double Tdf[3],
+                                  double* Swet, double* Vsub)
+{
+    if (!ctx) return HYDRO_ERR_INVALID_ARG;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (!settings || !valid_ocean(ocean) || !T_CG || !T_C || !v || !omega || !Fb || !Tb || !Fdq ||
+        !Tdq || !Fdf || !Tdf || !Swet || !Vsub)
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "surface forces: null argument");
+    if (mesh != HYDRO_NO_MESH && mesh >= ctx->meshes.size())
+        return fail(ctx, HYDRO_ERR_NOT_FOUND, "unknown mesh %u", mesh);
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, HYDRO_ERR_DEVICE, "cudaSetDevice");
+    hydro_body b{};
+    b.T_CG = *T_CG;
+    b.T_C = *T_C;
+    copy3(b.v, v);
+    copy3(b.omega, omega);
+    b.mesh = mesh;
+    b.mode = HYDRO_MODE_SUBMERGED;
+    b.buoyancy = 1;
+    hydro_wrench w{};
+    copy3(w.Fb, Fb); copy3(w.Tb, Tb); copy3(w.Fdq, Fdq); copy3(w.Tdq, Tdq);
+    copy3(w.Fdf, Fdf); copy3(w.Tdf, Tdf);
+    w.Swet = *Swet;
+    w.Vsub = *Vsub;
+    hydro_status st = run_single(ctx, b, ocean, settings, w, OP_SURFACE);
+    if (st != HYDRO_OK) return st;
+    copy3(Fb, w.Fb); copy3(Tb, w.Tb); copy3(Fdq, w.Fdq); copy3(Tdq, w.Tdq);
+    copy3(Fdf, w.Fdf); copy3(Tdf, w.Tdf);
+    *Swet = w.Swet;
+    *Vsub = w.Vsub;
+    return HYDRO_OK;
+}
+
+hydro_status hydro_submerged_forces(hydro_ctx* ctx, hydro_mesh_id mesh, const hydro_ocean* ocean,
+                                    const hydro_transform* T_CG, const hydro_transform* T_C,
+                                    const double v[3], const double omega[3], double Fdq[3],
+                                    double Tdq[3], double Fdf[3], double Tdf[3])
+{
+    if (!ctx) return HYDRO_ERR_INVALID_ARG;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (!valid_ocean(ocean) || !T_CG || !T_C || !v || !omega || !Fdq || !Tdq || !Fdf || !Tdf)
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "submerged forces: null argument");
+    if (mesh != HYDRO_NO_MESH && mesh >= ctx->meshes.size())
+        return fail(ctx, HYDRO_ERR_NOT_FOUND, "unknown mesh %u", mesh);
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, HYDRO_ERR_DEVICE, "cudaSetDevice");
+    hydro_body b{};
+    b.T_CG = *T_CG;
+    b.T_C = *T_C;
+    copy3(b.v, v);
+    copy3(b.omega, omega);
+    b.mesh = mesh;
+    b.mode = HYDRO_MODE_SUBMERGED;
+    hydro_wrench w{};
+    copy3(w.Fdq, Fdq); copy3(w.Tdq, Tdq); copy3(w.Fdf, Fdf); copy3(w.Tdf, Tdf);
+    hydro_settings s{1, 0};
+    hydro_status st = run_single(ctx, b, ocean, &s, w, OP_SUBMERGED);
+    if (st != HYDRO_OK) return st;
+    copy3(Fdq, w.Fdq); copy3(Tdq, w.Tdq); copy3(Fdf, w.Fdf); copy3(Tdf, w.Tdf);
+    return HYDRO_OK;
+}
+
+hydro_status hydro_correct_forces(hydro_ctx* ctx, const hydro_ocean* ocean, double Fdq[3],
+                                  double Tdq[3], double Fdf[3], double Tdf[3], const double Cd[3],
+                                  const double Cf[3], const double R_O[9])
+{
+    if (!ctx) return HYDRO_ERR_INVALID_ARG;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (!valid_ocean(ocean) || !Fdq || !Tdq || !Fdf || !Tdf || !Cd || !Cf || !R_O)
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "correct forces: null argument");
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, HYDRO_ERR_DEVICE, "cudaSetDevice");
+    hydro_status st = ensure_small(ctx, 64 * sizeof(double));
+    if (st != HYDRO_OK) return st;
+    double h[27];
+    copy3(h, Fdq); copy3(h + 3, Tdq); copy3(h + 6, Fdf); copy3(h + 9, Tdf);
+    copy3(h + 12, Cd); copy3(h + 15, Cf);
+    for (int i = 0; i < 9; ++i) h[18 + i] = R_O[i];
+    double* d = static_cast<double*>(ctx->small_d);
+    CK(ctx, cudaMemcpyAsync(d, h, sizeof(h), cudaMemcpyHostToDevice, ctx->stream));
+    cudaError_t e = launch_correct(ocean->density, d, d + 12, d + 15, d + 18, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "correct kernel");
+    CK(ctx, cudaMemcpyAsync(h, d, 12 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(ctx, cudaStreamSynchronize(ctx->stream));
+    copy3(Fdq, h); copy3(Tdq, h + 3); copy3(Fdf, h + 6); copy3(Tdf, h + 9);
+    return HYDRO_OK;
+}
+
+hydro_status hydro_fluid_position(hydro_ctx* ctx, const hydro_ocean* ocean, const double aabb_min[3],
+                                  const double aabb_max[3], int32_t* position)
+{
+    if (!ctx) return HYDRO_ERR_INVALID_ARG;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (!valid_ocean(ocean) || !aabb_min || !aabb_max || !position)
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "fluid position: null argument");
+    if (ocean->waves && !ctx->wave_d) return fail(ctx, HYDRO_ERR_INVALID_ARG, "no wave grid");
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, HYDRO_ERR_DEVICE, "cudaSetDevice");
+    hydro_status st = ensure_small(ctx, 64);
+    if (st != HYDRO_OK) return st;
+    double h[6];
+    copy3(h, aabb_min);
+    copy3(h + 3, aabb_max);
+    double* d = static_cast<double*>(ctx->small_d);
+    int* r = reinterpret_cast<int*>(d + 6);
+    CK(ctx, cudaMemcpyAsync(d, h, sizeof(h), cudaMemcpyHostToDevice, ctx->stream));
+    cudaError_t e = launch_fluid_position(make_ocean(ctx, ocean), d, r, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "fluid position kernel");
+    int32_t out = 0;
+    CK(ctx, cudaMemcpyAsync(&out, r, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(ctx, cudaStreamSynchronize(ctx->stream));
+    *position = out;
+    return HYDRO_OK;
+}
+
+// Per-face surface-loop terms of one body (n_faces * 23 floats, host).
+hydro_status hydro_debug_face_terms(hydro_ctx* ctx, const hydro_body* body, const hydro_ocean* ocean,
+                                    const hydro_settings* settings, float* out)
+{
+    if (!ctx) return HYDRO_ERR_INVALID_ARG;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (!body || !valid_ocean(ocean) || !settings || !out || body->mesh >= ctx->meshes.size())
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "face terms: bad arguments");
+    if (ocean->waves && !ctx->wave_d) return fail(ctx, HYDRO_ERR_INVALID_ARG, "no wave grid");
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, HYDRO_ERR_DEVICE, "cudaSetDevice");
+    hydro_status st = sync_tiles(ctx);
+    if (st != HYDRO_OK) return st;
+    const MeshRec& m = ctx->meshes[body->mesh];
+    const size_t terms = (size_t)m.n_faces * kQ * sizeof(float);
+    st = ensure_small(ctx, terms + sizeof(hydro_body) + 256);
+    if (st != HYDRO_OK) return st;
+    char* base = static_cast<char*>(ctx->small_d);
+    hydro_body* db = reinterpret_cast<hydro_body*>(base);
+    float* dout = reinterpret_cast<float*>(base + 256 * ((sizeof(hydro_body) + 255) / 256));
+    CK(ctx, cudaMemcpyAsync(db, body, sizeof(hydro_body), cudaMemcpyHostToDevice, ctx->stream));
+    SettingsDev sd{settings->damping_forces ? 1 : 0, settings->realistic_buoyancy ? 1 : 0};
+    cudaError_t e = launch_face_terms(ctx->tiles_d, m.first_tile, m.n_tiles, db, make_ocean(ctx, ocean), sd,
+                                      ctx->cfg.cut_precision == HYDRO_CUT_FP64, dout, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "face terms kernel");
+    CK(ctx, cudaMemcpyAsync(out, dout, terms, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(ctx, cudaStreamSynchronize(ctx->stream));
+    return HYDRO_OK;
+}
+
+}  // extern "C"

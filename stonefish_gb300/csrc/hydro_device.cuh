@@ -1,0 +1,439 @@
+// hydro_device.cuh -- device-side arithmetic of the hydrodynamic wrench path.
+//
+// Every per-face step restates Stonefish's SolidEntity hydrodynamics
+// (Library/src/entities/SolidEntity.cpp:1289-1797) in FP32 with the
+// operation order of the glm calls it uses (glm >= 0.9.9):
+//   dot(a,b)   = (a.x*b.x + a.y*b.y) + a.z*b.z
+//   cross(a,b) = (a.y*b.z - b.y*a.z, a.z*b.x - b.z*a.x, a.x*b.y - b.x*a.y)
+//   M*vec4(p,1) = (c0*x + c1*y) + (c2*z + c3)
+// The library is compiled with -fmad=false and IEEE division/square root, so
+// each face's contribution is bit-identical to a CPU evaluation in the same
+// order; the boundary and finalisation are FP64 as in the reference.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/stonefish_hydro.h"
+
+namespace sfh {
+
+// ------------------------------------------------------------ constants
+constexpr int kBlock = 256;          // threads per CTA
+constexpr int kWarps = kBlock / 32;
+constexpr int kTileFaces = 512;      // max faces per tile
+constexpr int kTileVerts = 512;      // max distinct vertices per tile
+constexpr int kQ = 23;               // accumulated quantities per body
+constexpr int kPartialStride = 24;   // doubles per chunk partial (23 + status)
+constexpr int kFlushFaces = 8;       // faces a thread sums in FP32 before a flush
+
+// indices of the accumulated quantities
+enum : int {
+    Q_FB = 0, Q_TB = 3, Q_FDQ = 6, Q_TDQ = 9, Q_FDF = 12, Q_TDF = 15,
+    Q_SWET = 18, Q_V6 = 19, Q_CB = 20
+};
+
+// loop kinds of a body in one launch
+enum : int { LOOP_NONE = 0, LOOP_SURFACE = 1, LOOP_SUBMERGED = 2 };
+// launch operations
+enum : int { OP_BODY = 0, OP_SURFACE = 1, OP_SUBMERGED = 2 };
+
+// ------------------------------------------------------------- data layout
+// One tile of a mesh: nv vertices stored as x[nvp], y[nvp], z[nvp] floats
+// (nvp = nv rounded up to 4) followed by 3*nf uint16 local indices, padded to
+// 16 bytes; `first_face` is the tile's first face in the uploaded order.
+struct TileDesc {
+    const float* block;
+    uint16_t nv;
+    uint16_t nf;
+    uint32_t first_face;
+};
+
+// One work item: tiles [first_tile, first_tile + n_tiles) of one body.
+struct ChunkDesc {
+    uint32_t body;
+    uint32_t first_tile;
+    uint32_t n_tiles;
+    uint32_t chunk_in_body;
+};
+
+// Per body of a batch.
+struct BodyInfo {
+    uint32_t first_chunk;
+    uint32_t n_chunks;
+    uint32_t mesh;       // mesh the batch was built with (HYDRO_NO_MESH = null)
+    uint32_t n_faces;
+};
+
+// Ocean as the kernels see it (kernel parameter, by value).
+struct OceanDev {
+    double density;
+    double gravity;
+    int waves;
+    int currents_enabled;
+    int n_currents;
+    int field_currents;          // 1 if an enabled JET/PIPE current exists
+    float U[3];                  // (float) of the FP64 sum of uniform currents
+    const float* wave_data;
+    uint32_t wave_n;
+    uint32_t wave_channels;
+    uint32_t wave_layers;
+    uint32_t wave_channel[HYDRO_MAX_WAVE_LAYERS];
+    float wave_grid[HYDRO_MAX_WAVE_LAYERS];
+    hydro_current currents[HYDRO_MAX_CURRENTS];
+};
+
+struct SettingsDev {
+    int damping;
+    int buoyancy;
+};
+
+// ------------------------------------------------------------ FP32 vectors
+struct v3 { float x, y, z; };
+
+__device__ __forceinline__ v3 mk(float x, float y, float z) { v3 r; r.x = x; r.y = y; r.z = z; return r; }
+__device__ __forceinline__ v3 add(v3 a, v3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ v3 sub(v3 a, v3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ v3 mul(v3 a, float s) { return mk(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ v3 dvs(v3 a, float s) { return mk(a.x / s, a.y / s, a.z / s); }
+__device__ __forceinline__ v3 neg(v3 a) { return mk(-a.x, -a.y, -a.z); }
+__device__ __forceinline__ float dot(v3 a, v3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ v3 cross(v3 a, v3 b)
+{
+    return mk(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);
+}
+
+// Per-body FP32 parameters (glMatrixFromTransform / glVectorFromVector casts,
+// Library/src/graphics/OpenGLDataStructs.cpp:148-171).
+struct BodyParams {
+    float TC[12];     // rows of T_C: R[r][0..2], origin[r]
+    v3 p;             // (float) T_CG origin
+    v3 p0;            // (p.x, p.y, 0)
+    v3 v;
+    v3 omega;
+    int loop;         // LOOP_*
+    int buoyancy;     // reallisticBuoyancy for this body
+    int damping;
+    int position;     // BodyFluidPosition or HYDRO_SKIPPED
+};
+
+__device__ __forceinline__ v3 xform(const float* M, float x, float y, float z)
+{
+    v3 r;
+    r.x = (M[0] * x + M[1] * y) + (M[2] * z + M[3]);
+    r.y = (M[4] * x + M[5] * y) + (M[6] * z + M[7]);
+    r.z = (M[8] * x + M[9] * y) + (M[10] * z + M[11]);
+    return r;
+}
+
+// ------------------------------------------------------------- wave height
+__device__ __forceinline__ float fracf_(float x) { return x - truncf(x); }
+
+// OpenGLRealOcean::ComputeInterpolatedWaveData (OpenGLRealOcean.cpp:282-319),
+// texel-centred periodic bilinear; the linear texel index wraps modulo N*N
+// where the reference would read texel N of a row.
+__device__ __forceinline__ float wave_interp(const OceanDev& o, float x, float y, uint32_t ch)
+{
+    const uint32_t N = o.wave_n;
+    const float Nf = (float)N;
+    const float half = 0.5f / Nf;
+    float i0f = fracf_(x - half);
+    float j0f = fracf_(y - half);
+    if (i0f < 0.f) i0f = 1.f - fabsf(i0f);
+    if (j0f < 0.f) j0f = 1.f - fabsf(j0f);
+    int i0 = (int)truncf(i0f * Nf);
+    int j0 = (int)truncf(j0f * Nf);
+    float i1f = fracf_(x + half);
+    float j1f = fracf_(y + half);
+    if (i1f < 0.f) i1f = 1.f - fabsf(i1f);
+    if (j1f < 0.f) j1f = 1.f - fabsf(j1f);
+    int i1 = (int)truncf(i1f * Nf);
+    int j1 = (int)truncf(j1f * Nf);
+    float alpha = fracf_(i0f * Nf);
+    float beta = fracf_(j0f * Nf);
+    const uint64_t NN = (uint64_t)N * N;
+    uint64_t l0 = (uint64_t)j0 * N + (uint64_t)i0; if (l0 >= NN) l0 -= NN;
+    uint64_t l1 = (uint64_t)j0 * N + (uint64_t)i1; if (l1 >= NN) l1 -= NN;
+    uint64_t l2 = (uint64_t)j1 * N + (uint64_t)i0; if (l2 >= NN) l2 -= NN;
+    uint64_t l3 = (uint64_t)j1 * N + (uint64_t)i1; if (l3 >= NN) l3 -= NN;
+    const float* d = o.wave_data;
+    const uint32_t C = o.wave_channels;
+    float t0 = __ldg(d + l0 * C + ch);
+    float t1 = __ldg(d + l1 * C + ch);
+    float t2 = __ldg(d + l2 * C + ch);
+    float t3 = __ldg(d + l3 * C + ch);
+    return (1.f - alpha) * (1.f - beta) * t0 + alpha * (1.f - beta) * t1
+         + (1.f - alpha) * beta * t2 + alpha * beta * t3;
+}
+
+// OpenGLRealOcean::ComputeWaveHeight (:321-331)
+__device__ __forceinline__ float wave_height(const OceanDev& o, float x, float y)
+{
+    float z = 0.f;
+    if (o.wave_data == nullptr) return z;
+    for (uint32_t l = 0; l < o.wave_layers; ++l) {
+        float gs = o.wave_grid[l];
+        z -= wave_interp(o, x / gs, y / gs, o.wave_channel[l]);
+    }
+    return z;
+}
+
+// Ocean::GetDepth(glm::vec3) (Ocean.cpp:149-168)
+__device__ __forceinline__ float depth_at(const OceanDev& o, float x, float y, float z)
+{
+    if (o.waves) return z - wave_height(o, x, y);
+    return z;
+}
+
+// ---------------------------------------------------------------- currents
+__device__ __forceinline__ double bdot(const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+__device__ __forceinline__ void bcross(const double* a, const double* b, double* r)
+{
+    double x = a[1] * b[2] - a[2] * b[1];
+    double y = a[2] * b[0] - a[0] * b[2];
+    double z = a[0] * b[1] - a[1] * b[0];
+    r[0] = x; r[1] = y; r[2] = z;
+}
+
+// Jet::GetVelocityAtPoint (Jet.cpp:59-80), FP64
+__device__ inline void jet_velocity(const hydro_current& c, const double* p, double* out)
+{
+    double cp[3] = {p[0] - c.point[0], p[1] - c.point[1], p[2] - c.point[2]};
+    double x[3];
+    bcross(cp, c.dir, x);
+    double d = sqrt(bdot(x, x));
+    double t = bdot(cp, c.dir);
+    out[0] = out[1] = out[2] = 0.0;
+    if (t < 0.0) return;
+    double r_ = 1.0 / 5.0 * (t + 5.0 * c.radius);
+    if (d >= r_) return;
+    double s = 10.0 * c.radius / (t + 5.0 * c.radius) * c.speed;
+    double f = exp(-50.0 * d * d / (t * t));
+    out[0] = (c.dir[0] * s) * f; out[1] = (c.dir[1] * s) * f; out[2] = (c.dir[2] * s) * f;
+}
+
+// Pipe::GetVelocityAtPoint (Pipe.cpp:57-79), FP64
+__device__ inline void pipe_velocity(const hydro_current& c, const double* p, double* out)
+{
+    double pp[3] = {p[0] - c.point[0], p[1] - c.point[1], p[2] - c.point[2]};
+    double x[3];
+    bcross(pp, c.dir, x);
+    double d = sqrt(bdot(x, x));
+    double t = bdot(pp, c.dir);
+    out[0] = out[1] = out[2] = 0.0;
+    if (t < 0.0 || t > c.length) return;
+    double r = c.radius + (c.radius2 - c.radius) * t / c.length;
+    if (d >= r) return;
+    double s = c.radius / r * c.speed;
+    double f = pow(1.0 - d / r, c.gamma);
+    out[0] = (c.dir[0] * s) * f; out[1] = (c.dir[1] * s) * f; out[2] = (c.dir[2] * s) * f;
+}
+
+// Ocean::GetFluidVelocity(glm::vec3) (Ocean.cpp:183-201): FP64 sum of the
+// enabled currents, cast to float.  Without position-dependent currents the
+// value is the same everywhere and was precomputed on the host.
+__device__ __forceinline__ v3 fluid_velocity(const OceanDev& o, v3 pt)
+{
+    if (!o.field_currents) return mk(o.U[0], o.U[1], o.U[2]);
+    double p[3] = {(double)pt.x, (double)pt.y, (double)pt.z};
+    double fv[3] = {0.0, 0.0, 0.0};
+    for (int i = 0; i < o.n_currents; ++i) {
+        const hydro_current& c = o.currents[i];
+        if (!c.enabled) continue;
+        double u[3] = {0.0, 0.0, 0.0};
+        if (c.type == HYDRO_CURRENT_UNIFORM) { u[0] = c.vel[0]; u[1] = c.vel[1]; u[2] = c.vel[2]; }
+        else if (c.type == HYDRO_CURRENT_JET) jet_velocity(c, p, u);
+        else if (c.type == HYDRO_CURRENT_PIPE) pipe_velocity(c, p, u);
+        fv[0] += u[0]; fv[1] += u[1]; fv[2] += u[2];
+    }
+    return mk((float)fv[0], (float)fv[1], (float)fv[2]);
+}
+
+// ------------------------------------------------------- per-face terms
+// Running FP32 sums of one thread (or the terms of one face).
+struct Acc {
+    float q[kQ];
+};
+
+__device__ __forceinline__ void acc_add3(Acc& a, int k, v3 v)
+{
+    a.q[k] += v.x; a.q[k + 1] += v.y; a.q[k + 2] += v.z;
+}
+
+// Cut point pa + (pb - pa) * (da / (|db| + da)) of the six clip cases
+// (SolidEntity.cpp:1364-1617), FP64 interpolation rounded once when CUT64.
+template <bool CUT64>
+__device__ __forceinline__ v3 cut(v3 pa, v3 pb, float da, float db)
+{
+    if (CUT64) {
+        double t = (double)da / (fabs((double)db) + (double)da);
+        v3 r;
+        r.x = (float)((double)pa.x + ((double)pb.x - (double)pa.x) * t);
+        r.y = (float)((double)pa.y + ((double)pb.y - (double)pa.y) * t);
+        r.z = (float)((double)pa.z + ((double)pb.z - (double)pa.z) * t);
+        return r;
+    }
+    return add(pa, mul(sub(pb, pa), da / (fabsf(db) + da)));
+}
+
+// Volume properties of one fan tetra (e.g. :1372-1378)
+__device__ __forceinline__ void tetra(Acc& a, v3 x, v3 y, v3 z)
+{
+    v3 cg = dvs(add(add(x, y), z), 4.f);
+    float v6 = dot(x, cross(y, z));
+    acc_add3(a, Q_CB, mul(cg, v6));
+    a.q[Q_V6] += v6;
+}
+
+// Damping of one face (:1661-1683 and :1778-1789)
+__device__ __forceinline__ void damping(const OceanDev& o, const BodyParams& B, Acc& a,
+                                        v3 fc, v3 fn1, float A)
+{
+    v3 r = sub(fc, B.p);
+    v3 vc = sub(fluid_velocity(o, fc), add(B.v, cross(B.omega, r)));
+    float vc_n = dot(vc, fn1);
+    v3 vn = mk(vc_n * fn1.x, vc_n * fn1.y, vc_n * fn1.z);
+    v3 vt = sub(vc, vn);
+    if (vc_n < -1e-12f) {
+        float vmag2 = dot(vc, vc);
+        v3 q = mul(mul(mul(vc, sqrtf(vmag2)), -vc_n), A);
+        acc_add3(a, Q_FDQ, q);
+        acc_add3(a, Q_TDQ, cross(r, q));
+    }
+    float vt2 = dot(vt, vt);
+    if (vt2 > 1e-9f) {
+        v3 s = mul(vt, A);
+        acc_add3(a, Q_FDF, s);
+        acc_add3(a, Q_TDF, cross(r, s));
+    }
+}
+
+// Triangle properties after clipping; returns false for a degenerate face.
+__device__ __forceinline__ bool tri_props(v3 p1, v3 p2, v3 p3, v3& fc, v3& fn1, float& A)
+{
+    v3 fv1 = sub(p2, p1);
+    v3 fv2 = sub(p3, p1);
+    fc = dvs(add(add(p1, p2), p3), 3.f);
+    v3 fn = cross(fv1, fv2);
+    float len = dot(fn, fn);
+    if (len < 1e-12f) return false;
+    len = sqrtf(len);
+    fn1 = dvs(fn, len);
+    A = len / 2.f;
+    return true;
+}
+
+// The part of a surface-loop face after its polygon is known (:1650-1686).
+__device__ __forceinline__ void face_forces(const OceanDev& o, const BodyParams& B, Acc& a,
+                                            v3 fc, v3 fn1, float A)
+{
+    if (B.buoyancy && o.waves) {
+        float depthc = depth_at(o, fc.x, fc.y, fc.z);
+        v3 Fbi = mul(mul(neg(fn1), A), depthc);
+        acc_add3(a, Q_FB, Fbi);
+        acc_add3(a, Q_TB, cross(sub(fc, B.p), Fbi));
+    }
+    if (B.damping) damping(o, B, a, fc, fn1, A);
+    a.q[Q_SWET] += A;
+}
+
+// One face straddling the surface: the six mixed clip cases (:1360-1617).
+template <bool CUT64>
+__device__ __forceinline__ void face_cut(const OceanDev& o, const BodyParams& B, Acc& a,
+                                      v3 p1, v3 p2, v3 p3, float d0, float d1, float d2)
+{
+    v3 p4 = mk(0.f, 0.f, 0.f);
+    bool quad = false;
+    int kind = 0;
+    if (d0 < 0.f) {
+        if (d1 < 0.f) {
+            p1 = cut<CUT64>(p3, p1, d2, d0);
+            p2 = cut<CUT64>(p3, p2, d2, d1);
+        } else if (d2 < 0.f) {
+            p1 = cut<CUT64>(p2, p1, d1, d0);
+            p3 = cut<CUT64>(p2, p3, d1, d2);
+        } else {
+            p4 = cut<CUT64>(p3, p1, d2, d0);
+            p1 = cut<CUT64>(p2, p1, d1, d0);
+            quad = true; kind = 0;
+        }
+    } else if (d1 < 0.f) {
+        if (d2 < 0.f) {
+            p2 = cut<CUT64>(p1, p2, d0, d1);
+            p3 = cut<CUT64>(p1, p3, d0, d2);
+        } else {
+            p4 = cut<CUT64>(p3, p2, d2, d1);
+            p2 = cut<CUT64>(p1, p2, d0, d1);
+            quad = true; kind = 1;
+        }
+    } else {
+        p4 = cut<CUT64>(p1, p3, d0, d2);
+        p3 = cut<CUT64>(p2, p3, d1, d2);
+        quad = true; kind = 0;
+    }
+    const v3 p01 = sub(p1, B.p0);
+    const v3 p02 = sub(p2, B.p0);
+    const v3 p03 = sub(p3, B.p0);
+    tetra(a, p01, p02, p03);
+    v3 fc, fn1;
+    float A;
+    if (!quad) {
+        if (!tri_props(p1, p2, p3, fc, fn1, A)) return;
+    } else {
+        v3 p04 = sub(p4, B.p0);
+        v3 fv1 = sub(p2, p1);
+        v3 fv2;
+        if (kind == 0) {
+            tetra(a, p01, p03, p04);
+            fv2 = sub(p4, p1);
+        } else {
+            tetra(a, p02, p04, p03);
+            fv2 = sub(p3, p1);
+        }
+        v3 fv3 = sub(p2, p3);
+        v3 fv4 = sub(p4, p3);
+        fc = dvs(add(add(add(p1, p2), p3), p4), 4.f);
+        v3 fn = cross(fv1, fv2);
+        float len = dot(fn, fn);
+        if (len < 1e-12f) return;
+        len = sqrtf(len);
+        fn1 = dvs(fn, len);
+        v3 c2 = cross(fv3, fv4);
+        A = (len + sqrtf(dot(c2, c2))) / 2.f;
+    }
+    face_forces(o, B, a, fc, fn1, A);
+}
+
+// One face of the surface loop (:1337-1687) given transformed vertices
+// (x, y, z, depth).
+template <bool CUT64>
+__device__ __forceinline__ void face_surface(const OceanDev& o, const BodyParams& B, Acc& a,
+                                             float4 q1, float4 q2, float4 q3)
+{
+    const float d0 = q1.w, d1 = q2.w, d2 = q3.w;
+    if (d0 < 0.f && d1 < 0.f && d2 < 0.f) return;
+    v3 p1 = mk(q1.x, q1.y, q1.z), p2 = mk(q2.x, q2.y, q2.z), p3 = mk(q3.x, q3.y, q3.z);
+    if (d0 < 0.f || d1 < 0.f || d2 < 0.f) {
+        face_cut<CUT64>(o, B, a, p1, p2, p3, d0, d1, d2);
+        return;
+    }
+    // all submerged (:1618-1647)
+    tetra(a, sub(p1, B.p0), sub(p2, B.p0), sub(p3, B.p0));
+    v3 fc, fn1;
+    float A;
+    if (!tri_props(p1, p2, p3, fc, fn1, A)) return;
+    face_forces(o, B, a, fc, fn1, A);
+}
+
+// One face of the submerged loop (:1748-1789)
+__device__ __forceinline__ void face_submerged(const OceanDev& o, const BodyParams& B, Acc& a,
+                                               float4 q1, float4 q2, float4 q3)
+{
+    v3 p1 = mk(q1.x, q1.y, q1.z), p2 = mk(q2.x, q2.y, q2.z), p3 = mk(q3.x, q3.y, q3.z);
+    v3 fc, fn1;
+    float A;
+    if (!tri_props(p1, p2, p3, fc, fn1, A)) return;
+    damping(o, B, a, fc, fn1, A);
+}
+
+}  // namespace sfh

@@ -1,0 +1,226 @@
+"""Python front end of the GB300 hydrodynamics library (C ABI via ctypes).
+
+The method names mirror the reference's call surface:
+
+* ``surface_forces``   -- SolidEntity::ComputeHydrodynamicForcesSurface
+  (Library/src/entities/SolidEntity.cpp:1289-1721)
+* ``submerged_forces`` -- SolidEntity::ComputeHydrodynamicForcesSubmerged (:1723-1797)
+* ``correct_forces``   -- SolidEntity::CorrectHydrodynamicForces (:1263-1287)
+* ``fluid_position``   -- SolidEntity::CheckBodyFluidPosition (:1239-1261)
+* ``body_forces``      -- SolidEntity::ComputeHydrodynamicForces (:1799-1850)
+* ``Batch.compute``    -- the per-body loop of the hydrodynamics block of
+  SimulationManager::SimulationTickCallback (SimulationManager.cpp:1620-1655)
+
+Every call runs on the GPU; there is no CPU path.  A missing library raises
+ImportError, a failing call raises ``abi.HydroError``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+
+
+def _check(lib, ctx, status: int) -> None:
+    if status != abi.HYDRO_OK:
+        msg = lib.hydro_last_error(ctx).decode(errors="replace") if ctx else ""
+        raise abi.HydroError(status, msg or lib.hydro_status_string(status).decode())
+
+
+def transform(R, origin) -> abi.Transform:
+    t = abi.Transform()
+    R = np.asarray(R, dtype=np.float64).reshape(9)
+    for i in range(9):
+        t.basis[i] = R[i]
+    for i in range(3):
+        t.origin[i] = float(origin[i])
+    return t
+
+
+def _d3(x):
+    a = np.ascontiguousarray(np.asarray(x, dtype=np.float64).reshape(3))
+    return a, a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class HydroContext:
+    """Owns a hydro_ctx: device meshes, the wave grid and small buffers."""
+
+    def __init__(self, device: int = 0, cut_precision: int = abi.CUT_FP64,
+                 tile_faces: int = 0, lib_path: str | None = None):
+        self.lib = abi.load_library(lib_path)
+        lib = self.lib
+        if not hasattr(lib, "_debug_declared"):
+            lib.hydro_debug_face_terms.restype = C.c_int32
+            lib.hydro_debug_face_terms.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(abi.Ocean),
+                                                   C.POINTER(abi.Settings), C.c_void_p]
+            lib._debug_declared = True
+        cfg = abi.Config()
+        lib.hydro_config_default(C.byref(cfg))
+        cfg.device = device
+        cfg.cut_precision = cut_precision
+        cfg.tile_faces = tile_faces
+        h = C.c_void_p()
+        st = lib.hydro_create(C.byref(h), C.byref(cfg))
+        if st != abi.HYDRO_OK:
+            raise abi.HydroError(st, "hydro_create: " + lib.hydro_status_string(st).decode())
+        self.ctx = h
+        self.mesh_faces: dict[int, int] = {}
+
+    def close(self) -> None:
+        if self.ctx:
+            self.lib.hydro_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, st: int) -> None:
+        _check(self.lib, self.ctx, st)
+
+    # --------------------------------------------------------------- meshes
+    def upload_mesh(self, xyz: np.ndarray, faces: np.ndarray, stride: int | None = None) -> int:
+        """Uploads a physics mesh.  ``xyz`` may be packed (V,3) float32 or the
+        reference's interleaved vertex array with ``stride`` bytes per vertex."""
+        xyz = np.ascontiguousarray(xyz)
+        faces = np.ascontiguousarray(faces, dtype=np.uint32)
+        if stride is None:
+            xyz = np.ascontiguousarray(xyz, dtype=np.float32).reshape(-1, 3)
+            stride = 12
+            nv = xyz.shape[0]
+        else:
+            nv = xyz.nbytes // stride
+        mid = C.c_uint32()
+        self._ck(self.lib.hydro_mesh_upload(self.ctx, xyz.ctypes.data, stride, nv,
+                                            faces.ctypes.data, faces.size // 3, C.byref(mid)))
+        self.mesh_faces[int(mid.value)] = faces.size // 3
+        return int(mid.value)
+
+    def mesh_info(self, mesh: int) -> tuple[int, int, int]:
+        nv, nf, nt = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        self._ck(self.lib.hydro_mesh_info(self.ctx, mesh, C.byref(nv), C.byref(nf), C.byref(nt)))
+        return nv.value, nf.value, nt.value
+
+    def set_wave_grid(self, waves: dict) -> None:
+        data = np.ascontiguousarray(waves["data"], dtype=np.float32)
+        n = data.shape[0]
+        ch = 1 if data.ndim == 2 else data.shape[2]
+        layers = waves["layers"]
+        lc = np.array([c for c, _ in layers], dtype=np.uint32)
+        gs = np.array([g for _, g in layers], dtype=np.float32)
+        self._ck(self.lib.hydro_wave_grid_set(self.ctx, data.ctypes.data, n, ch, len(layers),
+                                              lc.ctypes.data, gs.ctypes.data))
+
+    # ---------------------------------------------------------- entry points
+    def depth(self, ocean: abi.Ocean, xyz: np.ndarray) -> np.ndarray:
+        xyz = np.ascontiguousarray(xyz, dtype=np.float32).reshape(-1, 3)
+        out = np.empty(xyz.shape[0], dtype=np.float32)
+        self._ck(self.lib.hydro_depth(self.ctx, C.byref(ocean), xyz.ctypes.data, xyz.shape[0],
+                                      out.ctypes.data))
+        return out
+
+    def fluid_position(self, ocean: abi.Ocean, aabb_min, aabb_max) -> int:
+        a, pa = _d3(aabb_min)
+        b, pb = _d3(aabb_max)
+        r = C.c_int32()
+        self._ck(self.lib.hydro_fluid_position(self.ctx, C.byref(ocean), pa, pb, C.byref(r)))
+        return int(r.value)
+
+    def body_forces(self, body: np.ndarray, ocean: abi.Ocean, settings: abi.Settings,
+                    io: np.ndarray) -> np.ndarray:
+        """SolidEntity::ComputeHydrodynamicForces for one body record; io is updated in place."""
+        assert body.dtype == abi.BODY_DTYPE and io.dtype == abi.WRENCH_DTYPE
+        self._ck(self.lib.hydro_body_forces(self.ctx, body.ctypes.data, C.byref(ocean),
+                                            C.byref(settings), io.ctypes.data))
+        return io
+
+    def surface_forces(self, settings, mesh, ocean, T_CG, T_C, v, omega, io: dict) -> dict:
+        """io: dict of float64 arrays Fb, Tb, Fdq, Tdq, Fdf, Tdf (3,), Swet, Vsub (1,)."""
+        vv, pv = _d3(v)
+        ww, pw = _d3(omega)
+        P = C.POINTER(C.c_double)
+        ptrs = [io[k].ctypes.data_as(P) for k in ("Fb", "Tb", "Fdq", "Tdq", "Fdf", "Tdf", "Swet", "Vsub")]
+        self._ck(self.lib.hydro_surface_forces(self.ctx, C.byref(settings), mesh, C.byref(ocean),
+                                               C.byref(T_CG), C.byref(T_C), pv, pw, *ptrs))
+        return io
+
+    def submerged_forces(self, mesh, ocean, T_CG, T_C, v, omega, io: dict) -> dict:
+        vv, pv = _d3(v)
+        ww, pw = _d3(omega)
+        P = C.POINTER(C.c_double)
+        ptrs = [io[k].ctypes.data_as(P) for k in ("Fdq", "Tdq", "Fdf", "Tdf")]
+        self._ck(self.lib.hydro_submerged_forces(self.ctx, mesh, C.byref(ocean), C.byref(T_CG),
+                                                 C.byref(T_C), pv, pw, *ptrs))
+        return io
+
+    def correct_forces(self, ocean, io: dict, Cd, Cf, R_O) -> dict:
+        cd, pcd = _d3(Cd)
+        cf, pcf = _d3(Cf)
+        ro = np.ascontiguousarray(np.asarray(R_O, dtype=np.float64).reshape(9))
+        P = C.POINTER(C.c_double)
+        ptrs = [io[k].ctypes.data_as(P) for k in ("Fdq", "Tdq", "Fdf", "Tdf")]
+        self._ck(self.lib.hydro_correct_forces(self.ctx, C.byref(ocean), *ptrs, pcd, pcf,
+                                               ro.ctypes.data_as(P)))
+        return io
+
+    def face_terms(self, body: np.ndarray, ocean, settings) -> np.ndarray:
+        """Per-face surface-loop terms (n_faces, 23) float32 of one body."""
+        nf = self.mesh_faces[int(body["mesh"][0])]
+        out = np.zeros((nf, 23), dtype=np.float32)
+        self._ck(self.lib.hydro_debug_face_terms(self.ctx, body.ctypes.data, C.byref(ocean),
+                                                 C.byref(settings), out.ctypes.data))
+        return out
+
+    def batch(self, mesh_of_body) -> "Batch":
+        return Batch(self, mesh_of_body)
+
+
+class Batch:
+    """A fixed set of bodies (mesh per body) stepped together."""
+
+    def __init__(self, hctx: HydroContext, mesh_of_body):
+        self.h = hctx
+        self.lib = hctx.lib
+        ids = np.ascontiguousarray(mesh_of_body, dtype=np.uint32)
+        self.n = ids.size
+        b = C.c_void_p()
+        _check(self.lib, hctx.ctx, self.lib.hydro_batch_create(hctx.ctx, ids.ctypes.data, ids.size,
+                                                               C.byref(b)))
+        self.b = b
+
+    def close(self) -> None:
+        if self.b:
+            self.lib.hydro_batch_destroy(self.b)
+            self.b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def compute(self, bodies: np.ndarray, ocean, settings, io: np.ndarray) -> np.ndarray:
+        """Host buffers in/out (copies inside the call)."""
+        assert bodies.dtype == abi.BODY_DTYPE and io.dtype == abi.WRENCH_DTYPE
+        assert bodies.size == self.n and io.size == self.n
+        _check(self.lib, self.h.ctx, self.lib.hydro_batch_compute(self.b, bodies.ctypes.data,
+                                                                  C.byref(ocean), C.byref(settings),
+                                                                  io.ctypes.data))
+        return io
+
+    def compute_ptr(self, bodies_ptr: int, ocean, settings, io_ptr: int) -> None:
+        """Host pointers (e.g. pinned torch tensors) in/out."""
+        _check(self.lib, self.h.ctx, self.lib.hydro_batch_compute(self.b, bodies_ptr, C.byref(ocean),
+                                                                  C.byref(settings), io_ptr))
+
+    def compute_device(self, d_bodies: int, ocean, settings, d_io: int, stream: int = 0) -> None:
+        """Device pointers in/out; enqueued on ``stream`` (cudaStream_t as int)."""
+        _check(self.lib, self.h.ctx, self.lib.hydro_batch_compute_device(
+            self.b, d_bodies, C.byref(ocean), C.byref(settings), d_io, stream or None))
+
+    def last_launches(self) -> int:
+        return int(self.lib.hydro_batch_last_launches(self.b))
