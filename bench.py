@@ -206,7 +206,8 @@ def run_gpu(args, rank: int, world: int, local_rank: int, dist):
     sc = build_workload(args.workload, args.n_bodies)
     cfg, per_body_faces = workload_config(args.workload, sc)
     log(f"[rank {rank}] workload built in {time.perf_counter() - t0:.1f}s: {cfg}")
-    h = HydroContext(device=local_rank)
+    h = HydroContext(device=local_rank, cut_precision=abi.CUT_FP32 if args.cut == "fp32" else abi.CUT_FP64,
+                     tile_faces=args.chunk_faces, ctas_per_sm=args.ctas_per_sm)
     t0 = time.perf_counter()
     if sc.get("waves") is not None:
         h.set_wave_grid(sc["waves"])
@@ -302,6 +303,8 @@ def run_gpu(args, rank: int, world: int, local_rank: int, dist):
                      "algorithmic_bytes_per_launch": alg_bytes,
                      "bytes_rule": "18 B per processed face + 200 B per body"},
         "gpu_launches": args.steps * batch.last_launches(),
+        "kernel_config": {"cut": args.cut, "chunk_faces": args.chunk_faces or 4096,
+                          "ctas_per_sm": args.ctas_per_sm or 2},
         "clocks": clocks,
     }
     if not args.no_error:
@@ -358,6 +361,9 @@ def main():
     ap.add_argument("--n-bodies", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-error", action="store_true")
+    ap.add_argument("--cut", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--chunk-faces", type=int, default=0)
+    ap.add_argument("--ctas-per-sm", type=int, default=0)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -39,6 +39,7 @@ struct hydro_batch;
 
 struct hydro_ctx {
     int device = 0;
+    int sm_count = 1;
     hydro_config cfg{};
     cudaStream_t stream = nullptr;
     std::recursive_mutex mu;
@@ -68,7 +69,8 @@ struct hydro_batch {
     ChunkDesc* chunks_d = nullptr;
     BodyInfo* binfo_d = nullptr;
     double* partials_d = nullptr;
-    unsigned* counters_d = nullptr;
+    BodyParams* bparams_d = nullptr;
+    unsigned* err_d = nullptr;
     hydro_body* bodies_d = nullptr;    // staging for the host-buffer entry point
     hydro_wrench* io_d = nullptr;
     cudaStream_t stream = nullptr;
@@ -210,7 +212,8 @@ void batch_free(hydro_batch* b)
     cudaFree(b->chunks_d);
     cudaFree(b->binfo_d);
     cudaFree(b->partials_d);
-    cudaFree(b->counters_d);
+    cudaFree(b->bparams_d);
+    cudaFree(b->err_d);
     cudaFree(b->bodies_d);
     cudaFree(b->io_d);
     if (b->stream) cudaStreamDestroy(b->stream);
@@ -267,10 +270,11 @@ hydro_status batch_build(hydro_ctx* ctx, const hydro_mesh_id* mesh_of_body, uint
     BK(cudaMalloc(&b->chunks_d, chunks.size() * sizeof(ChunkDesc)));
     BK(cudaMalloc(&b->binfo_d, n * sizeof(BodyInfo)));
     BK(cudaMalloc(&b->partials_d, chunks.size() * kPartialStride * sizeof(double)));
-    BK(cudaMalloc(&b->counters_d, n * sizeof(unsigned)));
+    BK(cudaMalloc(&b->bparams_d, n * sizeof(BodyParams)));
+    BK(cudaMalloc(&b->err_d, 256));
     BK(cudaMemcpy(b->chunks_d, chunks.data(), chunks.size() * sizeof(ChunkDesc), cudaMemcpyHostToDevice));
     BK(cudaMemcpy(b->binfo_d, info.data(), n * sizeof(BodyInfo), cudaMemcpyHostToDevice));
-    BK(cudaMemset(b->counters_d, 0, n * sizeof(unsigned)));
+    BK(cudaMemset(b->err_d, 0, 256));
     BK(cudaMemset(b->partials_d, 0, chunks.size() * kPartialStride * sizeof(double)));
 #undef BK
     *out = b;
@@ -291,16 +295,25 @@ hydro_status batch_launch(hydro_batch* b, const hydro_body* d_bodies, const hydr
     P.bodies = d_bodies;
     P.io = d_io;
     P.partials = b->partials_d;
-    P.counters = b->counters_d;
+    P.bparams = b->bparams_d;
+    P.err = b->err_d;
+    P.n_bodies = b->n_bodies;
+    P.n_chunks = b->n_chunks;
     P.ocean = make_ocean(ctx, ocean);
     P.st.damping = settings->damping_forces ? 1 : 0;
     P.st.buoyancy = settings->realistic_buoyancy ? 1 : 0;
     P.op = op;
     if (P.ocean.waves && ctx->wave_d == nullptr)
         return fail(ctx, HYDRO_ERR_INVALID_ARG, "ocean.waves set but no wave grid was given");
-    cudaError_t e = launch_chunks(P, b->n_chunks, ctx->cfg.cut_precision == HYDRO_CUT_FP64, s);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "chunk kernel launch");
-    b->last_launches = 1;
+    const int cut64 = ctx->cfg.cut_precision == HYDRO_CUT_FP64;
+    LaunchShape shape{};
+    const int want = ctx->cfg.ctas_per_sm ? (int)ctx->cfg.ctas_per_sm : 2;
+    shape.ctas_per_sm = std::max(1, std::min(want, chunk_kernel_occupancy(cut64, P.ocean.waves, want)));
+    shape.grid = ctx->sm_count * shape.ctas_per_sm;
+    uint32_t launches = 0;
+    cudaError_t e = launch_step(P, shape, cut64, s, &launches);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "wrench step launch");
+    b->last_launches = launches;
     return HYDRO_OK;
 }
 
@@ -399,6 +412,8 @@ hydro_status hydro_create(hydro_ctx** out, const hydro_config* cfg)
     if (!ctx) return HYDRO_ERR_OOM;
     ctx->device = c.device;
     ctx->cfg = c;
+    if (cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, c.device) != cudaSuccess)
+        ctx->sm_count = 1;
     ctx->cfg.tune_cache_path = nullptr;
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
         delete ctx;

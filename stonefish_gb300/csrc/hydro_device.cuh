@@ -105,7 +105,8 @@ __device__ __forceinline__ v3 cross(v3 a, v3 b)
 
 // Per-body FP32 parameters (glMatrixFromTransform / glVectorFromVector casts,
 // Library/src/graphics/OpenGLDataStructs.cpp:148-171).
-struct BodyParams {
+// 128 bytes, so that a copy can be staged next to each tile.
+struct __align__(16) BodyParams {
     float TC[12];     // rows of T_C: R[r][0..2], origin[r]
     v3 p;             // (float) T_CG origin
     v3 p0;            // (p.x, p.y, 0)
@@ -115,7 +116,10 @@ struct BodyParams {
     int buoyancy;     // reallisticBuoyancy for this body
     int damping;
     int position;     // BodyFluidPosition or HYDRO_SKIPPED
+    int mismatch;     // body.mesh differs from the batch's mesh
+    int pad[3];
 };
+static_assert(sizeof(BodyParams) == 128, "BodyParams is staged as a 128-byte block");
 
 __device__ __forceinline__ v3 xform(const float* M, float x, float y, float z)
 {

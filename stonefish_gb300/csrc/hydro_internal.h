@@ -14,16 +14,34 @@ struct KParams {
     const TileDesc* tiles;
     const hydro_body* bodies;
     hydro_wrench* io;
+    BodyParams* bparams;     // per body, written by the prep kernel
     double* partials;        // n_chunks * kPartialStride
-    unsigned* counters;      // per body, zero between launches
+    unsigned* err;           // per-launch error word (bit 0: a bounded wait timed out)
+    uint32_t n_bodies;
+    uint32_t n_chunks;
     OceanDev ocean;
     SettingsDev st;
     int op;                  // OP_BODY / OP_SURFACE / OP_SUBMERGED
 };
 
-// The batched wrench step: one CTA per chunk; the last chunk of each body
-// finalises it.  `cut64` selects FP64 cut points.
-cudaError_t launch_chunks(const KParams& P, uint32_t n_chunks, int cut64, cudaStream_t s);
+// Launch shape of the persistent chunk kernel.
+struct LaunchShape {
+    int grid;                // CTAs (a multiple of the SM count when work allows)
+    int ctas_per_sm;
+};
+
+// Shared-memory bytes of the chunk kernel.
+size_t chunk_kernel_smem();
+
+// Resident CTAs per SM that the chunk-kernel variant compiled for
+// `ctas_per_sm` (1 or 2) reaches (0 on error).
+int chunk_kernel_occupancy(int cut64, int waves, int ctas_per_sm);
+
+// The batched wrench step: prep (per body), persistent chunk kernel with a
+// TMA-fed tile pipeline, finalise (per body).  `cut64` selects FP64 cut
+// points.  Returns the number of kernels launched in *launches.
+cudaError_t launch_step(const KParams& P, LaunchShape shape, int cut64, cudaStream_t s,
+                        uint32_t* launches);
 
 // Per-face surface-loop terms of one body for the parity tests: out holds
 // n_faces * kQ floats in uploaded face order.

@@ -1,24 +1,27 @@
 // hydro_kernels.cu -- GB300 kernels of the hydrodynamic wrench path.
 //
 // The batched step replaces the per-body loop of the hydrodynamics block of
-// SimulationManager::SimulationTickCallback (SimulationManager.cpp:1620-1655):
-// one CTA per chunk (a run of tiles of one body's mesh).  A CTA
-//   1. derives the body's FP32 parameters and its fluid position
-//      (SolidEntity::ComputeHydrodynamicForces :1799-1850,
-//      CheckBodyFluidPosition :1239-1261);
-//   2. per tile, transforms each distinct vertex once into shared memory
-//      with its depth (Ocean::GetDepth), then gives each thread faces that
-//      gather their corners from shared memory (surface loop :1337-1687 or
-//      submerged loop :1748-1789);
-//   3. sums the 23 per-face quantities: FP32 per thread over at most
-//      kFlushFaces faces, a butterfly reduce-scatter across the warp, then a
-//      two-sum (float-float) accumulator per warp lane, combined across warps
-//      and stored as one FP64 partial per chunk;
-//   4. the CTA that completes a body's last chunk (per-body ticket counter)
-//      adds the body's partials in chunk order in FP64 and applies the FP64
-//      finalisation: buoyancy (:1689-1720, :1828-1836), the stale-output
-//      rules and CorrectHydrodynamicForces (:1263-1287).
-// The result does not depend on scheduling: every sum has a fixed order.
+// SimulationManager::SimulationTickCallback (SimulationManager.cpp:1620-1655)
+// with three launches:
+//   prep      one thread per body: fluid position (CheckBodyFluidPosition,
+//             SolidEntity.cpp:1239-1261), loop kind and the body's FP32
+//             parameters (the glm casts of ComputeHydrodynamicForcesSurface);
+//   chunk     persistent CTAs.  One producer lane streams the CTA's tiles
+//             (runs of <= 512 faces with their <= 512 distinct vertices,
+//             contiguous in HBM) into a 4-stage shared-memory ring with 1-D
+//             TMA bulk copies signalled on mbarriers; 8 consumer warps
+//             transform each vertex once (with its depth, Ocean::GetDepth)
+//             and evaluate the faces (surface loop :1337-1687 or submerged
+//             loop :1748-1789) from shared memory.  Per-face quantities are
+//             summed in FP32 over at most kFlushFaces faces per thread, then
+//             by a butterfly reduce-scatter across the warp into a two-sum
+//             (float-float) accumulator per lane, combined across warps and
+//             stored as one FP64 partial per chunk;
+//   finalise  one warp per body: the body's chunk partials are added in
+//             chunk order in FP64 and the FP64 finalisation is applied:
+//             buoyancy (:1689-1720, :1828-1836), the stale-output rules and
+//             CorrectHydrodynamicForces (:1263-1287).
+// No result depends on scheduling: every sum has a fixed order.
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -136,15 +139,15 @@ __device__ void finalize_surface(const OceanDev& o, int buoyancy, int damping,
 }
 
 // --------------------------------------------------------------- prologue
-__device__ void body_prologue(const KParams& P, uint32_t body, const BodyInfo& bi,
-                              BodyParams& B, int& mismatch)
+// Per-body FP32 parameters and loop kind (SolidEntity.cpp:1799-1846).
+__device__ void body_prologue(const hydro_body* b, uint32_t batch_mesh, int op, const OceanDev& o,
+                              SettingsDev st, BodyParams& B)
 {
-    const hydro_body* b = P.bodies + body;
-    int loop = LOOP_NONE, pos = HYDRO_SKIPPED, buoy = P.st.buoyancy, damp = P.st.damping;
-    mismatch = (b->mesh != bi.mesh);
-    if (P.op == OP_BODY) {
+    int loop = LOOP_NONE, pos = HYDRO_SKIPPED, buoy = st.buoyancy, damp = st.damping;
+    const int mismatch = (b->mesh != batch_mesh);
+    if (op == OP_BODY) {
         if (!mismatch && (b->mode == HYDRO_MODE_FLOATING || b->mode == HYDRO_MODE_SUBMERGED)) {
-            pos = classify(P.ocean, b->aabb_min, b->aabb_max);
+            pos = classify(o, b->aabb_min, b->aabb_max);
             if (pos == HYDRO_INSIDE) {
                 loop = damp ? LOOP_SUBMERGED : LOOP_NONE;
             } else if (pos == HYDRO_CROSSING_SURFACE) {
@@ -153,11 +156,11 @@ __device__ void body_prologue(const KParams& P, uint32_t body, const BodyInfo& b
             }
         }
     } else if (!mismatch) {
-        loop = (P.op == OP_SURFACE) ? LOOP_SURFACE : LOOP_SUBMERGED;
-        pos = (P.op == OP_SURFACE) ? HYDRO_CROSSING_SURFACE : HYDRO_INSIDE;
-        if (P.op == OP_SUBMERGED) damp = 1;
+        loop = (op == OP_SURFACE) ? LOOP_SURFACE : LOOP_SUBMERGED;
+        pos = (op == OP_SURFACE) ? HYDRO_CROSSING_SURFACE : HYDRO_INSIDE;
+        if (op == OP_SUBMERGED) damp = 1;
     }
-    if (bi.mesh == HYDRO_NO_MESH) loop = LOOP_NONE;
+    if (batch_mesh == HYDRO_NO_MESH) loop = LOOP_NONE;
     for (int r = 0; r < 3; ++r) {
         for (int c = 0; c < 3; ++c) B.TC[4 * r + c] = (float)b->T_C.basis[3 * r + c];
         B.TC[4 * r + 3] = (float)b->T_C.origin[r];
@@ -170,17 +173,19 @@ __device__ void body_prologue(const KParams& P, uint32_t body, const BodyInfo& b
     B.buoyancy = buoy;
     B.damping = damp;
     B.position = pos;
+    B.mismatch = mismatch;
+    B.pad[0] = B.pad[1] = B.pad[2] = 0;
 }
 
-// Finalisation of one body by the CTA that completed its last chunk.
+// Finalisation of one body from its FP64 sums S (kQ values).
 __device__ void body_finalize(const KParams& P, uint32_t body, const BodyParams& B,
-                              int mismatch, const double* S, int status)
+                              const double* S, int status)
 {
     const hydro_body* b = P.bodies + body;
     hydro_wrench w = P.io[body];
     const BodyInfo bi = P.binfo[body];
     const bool null_mesh = (bi.mesh == HYDRO_NO_MESH);
-    if (mismatch) {
+    if (B.mismatch) {
         w.status = HYDRO_ERR_MISMATCH;
         P.io[body] = w;
         return;
@@ -289,127 +294,345 @@ __device__ __forceinline__ void flush(Acc& a, float& hi, float& lo)
     for (int k = 0; k < kQ; ++k) a.q[k] = 0.f;
 }
 
-// ------------------------------------------------------------ main kernel
-struct __align__(16) ChunkSmem {
-    float4 verts[kTileVerts];
-    float2 red[kWarps][32];
-    double sums[32];
+// ---------------------------------------------------- TMA / mbarrier PTX
+__device__ __forceinline__ uint32_t smem_u32(const void* p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_fence_init()
+{
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                 ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// One bounded try: returns true when the phase with `parity` has completed;
+// the hardware may suspend the thread for up to ~1 us inside the call.
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity), "r"(1000u)
+        : "memory");
+    return ok != 0u;
+}
+
+// Bounded wait (about two seconds): false means it gave up.
+constexpr uint32_t kWaitLimit = 1u << 21;
+
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
+{
+    for (uint32_t i = 0; i < kWaitLimit; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+// 1-D bulk copy global -> shared (TMA), completion counted on `bar`.
+__device__ __forceinline__ void tma_copy(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+        ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void consumer_sync()
+{
+    asm volatile("bar.sync 1, %0;" ::"n"(kBlock) : "memory");
+}
+
+// Barrier of the consumer warps that also ANDs a predicate across them, so
+// that a wait that gave up in any thread is seen by all (no thread is left
+// waiting at a later barrier).
+__device__ __forceinline__ bool consumer_all(bool x)
+{
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.and.pred q, 1, %2, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"((uint32_t)x), "n"(kBlock)
+        : "memory");
+    return r != 0u;
+}
+
+// ------------------------------------------------------------ prep kernel
+__global__ void prep_kernel(const KParams P)
+{
+    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b == 0) *P.err = 0u;
+    if (b >= P.n_bodies) return;
     BodyParams B;
-    int mismatch;
-    int last;
+    body_prologue(P.bodies + b, P.binfo[b].mesh, P.op, P.ocean, P.st, B);
+    P.bparams[b] = B;
+}
+
+// ------------------------------------------------------------ main kernel
+// Persistent CTAs: warps 0..7 compute, warp 8 (one lane) streams the CTA's
+// tiles into a ring of kStages shared-memory stages with 1-D TMA bulk
+// copies.  A CTA takes chunks blockIdx.x, blockIdx.x + gridDim.x, ...; the
+// chunks of bodies without a face loop are skipped.
+constexpr int kStages = 4;
+constexpr int kStageRaw = kTileVerts * 12 + kTileFaces * 6;   // 9216 bytes
+constexpr int kThreads = kBlock + 32;
+
+enum : int { ITEM_FIRST = 1, ITEM_LAST = 2, ITEM_END = 4 };
+
+struct ItemMeta {
+    uint32_t chunk;
+    int flags;
+    uint16_t nv, nf;
+    uint32_t pad;
 };
 
-template <bool CUT64, bool WAVES>
-__global__ void __launch_bounds__(kBlock, 2) chunk_kernel(const KParams P)
+struct __align__(128) StageBuf {
+    BodyParams bp;
+    unsigned char raw[kStageRaw];
+};
+
+struct __align__(128) ChunkSmem {
+    StageBuf stage[kStages];
+    float4 verts[kTileVerts];
+    float2 red[kWarps][32];
+    ItemMeta meta[kStages];
+    uint64_t full[kStages];
+    uint64_t empty[kStages];
+};
+
+size_t chunk_kernel_smem() { return sizeof(ChunkSmem); }
+
+__device__ __forceinline__ void producer(const KParams& P, ChunkSmem& S)
 {
-    __shared__ ChunkSmem S;
+    uint32_t item = 0;
+    bool ok = true;
+    for (uint32_t c = blockIdx.x; c < P.n_chunks && ok; c += gridDim.x) {
+        const ChunkDesc ch = P.chunks[c];
+        const int loop = P.bparams[ch.body].loop;
+        if (loop == LOOP_NONE || ch.n_tiles == 0) continue;
+        for (uint32_t t = 0; t < ch.n_tiles; ++t, ++item) {
+            const int s = (int)(item % kStages);
+            if (item >= (uint32_t)kStages && !mbar_wait(&S.empty[s], ((item / kStages) - 1u) & 1u)) {
+                atomicOr(P.err, 1u);
+                ok = false;
+                break;
+            }
+            const TileDesc td = P.tiles[ch.first_tile + t];
+            const uint32_t nvp = (td.nv + 3u) & ~3u;
+            const uint32_t bytes = (nvp * 12u + td.nf * 6u + 15u) & ~15u;
+            ItemMeta m;
+            m.chunk = c;
+            m.flags = (t == 0 ? ITEM_FIRST : 0) | (t + 1 == ch.n_tiles ? ITEM_LAST : 0);
+            m.nv = td.nv;
+            m.nf = td.nf;
+            m.pad = 0;
+            S.meta[s] = m;
+            mbar_arrive_expect_tx(&S.full[s], bytes + (uint32_t)sizeof(BodyParams));
+            tma_copy(&S.stage[s].bp, P.bparams + ch.body, (uint32_t)sizeof(BodyParams), &S.full[s]);
+            tma_copy(S.stage[s].raw, td.block, bytes, &S.full[s]);
+        }
+    }
+    // end of stream
+    const int s = (int)(item % kStages);
+    if (item >= (uint32_t)kStages && !mbar_wait(&S.empty[s], ((item / kStages) - 1u) & 1u)) {
+        atomicOr(P.err, 1u);
+    }
+    ItemMeta m{0u, ITEM_END, 0, 0, 0u};
+    S.meta[s] = m;
+    mbar_arrive(&S.full[s]);
+    // Stay until every copy this thread issued has landed (bounded).  Item
+    // item - kStages shares its stage with the end marker, whose arrive has
+    // already moved that barrier one phase further, and was consumed before
+    // the end marker could be armed, so it is skipped.
+    const uint32_t first = item >= (uint32_t)kStages ? item - (uint32_t)kStages + 1u : 0u;
+    for (uint32_t i = first; i < item; ++i)
+        if (!mbar_wait(&S.full[i % kStages], (i / kStages) & 1u)) atomicOr(P.err, 1u);
+}
+
+template <bool CUT64, bool WAVES>
+__device__ __forceinline__ void consumer(const KParams& P, ChunkSmem& S)
+{
     const int tid = threadIdx.x;
     const int lane = tid & 31;
     const int warp = tid >> 5;
-    const ChunkDesc ch = P.chunks[blockIdx.x];
-    if (tid == 0) {
-        const BodyInfo bi = P.binfo[ch.body];
-        int mm = 0;
-        body_prologue(P, ch.body, bi, S.B, mm);
-        S.mismatch = mm;
-    }
-    __syncthreads();
-    const BodyParams B = S.B;
-    double* part = P.partials + (size_t)blockIdx.x * kPartialStride;
-
-    if (B.loop != LOOP_NONE) {
-        Acc acc;
+    Acc acc;
 #pragma unroll
-        for (int k = 0; k < kQ; ++k) acc.q[k] = 0.f;
-        float hi = 0.f, lo = 0.f;
-        int since_flush = 0;
-        for (uint32_t t = 0; t < ch.n_tiles; ++t) {
-            const TileDesc td = P.tiles[ch.first_tile + t];
-            const int nv = td.nv;
-            const int nvp = (nv + 3) & ~3;
-            for (int v = tid; v < nv; v += kBlock) {
-                float x = __ldg(td.block + v);
-                float y = __ldg(td.block + nvp + v);
-                float z = __ldg(td.block + 2 * nvp + v);
-                v3 p = xform(B.TC, x, y, z);
-                float d = WAVES ? depth_at(P.ocean, p.x, p.y, p.z) : p.z;
-                S.verts[v] = make_float4(p.x, p.y, p.z, d);
-            }
-            __syncthreads();
-            const uint16_t* idx = reinterpret_cast<const uint16_t*>(td.block + 3 * nvp);
-            for (int f = tid; f < td.nf; f += kBlock) {
-                const int i0 = __ldg(idx + 3 * f);
-                const int i1 = __ldg(idx + 3 * f + 1);
-                const int i2 = __ldg(idx + 3 * f + 2);
-                const float4 q1 = S.verts[i0], q2 = S.verts[i1], q3 = S.verts[i2];
-                if (B.loop == LOOP_SURFACE) face_surface<CUT64>(P.ocean, B, acc, q1, q2, q3);
-                else face_submerged(P.ocean, B, acc, q1, q2, q3);
-            }
-            __syncthreads();
-            since_flush += (kTileFaces + kBlock - 1) / kBlock;
-            if (since_flush + (kTileFaces + kBlock - 1) / kBlock > kFlushFaces) {
-                flush(acc, hi, lo);
-                since_flush = 0;
+    for (int k = 0; k < kQ; ++k) acc.q[k] = 0.f;
+    float hi = 0.f, lo = 0.f;
+    int since_flush = 0;
+    constexpr int kFacesPerTile = (kTileFaces + kBlock - 1) / kBlock;
+    for (uint32_t item = 0;; ++item) {
+        const int s = (int)(item % kStages);
+        const bool ok = mbar_wait(&S.full[s], (item / kStages) & 1u);
+        if (!consumer_all(ok)) {
+            if (tid == 0) atomicOr(P.err, 1u);
+            break;
+        }
+        const ItemMeta m = S.meta[s];
+        if (m.flags & ITEM_END) break;
+        const BodyParams& B = S.stage[s].bp;
+        const float* raw = reinterpret_cast<const float*>(S.stage[s].raw);
+        const int nv = m.nv, nf = m.nf, nvp = (nv + 3) & ~3;
+        float TC[12];
+#pragma unroll
+        for (int k = 0; k < 12; ++k) TC[k] = B.TC[k];
+        for (int v = tid; v < nv; v += kBlock) {
+            v3 p = xform(TC, raw[v], raw[nvp + v], raw[2 * nvp + v]);
+            float d = WAVES ? depth_at(P.ocean, p.x, p.y, p.z) : p.z;
+            S.verts[v] = make_float4(p.x, p.y, p.z, d);
+        }
+        consumer_sync();
+        {
+            BodyParams Bl;
+            Bl.p = B.p; Bl.p0 = B.p0; Bl.v = B.v; Bl.omega = B.omega;
+            Bl.loop = B.loop; Bl.buoyancy = B.buoyancy; Bl.damping = B.damping;
+            const uint16_t* idx = reinterpret_cast<const uint16_t*>(raw + 3 * nvp);
+            for (int f = tid; f < nf; f += kBlock) {
+                const float4 q1 = S.verts[idx[3 * f]];
+                const float4 q2 = S.verts[idx[3 * f + 1]];
+                const float4 q3 = S.verts[idx[3 * f + 2]];
+                if (Bl.loop == LOOP_SURFACE) face_surface<CUT64>(P.ocean, Bl, acc, q1, q2, q3);
+                else face_submerged(P.ocean, Bl, acc, q1, q2, q3);
             }
         }
-        flush(acc, hi, lo);
-        S.red[warp][lane] = make_float2(hi, lo);
-        __syncthreads();
-        if (warp == 0) {
-            float H = S.red[0][lane].x, L = S.red[0][lane].y;
-            for (int w = 1; w < kWarps; ++w) {
-                two_sum_acc(H, L, S.red[w][lane].x);
-                L += S.red[w][lane].y;
-            }
-            if (lane < kQ) part[lane] = (double)H + (double)L;
-            if (lane == kQ) part[lane] = 0.0;   // status slot
-            __threadfence();
+        consumer_sync();
+        if (tid == 0) mbar_arrive(&S.empty[s]);
+        since_flush += kFacesPerTile;
+        const bool last = (m.flags & ITEM_LAST) != 0;
+        if (last || since_flush + kFacesPerTile > kFlushFaces) {
+            flush(acc, hi, lo);
+            since_flush = 0;
         }
-    }
-    __syncthreads();
-
-    // ticket: the CTA finishing a body's last chunk finalises the body
-    const BodyInfo bi = P.binfo[ch.body];
-    if (tid == 0) {
-        __threadfence();
-        unsigned prev = atomicAdd(P.counters + ch.body, 1u);
-        S.last = (prev + 1u == bi.n_chunks);
-    }
-    __syncthreads();
-    if (!S.last) return;
-    __threadfence();
-    if (warp == 0) {
-        double s = 0.0;
-        int status = 0;
-        if (B.loop != LOOP_NONE) {
-            for (uint32_t c = 0; c < bi.n_chunks; ++c) {
-                const double* pc = P.partials + (size_t)(bi.first_chunk + c) * kPartialStride;
-                if (lane < kQ) s += __ldcg(pc + lane);
-                else if (lane == kQ) status |= (int)__ldcg(pc + lane);
+        if (last) {
+            S.red[warp][lane] = make_float2(hi, lo);
+            consumer_sync();
+            if (warp == 0) {
+                float H = S.red[0][lane].x, L = S.red[0][lane].y;
+                for (int w = 1; w < kWarps; ++w) {
+                    two_sum_acc(H, L, S.red[w][lane].x);
+                    L += S.red[w][lane].y;
+                }
+                double* part = P.partials + (size_t)m.chunk * kPartialStride;
+                if (lane < kQ) part[lane] = (double)H + (double)L;
+                else if (lane == kQ) part[lane] = 0.0;
             }
+            hi = 0.f;
+            lo = 0.f;
+            consumer_sync();
         }
-        S.sums[lane] = (lane < kQ) ? s : (double)status;
-    }
-    __syncthreads();
-    if (tid == 0) {
-        body_finalize(P, ch.body, B, S.mismatch, S.sums, (int)S.sums[kQ]);
-        P.counters[ch.body] = 0u;
     }
 }
 
-cudaError_t launch_chunks(const KParams& P, uint32_t n_chunks, int cut64, cudaStream_t s)
+template <bool CUT64, bool WAVES, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) chunk_kernel(const KParams P)
 {
-    if (n_chunks == 0) return cudaSuccess;
-    dim3 grid(n_chunks), block(kBlock);
-    const bool waves = P.ocean.waves != 0;
-    if (cut64) {
-        if (waves) chunk_kernel<true, true><<<grid, block, 0, s>>>(P);
-        else chunk_kernel<true, false><<<grid, block, 0, s>>>(P);
-    } else {
-        if (waves) chunk_kernel<false, true><<<grid, block, 0, s>>>(P);
-        else chunk_kernel<false, false><<<grid, block, 0, s>>>(P);
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    ChunkSmem& S = *reinterpret_cast<ChunkSmem*>(smem_raw);
+    const int tid = threadIdx.x;
+    if (tid == kBlock) {
+        for (int s = 0; s < kStages; ++s) {
+            mbar_init(&S.full[s], 1u);
+            mbar_init(&S.empty[s], 1u);
+        }
+        mbar_fence_init();
     }
-    return cudaGetLastError();
+    __syncthreads();
+    if (tid >= kBlock) {
+        if (tid == kBlock) producer(P, S);
+        return;
+    }
+    consumer<CUT64, WAVES>(P, S);
+}
+
+// ----------------------------------------------------------- finalise kernel
+// One warp per body: lanes 0..22 add the body's chunk partials in chunk
+// order (FP64), lane 0 finalises.
+__global__ void finalize_kernel(const KParams P)
+{
+    __shared__ double sums[kWarps][32];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const uint32_t body = blockIdx.x * kWarps + warp;
+    if (body >= P.n_bodies) return;
+    const BodyParams B = P.bparams[body];
+    const BodyInfo bi = P.binfo[body];
+    double s = 0.0;
+    if (B.loop != LOOP_NONE && lane < kQ) {
+        const double* p = P.partials + (size_t)bi.first_chunk * kPartialStride + lane;
+        for (uint32_t c = 0; c < bi.n_chunks; ++c) s += p[(size_t)c * kPartialStride];
+    }
+    sums[warp][lane] = s;
+    __syncwarp();
+    if (lane == 0) {
+        const int status = (*P.err & 1u) ? HYDRO_ERR_TIMEOUT : 0;
+        body_finalize(P, body, B, sums[warp], status);
+    }
+}
+
+template <int MINB>
+static void* kernel_ptr(int cut64, int waves)
+{
+    if (cut64) return waves ? (void*)chunk_kernel<true, true, MINB> : (void*)chunk_kernel<true, false, MINB>;
+    return waves ? (void*)chunk_kernel<false, true, MINB> : (void*)chunk_kernel<false, false, MINB>;
+}
+
+// The kernel variant compiled for `ctas_per_sm` resident CTAs (1 or 2).
+static void* chunk_kernel_for(int cut64, int waves, int ctas_per_sm)
+{
+    return ctas_per_sm >= 2 ? kernel_ptr<2>(cut64, waves) : kernel_ptr<1>(cut64, waves);
+}
+
+int chunk_kernel_occupancy(int cut64, int waves, int ctas_per_sm)
+{
+    int n = 0;
+    const void* k = chunk_kernel_for(cut64, waves, ctas_per_sm);
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ChunkSmem)) != cudaSuccess)
+        return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, kThreads, sizeof(ChunkSmem)) != cudaSuccess)
+        return 0;
+    return n;
+}
+
+cudaError_t launch_step(const KParams& P, LaunchShape shape, int cut64, cudaStream_t s,
+                        uint32_t* launches)
+{
+    *launches = 0;
+    if (P.n_bodies == 0) return cudaSuccess;
+    cudaError_t e;
+    prep_kernel<<<(P.n_bodies + 127) / 128, 128, 0, s>>>(P);
+    if ((e = cudaGetLastError())) return e;
+    int grid = shape.grid;
+    if (grid > (int)P.n_chunks) grid = (int)P.n_chunks;
+    if (grid < 1) grid = 1;
+    const void* k = chunk_kernel_for(cut64, P.ocean.waves != 0, shape.ctas_per_sm);
+    if ((e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ChunkSmem))))
+        return e;
+    void* args[] = {const_cast<KParams*>(&P)};
+    if ((e = cudaLaunchKernel(k, dim3(grid), dim3(kThreads), args, sizeof(ChunkSmem), s))) return e;
+    finalize_kernel<<<(P.n_bodies + kWarps - 1) / kWarps, kBlock, 0, s>>>(P);
+    if ((e = cudaGetLastError())) return e;
+    *launches = 3;
+    return cudaSuccess;
 }
 
 // ------------------------------------------------------- debug face terms
@@ -422,16 +645,7 @@ __global__ void __launch_bounds__(kBlock) face_terms_kernel(const TileDesc* tile
     __shared__ BodyParams Bs;
     const int tid = threadIdx.x;
     const TileDesc td = tiles[first_tile + blockIdx.x];
-    if (tid == 0) {
-        KParams P{};
-        P.bodies = body;
-        P.ocean = ocean;
-        P.st = st;
-        P.op = OP_SURFACE;
-        BodyInfo bi{0u, 1u, body->mesh, 0u};
-        int mm = 0;
-        body_prologue(P, 0, bi, Bs, mm);
-    }
+    if (tid == 0) body_prologue(body, body->mesh, OP_SURFACE, ocean, st, Bs);
     __syncthreads();
     const BodyParams B = Bs;
     const int nv = td.nv, nvp = (nv + 3) & ~3;

@@ -48,7 +48,7 @@ class HydroContext:
     """Owns a hydro_ctx: device meshes, the wave grid and small buffers."""
 
     def __init__(self, device: int = 0, cut_precision: int = abi.CUT_FP64,
-                 tile_faces: int = 0, lib_path: str | None = None):
+                 tile_faces: int = 0, ctas_per_sm: int = 0, lib_path: str | None = None):
         self.lib = abi.load_library(lib_path)
         lib = self.lib
         if not hasattr(lib, "_debug_declared"):
@@ -61,6 +61,7 @@ class HydroContext:
         cfg.device = device
         cfg.cut_precision = cut_precision
         cfg.tile_faces = tile_faces
+        cfg.ctas_per_sm = ctas_per_sm
         h = C.c_void_p()
         st = lib.hydro_create(C.byref(h), C.byref(cfg))
         if st != abi.HYDRO_OK:
