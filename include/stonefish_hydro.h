@@ -77,10 +77,15 @@ enum {
     HYDRO_CURRENT_PIPE = 2
 };
 
-/* Precision of the waterline cut points (faces that straddle the surface). */
+/* Precision of the waterline cut points (faces that straddle the surface).
+ * HYDRO_CUT_FP32 (default) is the reference's own arithmetic: every face's
+ * contribution equals the FP32 glm evaluation bit for bit.  HYDRO_CUT_FP64
+ * interpolates the cut points in FP64 and rounds them once; GB300's FP64
+ * rate makes that path several times slower for no measurable gain in the
+ * wrench error against an all-FP64 evaluation. */
 enum {
-    HYDRO_CUT_FP64 = 0,         /* cut point interpolated in FP64, rounded once */
-    HYDRO_CUT_FP32 = 1          /* FP32 in the reference's own operation order */
+    HYDRO_CUT_FP64 = 0,
+    HYDRO_CUT_FP32 = 1
 };
 
 #define HYDRO_MAX_CURRENTS 8
@@ -167,14 +172,14 @@ typedef struct hydro_wrench {
 
 typedef struct hydro_config {
     int32_t device;              /* CUDA device ordinal */
-    int32_t cut_precision;       /* HYDRO_CUT_FP64 (default) or HYDRO_CUT_FP32 */
+    int32_t cut_precision;       /* HYDRO_CUT_FP32 (default) or HYDRO_CUT_FP64 */
     uint32_t tile_faces;         /* faces per work tile; 0 = autotune */
     uint32_t ctas_per_sm;        /* resident CTAs per SM; 0 = autotune */
     const char* tune_cache_path; /* autotuner cache file, NULL = none */
 } hydro_config;
 
 /* -------------------------------------------------------------- lifecycle */
-/* Fills *cfg with defaults (device 0, FP64 cut points, autotuned tiles). */
+/* Fills *cfg with defaults (device 0, FP32 cut points, autotuned tiles). */
 void hydro_config_default(hydro_config* cfg);
 
 hydro_status hydro_create(hydro_ctx** ctx, const hydro_config* cfg);
@@ -305,6 +310,14 @@ hydro_status hydro_fluid_position(hydro_ctx* ctx, const hydro_ocean* ocean,
 hydro_status hydro_debug_face_terms(hydro_ctx* ctx, const hydro_body* body,
                                     const hydro_ocean* ocean,
                                     const hydro_settings* settings, float* out);
+
+/* Checks on the GPU that the division the kernels use for x/|n| and x/3
+ * (a correctly rounded reciprocal plus one FMA correction) returns the bits
+ * of IEEE round-to-nearest division: x/3 over every float, x/b over n_pairs
+ * seeded random pairs in the face-length range and over n_pairs pairs of
+ * normal floats.  mismatches[0..2] receive the three mismatch counts. */
+hydro_status hydro_debug_division_check(hydro_ctx* ctx, uint64_t n_pairs, uint64_t seed,
+                                        uint64_t mismatches[3]);
 
 #ifdef __cplusplus
 }

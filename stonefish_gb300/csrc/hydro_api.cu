@@ -297,6 +297,7 @@ hydro_status batch_launch(hydro_batch* b, const hydro_body* d_bodies, const hydr
     P.partials = b->partials_d;
     P.bparams = b->bparams_d;
     P.err = b->err_d;
+    P.work = b->err_d + 32;
     P.n_bodies = b->n_bodies;
     P.n_chunks = b->n_chunks;
     P.ocean = make_ocean(ctx, ocean);
@@ -366,7 +367,7 @@ void hydro_config_default(hydro_config* cfg)
     if (!cfg) return;
     std::memset(cfg, 0, sizeof(*cfg));
     cfg->device = 0;
-    cfg->cut_precision = HYDRO_CUT_FP64;
+    cfg->cut_precision = HYDRO_CUT_FP32;
     cfg->tile_faces = 0;
     cfg->ctas_per_sm = 0;
     cfg->tune_cache_path = nullptr;
@@ -801,6 +802,26 @@ hydro_status hydro_debug_face_terms(hydro_ctx* ctx, const hydro_body* body, cons
     if (e != cudaSuccess) return cuda_fail(ctx, e, "face terms kernel");
     CK(ctx, cudaMemcpyAsync(out, dout, terms, cudaMemcpyDeviceToHost, ctx->stream));
     CK(ctx, cudaStreamSynchronize(ctx->stream));
+    return HYDRO_OK;
+}
+
+hydro_status hydro_debug_division_check(hydro_ctx* ctx, uint64_t n_pairs, uint64_t seed,
+                                       uint64_t mismatches[3])
+{
+    if (!ctx) return HYDRO_ERR_INVALID_ARG;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (!mismatches) return fail(ctx, HYDRO_ERR_INVALID_ARG, "division check: null output");
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, HYDRO_ERR_DEVICE, "cudaSetDevice");
+    hydro_status st = ensure_small(ctx, 64);
+    if (st != HYDRO_OK) return st;
+    unsigned long long* d = static_cast<unsigned long long*>(ctx->small_d);
+    CK(ctx, cudaMemsetAsync(d, 0, 3 * sizeof(unsigned long long), ctx->stream));
+    cudaError_t e = launch_division_check(n_pairs, seed, d, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "division check kernel");
+    unsigned long long h[3];
+    CK(ctx, cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int i = 0; i < 3; ++i) mismatches[i] = h[i];
     return HYDRO_OK;
 }
 

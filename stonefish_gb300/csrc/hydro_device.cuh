@@ -103,6 +103,34 @@ __device__ __forceinline__ v3 cross(v3 a, v3 b)
     return mk(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);
 }
 
+// ----------------------------------------------------- correctly rounded x/y
+// Division with the result of IEEE round-to-nearest division, from a
+// correctly rounded reciprocal and one FMA correction (Markstein's theorem:
+// if y = RN(1/b) and q is within one ulp of a/b, then with the exact
+// remainder r = a - b*q, RN(q + r*y) = RN(a/b); P. Markstein, "IA-64 and
+// Elementary Functions", 2000; Muller et al., Handbook of Floating-Point
+// Arithmetic, 2018, section 4.7).  The theorem needs a normal quotient, so
+// tiny numerators take the IEEE division instead.  Bit-identity with IEEE
+// division is checked on the GPU by hydro_debug_division_check.
+__device__ __forceinline__ float div_by_rcp(float a, float b, float y)
+{
+    if (fabsf(a) < 0x1p-100f) return __fdiv_rn(a, b);
+    float q = a * y;
+    float r = __fmaf_rn(-b, q, a);
+    return __fmaf_rn(r, y, q);
+}
+
+// a / 3 with RN(1/3) = 0x1.555556p-2
+__device__ __forceinline__ float div3(float a) { return div_by_rcp(a, 3.f, 0x1.555556p-2f); }
+
+__device__ __forceinline__ v3 dvs_rcp(v3 a, float b)
+{
+    const float y = __frcp_rn(b);
+    return mk(div_by_rcp(a.x, b, y), div_by_rcp(a.y, b, y), div_by_rcp(a.z, b, y));
+}
+
+__device__ __forceinline__ v3 dvs3(v3 a) { return mk(div3(a.x), div3(a.y), div3(a.z)); }
+
 // Per-body FP32 parameters (glMatrixFromTransform / glVectorFromVector casts,
 // Library/src/graphics/OpenGLDataStructs.cpp:148-171).
 // 128 bytes, so that a copy can be staged next to each tile.
@@ -283,7 +311,7 @@ __device__ __forceinline__ v3 cut(v3 pa, v3 pb, float da, float db)
 // Volume properties of one fan tetra (e.g. :1372-1378)
 __device__ __forceinline__ void tetra(Acc& a, v3 x, v3 y, v3 z)
 {
-    v3 cg = dvs(add(add(x, y), z), 4.f);
+    v3 cg = mul(add(add(x, y), z), 0.25f);     // /4 is exact: same bits as division
     float v6 = dot(x, cross(y, z));
     acc_add3(a, Q_CB, mul(cg, v6));
     a.q[Q_V6] += v6;
@@ -317,21 +345,24 @@ __device__ __forceinline__ bool tri_props(v3 p1, v3 p2, v3 p3, v3& fc, v3& fn1, 
 {
     v3 fv1 = sub(p2, p1);
     v3 fv2 = sub(p3, p1);
-    fc = dvs(add(add(p1, p2), p3), 3.f);
+    fc = dvs3(add(add(p1, p2), p3));
     v3 fn = cross(fv1, fv2);
     float len = dot(fn, fn);
     if (len < 1e-12f) return false;
     len = sqrtf(len);
-    fn1 = dvs(fn, len);
-    A = len / 2.f;
+    fn1 = dvs_rcp(fn, len);
+    A = len * 0.5f;
     return true;
 }
 
 // The part of a surface-loop face after its polygon is known (:1650-1686).
+// WAVES is Ocean::hasWaves(): the pressure buoyancy is summed per face only
+// with waves.
+template <bool WAVES>
 __device__ __forceinline__ void face_forces(const OceanDev& o, const BodyParams& B, Acc& a,
                                             v3 fc, v3 fn1, float A)
 {
-    if (B.buoyancy && o.waves) {
+    if (WAVES && B.buoyancy) {
         float depthc = depth_at(o, fc.x, fc.y, fc.z);
         v3 Fbi = mul(mul(neg(fn1), A), depthc);
         acc_add3(a, Q_FB, Fbi);
@@ -342,7 +373,7 @@ __device__ __forceinline__ void face_forces(const OceanDev& o, const BodyParams&
 }
 
 // One face straddling the surface: the six mixed clip cases (:1360-1617).
-template <bool CUT64>
+template <bool CUT64, bool WAVES>
 __device__ __forceinline__ void face_cut(const OceanDev& o, const BodyParams& B, Acc& a,
                                       v3 p1, v3 p2, v3 p3, float d0, float d1, float d2)
 {
@@ -396,37 +427,55 @@ __device__ __forceinline__ void face_cut(const OceanDev& o, const BodyParams& B,
         }
         v3 fv3 = sub(p2, p3);
         v3 fv4 = sub(p4, p3);
-        fc = dvs(add(add(add(p1, p2), p3), p4), 4.f);
+        fc = mul(add(add(add(p1, p2), p3), p4), 0.25f);
         v3 fn = cross(fv1, fv2);
         float len = dot(fn, fn);
         if (len < 1e-12f) return;
         len = sqrtf(len);
-        fn1 = dvs(fn, len);
+        fn1 = dvs_rcp(fn, len);
         v3 c2 = cross(fv3, fv4);
-        A = (len + sqrtf(dot(c2, c2))) / 2.f;
+        A = (len + sqrtf(dot(c2, c2))) * 0.5f;
     }
-    face_forces(o, B, a, fc, fn1, A);
+    face_forces<WAVES>(o, B, a, fc, fn1, A);
 }
 
-// One face of the surface loop (:1337-1687) given transformed vertices
-// (x, y, z, depth).
-template <bool CUT64>
-__device__ __forceinline__ void face_surface(const OceanDev& o, const BodyParams& B, Acc& a,
-                                             float4 q1, float4 q2, float4 q3)
+// A surface-loop face whose three corners are all under water
+// (:1618-1647, then :1650-1686).
+template <bool WAVES>
+__device__ __forceinline__ void face_full(const OceanDev& o, const BodyParams& B, Acc& a,
+                                          float4 q1, float4 q2, float4 q3)
 {
-    const float d0 = q1.w, d1 = q2.w, d2 = q3.w;
-    if (d0 < 0.f && d1 < 0.f && d2 < 0.f) return;
     v3 p1 = mk(q1.x, q1.y, q1.z), p2 = mk(q2.x, q2.y, q2.z), p3 = mk(q3.x, q3.y, q3.z);
-    if (d0 < 0.f || d1 < 0.f || d2 < 0.f) {
-        face_cut<CUT64>(o, B, a, p1, p2, p3, d0, d1, d2);
-        return;
-    }
-    // all submerged (:1618-1647)
     tetra(a, sub(p1, B.p0), sub(p2, B.p0), sub(p3, B.p0));
     v3 fc, fn1;
     float A;
     if (!tri_props(p1, p2, p3, fc, fn1, A)) return;
-    face_forces(o, B, a, fc, fn1, A);
+    face_forces<WAVES>(o, B, a, fc, fn1, A);
+}
+
+// Face class of the surface loop from the corner depths: 0 above water
+// (skipped, :1353-1354), 1 all corners under water, 2 straddling.
+__device__ __forceinline__ int face_class(float d0, float d1, float d2)
+{
+    if (d0 < 0.f && d1 < 0.f && d2 < 0.f) return 0;
+    if (d0 < 0.f || d1 < 0.f || d2 < 0.f) return 2;
+    return 1;
+}
+
+// One face of the surface loop (:1337-1687) given transformed vertices
+// (x, y, z, depth).
+template <bool CUT64, bool WAVES>
+__device__ __forceinline__ void face_surface(const OceanDev& o, const BodyParams& B, Acc& a,
+                                             float4 q1, float4 q2, float4 q3)
+{
+    const int cls = face_class(q1.w, q2.w, q3.w);
+    if (cls == 0) return;
+    if (cls == 2) {
+        face_cut<CUT64, WAVES>(o, B, a, mk(q1.x, q1.y, q1.z), mk(q2.x, q2.y, q2.z),
+                               mk(q3.x, q3.y, q3.z), q1.w, q2.w, q3.w);
+        return;
+    }
+    face_full<WAVES>(o, B, a, q1, q2, q3);
 }
 
 // One face of the submerged loop (:1748-1789)

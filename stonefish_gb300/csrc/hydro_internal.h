@@ -17,6 +17,7 @@ struct KParams {
     BodyParams* bparams;     // per body, written by the prep kernel
     double* partials;        // n_chunks * kPartialStride
     unsigned* err;           // per-launch error word (bit 0: a bounded wait timed out)
+    unsigned* work;          // chunk counter of the persistent kernel
     uint32_t n_bodies;
     uint32_t n_chunks;
     OceanDev ocean;
@@ -54,6 +55,11 @@ cudaError_t launch_correct(double density, double* io12, const double* Cd, const
                            const double* R_O, cudaStream_t s);
 
 cudaError_t launch_fluid_position(OceanDev ocean, const double* aabb6, int* out, cudaStream_t s);
+
+// Counts mismatches of the FMA-corrected divisions against IEEE division:
+// counts[0] a/3 over all floats, counts[1] and counts[2] random pairs.
+cudaError_t launch_division_check(uint64_t n_pairs, uint64_t seed, unsigned long long* counts,
+                                  cudaStream_t s);
 
 cudaError_t launch_depth(OceanDev ocean, const float* xyz, uint32_t n, float* out, cudaStream_t s);
 

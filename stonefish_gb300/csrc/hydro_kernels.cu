@@ -381,7 +381,10 @@ __device__ __forceinline__ bool consumer_all(bool x)
 __global__ void prep_kernel(const KParams P)
 {
     const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b == 0) *P.err = 0u;
+    if (b == 0) {
+        *P.err = 0u;
+        *P.work = 0u;
+    }
     if (b >= P.n_bodies) return;
     BodyParams B;
     body_prologue(P.bodies + b, P.binfo[b].mesh, P.op, P.ocean, P.st, B);
@@ -391,8 +394,9 @@ __global__ void prep_kernel(const KParams P)
 // ------------------------------------------------------------ main kernel
 // Persistent CTAs: warps 0..7 compute, warp 8 (one lane) streams the CTA's
 // tiles into a ring of kStages shared-memory stages with 1-D TMA bulk
-// copies.  A CTA takes chunks blockIdx.x, blockIdx.x + gridDim.x, ...; the
-// chunks of bodies without a face loop are skipped.
+// copies.  The producer claims chunks from a global counter (reset by the
+// prep kernel) and skips the chunks of bodies without a face loop; which CTA
+// takes a chunk does not change the chunk's result.
 constexpr int kStages = 4;
 constexpr int kStageRaw = kTileVerts * 12 + kTileFaces * 6;   // 9216 bytes
 constexpr int kThreads = kBlock + 32;
@@ -415,6 +419,7 @@ struct __align__(128) ChunkSmem {
     StageBuf stage[kStages];
     float4 verts[kTileVerts];
     float2 red[kWarps][32];
+    uint16_t flist[kWarps][64];       // per-warp compacted face lists
     ItemMeta meta[kStages];
     uint64_t full[kStages];
     uint64_t empty[kStages];
@@ -426,7 +431,9 @@ __device__ __forceinline__ void producer(const KParams& P, ChunkSmem& S)
 {
     uint32_t item = 0;
     bool ok = true;
-    for (uint32_t c = blockIdx.x; c < P.n_chunks && ok; c += gridDim.x) {
+    while (ok) {
+        const uint32_t c = atomicAdd(P.work, 1u);      // dynamic: next unclaimed chunk
+        if (c >= P.n_chunks) break;
         const ChunkDesc ch = P.chunks[c];
         const int loop = P.bparams[ch.body].loop;
         if (loop == LOOP_NONE || ch.n_tiles == 0) continue;
@@ -480,7 +487,7 @@ __device__ __forceinline__ void consumer(const KParams& P, ChunkSmem& S)
     for (int k = 0; k < kQ; ++k) acc.q[k] = 0.f;
     float hi = 0.f, lo = 0.f;
     int since_flush = 0;
-    constexpr int kFacesPerTile = (kTileFaces + kBlock - 1) / kBlock;
+    constexpr int kMaxFacesPerTile = 3;   // ceil(nfull/32) + ceil(ncut/32) with nfull + ncut <= 64
     for (uint32_t item = 0;; ++item) {
         const int s = (int)(item % kStages);
         const bool ok = mbar_wait(&S.full[s], (item / kStages) & 1u);
@@ -502,24 +509,63 @@ __device__ __forceinline__ void consumer(const KParams& P, ChunkSmem& S)
             S.verts[v] = make_float4(p.x, p.y, p.z, d);
         }
         consumer_sync();
+        int iters = 0;
         {
             BodyParams Bl;
             Bl.p = B.p; Bl.p0 = B.p0; Bl.v = B.v; Bl.omega = B.omega;
             Bl.loop = B.loop; Bl.buoyancy = B.buoyancy; Bl.damping = B.damping;
             const uint16_t* idx = reinterpret_cast<const uint16_t*>(raw + 3 * nvp);
-            for (int f = tid; f < nf; f += kBlock) {
+            // Warp w takes faces (k*32 + lane)*8 + w, k = 0, 1: a spread
+            // sample of the tile, so that the warps get similar work.  Its
+            // faces are compacted (deterministically, by ballot) into a list
+            // of fully submerged faces and a list of straddling faces, which
+            // the warp then evaluates with all lanes busy.
+            uint16_t* list = S.flist[warp];
+            int nfull = 0, ncut = 0;
+            const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                const int f = (k * 32 + lane) * kWarps + warp;
+                int cls = 0;
+                if (f < nf) {
+                    if (Bl.loop == LOOP_SURFACE)
+                        cls = face_class(S.verts[idx[3 * f]].w, S.verts[idx[3 * f + 1]].w,
+                                         S.verts[idx[3 * f + 2]].w);
+                    else
+                        cls = 1;
+                }
+                const unsigned mf = __ballot_sync(0xffffffffu, cls == 1);
+                const unsigned mc = __ballot_sync(0xffffffffu, cls == 2);
+                if (cls == 1) list[nfull + __popc(mf & lt)] = (uint16_t)f;
+                if (cls == 2) list[63 - (ncut + __popc(mc & lt))] = (uint16_t)f;
+                nfull += __popc(mf);
+                ncut += __popc(mc);
+            }
+            __syncwarp();
+            for (int i = lane; i < nfull; i += 32) {
+                const int f = list[i];
                 const float4 q1 = S.verts[idx[3 * f]];
                 const float4 q2 = S.verts[idx[3 * f + 1]];
                 const float4 q3 = S.verts[idx[3 * f + 2]];
-                if (Bl.loop == LOOP_SURFACE) face_surface<CUT64>(P.ocean, Bl, acc, q1, q2, q3);
+                if (Bl.loop == LOOP_SURFACE) face_full<WAVES>(P.ocean, Bl, acc, q1, q2, q3);
                 else face_submerged(P.ocean, Bl, acc, q1, q2, q3);
             }
+            for (int i = lane; i < ncut; i += 32) {
+                const int f = list[63 - i];
+                const float4 q1 = S.verts[idx[3 * f]];
+                const float4 q2 = S.verts[idx[3 * f + 1]];
+                const float4 q3 = S.verts[idx[3 * f + 2]];
+                face_cut<CUT64, WAVES>(P.ocean, Bl, acc, mk(q1.x, q1.y, q1.z), mk(q2.x, q2.y, q2.z),
+                                mk(q3.x, q3.y, q3.z), q1.w, q2.w, q3.w);
+            }
+            iters = (nfull + 31) / 32 + (ncut + 31) / 32;
+            __syncwarp();
         }
         consumer_sync();
         if (tid == 0) mbar_arrive(&S.empty[s]);
-        since_flush += kFacesPerTile;
+        since_flush += iters;                      // warp-uniform
         const bool last = (m.flags & ITEM_LAST) != 0;
-        if (last || since_flush + kFacesPerTile > kFlushFaces) {
+        if (last || since_flush + kMaxFacesPerTile > kFlushFaces) {
             flush(acc, hi, lo);
             since_flush = 0;
         }
@@ -658,7 +704,10 @@ __global__ void __launch_bounds__(kBlock) face_terms_kernel(const TileDesc* tile
     for (int f = tid; f < td.nf; f += kBlock) {
         Acc a;
         for (int k = 0; k < kQ; ++k) a.q[k] = 0.f;
-        face_surface<CUT64>(ocean, B, a, verts[idx[3 * f]], verts[idx[3 * f + 1]], verts[idx[3 * f + 2]]);
+        if (ocean.waves)
+            face_surface<CUT64, true>(ocean, B, a, verts[idx[3 * f]], verts[idx[3 * f + 1]], verts[idx[3 * f + 2]]);
+        else
+            face_surface<CUT64, false>(ocean, B, a, verts[idx[3 * f]], verts[idx[3 * f + 1]], verts[idx[3 * f + 2]]);
         float* o = out + (size_t)(td.first_face + f) * kQ;
         for (int k = 0; k < kQ; ++k) o[k] = a.q[k];
     }
@@ -710,6 +759,64 @@ cudaError_t launch_depth(OceanDev ocean, const float* xyz, uint32_t n, float* ou
 {
     if (n == 0) return cudaSuccess;
     depth_kernel<<<(n + 255) / 256, 256, 0, s>>>(ocean, xyz, n, out);
+    return cudaGetLastError();
+}
+
+}  // namespace sfh
+
+namespace sfh {
+
+// ------------------------------------------------------ division self-check
+__device__ __forceinline__ uint64_t splitmix64(uint64_t& s)
+{
+    uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+__device__ __forceinline__ bool same_float(float x, float y)
+{
+    return __float_as_uint(x) == __float_as_uint(y) || (x != x && y != y);
+}
+
+// counts[0]: a/3 over every float bit pattern; counts[1]: a/b over random
+// pairs with b in [1e-6, 1e3] (the face-length range); counts[2]: a/b over
+// random pairs of normal floats whose quotient is normal.
+__global__ void division_check_kernel(uint64_t n_pairs, uint64_t seed, unsigned long long* counts)
+{
+    const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
+    unsigned long long bad3 = 0, badr = 0, badw = 0;
+    for (uint64_t i = tid; i < (1ull << 32); i += nthreads) {
+        float a = __uint_as_float((uint32_t)i);
+        if (!isfinite(a)) continue;
+        if (!same_float(div3(a), __fdiv_rn(a, 3.f))) ++bad3;
+    }
+    uint64_t s = seed ^ (tid * 0x632BE59BD9B4E019ull);
+    for (uint64_t i = tid; i < n_pairs; i += nthreads) {
+        uint64_t r = splitmix64(s);
+        // a: random sign/significand, exponent in [-40, 40]; b in [1e-6, 1e3]
+        uint32_t ea = (uint32_t)(127 - 40 + (r % 81));
+        float a = __uint_as_float(((uint32_t)(r >> 40) & 0x807FFFFFu) | (ea << 23));
+        float b = 1e-6f * __powf(1e9f, (float)((r >> 8) & 0xFFFFFF) * 0x1p-24f);
+        if (!same_float(div_by_rcp(a, b, __frcp_rn(b)), __fdiv_rn(a, b))) ++badr;
+        uint64_t r2 = splitmix64(s);
+        uint32_t eb = (uint32_t)(1 + (r2 % 253));
+        float w = __uint_as_float(((uint32_t)(r2 >> 32) & 0x807FFFFFu) | (eb << 23));
+        float q = __fdiv_rn(a, w);
+        if (isfinite(q) && fabsf(q) >= 0x1p-126f && fabsf(q) < 0x1p126f &&
+            !same_float(div_by_rcp(a, w, __frcp_rn(w)), q)) ++badw;
+    }
+    atomicAdd(counts + 0, bad3);
+    atomicAdd(counts + 1, badr);
+    atomicAdd(counts + 2, badw);
+}
+
+cudaError_t launch_division_check(uint64_t n_pairs, uint64_t seed, unsigned long long* counts,
+                                  cudaStream_t s)
+{
+    division_check_kernel<<<1216, 256, 0, s>>>(n_pairs, seed, counts);
     return cudaGetLastError();
 }
 

@@ -47,7 +47,7 @@ def _d3(x):
 class HydroContext:
     """Owns a hydro_ctx: device meshes, the wave grid and small buffers."""
 
-    def __init__(self, device: int = 0, cut_precision: int = abi.CUT_FP64,
+    def __init__(self, device: int = 0, cut_precision: int = abi.CUT_FP32,
                  tile_faces: int = 0, ctas_per_sm: int = 0, lib_path: str | None = None):
         self.lib = abi.load_library(lib_path)
         lib = self.lib
@@ -67,6 +67,7 @@ class HydroContext:
         if st != abi.HYDRO_OK:
             raise abi.HydroError(st, "hydro_create: " + lib.hydro_status_string(st).decode())
         self.ctx = h
+        self.cut_precision = cut_precision
         self.mesh_faces: dict[int, int] = {}
 
     def close(self) -> None:
@@ -175,6 +176,13 @@ class HydroContext:
         self._ck(self.lib.hydro_debug_face_terms(self.ctx, body.ctypes.data, C.byref(ocean),
                                                  C.byref(settings), out.ctypes.data))
         return out
+
+    def division_check(self, n_pairs: int = 1 << 26, seed: int = 1) -> list[int]:
+        """Mismatch counts of the kernels' FMA-corrected division against IEEE
+        division (x/3 over all floats, two sets of random pairs)."""
+        out = (C.c_uint64 * 3)()
+        self._ck(self.lib.hydro_debug_division_check(self.ctx, n_pairs, seed, out))
+        return list(out)
 
     def batch(self, mesh_of_body) -> "Batch":
         return Batch(self, mesh_of_body)

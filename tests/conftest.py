@@ -31,16 +31,20 @@ def built_library():
 
 @pytest.fixture(scope="session")
 def hctx(built_library):
+    """Default context: FP32 cut points in the reference's operation order."""
+    from stonefish_gb300 import abi
     from stonefish_gb300.hydro import HydroContext
     h = HydroContext()
+    assert h.cut_precision == abi.CUT_FP32
     yield h
     h.close()
 
 
 @pytest.fixture(scope="session")
-def hctx32(built_library):
+def hctx64(built_library):
+    """Context with FP64 cut points."""
     from stonefish_gb300 import abi
     from stonefish_gb300.hydro import HydroContext
-    h = HydroContext(cut_precision=abi.CUT_FP32)
+    h = HydroContext(cut_precision=abi.CUT_FP64)
     yield h
     h.close()

@@ -74,7 +74,7 @@ def test_null_context_is_rejected_without_device(built_library):
     assert lib.hydro_abi_version() == 1
     cfg = abi.Config()
     lib.hydro_config_default(C.byref(cfg))
-    assert cfg.cut_precision == abi.CUT_FP64 and cfg.tile_faces == 0
+    assert cfg.cut_precision == abi.CUT_FP32 and cfg.tile_faces == 0
     oc = abi.Ocean()
     st = abi.Settings(1, 1)
     xyz = np.zeros((3, 3), np.float32)

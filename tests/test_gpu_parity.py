@@ -2,7 +2,8 @@
 
 Bars:
 * per-face contributions: bit-identical to the oracle variant with the same
-  arithmetic (MIRROR64 for FP64 cut points, MIRROR32 for FP32 cut points);
+  arithmetic (MIRROR32 for the default FP32 cut points, which is also the
+  reference's own face arithmetic; MIRROR64 for FP64 cut points);
 * per-body wrenches: within 2e-6 of the body's force scale (torques: force
   scale x body size) of MIRROR (same face arithmetic, exact sums); the GPU's
   only difference is the summation order of FP32 face terms;
@@ -62,11 +63,11 @@ def body_lengths(sc):
 
 # ------------------------------------------------------------- face terms
 @pytest.mark.parametrize("cut", ["fp64", "fp32"])
-def test_face_terms_bit_identical(oracle, hctx, hctx32, sphere_run, cut):
-    h = hctx if cut == "fp64" else hctx32
+def test_face_terms_bit_identical(oracle, hctx, hctx64, sphere_run, cut):
+    h = hctx64 if cut == "fp64" else hctx
     variant = MIRROR64 if cut == "fp64" else MIRROR32
     sc = sphere_run
-    mid = h.upload_mesh(*sc["meshes"][0]) if h is hctx32 else sc["_ids"][0]
+    mid = h.upload_mesh(*sc["meshes"][0]) if h is hctx64 else sc["_ids"][0]
     checked = 0
     for i in range(0, 1000, 7):
         b = sc["bodies"][i:i + 1].copy()
@@ -81,9 +82,12 @@ def test_face_terms_bit_identical(oracle, hctx, hctx32, sphere_run, cut):
     assert checked > 50
 
 
-def test_face_terms_every_sign_pattern(oracle, hctx):
+@pytest.mark.parametrize("cut", ["fp64", "fp32"])
+def test_face_terms_every_sign_pattern(oracle, hctx, hctx64, cut):
     """One triangle placed so that each corner is above, on, or below the
     surface: all 27 depth-sign patterns, bit-identical terms."""
+    h = hctx64 if cut == "fp64" else hctx
+    variant = MIRROR64 if cut == "fp64" else MIRROR32
     xyz = np.array([[0.0, 0.0, 0.0], [1.0, 0.1, 0.0], [0.2, 1.0, 0.0]], dtype=np.float32)
     faces = np.array([[0, 1, 2]], dtype=np.uint32)
     levels = (-0.3, 0.0, 0.25)
@@ -93,13 +97,13 @@ def test_face_terms_every_sign_pattern(oracle, hctx):
             for c in levels:
                 p = xyz.copy()
                 p[:, 2] = (a, b_, c)
-                mid = hctx.upload_mesh(p, faces)
+                mid = h.upload_mesh(p, faces)
                 body = scenarios.fill_bodies(1, np.eye(3)[None], np.zeros((1, 3)),
                                              np.array([[0.3, -0.2, 0.1]]), np.array([[0.1, 0.2, -0.3]]),
                                              np.ones((1, 3)), 1.0, 1.0, (1, 1, 1), (.1, .1, .1), mid)
-                gpu = hctx.face_terms(body, oc, scenarios.settings())
+                gpu = h.face_terms(body, oc, scenarios.settings())
                 T = body_transform(body)
-                cpu = oracle.face_terms(MIRROR64, scenarios.settings(), (p, faces), oc, T, T,
+                cpu = oracle.face_terms(variant, scenarios.settings(), (p, faces), oc, T, T,
                                         body["v"][0], body["omega"][0])
                 assert np.array_equal(gpu, cpu), (a, b_, c)
 
@@ -108,7 +112,7 @@ def test_face_terms_every_sign_pattern(oracle, hctx):
 def test_single_sphere_matches_mirror_and_fp64(oracle, hctx, sphere_run):
     sc = sphere_run
     gpu = run_batch(hctx, sc)
-    mir = run_oracle(oracle, MIRROR64, sc)
+    mir = run_oracle(oracle, MIRROR32, sc)
     r32 = run_oracle(oracle, REF32, sc)
     r64 = run_oracle(oracle, REF64, sc)
     assert np.array_equal(gpu["position"], mir["position"])
@@ -134,7 +138,7 @@ def test_single_sphere_fully_submerged(oracle, hctx):
     io0 = scenarios.new_wrenches(200)
     io0["Vsub"] = 0.25
     gpu = run_batch(hctx, sc, io=io0.copy())
-    mir = run_oracle(oracle, MIRROR64, sc, io=io0.copy())
+    mir = run_oracle(oracle, MIRROR32, sc, io=io0.copy())
     assert np.array_equal(gpu["position"], mir["position"])
     inside = gpu["position"] == abi.INSIDE
     assert inside.sum() > 20
@@ -179,7 +183,7 @@ def test_static_entry_points(oracle, hctx, sphere_run):
                 d["Fb"][:] = 1.5
                 d["Vsub"][:] = 0.5
             hctx.surface_forces(settings, sc["_ids"][0], sc["ocean"], T_CG, T_C, b["v"][0], b["omega"][0], g)
-            oracle.surface_forces(MIRROR64, settings, mesh, sc["ocean"], T_CG, T_C, b["v"][0], b["omega"][0], c)
+            oracle.surface_forces(MIRROR32, settings, mesh, sc["ocean"], T_CG, T_C, b["v"][0], b["omega"][0], c)
             S = max(np.linalg.norm(c["Fb"]), np.linalg.norm(c["Fdq"]), np.linalg.norm(c["Fdf"]), 1e-30)
             for k in ("Fb", "Fdq", "Fdf"):
                 assert np.linalg.norm(g[k] - c[k]) <= TOL_MIRROR * S, k
@@ -189,7 +193,7 @@ def test_static_entry_points(oracle, hctx, sphere_run):
             assert g["Vsub"][0] == pytest.approx(c["Vsub"][0], rel=TOL_MIRROR, abs=1e-12)
         g, c = io_dict(), io_dict()
         hctx.submerged_forces(sc["_ids"][0], sc["ocean"], T_CG, T_C, b["v"][0], b["omega"][0], g)
-        oracle.submerged_forces(MIRROR64, mesh, sc["ocean"], T_CG, T_C, b["v"][0], b["omega"][0], c)
+        oracle.submerged_forces(MIRROR32, mesh, sc["ocean"], T_CG, T_C, b["v"][0], b["omega"][0], c)
         S = max(np.linalg.norm(c["Fdq"]), np.linalg.norm(c["Fdf"]))
         for k in ("Fdq", "Fdf", "Tdq", "Tdf"):
             assert np.linalg.norm(g[k] - c[k]) <= TOL_MIRROR * S, k
@@ -249,7 +253,7 @@ def test_jet_and_pipe_currents(oracle, hctx, sphere_run):
     p.radius, p.radius2, p.length, p.speed, p.gamma = 0.5, 1.0, 5.0, 1.5, 0.7
     sub = {"meshes": sc["meshes"], "bodies": sc["bodies"][:200].copy(), "ocean": oc, "_ids": sc["_ids"]}
     gpu = run_batch(hctx, sub)
-    mir = run_oracle(oracle, MIRROR64, sub)
+    mir = run_oracle(oracle, MIRROR32, sub)
     cross = gpu["position"] == abi.CROSSING_SURFACE
     e = scaled_errors(gpu, mir, body_lengths(sub))
     # exp/pow of CUDA and the host libm may differ by an ulp in FP64
@@ -258,10 +262,12 @@ def test_jet_and_pipe_currents(oracle, hctx, sphere_run):
 
 
 # ------------------------------------------------------------- batches
-def test_mixed_batch_matches_mirror(oracle, hctx):
-    sc = upload(hctx, scenarios.mixed_batch(n_bodies=96, seed=11, scale_faces=0.1))
-    gpu = run_batch(hctx, sc)
-    mir = run_oracle(oracle, MIRROR64, sc)
+@pytest.mark.parametrize("cut", ["fp64", "fp32"])
+def test_mixed_batch_matches_mirror(oracle, hctx, hctx64, cut):
+    h = hctx64 if cut == "fp64" else hctx
+    sc = upload(h, scenarios.mixed_batch(n_bodies=96, seed=11, scale_faces=0.1))
+    gpu = run_batch(h, sc)
+    mir = run_oracle(oracle, MIRROR64 if cut == "fp64" else MIRROR32, sc)
     assert np.array_equal(gpu["position"], mir["position"])
     act = gpu["position"] != abi.OUTSIDE
     e = scaled_errors(gpu, mir, body_lengths(sc))
@@ -286,13 +292,13 @@ def test_host_and_device_entry_points_agree(hctx):
     torch.cuda.synchronize()
     dev = d_w.cpu().numpy().view(abi.WRENCH_DTYPE)
     assert dev.tobytes() == host.tobytes()
-    assert bt.last_launches() == 1
+    assert bt.last_launches() == 3          # prep, chunk, finalise
     bt.close()
 
 
 @pytest.mark.parametrize("cut", ["fp64", "fp32"])
-def test_waves_batch(oracle, hctx, hctx32, cut):
-    h = hctx if cut == "fp64" else hctx32
+def test_waves_batch(oracle, hctx, hctx64, cut):
+    h = hctx64 if cut == "fp64" else hctx
     sc = scenarios.torpedo_waves(n_bodies=64, faces=2000, grid_n=256)
     upload(h, sc)
     gpu = run_batch(h, sc)
@@ -314,10 +320,10 @@ def test_waves_batch(oracle, hctx, hctx32, cut):
     assert np.array_equal(d, ref)
 
 
-def test_cut_fp32_matches_mirror32(oracle, hctx32):
-    sc = upload(hctx32, scenarios.single_sphere(steps=300, seed=9))
-    gpu = run_batch(hctx32, sc)
-    mir = run_oracle(oracle, MIRROR32, sc)
+def test_cut_fp64_matches_mirror64(oracle, hctx64):
+    sc = upload(hctx64, scenarios.single_sphere(steps=300, seed=9))
+    gpu = run_batch(hctx64, sc)
+    mir = run_oracle(oracle, MIRROR64, sc)
     cross = gpu["position"] == abi.CROSSING_SURFACE
     e = scaled_errors(gpu, mir, body_lengths(sc))
     for k, v in e.items():
