@@ -306,10 +306,14 @@ hydro_status hydro_fluid_position(hydro_ctx* ctx, const hydro_ocean* ocean,
  * as the batched kernel: out receives n_faces * 23 floats in uploaded face
  * order, laid out Fb[3] Tb[3] Fdq[3] Tdq[3] Fdf[3] Tdf[3] Swet V6 CB6[3]
  * (V6 = 6 x the face's fan-tetra volume, CB6 = V6-weighted centroid).  For
- * validating the face arithmetic against a CPU restatement bit for bit. */
+ * validating the face arithmetic against a CPU restatement bit for bit.
+ * packed != 0 evaluates pairs of consecutive fully submerged faces on the
+ * packed FP32 path that the batched kernel uses; packed == 0 evaluates every
+ * face on the scalar path. */
 hydro_status hydro_debug_face_terms(hydro_ctx* ctx, const hydro_body* body,
                                     const hydro_ocean* ocean,
-                                    const hydro_settings* settings, float* out);
+                                    const hydro_settings* settings, int32_t packed,
+                                    float* out);
 
 /* Checks on the GPU that the division the kernels use for x/|n| and x/3
  * (a correctly rounded reciprocal plus one FMA correction) returns the bits
@@ -318,6 +322,16 @@ hydro_status hydro_debug_face_terms(hydro_ctx* ctx, const hydro_body* body,
  * normal floats.  mismatches[0..2] receive the three mismatch counts. */
 hydro_status hydro_debug_division_check(hydro_ctx* ctx, uint64_t n_pairs, uint64_t seed,
                                         uint64_t mismatches[3]);
+
+/* The division check above plus a check that the packed FP32 pair
+ * instructions the kernels use for two faces at a time (mul, add, sub, fma
+ * .rn.f32x2) return, in each half, the bits of the scalar IEEE operation:
+ * packed[0..3] receive the mismatch counts over n_pairs random operand sets,
+ * examples[4k..4k+3] one failing set (a, b, c, result) of op k.  packed and
+ * examples may be NULL. */
+hydro_status hydro_debug_arith_check(hydro_ctx* ctx, uint64_t n_pairs, uint64_t seed,
+                                     uint64_t division[3], uint64_t packed[4],
+                                     float examples[16]);
 
 #ifdef __cplusplus
 }

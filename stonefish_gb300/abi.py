@@ -169,6 +169,7 @@ def _declare(lib: C.CDLL) -> None:
         "hydro_correct_forces": (i32, [vp, C.POINTER(Ocean), d, d, d, d, d, d, d]),
         "hydro_fluid_position": (i32, [vp, C.POINTER(Ocean), d, d, C.POINTER(i32)]),
         "hydro_debug_division_check": (i32, [vp, C.c_uint64, C.c_uint64, vp]),
+        "hydro_debug_arith_check": (i32, [vp, C.c_uint64, C.c_uint64, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

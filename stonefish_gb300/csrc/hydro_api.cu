@@ -71,6 +71,7 @@ struct hydro_batch {
     double* partials_d = nullptr;
     BodyParams* bparams_d = nullptr;
     unsigned* err_d = nullptr;
+    uint8_t* chunk_active_d = nullptr;
     hydro_body* bodies_d = nullptr;    // staging for the host-buffer entry point
     hydro_wrench* io_d = nullptr;
     cudaStream_t stream = nullptr;
@@ -203,7 +204,8 @@ OceanDev make_ocean(const hydro_ctx* ctx, const hydro_ocean* o)
 uint32_t tiles_per_chunk(const hydro_ctx* ctx)
 {
     uint32_t faces = ctx->cfg.tile_faces ? ctx->cfg.tile_faces : 4096u;
-    return std::max<uint32_t>(1u, (faces + kTileFaces - 1) / kTileFaces);
+    return std::min<uint32_t>((uint32_t)kMaxTilesPerChunk,
+                              std::max<uint32_t>(1u, (faces + kTileFaces - 1) / kTileFaces));
 }
 
 void batch_free(hydro_batch* b)
@@ -214,6 +216,7 @@ void batch_free(hydro_batch* b)
     cudaFree(b->partials_d);
     cudaFree(b->bparams_d);
     cudaFree(b->err_d);
+    cudaFree(b->chunk_active_d);
     cudaFree(b->bodies_d);
     cudaFree(b->io_d);
     if (b->stream) cudaStreamDestroy(b->stream);
@@ -272,6 +275,7 @@ hydro_status batch_build(hydro_ctx* ctx, const hydro_mesh_id* mesh_of_body, uint
     BK(cudaMalloc(&b->partials_d, chunks.size() * kPartialStride * sizeof(double)));
     BK(cudaMalloc(&b->bparams_d, n * sizeof(BodyParams)));
     BK(cudaMalloc(&b->err_d, 256));
+    BK(cudaMalloc(&b->chunk_active_d, chunks.size()));
     BK(cudaMemcpy(b->chunks_d, chunks.data(), chunks.size() * sizeof(ChunkDesc), cudaMemcpyHostToDevice));
     BK(cudaMemcpy(b->binfo_d, info.data(), n * sizeof(BodyInfo), cudaMemcpyHostToDevice));
     BK(cudaMemset(b->err_d, 0, 256));
@@ -298,6 +302,7 @@ hydro_status batch_launch(hydro_batch* b, const hydro_body* d_bodies, const hydr
     P.bparams = b->bparams_d;
     P.err = b->err_d;
     P.work = b->err_d + 32;
+    P.chunk_active = b->chunk_active_d;
     P.n_bodies = b->n_bodies;
     P.n_chunks = b->n_chunks;
     P.ocean = make_ocean(ctx, ocean);
@@ -461,17 +466,16 @@ hydro_status hydro_mesh_upload(hydro_ctx* ctx, const void* vertex_data, size_t v
     // kTileFaces faces or kTileVerts distinct vertices.
     std::vector<int32_t> local(n_vertices, -1);
     std::vector<uint32_t> tv;              // global ids of the open tile's vertices
-    std::vector<uint16_t> ti;              // local indices of the open tile's faces
+    std::vector<uint32_t> ti;              // packed local indices of the open tile's faces
     std::vector<char> host;                // all tile blocks of this mesh
     struct Pending { size_t offset; uint16_t nv, nf; uint32_t first_face; };
     std::vector<Pending> pend;
     uint32_t tile_first_face = 0;
     auto close_tile = [&](uint32_t next_face) {
         if (ti.empty()) return;
-        const uint32_t nv = (uint32_t)tv.size(), nf = (uint32_t)(ti.size() / 3);
+        const uint32_t nv = (uint32_t)tv.size(), nf = (uint32_t)ti.size();
         const uint32_t nvp = (nv + 3) & ~3u;
-        size_t bytes = (size_t)nvp * 12 + (size_t)nf * 6;
-        bytes = (bytes + 15) & ~size_t(15);
+        const size_t bytes = tile_bytes(nv, nf);
         size_t off = host.size();
         host.resize(off + bytes, 0);
         float* f = reinterpret_cast<float*>(host.data() + off);
@@ -482,7 +486,7 @@ hydro_status hydro_mesh_upload(hydro_ctx* ctx, const void* vertex_data, size_t v
             f[nvp + k] = p[1];
             f[2 * nvp + k] = p[2];
         }
-        std::memcpy(host.data() + off + (size_t)nvp * 12, ti.data(), ti.size() * 2);
+        std::memcpy(host.data() + off + (size_t)nvp * 12, ti.data(), ti.size() * 4);
         pend.push_back(Pending{off, (uint16_t)nv, (uint16_t)nf, tile_first_face});
         for (uint32_t g : tv) local[g] = -1;
         tv.clear();
@@ -497,15 +501,17 @@ hydro_status hydro_mesh_upload(hydro_ctx* ctx, const void* vertex_data, size_t v
             for (int j = 0; j < k; ++j) dup |= (fi[j] == fi[k]);
             if (local[fi[k]] < 0 && !dup) ++fresh;
         }
-        if (ti.size() / 3 + 1 > (size_t)kTileFaces || tv.size() + fresh > (size_t)kTileVerts)
+        if (ti.size() + 1 > (size_t)kTileFaces || tv.size() + fresh > (size_t)kTileVerts)
             close_tile(f);
+        uint32_t word = 0;
         for (int k = 0; k < 3; ++k) {
             if (local[fi[k]] < 0) {
                 local[fi[k]] = (int32_t)tv.size();
                 tv.push_back(fi[k]);
             }
-            ti.push_back((uint16_t)local[fi[k]]);
+            word |= (uint32_t)local[fi[k]] << (9 * k);
         }
+        ti.push_back(word);
     }
     close_tile(n_faces);
 
@@ -778,7 +784,7 @@ hydro_status hydro_fluid_position(hydro_ctx* ctx, const hydro_ocean* ocean, cons
 
 // Per-face surface-loop terms of one body (n_faces * 23 floats, host).
 hydro_status hydro_debug_face_terms(hydro_ctx* ctx, const hydro_body* body, const hydro_ocean* ocean,
-                                    const hydro_settings* settings, float* out)
+                                    const hydro_settings* settings, int32_t packed, float* out)
 {
     if (!ctx) return HYDRO_ERR_INVALID_ARG;
     std::lock_guard<std::recursive_mutex> lk(ctx->mu);
@@ -798,7 +804,8 @@ hydro_status hydro_debug_face_terms(hydro_ctx* ctx, const hydro_body* body, cons
     CK(ctx, cudaMemcpyAsync(db, body, sizeof(hydro_body), cudaMemcpyHostToDevice, ctx->stream));
     SettingsDev sd{settings->damping_forces ? 1 : 0, settings->realistic_buoyancy ? 1 : 0};
     cudaError_t e = launch_face_terms(ctx->tiles_d, m.first_tile, m.n_tiles, db, make_ocean(ctx, ocean), sd,
-                                      ctx->cfg.cut_precision == HYDRO_CUT_FP64, dout, ctx->stream);
+                                      ctx->cfg.cut_precision == HYDRO_CUT_FP64, packed ? 1 : 0, dout,
+                                      ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "face terms kernel");
     CK(ctx, cudaMemcpyAsync(out, dout, terms, cudaMemcpyDeviceToHost, ctx->stream));
     CK(ctx, cudaStreamSynchronize(ctx->stream));
@@ -808,20 +815,37 @@ hydro_status hydro_debug_face_terms(hydro_ctx* ctx, const hydro_body* body, cons
 hydro_status hydro_debug_division_check(hydro_ctx* ctx, uint64_t n_pairs, uint64_t seed,
                                        uint64_t mismatches[3])
 {
+    return hydro_debug_arith_check(ctx, n_pairs, seed, mismatches, nullptr, nullptr);
+}
+
+hydro_status hydro_debug_arith_check(hydro_ctx* ctx, uint64_t n_pairs, uint64_t seed,
+                                     uint64_t division[3], uint64_t packed[4], float examples[16])
+{
     if (!ctx) return HYDRO_ERR_INVALID_ARG;
     std::lock_guard<std::recursive_mutex> lk(ctx->mu);
-    if (!mismatches) return fail(ctx, HYDRO_ERR_INVALID_ARG, "division check: null output");
+    if (!division) return fail(ctx, HYDRO_ERR_INVALID_ARG, "arithmetic check: null output");
     if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, HYDRO_ERR_DEVICE, "cudaSetDevice");
-    hydro_status st = ensure_small(ctx, 64);
+    hydro_status st = ensure_small(ctx, 256);
     if (st != HYDRO_OK) return st;
     unsigned long long* d = static_cast<unsigned long long*>(ctx->small_d);
-    CK(ctx, cudaMemsetAsync(d, 0, 3 * sizeof(unsigned long long), ctx->stream));
+    float* dex = reinterpret_cast<float*>(d + 8);
+    CK(ctx, cudaMemsetAsync(d, 0, 8 * sizeof(unsigned long long) + 16 * sizeof(float), ctx->stream));
     cudaError_t e = launch_division_check(n_pairs, seed, d, ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "division check kernel");
-    unsigned long long h[3];
+    if (packed) {
+        e = launch_packed_check(n_pairs, seed + 1, d, dex, ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "packed check kernel");
+    }
+    unsigned long long h[8];
+    float hex[16];
     CK(ctx, cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(ctx, cudaMemcpyAsync(hex, dex, sizeof(hex), cudaMemcpyDeviceToHost, ctx->stream));
     CK(ctx, cudaStreamSynchronize(ctx->stream));
-    for (int i = 0; i < 3; ++i) mismatches[i] = h[i];
+    for (int i = 0; i < 3; ++i) division[i] = h[i];
+    if (packed)
+        for (int i = 0; i < 4; ++i) packed[i] = h[3 + i];
+    if (examples)
+        for (int i = 0; i < 16; ++i) examples[i] = hex[i];
     return HYDRO_OK;
 }
 

@@ -19,10 +19,10 @@
 namespace sfh {
 
 // ------------------------------------------------------------ constants
-constexpr int kBlock = 256;          // threads per CTA
+constexpr int kBlock = 192;          // compute threads per CTA
 constexpr int kWarps = kBlock / 32;
-constexpr int kTileFaces = 512;      // max faces per tile
-constexpr int kTileVerts = 512;      // max distinct vertices per tile
+constexpr int kTileFaces = 384;      // max faces per tile (64 per compute warp)
+constexpr int kTileVerts = 384;      // max distinct vertices per tile (< 512: 9-bit indices)
 constexpr int kQ = 23;               // accumulated quantities per body
 constexpr int kPartialStride = 24;   // doubles per chunk partial (23 + status)
 constexpr int kFlushFaces = 8;       // faces a thread sums in FP32 before a flush
@@ -40,14 +40,25 @@ enum : int { OP_BODY = 0, OP_SURFACE = 1, OP_SUBMERGED = 2 };
 
 // ------------------------------------------------------------- data layout
 // One tile of a mesh: nv vertices stored as x[nvp], y[nvp], z[nvp] floats
-// (nvp = nv rounded up to 4) followed by 3*nf uint16 local indices, padded to
-// 16 bytes; `first_face` is the tile's first face in the uploaded order.
+// (nvp = nv rounded up to 4) followed by one uint32 per face holding its
+// three local vertex indices (9 bits each: i0 | i1 << 9 | i2 << 18), padded
+// to 16 bytes; `first_face` is the tile's first face in the uploaded order.
 struct TileDesc {
     const float* block;
     uint16_t nv;
     uint16_t nf;
     uint32_t first_face;
 };
+
+// Bytes of one tile block: x, y, z (nv rounded up to 4 each) and one packed
+// index word per face, rounded up to 16 (the TMA size rule).
+__host__ __device__ __forceinline__ uint32_t tile_bytes(uint32_t nv, uint32_t nf)
+{
+    const uint32_t nvp = (nv + 3u) & ~3u;
+    return (nvp * 12u + nf * 4u + 15u) & ~15u;
+}
+
+constexpr int kMaxTilesPerChunk = 16;
 
 // One work item: tiles [first_tile, first_tile + n_tiles) of one body.
 struct ChunkDesc {
@@ -123,6 +134,10 @@ __device__ __forceinline__ float div_by_rcp(float a, float b, float y)
 // a / 3 with RN(1/3) = 0x1.555556p-2
 __device__ __forceinline__ float div3(float a) { return div_by_rcp(a, 3.f, 0x1.555556p-2f); }
 
+#ifdef HYDRO_FAST_MATH
+__device__ __forceinline__ v3 dvs_rcp(v3 a, float b) { const float y = 1.f / b; return mul(a, y); }
+__device__ __forceinline__ v3 dvs3(v3 a) { return mul(a, 0x1.555556p-2f); }
+#else
 __device__ __forceinline__ v3 dvs_rcp(v3 a, float b)
 {
     const float y = __frcp_rn(b);
@@ -130,6 +145,7 @@ __device__ __forceinline__ v3 dvs_rcp(v3 a, float b)
 }
 
 __device__ __forceinline__ v3 dvs3(v3 a) { return mk(div3(a.x), div3(a.y), div3(a.z)); }
+#endif
 
 // Per-body FP32 parameters (glMatrixFromTransform / glVectorFromVector casts,
 // Library/src/graphics/OpenGLDataStructs.cpp:148-171).

@@ -18,6 +18,7 @@ struct KParams {
     double* partials;        // n_chunks * kPartialStride
     unsigned* err;           // per-launch error word (bit 0: a bounded wait timed out)
     unsigned* work;          // chunk counter of the persistent kernel
+    uint8_t* chunk_active;   // per chunk: 1 when its body runs a face loop
     uint32_t n_bodies;
     uint32_t n_chunks;
     OceanDev ocean;
@@ -45,10 +46,12 @@ cudaError_t launch_step(const KParams& P, LaunchShape shape, int cut64, cudaStre
                         uint32_t* launches);
 
 // Per-face surface-loop terms of one body for the parity tests: out holds
-// n_faces * kQ floats in uploaded face order.
+// n_faces * kQ floats in uploaded face order.  packed = 1 sends pairs of
+// fully submerged faces through the packed FP32 path, 0 uses the scalar
+// path for every face.
 cudaError_t launch_face_terms(const TileDesc* tiles, uint32_t first_tile, uint32_t n_tiles,
                              const hydro_body* body, OceanDev ocean, SettingsDev st,
-                             int cut64, float* out, cudaStream_t s);
+                             int cut64, int packed, float* out, cudaStream_t s);
 
 // CorrectHydrodynamicForces on 4 vectors (io: Fdq, Tdq, Fdf, Tdf), one thread.
 cudaError_t launch_correct(double density, double* io12, const double* Cd, const double* Cf,
@@ -60,6 +63,11 @@ cudaError_t launch_fluid_position(OceanDev ocean, const double* aabb6, int* out,
 // counts[0] a/3 over all floats, counts[1] and counts[2] random pairs.
 cudaError_t launch_division_check(uint64_t n_pairs, uint64_t seed, unsigned long long* counts,
                                   cudaStream_t s);
+
+// Counts mismatches of the packed f32x2 ops against scalar IEEE ops in
+// counts[3..6] (mul, add, sub, fma); ex receives one failing case per op.
+cudaError_t launch_packed_check(uint64_t n, uint64_t seed, unsigned long long* counts, float* ex,
+                                cudaStream_t s);
 
 cudaError_t launch_depth(OceanDev ocean, const float* xyz, uint32_t n, float* out, cudaStream_t s);
 

@@ -26,6 +26,7 @@
 #include <cuda_runtime.h>
 
 #include "hydro_internal.h"
+#include "hydro_pair.cuh"
 
 namespace sfh {
 
@@ -321,29 +322,52 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar)
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-// One bounded try: returns true when the phase with `parity` has completed;
-// the hardware may suspend the thread for up to ~1 us inside the call.
+// One try: true when the phase with `parity` has completed (the hardware
+// may hold the thread for a short, implementation-defined time).
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
 {
     uint32_t ok;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity), "r"(1000u)
+        : "r"(smem_u32(bar)), "r"(parity)
         : "memory");
     return ok != 0u;
 }
 
-// Bounded wait (about two seconds): false means it gave up.
-constexpr uint32_t kWaitLimit = 1u << 21;
+__device__ __forceinline__ uint64_t global_ns()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Bounded wait: gives up (returns false) after about two seconds.
+constexpr uint64_t kWaitLimitNs = 2000000000ull;
 
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
 {
-    for (uint32_t i = 0; i < kWaitLimit; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = global_ns();
+    for (;;) {
+        for (int i = 0; i < 64; ++i)
+            if (mbar_try_wait(bar, parity)) return true;
+        if (global_ns() - t0 > kWaitLimitNs) return false;
+    }
+}
+
+// The producer's wait for a free stage: it is ahead of the compute warps,
+// so it sleeps between polls instead of taking their issue slots.
+__device__ __forceinline__ bool mbar_wait_sleep(uint64_t* bar, uint32_t parity)
+{
+    const uint64_t t0 = global_ns();
+    for (;;) {
         if (mbar_try_wait(bar, parity)) return true;
-    return false;
+        __nanosleep(200);
+        if (global_ns() - t0 > kWaitLimitNs) return false;
+    }
 }
 
 // 1-D bulk copy global -> shared (TMA), completion counted on `bar`.
@@ -387,8 +411,11 @@ __global__ void prep_kernel(const KParams P)
     }
     if (b >= P.n_bodies) return;
     BodyParams B;
-    body_prologue(P.bodies + b, P.binfo[b].mesh, P.op, P.ocean, P.st, B);
+    const BodyInfo bi = P.binfo[b];
+    body_prologue(P.bodies + b, bi.mesh, P.op, P.ocean, P.st, B);
     P.bparams[b] = B;
+    const uint8_t active = (B.loop != LOOP_NONE) ? 1 : 0;
+    for (uint32_t c = 0; c < bi.n_chunks; ++c) P.chunk_active[bi.first_chunk + c] = active;
 }
 
 // ------------------------------------------------------------ main kernel
@@ -397,8 +424,8 @@ __global__ void prep_kernel(const KParams P)
 // copies.  The producer claims chunks from a global counter (reset by the
 // prep kernel) and skips the chunks of bodies without a face loop; which CTA
 // takes a chunk does not change the chunk's result.
-constexpr int kStages = 4;
-constexpr int kStageRaw = kTileVerts * 12 + kTileFaces * 6;   // 9216 bytes
+constexpr int kStages = 8;
+constexpr int kStageRaw = kTileVerts * 12 + kTileFaces * 4;   // 6144 bytes
 constexpr int kThreads = kBlock + 32;
 
 enum : int { ITEM_FIRST = 1, ITEM_LAST = 2, ITEM_END = 4 };
@@ -417,7 +444,7 @@ struct __align__(128) StageBuf {
 
 struct __align__(128) ChunkSmem {
     StageBuf stage[kStages];
-    float4 verts[kTileVerts];
+    float4 verts[2][kTileVerts];      // transformed vertices, double-buffered
     float2 red[kWarps][32];
     uint16_t flist[kWarps][64];       // per-warp compacted face lists
     ItemMeta meta[kStages];
@@ -431,37 +458,47 @@ __device__ __forceinline__ void producer(const KParams& P, ChunkSmem& S)
 {
     uint32_t item = 0;
     bool ok = true;
-    while (ok) {
-        const uint32_t c = atomicAdd(P.work, 1u);      // dynamic: next unclaimed chunk
-        if (c >= P.n_chunks) break;
+    // claims run one chunk ahead so that the atomic's latency overlaps work
+    uint32_t next = atomicAdd(P.work, 1u);
+    while (ok && next < P.n_chunks) {
+        const uint32_t c = next;
         const ChunkDesc ch = P.chunks[c];
-        const int loop = P.bparams[ch.body].loop;
-        if (loop == LOOP_NONE || ch.n_tiles == 0) continue;
-        for (uint32_t t = 0; t < ch.n_tiles; ++t, ++item) {
+        const uint8_t active = P.chunk_active[c];
+        next = atomicAdd(P.work, 1u);
+        if (!active) continue;
+        const uint32_t nt = ch.n_tiles < (uint32_t)kMaxTilesPerChunk ? ch.n_tiles : (uint32_t)kMaxTilesPerChunk;
+        TileDesc td[kMaxTilesPerChunk];
+#pragma unroll
+        for (int t = 0; t < kMaxTilesPerChunk; ++t)
+            if ((uint32_t)t < nt) td[t] = P.tiles[ch.first_tile + t];
+#pragma unroll 1
+        for (uint32_t t = 0; t < nt; ++t, ++item) {
             const int s = (int)(item % kStages);
-            if (item >= (uint32_t)kStages && !mbar_wait(&S.empty[s], ((item / kStages) - 1u) & 1u)) {
+            if (item >= (uint32_t)kStages && !mbar_wait_sleep(&S.empty[s], ((item / kStages) - 1u) & 1u)) {
                 atomicOr(P.err, 1u);
                 ok = false;
                 break;
             }
-            const TileDesc td = P.tiles[ch.first_tile + t];
-            const uint32_t nvp = (td.nv + 3u) & ~3u;
-            const uint32_t bytes = (nvp * 12u + td.nf * 6u + 15u) & ~15u;
+            TileDesc d = td[0];
+#pragma unroll
+            for (int k = 1; k < kMaxTilesPerChunk; ++k)
+                if ((uint32_t)k == t) d = td[k];
+            const uint32_t bytes = tile_bytes(d.nv, d.nf);
             ItemMeta m;
             m.chunk = c;
-            m.flags = (t == 0 ? ITEM_FIRST : 0) | (t + 1 == ch.n_tiles ? ITEM_LAST : 0);
-            m.nv = td.nv;
-            m.nf = td.nf;
+            m.flags = (t == 0 ? ITEM_FIRST : 0) | (t + 1 == nt ? ITEM_LAST : 0);
+            m.nv = d.nv;
+            m.nf = d.nf;
             m.pad = 0;
             S.meta[s] = m;
             mbar_arrive_expect_tx(&S.full[s], bytes + (uint32_t)sizeof(BodyParams));
             tma_copy(&S.stage[s].bp, P.bparams + ch.body, (uint32_t)sizeof(BodyParams), &S.full[s]);
-            tma_copy(S.stage[s].raw, td.block, bytes, &S.full[s]);
+            tma_copy(S.stage[s].raw, d.block, bytes, &S.full[s]);
         }
     }
     // end of stream
     const int s = (int)(item % kStages);
-    if (item >= (uint32_t)kStages && !mbar_wait(&S.empty[s], ((item / kStages) - 1u) & 1u)) {
+    if (item >= (uint32_t)kStages && !mbar_wait_sleep(&S.empty[s], ((item / kStages) - 1u) & 1u)) {
         atomicOr(P.err, 1u);
     }
     ItemMeta m{0u, ITEM_END, 0, 0, 0u};
@@ -473,9 +510,95 @@ __device__ __forceinline__ void producer(const KParams& P, ChunkSmem& S)
     // the end marker could be armed, so it is skipped.
     const uint32_t first = item >= (uint32_t)kStages ? item - (uint32_t)kStages + 1u : 0u;
     for (uint32_t i = first; i < item; ++i)
-        if (!mbar_wait(&S.full[i % kStages], (i / kStages) & 1u)) atomicOr(P.err, 1u);
+        if (!mbar_wait_sleep(&S.full[i % kStages], (i / kStages) & 1u)) atomicOr(P.err, 1u);
 }
 
+// Transforms the vertices of the tile in stage `st` into `out` (x, y, z,
+// depth), each vertex once.
+template <bool WAVES>
+__device__ __forceinline__ void transform_tile(const KParams& P, const StageBuf& st, const ItemMeta& m,
+                                               float4* out)
+{
+    const float* raw = reinterpret_cast<const float*>(st.raw);
+    const int nv = m.nv, nvp = (nv + 3) & ~3;
+    float TC[12];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) TC[k] = st.bp.TC[k];
+    for (int v = threadIdx.x; v < nv; v += kBlock) {
+        v3 p = xform(TC, raw[v], raw[nvp + v], raw[2 * nvp + v]);
+        float d = WAVES ? depth_at(P.ocean, p.x, p.y, p.z) : p.z;
+        out[v] = make_float4(p.x, p.y, p.z, d);
+    }
+}
+
+// Faces of one tile: per-warp compaction, then the packed path for pairs of
+// fully submerged faces and the scalar path for straddling faces.
+template <bool CUT64, bool WAVES>
+__device__ __forceinline__ void tile_faces(const KParams& P, const StageBuf& st, const ItemMeta& m,
+                                           const float4* verts, uint16_t* list, Acc& acc)
+{
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const BodyParams& B = st.bp;
+    BodyParams Bl;
+    Bl.p = B.p; Bl.p0 = B.p0; Bl.v = B.v; Bl.omega = B.omega;
+    Bl.loop = B.loop; Bl.buoyancy = B.buoyancy; Bl.damping = B.damping;
+    const int nf = m.nf, nvp = (m.nv + 3) & ~3;
+    const uint32_t* idx = reinterpret_cast<const uint32_t*>(reinterpret_cast<const float*>(st.raw) + 3 * nvp);
+    // Warp w takes faces (k*32 + lane)*kWarps + w, k = 0, 1: a spread sample
+    // of the tile, so that the warps get similar work.  Its faces are
+    // compacted (deterministically, by ballot) into a list of fully
+    // submerged faces and a list of straddling faces.  The first list is
+    // evaluated two faces per lane on the packed FP32 pipe (faces
+    // list[lane] and list[lane + 32]), the second face by face.
+    int nfull = 0, ncut = 0;
+    const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+        const int f = (k * 32 + lane) * kWarps + warp;
+        int cls = 0;
+        if (f < nf) {
+            if (Bl.loop == LOOP_SURFACE) {
+                const uint32_t w = idx[f];
+                cls = face_class(verts[w & 511u].w, verts[(w >> 9) & 511u].w, verts[w >> 18].w);
+            } else {
+                cls = 1;
+            }
+        }
+        const unsigned mf = __ballot_sync(0xffffffffu, cls == 1);
+        const unsigned mc = __ballot_sync(0xffffffffu, cls == 2);
+        if (cls == 1) list[nfull + __popc(mf & lt)] = (uint16_t)f;
+        if (cls == 2) list[63 - (ncut + __popc(mc & lt))] = (uint16_t)f;
+        nfull += __popc(mf);
+        ncut += __popc(mc);
+    }
+    __syncwarp();
+    if (lane < nfull) {
+        const bool hasB = lane + 32 < nfull;
+        const uint32_t wa = idx[list[lane]];
+        const uint32_t wb = idx[list[hasB ? lane + 32 : lane]];
+        const P3 p1 = corners(verts[wa & 511u], verts[wb & 511u]);
+        const P3 p2 = corners(verts[(wa >> 9) & 511u], verts[(wb >> 9) & 511u]);
+        const P3 p3 = corners(verts[wa >> 18], verts[wb >> 18]);
+        const BodyPair Bp = body_pair(Bl, P.ocean);
+        if (Bl.loop == LOOP_SURFACE) face_full2<WAVES>(P.ocean, Bl, Bp, acc, p1, p2, p3, hasB);
+        else face_submerged2(P.ocean, Bp, acc, p1, p2, p3, hasB);
+    }
+    for (int i = lane; i < ncut; i += 32) {
+        const uint32_t w = idx[list[63 - i]];
+        const float4 q1 = verts[w & 511u];
+        const float4 q2 = verts[(w >> 9) & 511u];
+        const float4 q3 = verts[w >> 18];
+        face_cut<CUT64, WAVES>(P.ocean, Bl, acc, mk(q1.x, q1.y, q1.z), mk(q2.x, q2.y, q2.z),
+                               mk(q3.x, q3.y, q3.z), q1.w, q2.w, q3.w);
+    }
+    __syncwarp();
+}
+
+// Compute warps.  Iteration i evaluates the faces of tile i and transforms
+// the vertices of tile i + 1 into the other vertex buffer; one barrier (which
+// also checks that every thread's wait for tile i + 1 succeeded) separates
+// iterations, so a warp that finishes its faces early starts transforming.
 template <bool CUT64, bool WAVES>
 __device__ __forceinline__ void consumer(const KParams& P, ChunkSmem& S)
 {
@@ -486,88 +609,38 @@ __device__ __forceinline__ void consumer(const KParams& P, ChunkSmem& S)
 #pragma unroll
     for (int k = 0; k < kQ; ++k) acc.q[k] = 0.f;
     float hi = 0.f, lo = 0.f;
-    int since_flush = 0;
-    constexpr int kMaxFacesPerTile = 3;   // ceil(nfull/32) + ceil(ncut/32) with nfull + ncut <= 64
-    for (uint32_t item = 0;; ++item) {
+    int tiles_since_flush = 0;
+    // A thread adds at most two paired faces and two straddling faces per
+    // tile; a flush every kFlushTiles tiles keeps its FP32 runs short (at
+    // most 8 faces).
+    constexpr int kFlushTiles = 2;
+
+    // first tile
+    bool ok = mbar_wait(&S.full[0], 0u);
+    ItemMeta m = S.meta[0];
+    if (ok && !(m.flags & ITEM_END)) transform_tile<WAVES>(P, S.stage[0], m, S.verts[0]);
+    if (!consumer_all(ok)) {
+        if (tid == 0) atomicOr(P.err, 1u);
+        return;
+    }
+    for (uint32_t item = 0; !(m.flags & ITEM_END); ++item) {
         const int s = (int)(item % kStages);
-        const bool ok = mbar_wait(&S.full[s], (item / kStages) & 1u);
+        tile_faces<CUT64, WAVES>(P, S.stage[s], m, S.verts[item & 1u], S.flist[warp], acc);
+        // next tile: wait, read its metadata, transform its vertices
+        const uint32_t nx = item + 1u;
+        const int sn = (int)(nx % kStages);
+        ok = mbar_wait(&S.full[sn], (nx / kStages) & 1u);
+        const ItemMeta mn = S.meta[sn];
+        if (ok && !(mn.flags & ITEM_END)) transform_tile<WAVES>(P, S.stage[sn], mn, S.verts[nx & 1u]);
         if (!consumer_all(ok)) {
             if (tid == 0) atomicOr(P.err, 1u);
-            break;
+            return;
         }
-        const ItemMeta m = S.meta[s];
-        if (m.flags & ITEM_END) break;
-        const BodyParams& B = S.stage[s].bp;
-        const float* raw = reinterpret_cast<const float*>(S.stage[s].raw);
-        const int nv = m.nv, nf = m.nf, nvp = (nv + 3) & ~3;
-        float TC[12];
-#pragma unroll
-        for (int k = 0; k < 12; ++k) TC[k] = B.TC[k];
-        for (int v = tid; v < nv; v += kBlock) {
-            v3 p = xform(TC, raw[v], raw[nvp + v], raw[2 * nvp + v]);
-            float d = WAVES ? depth_at(P.ocean, p.x, p.y, p.z) : p.z;
-            S.verts[v] = make_float4(p.x, p.y, p.z, d);
-        }
-        consumer_sync();
-        int iters = 0;
-        {
-            BodyParams Bl;
-            Bl.p = B.p; Bl.p0 = B.p0; Bl.v = B.v; Bl.omega = B.omega;
-            Bl.loop = B.loop; Bl.buoyancy = B.buoyancy; Bl.damping = B.damping;
-            const uint16_t* idx = reinterpret_cast<const uint16_t*>(raw + 3 * nvp);
-            // Warp w takes faces (k*32 + lane)*8 + w, k = 0, 1: a spread
-            // sample of the tile, so that the warps get similar work.  Its
-            // faces are compacted (deterministically, by ballot) into a list
-            // of fully submerged faces and a list of straddling faces, which
-            // the warp then evaluates with all lanes busy.
-            uint16_t* list = S.flist[warp];
-            int nfull = 0, ncut = 0;
-            const unsigned lt = (1u << lane) - 1u;
-#pragma unroll
-            for (int k = 0; k < 2; ++k) {
-                const int f = (k * 32 + lane) * kWarps + warp;
-                int cls = 0;
-                if (f < nf) {
-                    if (Bl.loop == LOOP_SURFACE)
-                        cls = face_class(S.verts[idx[3 * f]].w, S.verts[idx[3 * f + 1]].w,
-                                         S.verts[idx[3 * f + 2]].w);
-                    else
-                        cls = 1;
-                }
-                const unsigned mf = __ballot_sync(0xffffffffu, cls == 1);
-                const unsigned mc = __ballot_sync(0xffffffffu, cls == 2);
-                if (cls == 1) list[nfull + __popc(mf & lt)] = (uint16_t)f;
-                if (cls == 2) list[63 - (ncut + __popc(mc & lt))] = (uint16_t)f;
-                nfull += __popc(mf);
-                ncut += __popc(mc);
-            }
-            __syncwarp();
-            for (int i = lane; i < nfull; i += 32) {
-                const int f = list[i];
-                const float4 q1 = S.verts[idx[3 * f]];
-                const float4 q2 = S.verts[idx[3 * f + 1]];
-                const float4 q3 = S.verts[idx[3 * f + 2]];
-                if (Bl.loop == LOOP_SURFACE) face_full<WAVES>(P.ocean, Bl, acc, q1, q2, q3);
-                else face_submerged(P.ocean, Bl, acc, q1, q2, q3);
-            }
-            for (int i = lane; i < ncut; i += 32) {
-                const int f = list[63 - i];
-                const float4 q1 = S.verts[idx[3 * f]];
-                const float4 q2 = S.verts[idx[3 * f + 1]];
-                const float4 q3 = S.verts[idx[3 * f + 2]];
-                face_cut<CUT64, WAVES>(P.ocean, Bl, acc, mk(q1.x, q1.y, q1.z), mk(q2.x, q2.y, q2.z),
-                                mk(q3.x, q3.y, q3.z), q1.w, q2.w, q3.w);
-            }
-            iters = (nfull + 31) / 32 + (ncut + 31) / 32;
-            __syncwarp();
-        }
-        consumer_sync();
         if (tid == 0) mbar_arrive(&S.empty[s]);
-        since_flush += iters;                      // warp-uniform
         const bool last = (m.flags & ITEM_LAST) != 0;
-        if (last || since_flush + kMaxFacesPerTile > kFlushFaces) {
+        if (last || ++tiles_since_flush == kFlushTiles) {
             flush(acc, hi, lo);
-            since_flush = 0;
+            tiles_since_flush = 0;
         }
         if (last) {
             S.red[warp][lane] = make_float2(hi, lo);
@@ -586,6 +659,7 @@ __device__ __forceinline__ void consumer(const KParams& P, ChunkSmem& S)
             lo = 0.f;
             consumer_sync();
         }
+        m = mn;
     }
 }
 
@@ -685,7 +759,7 @@ cudaError_t launch_step(const KParams& P, LaunchShape shape, int cut64, cudaStre
 template <bool CUT64>
 __global__ void __launch_bounds__(kBlock) face_terms_kernel(const TileDesc* tiles, uint32_t first_tile,
                                                             const hydro_body* body, OceanDev ocean,
-                                                            SettingsDev st, float* out)
+                                                            SettingsDev st, float* out, int packed)
 {
     __shared__ float4 verts[kTileVerts];
     __shared__ BodyParams Bs;
@@ -700,26 +774,56 @@ __global__ void __launch_bounds__(kBlock) face_terms_kernel(const TileDesc* tile
         verts[v] = make_float4(p.x, p.y, p.z, depth_at(ocean, p.x, p.y, p.z));
     }
     __syncthreads();
-    const uint16_t* idx = reinterpret_cast<const uint16_t*>(td.block + 3 * nvp);
-    for (int f = tid; f < td.nf; f += kBlock) {
-        Acc a;
-        for (int k = 0; k < kQ; ++k) a.q[k] = 0.f;
-        if (ocean.waves)
-            face_surface<CUT64, true>(ocean, B, a, verts[idx[3 * f]], verts[idx[3 * f + 1]], verts[idx[3 * f + 2]]);
-        else
-            face_surface<CUT64, false>(ocean, B, a, verts[idx[3 * f]], verts[idx[3 * f + 1]], verts[idx[3 * f + 2]]);
-        float* o = out + (size_t)(td.first_face + f) * kQ;
-        for (int k = 0; k < kQ; ++k) o[k] = a.q[k];
+    const uint32_t* idx = reinterpret_cast<const uint32_t*>(td.block + 3 * nvp);
+    // Thread t takes faces 2t and 2t+1: a pair of fully submerged faces goes
+    // through the packed path (as in the batched kernel), any other face
+    // through the scalar path, so that both are checked.
+    for (int f = 2 * tid; f < td.nf; f += 2 * kBlock) {
+        const bool hasB = f + 1 < td.nf;
+        const uint32_t wa = idx[f], wb = idx[hasB ? f + 1 : f];
+        const float4 a1 = verts[wa & 511u], a2 = verts[(wa >> 9) & 511u], a3 = verts[wa >> 18];
+        const float4 b1 = verts[wb & 511u], b2 = verts[(wb >> 9) & 511u], b3 = verts[wb >> 18];
+        const int ca = face_class(a1.w, a2.w, a3.w), cb = face_class(b1.w, b2.w, b3.w);
+        float* oa = out + (size_t)(td.first_face + f) * kQ;
+        float* ob = oa + kQ;
+        if (packed && ca == 1 && cb == 1 && hasB) {
+            // the packed path adds face A then face B into one set of sums:
+            // evaluate (A, B) with B's half switched off, then (B, A)
+            const BodyPair Bp = body_pair(B, ocean);
+            for (int h = 0; h < 2; ++h) {
+                Acc a;
+                for (int k = 0; k < kQ; ++k) a.q[k] = 0.f;
+                const P3 c1 = h ? corners(b1, a1) : corners(a1, b1);
+                const P3 c2 = h ? corners(b2, a2) : corners(a2, b2);
+                const P3 c3 = h ? corners(b3, a3) : corners(a3, b3);
+                if (ocean.waves) face_full2<true>(ocean, B, Bp, a, c1, c2, c3, false);
+                else face_full2<false>(ocean, B, Bp, a, c1, c2, c3, false);
+                float* o = h ? ob : oa;
+                for (int k = 0; k < kQ; ++k) o[k] = a.q[k];
+            }
+            continue;
+        }
+        for (int h = 0; h < (hasB ? 2 : 1); ++h) {
+            Acc a;
+            for (int k = 0; k < kQ; ++k) a.q[k] = 0.f;
+            const float4 q1 = h ? b1 : a1, q2 = h ? b2 : a2, q3 = h ? b3 : a3;
+            if (ocean.waves)
+                face_surface<CUT64, true>(ocean, B, a, q1, q2, q3);
+            else
+                face_surface<CUT64, false>(ocean, B, a, q1, q2, q3);
+            float* o = h ? ob : oa;
+            for (int k = 0; k < kQ; ++k) o[k] = a.q[k];
+        }
     }
 }
 
 cudaError_t launch_face_terms(const TileDesc* tiles, uint32_t first_tile, uint32_t n_tiles,
                               const hydro_body* body, OceanDev ocean, SettingsDev st,
-                              int cut64, float* out, cudaStream_t s)
+                              int cut64, int packed, float* out, cudaStream_t s)
 {
     if (n_tiles == 0) return cudaSuccess;
-    if (cut64) face_terms_kernel<true><<<n_tiles, kBlock, 0, s>>>(tiles, first_tile, body, ocean, st, out);
-    else face_terms_kernel<false><<<n_tiles, kBlock, 0, s>>>(tiles, first_tile, body, ocean, st, out);
+    if (cut64) face_terms_kernel<true><<<n_tiles, kBlock, 0, s>>>(tiles, first_tile, body, ocean, st, out, packed);
+    else face_terms_kernel<false><<<n_tiles, kBlock, 0, s>>>(tiles, first_tile, body, ocean, st, out, packed);
     return cudaGetLastError();
 }
 
@@ -817,6 +921,53 @@ cudaError_t launch_division_check(uint64_t n_pairs, uint64_t seed, unsigned long
                                   cudaStream_t s)
 {
     division_check_kernel<<<1216, 256, 0, s>>>(n_pairs, seed, counts);
+    return cudaGetLastError();
+}
+
+}  // namespace sfh
+
+namespace sfh {
+
+// --------------------------------------------------- packed FP32 self-check
+// counts[k] mismatches of the packed op k (0 mul, 1 add, 2 sub, 3 fma)
+// against the scalar IEEE op on both halves; ex[4k..4k+3] one failing
+// operand set (a, b, c, packed result) of op k.
+__global__ void packed_check_kernel(uint64_t n, uint64_t seed, unsigned long long* counts, float* ex)
+{
+    const uint64_t tid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
+    uint64_t s = seed ^ (tid * 0x9E3779B97F4A7C15ull);
+    unsigned long long bad[4] = {0, 0, 0, 0};
+    for (uint64_t i = tid; i < n; i += nthreads) {
+        float v[6];
+        for (int k = 0; k < 6; ++k) {
+            uint64_t r = splitmix64(s);
+            uint32_t e = (uint32_t)(127 - 30 + (r % 61));
+            v[k] = __uint_as_float(((uint32_t)(r >> 32) & 0x807FFFFFu) | (e << 23));
+        }
+        const float2 a = make_float2(v[0], v[1]), b = make_float2(v[2], v[3]), c = make_float2(v[4], v[5]);
+        float2 r[4] = {mul2(a, b), add2(a, b), sub2(a, b), fma2(a, b, c)};
+        float2 w[4] = {make_float2(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)),
+                       make_float2(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y)),
+                       make_float2(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y)),
+                       make_float2(__fmaf_rn(a.x, b.x, c.x), __fmaf_rn(a.y, b.y, c.y))};
+        for (int k = 0; k < 4; ++k) {
+            if (!same_float(r[k].x, w[k].x) || !same_float(r[k].y, w[k].y)) {
+                if (bad[k] == 0) {
+                    ex[4 * k + 0] = a.x; ex[4 * k + 1] = b.x; ex[4 * k + 2] = c.x;
+                    ex[4 * k + 3] = r[k].x;
+                }
+                ++bad[k];
+            }
+        }
+    }
+    for (int k = 0; k < 4; ++k) atomicAdd(counts + 3 + k, bad[k]);
+}
+
+cudaError_t launch_packed_check(uint64_t n, uint64_t seed, unsigned long long* counts, float* ex,
+                                cudaStream_t s)
+{
+    packed_check_kernel<<<1216, 256, 0, s>>>(n, seed, counts, ex);
     return cudaGetLastError();
 }
 

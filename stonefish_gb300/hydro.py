@@ -54,7 +54,7 @@ class HydroContext:
         if not hasattr(lib, "_debug_declared"):
             lib.hydro_debug_face_terms.restype = C.c_int32
             lib.hydro_debug_face_terms.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(abi.Ocean),
-                                                   C.POINTER(abi.Settings), C.c_void_p]
+                                                   C.POINTER(abi.Settings), C.c_int32, C.c_void_p]
             lib._debug_declared = True
         cfg = abi.Config()
         lib.hydro_config_default(C.byref(cfg))
@@ -169,12 +169,13 @@ class HydroContext:
                                                ro.ctypes.data_as(P)))
         return io
 
-    def face_terms(self, body: np.ndarray, ocean, settings) -> np.ndarray:
-        """Per-face surface-loop terms (n_faces, 23) float32 of one body."""
+    def face_terms(self, body: np.ndarray, ocean, settings, packed: bool = True) -> np.ndarray:
+        """Per-face surface-loop terms (n_faces, 23) float32 of one body; packed
+        evaluates pairs of submerged faces on the packed FP32 path."""
         nf = self.mesh_faces[int(body["mesh"][0])]
         out = np.zeros((nf, 23), dtype=np.float32)
         self._ck(self.lib.hydro_debug_face_terms(self.ctx, body.ctypes.data, C.byref(ocean),
-                                                 C.byref(settings), out.ctypes.data))
+                                                 C.byref(settings), int(packed), out.ctypes.data))
         return out
 
     def division_check(self, n_pairs: int = 1 << 26, seed: int = 1) -> list[int]:
@@ -183,6 +184,14 @@ class HydroContext:
         out = (C.c_uint64 * 3)()
         self._ck(self.lib.hydro_debug_division_check(self.ctx, n_pairs, seed, out))
         return list(out)
+
+    def arith_check(self, n_pairs: int = 1 << 24, seed: int = 1):
+        """(division mismatches[3], packed-op mismatches[4], failing examples[16])."""
+        d = (C.c_uint64 * 3)()
+        p = (C.c_uint64 * 4)()
+        ex = (C.c_float * 16)()
+        self._ck(self.lib.hydro_debug_arith_check(self.ctx, n_pairs, seed, d, p, ex))
+        return list(d), list(p), list(ex)
 
     def batch(self, mesh_of_body) -> "Batch":
         return Batch(self, mesh_of_body)

@@ -72,12 +72,13 @@ def test_face_terms_bit_identical(oracle, hctx, hctx64, sphere_run, cut):
     for i in range(0, 1000, 7):
         b = sc["bodies"][i:i + 1].copy()
         b["mesh"] = mid
-        gpu = h.face_terms(b, sc["ocean"], scenarios.settings())
         cpu = oracle.face_terms(variant, scenarios.settings(), sc["meshes"][0], sc["ocean"],
                                 body_transform(b, "T_CG"), body_transform(b, "T_C"),
                                 b["v"][0], b["omega"][0])
-        bad = np.argwhere(gpu != cpu)
-        assert bad.size == 0, f"step {i}: {len(bad)} differing terms, first {bad[:3]}"
+        for packed in (False, True):
+            gpu = h.face_terms(b, sc["ocean"], scenarios.settings(), packed=packed)
+            bad = np.argwhere(gpu != cpu)
+            assert bad.size == 0, f"step {i} packed={packed}: {len(bad)} differing terms, first {bad[:3]}"
         checked += int(np.any(cpu != 0))
     assert checked > 50
 
@@ -101,7 +102,7 @@ def test_face_terms_every_sign_pattern(oracle, hctx, hctx64, cut):
                 body = scenarios.fill_bodies(1, np.eye(3)[None], np.zeros((1, 3)),
                                              np.array([[0.3, -0.2, 0.1]]), np.array([[0.1, 0.2, -0.3]]),
                                              np.ones((1, 3)), 1.0, 1.0, (1, 1, 1), (.1, .1, .1), mid)
-                gpu = h.face_terms(body, oc, scenarios.settings())
+                gpu = h.face_terms(body, oc, scenarios.settings(), packed=False)
                 T = body_transform(body)
                 cpu = oracle.face_terms(variant, scenarios.settings(), (p, faces), oc, T, T,
                                         body["v"][0], body["omega"][0])
