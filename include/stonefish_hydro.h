@@ -254,6 +254,32 @@ hydro_status hydro_batch_compute(hydro_batch* batch, const hydro_body* bodies,
 /* Number of kernel launches the last compute call enqueued. */
 uint32_t hydro_batch_last_launches(const hydro_batch* batch);
 
+/* Allocation-free step (no counterpart in the reference).  For callers that
+ * cannot allocate device memory while they run: a simulator evaluating the
+ * hydrodynamics inside its real-time tick, where cudaMalloc may synchronise
+ * the device and stall the tick, or an application whose device memory is
+ * reserved up front by another allocator.  Same result as
+ * hydro_batch_compute_device for the bodies (mesh_of_body is a host array,
+ * d_bodies and d_inout device arrays, enqueued on `stream`), but every byte
+ * of scratch lives in one static device array of HYDRO_STATIC_SCRATCH_BYTES
+ * that each GPU loading this library holds until the process exits; no
+ * cudaMalloc, cudaFree or other allocating routine is called.  Limits: at
+ * most HYDRO_STATIC_MAX_BODIES bodies and a work list that fits the array
+ * (about 16000 chunks of up to 8 tiles); larger requests return
+ * HYDRO_ERR_INVALID_ARG and launch nothing.  The first call on a device
+ * looks up the array's device address, so make it before any stream
+ * capture; meshes uploaded afterwards are accepted as long as the device
+ * tile table does not need to grow (otherwise HYDRO_ERR_INVALID_ARG).  All
+ * calls share the array and it keeps the last call's contents: calls whose
+ * work overlaps on the GPU race. */
+#define HYDRO_STATIC_SCRATCH_BYTES (4u << 20)
+#define HYDRO_STATIC_MAX_BODIES 4096u
+hydro_status hydro_compute_wrenches_static(hydro_ctx* ctx, const hydro_mesh_id* mesh_of_body,
+                                           uint32_t n_bodies, const hydro_body* d_bodies,
+                                           const hydro_ocean* ocean,
+                                           const hydro_settings* settings,
+                                           hydro_wrench* d_inout, void* stream);
+
 /* --------------------------------------------- reference call surface */
 /* SolidEntity::ComputeHydrodynamicForces (SolidEntity.cpp:1799-1850) for
  * one body: mode gate, CheckBodyFluidPosition, INSIDE/CROSSING branch and

@@ -38,6 +38,8 @@ CUT_FP64, CUT_FP32 = 0, 1
 MAX_CURRENTS = 8
 MAX_WAVE_LAYERS = 4
 NO_MESH = 0xFFFFFFFF
+STATIC_MAX_BODIES = 4096
+STATIC_SCRATCH_BYTES = 4 << 20
 
 _d3 = C.c_double * 3
 
@@ -170,6 +172,8 @@ def _declare(lib: C.CDLL) -> None:
         "hydro_fluid_position": (i32, [vp, C.POINTER(Ocean), d, d, C.POINTER(i32)]),
         "hydro_debug_division_check": (i32, [vp, C.c_uint64, C.c_uint64, vp]),
         "hydro_debug_arith_check": (i32, [vp, C.c_uint64, C.c_uint64, vp, vp, vp]),
+        "hydro_compute_wrenches_static": (i32, [vp, vp, u32, vp, C.POINTER(Ocean), C.POINTER(Settings),
+                                                vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

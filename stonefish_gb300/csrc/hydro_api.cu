@@ -850,3 +850,149 @@ hydro_status hydro_debug_arith_check(hydro_ctx* ctx, uint64_t n_pairs, uint64_t 
 }
 
 }  // extern "C"
+
+// ====================================================== allocation-free step
+// Some callers cannot allocate device memory while they run: a simulator
+// that evaluates the hydrodynamics inside its real-time tick (cudaMalloc
+// may synchronise the device and stall the tick for milliseconds), or an
+// application whose device memory is reserved up front by another
+// allocator.  hydro_compute_wrenches_static runs the batched step with all
+// of its scratch (work list, per-body parameters, per-chunk partial sums,
+// error word) in one static device array instead of memory it allocates.
+// Every GPU that loads this library holds the array until the process
+// exits.  Calls share it: the last call's contents stay in it, and calls
+// whose work overlaps on the GPU race.
+namespace {
+
+constexpr size_t kStaticScratchBytes = HYDRO_STATIC_SCRATCH_BYTES;
+constexpr uint32_t kStaticMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+
+std::mutex g_static_mu;
+void* g_static_ptr[kStaticMaxDevices] = {};
+ChunkDesc g_static_chunks[kStaticScratchBytes / 208];
+BodyInfo g_static_binfo[HYDRO_STATIC_MAX_BODIES];
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+}  // namespace
+
+extern "C" hydro_status hydro_compute_wrenches_static(hydro_ctx* ctx, const hydro_mesh_id* mesh_of_body,
+                                                      uint32_t n_bodies, const hydro_body* d_bodies,
+                                                      const hydro_ocean* ocean,
+                                                      const hydro_settings* settings,
+                                                      hydro_wrench* d_inout, void* stream)
+{
+    if (!ctx) return HYDRO_ERR_INVALID_ARG;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    std::lock_guard<std::mutex> slk(g_static_mu);
+    if (!mesh_of_body || !d_bodies || !d_inout || !settings || !valid_ocean(ocean) || n_bodies == 0)
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "static step: bad arguments");
+    if (n_bodies > HYDRO_STATIC_MAX_BODIES)
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "static step: %u bodies exceed the maximum of %u",
+                    n_bodies, (unsigned)HYDRO_STATIC_MAX_BODIES);
+    if (ocean->waves && !ctx->wave_d)
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "ocean.waves set but no wave grid was given");
+    if ((uint32_t)ctx->device >= kStaticMaxDevices)
+        return fail(ctx, HYDRO_ERR_UNSUPPORTED, "static step: device ordinal %d too large", ctx->device);
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, HYDRO_ERR_DEVICE, "cudaSetDevice");
+
+    // Set-up, once per device with that device current: the device address
+    // of the static array (its name in host code is only a stand-in).
+    void*& base_ptr = g_static_ptr[ctx->device];
+    if (!base_ptr) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaGetSymbolAddress(static scratch)");
+        base_ptr = p;
+    }
+
+    // The device tile table must already hold every uploaded mesh; copying
+    // missing entries is allowed, growing it (an allocation) is not.
+    if (ctx->tiles_h.size() > ctx->tiles_d_cap)
+        return fail(ctx, HYDRO_ERR_INVALID_ARG,
+                    "static step: the device tile table must grow; create a batch (or call any "
+                    "other compute entry point) once after uploading meshes");
+    if (ctx->tiles_d_count < ctx->tiles_h.size()) {
+        CK(ctx, cudaMemcpy(ctx->tiles_d + ctx->tiles_d_count, ctx->tiles_h.data() + ctx->tiles_d_count,
+                           (ctx->tiles_h.size() - ctx->tiles_d_count) * sizeof(TileDesc),
+                           cudaMemcpyHostToDevice));
+        ctx->tiles_d_count = ctx->tiles_h.size();
+    }
+
+    // Work list into static host arrays (no heap allocation).
+    const uint32_t tpc = tiles_per_chunk(ctx);
+    const size_t max_chunks = sizeof(g_static_chunks) / sizeof(g_static_chunks[0]);
+    size_t nc = 0;
+    for (uint32_t i = 0; i < n_bodies; ++i) {
+        const uint32_t mesh = mesh_of_body[i];
+        if (mesh != HYDRO_NO_MESH && mesh >= ctx->meshes.size())
+            return fail(ctx, HYDRO_ERR_NOT_FOUND, "body %u: unknown mesh %u", i, mesh);
+        BodyInfo& bi = g_static_binfo[i];
+        bi.first_chunk = (uint32_t)nc;
+        bi.mesh = mesh;
+        uint32_t first = 0, nt = 0;
+        if (mesh != HYDRO_NO_MESH) {
+            first = ctx->meshes[mesh].first_tile;
+            nt = ctx->meshes[mesh].n_tiles;
+            bi.n_faces = ctx->meshes[mesh].n_faces;
+        } else {
+            bi.n_faces = 0;
+        }
+        uint32_t k = 0;
+        for (uint32_t t = 0; t < nt || k == 0; t += tpc, ++k) {
+            if (nc >= max_chunks)
+                return fail(ctx, HYDRO_ERR_INVALID_ARG, "static step: more than %zu chunks", max_chunks);
+            g_static_chunks[nc++] = ChunkDesc{i, first + t, nt > t ? std::min(tpc, nt - t) : 0u, k};
+            if (nt == 0) { ++k; break; }
+        }
+        bi.n_chunks = (uint32_t)nc - bi.first_chunk;
+    }
+
+    // Layout of the static array.
+    const size_t off_err = 0;
+    const size_t off_binfo = align256(off_err + 256);
+    const size_t off_bparams = align256(off_binfo + (size_t)n_bodies * sizeof(BodyInfo));
+    const size_t off_chunks = align256(off_bparams + (size_t)n_bodies * sizeof(BodyParams));
+    const size_t off_active = align256(off_chunks + nc * sizeof(ChunkDesc));
+    const size_t off_partials = align256(off_active + nc);
+    const size_t total = off_partials + nc * kPartialStride * sizeof(double);
+    if (total > kStaticScratchBytes)
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "static step: needs %zu scratch bytes, the maximum is %zu",
+                    total, kStaticScratchBytes);
+
+    char* base = static_cast<char*>(base_ptr);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    CK(ctx, cudaMemcpyAsync(base + off_binfo, g_static_binfo, (size_t)n_bodies * sizeof(BodyInfo),
+                            cudaMemcpyHostToDevice, s));
+    CK(ctx, cudaMemcpyAsync(base + off_chunks, g_static_chunks, nc * sizeof(ChunkDesc),
+                            cudaMemcpyHostToDevice, s));
+
+    KParams P{};
+    P.chunks = reinterpret_cast<const ChunkDesc*>(base + off_chunks);
+    P.binfo = reinterpret_cast<const BodyInfo*>(base + off_binfo);
+    P.tiles = ctx->tiles_d;
+    P.bodies = d_bodies;
+    P.io = d_inout;
+    P.bparams = reinterpret_cast<BodyParams*>(base + off_bparams);
+    P.partials = reinterpret_cast<double*>(base + off_partials);
+    P.err = reinterpret_cast<unsigned*>(base + off_err);
+    P.work = reinterpret_cast<unsigned*>(base + off_err) + 32;
+    P.chunk_active = reinterpret_cast<uint8_t*>(base + off_active);
+    P.n_bodies = n_bodies;
+    P.n_chunks = (uint32_t)nc;
+    P.ocean = make_ocean(ctx, ocean);
+    P.st.damping = settings->damping_forces ? 1 : 0;
+    P.st.buoyancy = settings->realistic_buoyancy ? 1 : 0;
+    P.op = OP_BODY;
+    const int cut64 = ctx->cfg.cut_precision == HYDRO_CUT_FP64;
+    LaunchShape shape{};
+    const int want = ctx->cfg.ctas_per_sm ? (int)ctx->cfg.ctas_per_sm : 2;
+    shape.ctas_per_sm = std::max(1, std::min(want, chunk_kernel_occupancy(cut64, P.ocean.waves, want)));
+    shape.grid = ctx->sm_count * shape.ctas_per_sm;
+    uint32_t launches = 0;
+    cudaError_t e = launch_step(P, shape, cut64, s, &launches);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "static wrench step launch");
+    return HYDRO_OK;
+}

@@ -193,6 +193,15 @@ class HydroContext:
         self._ck(self.lib.hydro_debug_arith_check(self.ctx, n_pairs, seed, d, p, ex))
         return list(d), list(p), list(ex)
 
+    def compute_static(self, mesh_of_body, d_bodies: int, ocean, settings, d_io: int,
+                       stream: int = 0) -> None:
+        """Allocation-free step (hydro_compute_wrenches_static): device pointers
+        in/out, all scratch in the library's static device array."""
+        ids = np.ascontiguousarray(mesh_of_body, dtype=np.uint32)
+        self._ck(self.lib.hydro_compute_wrenches_static(self.ctx, ids.ctypes.data, ids.size, d_bodies,
+                                                        C.byref(ocean), C.byref(settings), d_io,
+                                                        stream or None))
+
     def batch(self, mesh_of_body) -> "Batch":
         return Batch(self, mesh_of_body)
 
