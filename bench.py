@@ -301,7 +301,9 @@ def run_gpu(args, rank: int, world: int, local_rank: int, dist):
                      "frac": achieved / peak, "peak_source": peak_kind,
                      "traffic": profile_traffic(args.workload),
                      "algorithmic_bytes_per_launch": alg_bytes,
-                     "bytes_rule": "18 B per processed face + 200 B per body"},
+                     "bytes_rule": "18 B per processed face + 200 B per body",
+                     "note": "whole step (prep + chunk + finalise kernels) timed; the chunk kernel "
+                             "is issue-bound (profiles/chunk_kernel_batch.txt)"},
         "gpu_launches": args.steps * batch.last_launches(),
         "kernel_config": {"cut": args.cut, "chunk_faces": args.chunk_faces or 4096,
                           "ctas_per_sm": args.ctas_per_sm or 2},
@@ -361,7 +363,7 @@ def main():
     ap.add_argument("--n-bodies", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-error", action="store_true")
-    ap.add_argument("--cut", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--cut", default="fp32", choices=["fp64", "fp32"])
     ap.add_argument("--chunk-faces", type=int, default=0)
     ap.add_argument("--ctas-per-sm", type=int, default=0)
     args = ap.parse_args()
