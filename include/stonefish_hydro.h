@@ -349,6 +349,13 @@ hydro_status hydro_debug_face_terms(hydro_ctx* ctx, const hydro_body* body,
 hydro_status hydro_debug_division_check(hydro_ctx* ctx, uint64_t n_pairs, uint64_t seed,
                                         uint64_t mismatches[3]);
 
+/* Failure detection without a GPU fault: one CTA waits, with the bounded
+ * wait of the tile pipeline, on an mbarrier that nothing completes, gives up
+ * after limit_us microseconds (1..2000000) and writes HYDRO_ERR_TIMEOUT to
+ * *status; the context stays usable.  The same bounded waits in the batched
+ * step turn a stalled pipeline into status HYDRO_ERR_TIMEOUT per body. */
+hydro_status hydro_debug_wait_timeout(hydro_ctx* ctx, uint32_t limit_us, int32_t* status);
+
 /* The division check above plus a check that the packed FP32 pair
  * instructions the kernels use for two faces at a time (mul, add, sub, fma
  * .rn.f32x2) return, in each half, the bits of the scalar IEEE operation:

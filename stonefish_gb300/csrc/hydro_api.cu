@@ -851,6 +851,26 @@ hydro_status hydro_debug_arith_check(hydro_ctx* ctx, uint64_t n_pairs, uint64_t 
 
 }  // extern "C"
 
+extern "C" hydro_status hydro_debug_wait_timeout(hydro_ctx* ctx, uint32_t limit_us, int32_t* status)
+{
+    if (!ctx) return HYDRO_ERR_INVALID_ARG;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (!status || limit_us == 0 || limit_us > 2000000u)
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "wait check: limit must be in 1..2000000 us");
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, HYDRO_ERR_DEVICE, "cudaSetDevice");
+    hydro_status st = ensure_small(ctx, 64);
+    if (st != HYDRO_OK) return st;
+    int* d = static_cast<int*>(ctx->small_d);
+    CK(ctx, cudaMemsetAsync(d, 0xff, sizeof(int), ctx->stream));
+    cudaError_t e = launch_wait_timeout((uint64_t)limit_us * 1000ull, d, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "wait check kernel");
+    int h = -1;
+    CK(ctx, cudaMemcpyAsync(&h, d, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(ctx, cudaStreamSynchronize(ctx->stream));
+    *status = h;
+    return HYDRO_OK;
+}
+
 // ====================================================== allocation-free step
 // Some callers cannot allocate device memory while they run: a simulator
 // that evaluates the hydrodynamics inside its real-time tick (cudaMalloc

@@ -69,6 +69,10 @@ cudaError_t launch_division_check(uint64_t n_pairs, uint64_t seed, unsigned long
 cudaError_t launch_packed_check(uint64_t n, uint64_t seed, unsigned long long* counts, float* ex,
                                 cudaStream_t s);
 
+// A 1-CTA wait on an mbarrier that is never completed, bounded by limit_ns:
+// writes HYDRO_ERR_TIMEOUT (or 0) to *status.
+cudaError_t launch_wait_timeout(uint64_t limit_ns, int* status, cudaStream_t s);
+
 cudaError_t launch_depth(OceanDev ocean, const float* xyz, uint32_t n, float* out, cudaStream_t s);
 
 }  // namespace sfh

@@ -347,15 +347,20 @@ __device__ __forceinline__ uint64_t global_ns()
 // Bounded wait: gives up (returns false) after about two seconds.
 constexpr uint64_t kWaitLimitNs = 2000000000ull;
 
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
+__device__ __forceinline__ bool mbar_wait_for(uint64_t* bar, uint32_t parity, uint64_t limit_ns)
 {
     if (mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = global_ns();
     for (;;) {
         for (int i = 0; i < 64; ++i)
             if (mbar_try_wait(bar, parity)) return true;
-        if (global_ns() - t0 > kWaitLimitNs) return false;
+        if (global_ns() - t0 > limit_ns) return false;
     }
+}
+
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity)
+{
+    return mbar_wait_for(bar, parity, kWaitLimitNs);
 }
 
 // The producer's wait for a free stage: it is ahead of the compute warps,
@@ -968,6 +973,33 @@ cudaError_t launch_packed_check(uint64_t n, uint64_t seed, unsigned long long* c
                                 cudaStream_t s)
 {
     packed_check_kernel<<<1216, 256, 0, s>>>(n, seed, counts, ex);
+    return cudaGetLastError();
+}
+
+}  // namespace sfh
+
+namespace sfh {
+
+// ------------------------------------------------------- bounded-wait check
+// One CTA waits, with the bounded wait of the pipeline, on an mbarrier that
+// nothing ever completes; it gives up after limit_ns and reports
+// HYDRO_ERR_TIMEOUT in *status, leaving nothing in flight.
+__global__ void wait_timeout_kernel(uint64_t limit_ns, int* status)
+{
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1u);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    const bool ok = mbar_wait_for(&bar, 0u, limit_ns);
+    const bool all = __syncthreads_and(ok ? 1 : 0) != 0;
+    if (threadIdx.x == 0) *status = all ? 0 : HYDRO_ERR_TIMEOUT;
+}
+
+cudaError_t launch_wait_timeout(uint64_t limit_ns, int* status, cudaStream_t s)
+{
+    wait_timeout_kernel<<<1, 64, 0, s>>>(limit_ns, status);
     return cudaGetLastError();
 }
 

@@ -185,6 +185,13 @@ class HydroContext:
         self._ck(self.lib.hydro_debug_division_check(self.ctx, n_pairs, seed, out))
         return list(out)
 
+    def wait_timeout(self, limit_us: int = 20000) -> int:
+        """Status of a bounded device wait that nothing completes (expects
+        HYDRO_ERR_TIMEOUT)."""
+        st = C.c_int32(-1)
+        self._ck(self.lib.hydro_debug_wait_timeout(self.ctx, limit_us, C.byref(st)))
+        return int(st.value)
+
     def arith_check(self, n_pairs: int = 1 << 24, seed: int = 1):
         """(division mismatches[3], packed-op mismatches[4], failing examples[16])."""
         d = (C.c_uint64 * 3)()
