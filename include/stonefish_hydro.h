@@ -366,6 +366,97 @@ hydro_status hydro_debug_arith_check(hydro_ctx* ctx, uint64_t n_pairs, uint64_t 
                                      uint64_t division[3], uint64_t packed[4],
                                      float examples[16]);
 
+/* ------------------------------------------------------------------------
+ * Learned wrench surrogate (no counterpart in the reference).
+ *
+ * Kernels of a small MLP that predicts a hull's body-frame wrench
+ * (F[3], T[3] about the CG) from 16 state features, trained on wrenches the
+ * exact step computes, and of the out-of-distribution gate that sends
+ * states outside the training domain to the exact step.  All pointers are
+ * device pointers; every call is asynchronous on `stream` (a cudaStream_t,
+ * NULL = the legacy default stream).  Matrices are row-major; "bf16" buffers
+ * hold IEEE bfloat16 values (uint16 bit patterns).
+ * ---------------------------------------------------------------------- */
+
+#define HYDRO_NN_FEATURES 16
+#define HYDRO_NN_EPI_F32 0        /* z = A B */
+#define HYDRO_NN_EPI_BIAS_SILU 1  /* z = A B + bias, y = bf16(silu(z)) */
+#define HYDRO_NN_EPI_BIAS 2       /* z = A B + bias */
+#define HYDRO_NN_EPI_SILU_GRAD 3  /* y = bf16((A B) * silu'(zprev)) */
+
+/* C[M,N] = A[M,K] (bf16, row stride lda) x B[K,N] (bf16, row stride ldb)
+ * on the BF16 tensor cores with FP32 accumulation, followed by `epilogue`;
+ * outputs z (FP32) and y (bf16) have row stride ldc.  M and N must be
+ * multiples of 64, K a multiple of 32. */
+hydro_status hydro_nn_gemm(hydro_ctx* ctx, int32_t epilogue, const void* A, int32_t lda,
+                           const void* B, int32_t ldb, int32_t M, int32_t N, int32_t K,
+                           float* z, void* y, const float* bias, const float* zprev,
+                           int32_t ldc, void* stream);
+
+/* dst[cols][rows] = transpose of the bf16 matrix src[rows][cols]. */
+hydro_status hydro_nn_transpose(hydro_ctx* ctx, const void* src, void* dst, int32_t rows,
+                                int32_t cols, void* stream);
+
+/* Mean-squared-error gradient over the first n_out of ld columns of z
+ * against target[rows][n_out]: dz (bf16, rows x ld, other columns zero)
+ * = 2 (z - target) / (rows n_out); *loss += the mean squared error. */
+hydro_status hydro_nn_mse_grad(hydro_ctx* ctx, const float* z, const float* target, int32_t rows,
+                               int32_t ld, int32_t n_out, void* dz, double* loss, void* stream);
+
+/* out[c] = sum over rows of the bf16 matrix g[rows][cols] (bias gradients). */
+hydro_status hydro_nn_colsum(hydro_ctx* ctx, const void* g, int32_t rows, int32_t cols, float* out,
+                             void* stream);
+
+/* One AdamW step (decoupled weight decay, bias-corrected moments, `step`
+ * counted from 1) on FP32 master weights w[rows][cols] with gradient
+ * grad (row stride ldg); then w16 = bf16(w) and wt16 = bf16(w)^T when
+ * non-NULL. */
+hydro_status hydro_nn_adamw(hydro_ctx* ctx, float* w, float* m, float* v, const float* grad,
+                            int32_t rows, int32_t cols, int32_t ldg, float lr, float beta1,
+                            float beta2, float eps, float weight_decay, int32_t step, void* w16,
+                            void* wt16, void* stream);
+
+/* y[rows][ld] = bf16((x - mean) * istd) of x[rows][n_in], zero in columns
+ * n_in..ld-1; mean and istd both NULL for a plain conversion. */
+hydro_status hydro_nn_to_bf16(hydro_ctx* ctx, const float* x, int32_t rows, int32_t n_in, int32_t ld,
+                              const float* mean, const float* istd, void* y, void* stream);
+
+/* The 16 features of each body state, FP32 [n][16]: depth of the CG below
+ * the local surface, roll, pitch, body-frame v[3], omega[3] and current[3],
+ * wave elevation, wave slope along and across the heading, and the
+ * surface's Laplacian at the CG (0 on a flat surface). */
+hydro_status hydro_nn_features(hydro_ctx* ctx, const hydro_body* d_bodies, uint32_t n,
+                               const hydro_ocean* ocean, float* d_features, void* stream);
+
+/* Out-of-distribution gate: d_mask[i] = 1 when features[i] lie in the box
+ * [lo, hi] and (f - mean)^T precision (f - mean) <= threshold (precision is
+ * the 16x16 inverse covariance of the training features), else 0.  lo, hi,
+ * mean, precision are device pointers. */
+hydro_status hydro_nn_gate(hydro_ctx* ctx, const float* d_features, uint32_t n, const float* lo,
+                           const float* hi, const float* mean, const float* precision,
+                           float threshold, uint8_t* d_mask, void* stream);
+
+/* Packs the bodies with d_mask[i] == 0, in index order, to the front of
+ * d_packed (n entries) and switches the rest of d_packed off (mode
+ * HYDRO_MODE_DISABLED), so an exact step over d_packed integrates only the
+ * rejected states; d_pos[i] = packed slot or -1, *d_n_packed = count.
+ * d_counts holds ceil(n / 256) words of scratch. */
+hydro_status hydro_nn_route(hydro_ctx* ctx, const hydro_body* d_bodies, const uint8_t* d_mask,
+                            uint32_t n, uint32_t* d_counts, hydro_body* d_packed, int32_t* d_pos,
+                            uint32_t* d_n_packed, void* stream);
+
+/* d_out[i][6] = body-frame wrench: columns 0..5 of d_z[i] (row stride ld)
+ * when d_pos[i] < 0, else R^T (Fb+Fdq+Fdf, Tb+Tdq+Tdf) of d_exact[d_pos[i]]. */
+hydro_status hydro_nn_merge(hydro_ctx* ctx, const hydro_body* d_bodies, const float* d_z, int32_t ld,
+                            const int32_t* d_pos, const hydro_wrench* d_exact, uint32_t n,
+                            float* d_out, void* stream);
+
+/* d_out[i][6] = R^T (Fb+Fdq+Fdf, Tb+Tdq+Tdf) of d_wrenches[i]: the
+ * surrogate's training target. */
+hydro_status hydro_nn_wrench_body(hydro_ctx* ctx, const hydro_body* d_bodies,
+                                  const hydro_wrench* d_wrenches, uint32_t n, float* d_out,
+                                  void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -175,6 +175,18 @@ def _declare(lib: C.CDLL) -> None:
         "hydro_debug_wait_timeout": (i32, [vp, u32, C.POINTER(i32)]),
         "hydro_compute_wrenches_static": (i32, [vp, vp, u32, vp, C.POINTER(Ocean), C.POINTER(Settings),
                                                 vp, vp]),
+        "hydro_nn_gemm": (i32, [vp, i32, vp, i32, vp, i32, i32, i32, i32, vp, vp, vp, vp, i32, vp]),
+        "hydro_nn_transpose": (i32, [vp, vp, vp, i32, i32, vp]),
+        "hydro_nn_mse_grad": (i32, [vp, vp, vp, i32, i32, i32, vp, vp, vp]),
+        "hydro_nn_colsum": (i32, [vp, vp, i32, i32, vp, vp]),
+        "hydro_nn_adamw": (i32, [vp, vp, vp, vp, vp, i32, i32, i32, C.c_float, C.c_float, C.c_float,
+                                 C.c_float, C.c_float, i32, vp, vp, vp]),
+        "hydro_nn_to_bf16": (i32, [vp, vp, i32, i32, i32, vp, vp, vp, vp]),
+        "hydro_nn_features": (i32, [vp, vp, u32, C.POINTER(Ocean), vp, vp]),
+        "hydro_nn_gate": (i32, [vp, vp, u32, vp, vp, vp, vp, C.c_float, vp, vp]),
+        "hydro_nn_route": (i32, [vp, vp, vp, u32, vp, vp, vp, vp, vp]),
+        "hydro_nn_merge": (i32, [vp, vp, vp, i32, vp, vp, u32, vp, vp]),
+        "hydro_nn_wrench_body": (i32, [vp, vp, vp, u32, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -302,6 +302,7 @@ hydro_status batch_launch(hydro_batch* b, const hydro_body* d_bodies, const hydr
     P.bparams = b->bparams_d;
     P.err = b->err_d;
     P.work = b->err_d + 32;
+    P.active_end = b->err_d + 48;
     P.chunk_active = b->chunk_active_d;
     P.n_bodies = b->n_bodies;
     P.n_chunks = b->n_chunks;
@@ -871,6 +872,132 @@ extern "C" hydro_status hydro_debug_wait_timeout(hydro_ctx* ctx, uint32_t limit_
     return HYDRO_OK;
 }
 
+// ====================================================== surrogate kernels
+#define NN_CTX_CHECK()                                                                        \
+    if (!ctx) return HYDRO_ERR_INVALID_ARG;                                                   \
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);                                        \
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, HYDRO_ERR_DEVICE, "cudaSetDevice")
+
+#define NN_RET(e, what) return (e) == cudaSuccess ? HYDRO_OK : cuda_fail(ctx, (e), (what))
+
+extern "C" hydro_status hydro_nn_gemm(hydro_ctx* ctx, int32_t epilogue, const void* A, int32_t lda,
+                                      const void* B, int32_t ldb, int32_t M, int32_t N, int32_t K,
+                                      float* z, void* y, const float* bias, const float* zprev,
+                                      int32_t ldc, void* stream)
+{
+    NN_CTX_CHECK();
+    if (!A || !B || M <= 0 || N <= 0 || K <= 0 || M % 64 || N % 64 || K % 32 || lda < K || ldb < N ||
+        ldc < N || epilogue < 0 || epilogue > 3)
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn gemm: bad shape (M, N multiples of 64, K of 32)");
+    if ((epilogue == 0 || epilogue == 1 || epilogue == 2) && !z)
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn gemm: missing z");
+    if ((epilogue == 1 || epilogue == 3) && !y) return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn gemm: missing y");
+    if ((epilogue == 1 || epilogue == 2) && !bias) return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn gemm: missing bias");
+    if (epilogue == 3 && !zprev) return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn gemm: missing zprev");
+    cudaError_t e = launch_gemm(epilogue, A, lda, B, ldb, M, N, K, z, y, bias, zprev, ldc,
+                                static_cast<cudaStream_t>(stream));
+    NN_RET(e, "nn gemm");
+}
+
+extern "C" hydro_status hydro_nn_transpose(hydro_ctx* ctx, const void* src, void* dst, int32_t rows,
+                                           int32_t cols, void* stream)
+{
+    NN_CTX_CHECK();
+    if (!src || !dst || rows <= 0 || cols <= 0) return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn transpose");
+    NN_RET(launch_transpose(src, dst, rows, cols, static_cast<cudaStream_t>(stream)), "nn transpose");
+}
+
+extern "C" hydro_status hydro_nn_mse_grad(hydro_ctx* ctx, const float* z, const float* target, int32_t rows,
+                                          int32_t ld, int32_t n_out, void* dz, double* loss, void* stream)
+{
+    NN_CTX_CHECK();
+    if (!z || !target || !dz || !loss || rows <= 0 || n_out <= 0 || ld < n_out)
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn mse");
+    NN_RET(launch_mse_grad(z, target, rows, ld, n_out, dz, loss, static_cast<cudaStream_t>(stream)), "nn mse");
+}
+
+extern "C" hydro_status hydro_nn_colsum(hydro_ctx* ctx, const void* g, int32_t rows, int32_t cols, float* out,
+                                        void* stream)
+{
+    NN_CTX_CHECK();
+    if (!g || !out || rows <= 0 || cols <= 0) return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn colsum");
+    NN_RET(launch_colsum(g, rows, cols, out, static_cast<cudaStream_t>(stream)), "nn colsum");
+}
+
+extern "C" hydro_status hydro_nn_adamw(hydro_ctx* ctx, float* w, float* m, float* v, const float* grad,
+                                       int32_t rows, int32_t cols, int32_t ldg, float lr, float beta1,
+                                       float beta2, float eps, float weight_decay, int32_t step, void* w16,
+                                       void* wt16, void* stream)
+{
+    NN_CTX_CHECK();
+    if (!w || !m || !v || !grad || rows <= 0 || cols <= 0 || ldg < cols || step < 1)
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn adamw");
+    NN_RET(launch_adamw(w, m, v, grad, rows, cols, ldg, lr, beta1, beta2, eps, weight_decay, step, w16, wt16,
+                        static_cast<cudaStream_t>(stream)), "nn adamw");
+}
+
+extern "C" hydro_status hydro_nn_to_bf16(hydro_ctx* ctx, const float* x, int32_t rows, int32_t n_in, int32_t ld,
+                                         const float* mean, const float* istd, void* y, void* stream)
+{
+    NN_CTX_CHECK();
+    if (!x || !y || rows <= 0 || n_in <= 0 || ld < n_in || (!mean) != (!istd))
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn to_bf16");
+    NN_RET(launch_to_bf16(x, rows, n_in, ld, mean, istd, y, static_cast<cudaStream_t>(stream)), "nn to_bf16");
+}
+
+extern "C" hydro_status hydro_nn_features(hydro_ctx* ctx, const hydro_body* d_bodies, uint32_t n,
+                                          const hydro_ocean* ocean, float* d_features, void* stream)
+{
+    NN_CTX_CHECK();
+    if (!d_bodies || !d_features || !valid_ocean(ocean)) return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn features");
+    if (ocean->waves && !ctx->wave_d) return fail(ctx, HYDRO_ERR_INVALID_ARG, "no wave grid");
+    NN_RET(launch_features(d_bodies, n, make_ocean(ctx, ocean), d_features, static_cast<cudaStream_t>(stream)),
+           "nn features");
+}
+
+extern "C" hydro_status hydro_nn_gate(hydro_ctx* ctx, const float* d_features, uint32_t n, const float* lo,
+                                      const float* hi, const float* mean, const float* precision,
+                                      float threshold, uint8_t* d_mask, void* stream)
+{
+    NN_CTX_CHECK();
+    if (!d_features || !lo || !hi || !mean || !precision || !d_mask)
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn gate");
+    NN_RET(launch_gate(d_features, n, lo, hi, mean, precision, threshold, d_mask,
+                       static_cast<cudaStream_t>(stream)), "nn gate");
+}
+
+extern "C" hydro_status hydro_nn_wrench_body(hydro_ctx* ctx, const hydro_body* d_bodies,
+                                             const hydro_wrench* d_wrenches, uint32_t n, float* d_out,
+                                             void* stream)
+{
+    NN_CTX_CHECK();
+    if (!d_bodies || !d_wrenches || !d_out) return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn wrench_body");
+    NN_RET(launch_wrench_body(d_bodies, d_wrenches, n, d_out, static_cast<cudaStream_t>(stream)),
+           "nn wrench_body");
+}
+
+extern "C" hydro_status hydro_nn_route(hydro_ctx* ctx, const hydro_body* d_bodies, const uint8_t* d_mask,
+                                       uint32_t n, uint32_t* d_counts, hydro_body* d_packed, int32_t* d_pos,
+                                       uint32_t* d_n_packed, void* stream)
+{
+    NN_CTX_CHECK();
+    if (!d_bodies || !d_mask || !d_counts || !d_packed || !d_pos || !d_n_packed)
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn route");
+    NN_RET(launch_route(d_bodies, d_mask, n, d_counts, d_packed, d_pos, d_n_packed,
+                        static_cast<cudaStream_t>(stream)), "nn route");
+}
+
+extern "C" hydro_status hydro_nn_merge(hydro_ctx* ctx, const hydro_body* d_bodies, const float* d_z, int32_t ld,
+                                       const int32_t* d_pos, const hydro_wrench* d_exact, uint32_t n,
+                                       float* d_out, void* stream)
+{
+    NN_CTX_CHECK();
+    if (!d_bodies || !d_z || ld < 6 || !d_pos || !d_exact || !d_out)
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn merge");
+    NN_RET(launch_merge(d_bodies, d_z, ld, d_pos, d_exact, n, d_out, static_cast<cudaStream_t>(stream)),
+           "nn merge");
+}
+
 // ====================================================== allocation-free step
 // Some callers cannot allocate device memory while they run: a simulator
 // that evaluates the hydrodynamics inside its real-time tick (cudaMalloc
@@ -999,6 +1126,7 @@ extern "C" hydro_status hydro_compute_wrenches_static(hydro_ctx* ctx, const hydr
     P.partials = reinterpret_cast<double*>(base + off_partials);
     P.err = reinterpret_cast<unsigned*>(base + off_err);
     P.work = reinterpret_cast<unsigned*>(base + off_err) + 32;
+    P.active_end = reinterpret_cast<unsigned*>(base + off_err) + 48;
     P.chunk_active = reinterpret_cast<uint8_t*>(base + off_active);
     P.n_bodies = n_bodies;
     P.n_chunks = (uint32_t)nc;

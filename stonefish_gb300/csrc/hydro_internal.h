@@ -18,6 +18,7 @@ struct KParams {
     double* partials;        // n_chunks * kPartialStride
     unsigned* err;           // per-launch error word (bit 0: a bounded wait timed out)
     unsigned* work;          // chunk counter of the persistent kernel
+    unsigned* active_end;    // 1 + last chunk with a face loop (atomicMax in prep, reset by finalize)
     uint8_t* chunk_active;   // per chunk: 1 when its body runs a face loop
     uint32_t n_bodies;
     uint32_t n_chunks;
@@ -74,5 +75,31 @@ cudaError_t launch_packed_check(uint64_t n, uint64_t seed, unsigned long long* c
 cudaError_t launch_wait_timeout(uint64_t limit_ns, int* status, cudaStream_t s);
 
 cudaError_t launch_depth(OceanDev ocean, const float* xyz, uint32_t n, float* out, cudaStream_t s);
+
+// ----------------------------------------------------- surrogate kernels
+// C[M,N] = A[M,K] * B[K,N] (BF16 row-major, FP32 accumulate) with epilogue
+// epi: 0 z = C; 1 z = C + bias, y = bf16(silu(z)); 2 z = C + bias;
+// 3 y = bf16(C * silu'(zprev)).  M, N multiples of 64, K of 32.
+cudaError_t launch_gemm(int epi, const void* A, int lda, const void* B, int ldb, int M, int N, int K,
+                        float* z, void* y, const float* bias, const float* zprev, int ldc,
+                        cudaStream_t s);
+cudaError_t launch_transpose(const void* src, void* dst, int rows, int cols, cudaStream_t s);
+cudaError_t launch_mse_grad(const float* z, const float* t, int rows, int ld, int n_out, void* dz,
+                            double* loss, cudaStream_t s);
+cudaError_t launch_colsum(const void* g, int rows, int cols, float* out, cudaStream_t s);
+cudaError_t launch_adamw(float* w, float* m, float* v, const float* grad, int rows, int cols, int ldg,
+                         float lr, float b1, float b2, float eps, float wd, int step, void* w16,
+                         void* wt16, cudaStream_t s);
+cudaError_t launch_to_bf16(const float* x, int rows, int n_in, int ld, const float* mean, const float* istd,
+                           void* y, cudaStream_t s);
+cudaError_t launch_features(const hydro_body* bodies, uint32_t n, OceanDev o, float* f, cudaStream_t s);
+cudaError_t launch_gate(const float* f, uint32_t n, const float* lo, const float* hi, const float* mean,
+                        const float* P, float thresh, uint8_t* mask, cudaStream_t s);
+cudaError_t launch_route(const hydro_body* bodies, const uint8_t* mask, uint32_t n, uint32_t* counts,
+                         hydro_body* packed, int32_t* pos, uint32_t* n_packed, cudaStream_t s);
+cudaError_t launch_merge(const hydro_body* bodies, const float* z, int ld, const int32_t* pos,
+                         const hydro_wrench* exact, uint32_t n, float* out, cudaStream_t s);
+cudaError_t launch_wrench_body(const hydro_body* bodies, const hydro_wrench* w, uint32_t n, float* out,
+                               cudaStream_t s);
 
 }  // namespace sfh

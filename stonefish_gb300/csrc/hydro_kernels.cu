@@ -421,6 +421,9 @@ __global__ void prep_kernel(const KParams P)
     P.bparams[b] = B;
     const uint8_t active = (B.loop != LOOP_NONE) ? 1 : 0;
     for (uint32_t c = 0; c < bi.n_chunks; ++c) P.chunk_active[bi.first_chunk + c] = active;
+    // chunks are numbered body by body, so the producers can stop after the
+    // last active one (bodies switched off at the end of a batch cost nothing)
+    if (active && bi.n_chunks) atomicMax(P.active_end, bi.first_chunk + bi.n_chunks);
 }
 
 // ------------------------------------------------------------ main kernel
@@ -464,8 +467,9 @@ __device__ __forceinline__ void producer(const KParams& P, ChunkSmem& S)
     uint32_t item = 0;
     bool ok = true;
     // claims run one chunk ahead so that the atomic's latency overlaps work
+    const uint32_t end = min(P.n_chunks, *P.active_end);
     uint32_t next = atomicAdd(P.work, 1u);
-    while (ok && next < P.n_chunks) {
+    while (ok && next < end) {
         const uint32_t c = next;
         const ChunkDesc ch = P.chunks[c];
         const uint8_t active = P.chunk_active[c];
@@ -698,6 +702,7 @@ __global__ void finalize_kernel(const KParams P)
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const uint32_t body = blockIdx.x * kWarps + warp;
+    if (body == 0 && lane == 0) *P.active_end = 0u;   // the chunk kernel has finished with it
     if (body >= P.n_bodies) return;
     const BodyParams B = P.bparams[body];
     const BodyInfo bi = P.binfo[body];
