@@ -194,6 +194,146 @@ def fp64_error_sample(sc, gpu_io, n: int = 128) -> dict:
             "sample_bodies": int(len(pick))}
 
 
+# ------------------------------------------------------------- surrogate
+MLP_FLOP_PER_EVAL = 2.0 * (16 * 256 + 256 * 256 + 256 * 256 + 256 * 6)   # unpadded 16-256-256-256-6
+
+
+def measured_tensor_peak() -> tuple[float, str]:
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        if "bf16_tflops" in d:
+            return float(d["bf16_tflops"]), "measured"
+    return 1900.0, "fallback"
+
+
+def surrogate_bench(args, device: int) -> dict:
+    """The learned wrench surrogate on the 12000-face torpedo hull over the
+    wave field: label ``--sur-train`` states with the exact step (FP64 cut
+    points), train the MLP with the library's kernels, then time gated
+    inference over batches of 65536 states against the exact FP32 step on
+    the same states.  Eight distinct state batches (240 MB of body records,
+    more than L2) are cycled through the timed steps."""
+    import torch
+
+    from stonefish_gb300 import abi, scenarios
+    from stonefish_gb300 import surrogate as S
+    from stonefish_gb300.hydro import HydroContext
+
+    t_setup = time.perf_counter()
+    h64 = HydroContext(device, cut_precision=abi.CUT_FP64)
+    h32 = HydroContext(device)
+    xyz, fc = S.hull_mesh()
+    waves = scenarios.wave_grid()
+    m64, m32 = h64.upload_mesh(xyz, fc), h32.upload_mesh(xyz, fc)
+    h64.set_wave_grid(waves)
+    h32.set_wave_grid(waves)
+    ocean, st = S.wave_ocean(), scenarios.settings()
+    lab = S.Labeller(h64, m64, ocean, st)
+    t0 = time.perf_counter()
+    F, T = S.generate(lab, args.sur_train, seed=101)
+    torch.cuda.synchronize()
+    t_gen = time.perf_counter() - t0
+    sur = S.Surrogate(h32, batch=args.sur_batch)
+    info = sur.fit(F, T, epochs=args.sur_epochs, lr=args.sur_lr)
+    del F, T
+    nB, n_sets = 65536, 8
+    rng = np.random.default_rng(202)
+    sets, d_sets = [], []
+    for _ in range(n_sets):
+        b = S.sample_states(rng, nB)
+        b["mesh"] = m32
+        sets.append(b)
+        d_sets.append(torch.from_numpy(np.frombuffer(b.tobytes(), dtype=np.uint8).copy()).cuda())
+    Ft = torch.empty((nB, 16), dtype=torch.float32, device="cuda")
+    Tt = torch.empty((nB, 6), dtype=torch.float32, device="cuda")
+    lab.label(sets[0], Ft, Tt)
+    gp = S.GatedPredictor(sur, h32, m32, nB, ocean, st)
+    out = gp.predict(d_sets[0]).cpu().numpy()
+    err = S.wrench_errors(out, Tt.cpu().numpy(), ocean)
+    rejected = gp.rejected()
+    setup_s = time.perf_counter() - t_setup
+
+    steps = max(8, min(args.steps, 400))
+    stream = torch.cuda.current_stream()
+    for i in range(max(args.warmup, 3)):
+        gp.predict(d_sets[i % n_sets])
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in range(steps):
+        gp.predict(d_sets[i % n_sets])
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    # the MLP alone (four GEMMs), for the tensor-core roofline
+    bufs = sur._infer_bufs(nB)
+    for _ in range(3):
+        sur._mlp(bufs, nB)
+    e0.record(stream)
+    for _ in range(steps):
+        sur._mlp(bufs, nB)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_mlp = e0.elapsed_time(e1) / steps
+    # the exact FP32 step on the same states
+    bx = h32.batch(np.full(nB, m32, dtype=np.uint32))
+    io = torch.zeros(nB * abi.WRENCH_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    sp = stream.cuda_stream
+    for i in range(2):
+        bx.compute_device(d_sets[i].data_ptr(), ocean, st, io.data_ptr(), sp)
+    torch.cuda.synchronize()
+    ex_steps = 4
+    e0.record(stream)
+    for i in range(ex_steps):
+        bx.compute_device(d_sets[i % n_sets].data_ptr(), ocean, st, io.data_ptr(), sp)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_exact = e0.elapsed_time(e1) / ex_steps
+    # end to end: pinned host states in, body-frame wrenches out
+    h_in = torch.from_numpy(np.frombuffer(sets[0].tobytes(), dtype=np.uint8).copy()).pin_memory()
+    h_out = torch.empty((nB, 6), dtype=torch.float32).pin_memory()
+    d_in = torch.empty_like(d_sets[0])
+    e2e_steps = max(4, steps // 4)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        d_in.copy_(h_in, non_blocking=True)
+        h_out.copy_(gp.predict(d_in), non_blocking=True)
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    peak, kind = measured_tensor_peak()
+    achieved = MLP_FLOP_PER_EVAL * nB / (ms_mlp / 1e3) / 1e12
+    res = {
+        "value": nB / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "states_per_step": nB,
+        "workload": "torpedo_12000_faces_on_1024x1024_wave_grid, 65536 states per step",
+        "exact_fp32_gpu": {"value": nB / (ms_exact / 1e3), "unit": UNIT, "ms_per_step": ms_exact,
+                           "faces_per_s": nB * len(fc) / (ms_exact / 1e3)},
+        "speedup_vs_exact_gpu": ms_exact / ms,
+        "error": dict(err, metric="|dF| / (rho g V), |dT| / (rho g V L/2); wrench = max of the two; "
+                                  "against exact labels (FP32 faces, FP64 cut points and sums)"),
+        "gate_rejected_frac": rejected / nB,
+        "train": {"samples": args.sur_train, "epochs": args.sur_epochs, "batch": args.sur_batch,
+                  "lr": args.sur_lr, "label_s": t_gen, "train_s": info["seconds"],
+                  "train_samples_per_s": info["samples_per_s"], "final_loss": info["loss"][-1]},
+        "e2e": {"value": nB / e2e_s, "unit": UNIT,
+                "h2d_bytes_per_step": int(nB * abi.BODY_DTYPE.itemsize),
+                "d2h_bytes_per_step": int(nB * 6 * 4)},
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "peak_source": kind, "traffic": None,
+                     "kernel": "four BF16 GEMMs of the MLP (mma.sync m16n8k16), timed together",
+                     "flop_rule": f"{MLP_FLOP_PER_EVAL:.0f} FLOP per state (unpadded layers)"},
+        "gpu_launches_per_step": gp.launches,
+        "setup_s": setup_s,
+    }
+    for o in (bx, gp, lab):
+        o.close()
+    h32.close()
+    h64.close()
+    return res
+
+
 # ---------------------------------------------------------------- GPU arm
 def run_gpu(args, rank: int, world: int, local_rank: int, dist):
     import torch
@@ -311,6 +451,9 @@ def run_gpu(args, rank: int, world: int, local_rank: int, dist):
     }
     if not args.no_error:
         result["error_vs_fp64"] = fp64_error_sample(sc, gpu_io)
+    if not args.no_surrogate and world == 1:
+        batch.close()
+        result["surrogate"] = surrogate_bench(args, local_rank)
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         cpu_s, n = cpu_baseline(sc, threads)
@@ -366,6 +509,11 @@ def main():
     ap.add_argument("--cut", default="fp32", choices=["fp64", "fp32"])
     ap.add_argument("--chunk-faces", type=int, default=0)
     ap.add_argument("--ctas-per-sm", type=int, default=0)
+    ap.add_argument("--no-surrogate", action="store_true")
+    ap.add_argument("--sur-train", type=int, default=10_000_000)
+    ap.add_argument("--sur-epochs", type=int, default=6)
+    ap.add_argument("--sur-batch", type=int, default=1024)
+    ap.add_argument("--sur-lr", type=float, default=1e-3)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

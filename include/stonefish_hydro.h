@@ -380,7 +380,7 @@ hydro_status hydro_debug_arith_check(hydro_ctx* ctx, uint64_t n_pairs, uint64_t 
 
 #define HYDRO_NN_FEATURES 16
 #define HYDRO_NN_EPI_F32 0        /* z = A B */
-#define HYDRO_NN_EPI_BIAS_SILU 1  /* z = A B + bias, y = bf16(silu(z)) */
+#define HYDRO_NN_EPI_BIAS_SILU 1  /* z = A B + bias, y = bf16(silu(z)); z may be NULL */
 #define HYDRO_NN_EPI_BIAS 2       /* z = A B + bias */
 #define HYDRO_NN_EPI_SILU_GRAD 3  /* y = bf16((A B) * silu'(zprev)) */
 
@@ -398,10 +398,13 @@ hydro_status hydro_nn_transpose(hydro_ctx* ctx, const void* src, void* dst, int3
                                 int32_t cols, void* stream);
 
 /* Mean-squared-error gradient over the first n_out of ld columns of z
- * against target[rows][n_out]: dz (bf16, rows x ld, other columns zero)
- * = 2 (z - target) / (rows n_out); *loss += the mean squared error. */
+ * against the normalised target t' = (target - tmean) * tistd (tmean and
+ * tistd both NULL: t' = target), target[rows][n_out]: dz (bf16, rows x ld,
+ * other columns zero) = 2 (z - t') / (rows n_out); *loss += the mean
+ * squared error when loss is non-NULL. */
 hydro_status hydro_nn_mse_grad(hydro_ctx* ctx, const float* z, const float* target, int32_t rows,
-                               int32_t ld, int32_t n_out, void* dz, double* loss, void* stream);
+                               int32_t ld, int32_t n_out, const float* tmean, const float* tistd,
+                               void* dz, double* loss, void* stream);
 
 /* out[c] = sum over rows of the bf16 matrix g[rows][cols] (bias gradients). */
 hydro_status hydro_nn_colsum(hydro_ctx* ctx, const void* g, int32_t rows, int32_t cols, float* out,
@@ -423,8 +426,9 @@ hydro_status hydro_nn_to_bf16(hydro_ctx* ctx, const float* x, int32_t rows, int3
 
 /* The 16 features of each body state, FP32 [n][16]: depth of the CG below
  * the local surface, roll, pitch, body-frame v[3], omega[3] and current[3],
- * wave elevation, wave slope along and across the heading, and the
- * surface's Laplacian at the CG (0 on a flat surface). */
+ * wave elevation at the CG, mean wave slope along and across the heading
+ * over +-1 m, and the surface curvature along the heading over +-1 m (the
+ * wave terms are 0 on a flat surface). */
 hydro_status hydro_nn_features(hydro_ctx* ctx, const hydro_body* d_bodies, uint32_t n,
                                const hydro_ocean* ocean, float* d_features, void* stream);
 

@@ -177,7 +177,7 @@ def _declare(lib: C.CDLL) -> None:
                                                 vp, vp]),
         "hydro_nn_gemm": (i32, [vp, i32, vp, i32, vp, i32, i32, i32, i32, vp, vp, vp, vp, i32, vp]),
         "hydro_nn_transpose": (i32, [vp, vp, vp, i32, i32, vp]),
-        "hydro_nn_mse_grad": (i32, [vp, vp, vp, i32, i32, i32, vp, vp, vp]),
+        "hydro_nn_mse_grad": (i32, [vp, vp, vp, i32, i32, i32, vp, vp, vp, vp, vp]),
         "hydro_nn_colsum": (i32, [vp, vp, i32, i32, vp, vp]),
         "hydro_nn_adamw": (i32, [vp, vp, vp, vp, vp, i32, i32, i32, C.c_float, C.c_float, C.c_float,
                                  C.c_float, C.c_float, i32, vp, vp, vp]),

@@ -889,7 +889,7 @@ extern "C" hydro_status hydro_nn_gemm(hydro_ctx* ctx, int32_t epilogue, const vo
     if (!A || !B || M <= 0 || N <= 0 || K <= 0 || M % 64 || N % 64 || K % 32 || lda < K || ldb < N ||
         ldc < N || epilogue < 0 || epilogue > 3)
         return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn gemm: bad shape (M, N multiples of 64, K of 32)");
-    if ((epilogue == 0 || epilogue == 1 || epilogue == 2) && !z)
+    if ((epilogue == 0 || epilogue == 2) && !z)
         return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn gemm: missing z");
     if ((epilogue == 1 || epilogue == 3) && !y) return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn gemm: missing y");
     if ((epilogue == 1 || epilogue == 2) && !bias) return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn gemm: missing bias");
@@ -908,12 +908,14 @@ extern "C" hydro_status hydro_nn_transpose(hydro_ctx* ctx, const void* src, void
 }
 
 extern "C" hydro_status hydro_nn_mse_grad(hydro_ctx* ctx, const float* z, const float* target, int32_t rows,
-                                          int32_t ld, int32_t n_out, void* dz, double* loss, void* stream)
+                                          int32_t ld, int32_t n_out, const float* tmean, const float* tistd,
+                                          void* dz, double* loss, void* stream)
 {
     NN_CTX_CHECK();
-    if (!z || !target || !dz || !loss || rows <= 0 || n_out <= 0 || ld < n_out)
+    if (!z || !target || !dz || rows <= 0 || n_out <= 0 || ld < n_out || (!tmean) != (!tistd))
         return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn mse");
-    NN_RET(launch_mse_grad(z, target, rows, ld, n_out, dz, loss, static_cast<cudaStream_t>(stream)), "nn mse");
+    NN_RET(launch_mse_grad(z, target, rows, ld, n_out, tmean, tistd, dz, loss, static_cast<cudaStream_t>(stream)),
+           "nn mse");
 }
 
 extern "C" hydro_status hydro_nn_colsum(hydro_ctx* ctx, const void* g, int32_t rows, int32_t cols, float* out,

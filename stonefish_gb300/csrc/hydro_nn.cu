@@ -127,8 +127,10 @@ __global__ void __launch_bounds__(128) gemm_kernel(const bf16* __restrict__ A, i
                 } else if (EPI == EPI_BIAS || EPI == EPI_BIAS_SILU) {
                     v0 += e.bias[c];
                     v1 += e.bias[c + 1];
-                    e.z[o] = v0;
-                    e.z[o + 1] = v1;
+                    if (EPI == EPI_BIAS || e.z) {   // inference needs no pre-activations
+                        e.z[o] = v0;
+                        e.z[o + 1] = v1;
+                    }
                     if (EPI == EPI_BIAS_SILU) {
                         e.y[o] = __float2bfloat16(v0 * sigmoidf_(v0));
                         e.y[o + 1] = __float2bfloat16(v1 * sigmoidf_(v1));
@@ -187,11 +189,14 @@ cudaError_t launch_transpose(const void* src, void* dst, int rows, int cols, cud
     return cudaGetLastError();
 }
 
-// Masked mean-squared error on the first n_out of ld columns: dZ (BF16,
-// padded columns zero) = 2 (z - t) / (rows * n_out), loss_acc += sum (z - t)^2
-// / (rows * n_out), summed per block in FP32 and added in FP64.
+// Masked mean-squared error on the first n_out of ld columns against the
+// normalised target t' = (t - tmean) * tistd (identity when tmean is null):
+// dZ (BF16, padded columns zero) = 2 (z - t') / (rows * n_out), and
+// loss += sum (z - t')^2 / (rows * n_out), summed per block in FP32 and
+// added in FP64.
 __global__ void mse_grad_kernel(const float* __restrict__ z, const float* __restrict__ t, int rows, int ld,
-                                int n_out, bf16* __restrict__ dz, double* loss)
+                                int n_out, const float* __restrict__ tmean, const float* __restrict__ tistd,
+                                bf16* __restrict__ dz, double* loss)
 {
     __shared__ float red[256];
     const size_t n = (size_t)rows * ld;
@@ -201,7 +206,9 @@ __global__ void mse_grad_kernel(const float* __restrict__ z, const float* __rest
         const int c = (int)(i % ld);
         float g = 0.f;
         if (c < n_out) {
-            const float d = z[i] - t[(i / ld) * n_out + c];
+            float tv = t[(i / ld) * n_out + c];
+            if (tmean) tv = (tv - tmean[c]) * tistd[c];
+            const float d = z[i] - tv;
             acc += d * d;
             g = 2.f * d * scale;
         }
@@ -213,13 +220,13 @@ __global__ void mse_grad_kernel(const float* __restrict__ z, const float* __rest
         if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
         __syncthreads();
     }
-    if (threadIdx.x == 0) atomicAdd(loss, (double)red[0] * (double)scale);
+    if (threadIdx.x == 0 && loss) atomicAdd(loss, (double)red[0] * (double)scale);
 }
 
-cudaError_t launch_mse_grad(const float* z, const float* t, int rows, int ld, int n_out, void* dz,
-                            double* loss, cudaStream_t s)
+cudaError_t launch_mse_grad(const float* z, const float* t, int rows, int ld, int n_out, const float* tmean,
+                            const float* tistd, void* dz, double* loss, cudaStream_t s)
 {
-    mse_grad_kernel<<<256, 256, 0, s>>>(z, t, rows, ld, n_out, static_cast<bf16*>(dz), loss);
+    mse_grad_kernel<<<256, 256, 0, s>>>(z, t, rows, ld, n_out, tmean, tistd, static_cast<bf16*>(dz), loss);
     return cudaGetLastError();
 }
 
@@ -311,13 +318,16 @@ cudaError_t launch_to_bf16(const float* x, int rows, int n_in, int ld, const flo
 }
 
 // ---------------------------------------------------------------- features
-// The 16 surrogate features of a body state: depth (CG z minus the surface
-// z at the CG, NED), roll, pitch (Z-Y-X Euler angles of T_CG), body-frame
-// linear velocity, body-frame angular velocity, body-frame current, wave
-// elevation, wave slope (central differences of the lookup, rotated into the
-// heading frame so that the features do not depend on yaw through the
-// slope), and the wave-surface curvature (five-point Laplacian) at the CG,
-// which stands in for the phase of a multi-component sea.
+// The 16 surrogate features of a body state: depth of the CG below the
+// local surface (NED), roll, pitch (Z-Y-X Euler angles of T_CG), body-frame
+// linear velocity, body-frame angular velocity, body-frame current, and four
+// numbers describing the wave surface around the hull: the elevation at the
+// CG, the mean slope along and across the heading over +-kWaveReach, and the
+// curvature along the heading over the same reach (second difference of the
+// elevations ahead of and behind the CG).  The heading is the horizontal
+// projection of the body x axis, so the wave features do not depend on yaw.
+constexpr float kWaveReach = 1.0f;
+
 __global__ void features_kernel(const hydro_body* __restrict__ bodies, uint32_t n, OceanDev o, float* __restrict__ f)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -325,16 +335,27 @@ __global__ void features_kernel(const hydro_body* __restrict__ bodies, uint32_t 
     const hydro_body& b = bodies[i];
     const double* R = b.T_CG.basis;
     const double x = b.T_CG.origin[0], y = b.T_CG.origin[1], z = b.T_CG.origin[2];
-    float h = 0.f, hx = 0.f, hy = 0.f, lap = 0.f;
+    double hx = R[0], hy = R[3];
+    const double hn = sqrt(hx * hx + hy * hy);
+    if (hn > 1e-9) {
+        hx /= hn;
+        hy /= hn;
+    } else {   // body x axis vertical: any heading
+        hx = 1.0;
+        hy = 0.0;
+    }
+    float h = 0.f, s_al = 0.f, s_ac = 0.f, k_al = 0.f;
     if (o.waves) {
-        const float d = 0.05f;
-        const float fx = (float)x, fy = (float)y;
+        const float a = kWaveReach;
+        const float fx = (float)x, fy = (float)y, ux = (float)hx, uy = (float)hy;
         h = -wave_height(o, fx, fy);
-        const float hxp = -wave_height(o, fx + d, fy), hxm = -wave_height(o, fx - d, fy);
-        const float hyp = -wave_height(o, fx, fy + d), hym = -wave_height(o, fx, fy - d);
-        hx = (hxp - hxm) / (2.f * d);
-        hy = (hyp - hym) / (2.f * d);
-        lap = (hxp + hxm + hyp + hym - 4.f * h) / (d * d);
+        const float ef = -wave_height(o, fx + a * ux, fy + a * uy);
+        const float eb = -wave_height(o, fx - a * ux, fy - a * uy);
+        const float el = -wave_height(o, fx - a * uy, fy + a * ux);
+        const float er = -wave_height(o, fx + a * uy, fy - a * ux);
+        s_al = (ef - eb) / (2.f * a);
+        s_ac = (el - er) / (2.f * a);
+        k_al = (ef + eb - 2.f * h) / (a * a);
     }
     // R^T u for the body-frame vectors
     auto tb = [&](const double* u, float* out) {
@@ -350,12 +371,10 @@ __global__ void features_kernel(const hydro_body* __restrict__ bodies, uint32_t 
     tb(b.omega, o16 + 6);
     double u[3] = {o.U[0], o.U[1], o.U[2]};
     tb(u, o16 + 9);
-    const double yaw = atan2(R[3], R[0]);
-    const float cy = (float)cos(yaw), sy = (float)sin(yaw);
     o16[12] = h;
-    o16[13] = hx * cy + hy * sy;
-    o16[14] = hy * cy - hx * sy;
-    o16[15] = lap;
+    o16[13] = s_al;
+    o16[14] = s_ac;
+    o16[15] = k_al;
 }
 
 cudaError_t launch_features(const hydro_body* bodies, uint32_t n, OceanDev o, float* f, cudaStream_t s)

@@ -67,6 +67,7 @@ class HydroContext:
         if st != abi.HYDRO_OK:
             raise abi.HydroError(st, "hydro_create: " + lib.hydro_status_string(st).decode())
         self.ctx = h
+        self.device = device
         self.cut_precision = cut_precision
         self.mesh_faces: dict[int, int] = {}
 

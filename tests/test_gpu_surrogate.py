@@ -1,0 +1,280 @@
+"""GPU checks of the learned wrench surrogate: each kernel against a CPU
+restatement (oracle/mlp.py for the network and its gradients), the gate
+routing, and an end-to-end run that trains a small network and shows what
+it gains over the exact step."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from oracle import mlp  # noqa: E402
+from stonefish_gb300 import abi, scenarios  # noqa: E402
+from stonefish_gb300 import surrogate as S  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def _bf16(t):
+    return mlp.bf16_bits_to_f32(t.contiguous().view(torch.int16).cpu().numpy())
+
+
+def _dev(a, dtype=torch.float32):
+    return torch.tensor(np.asarray(a), dtype=dtype, device="cuda")
+
+
+def _ck(h, st):
+    assert st == abi.HYDRO_OK, h.lib.hydro_last_error(h.ctx)
+
+
+@pytest.mark.parametrize("epi", [0, 1, 2, 3])
+def test_gemm_epilogues(hctx, epi):
+    rng = np.random.default_rng(epi)
+    M, N, K = 128, 192, 96
+    A = mlp.bf16_round(rng.normal(size=(M, K)).astype(np.float32))
+    B = mlp.bf16_round(rng.normal(size=(K, N)).astype(np.float32))
+    bias = rng.normal(size=N).astype(np.float32)
+    zprev = rng.normal(size=(M, N)).astype(np.float32)
+    dA, dB = _dev(A, torch.bfloat16), _dev(B, torch.bfloat16)
+    z = torch.zeros((M, N), dtype=torch.float32, device="cuda")
+    y = torch.zeros((M, N), dtype=torch.bfloat16, device="cuda")
+    db, dzp = _dev(bias), _dev(zprev)
+    P = S._ptr
+    _ck(hctx, hctx.lib.hydro_nn_gemm(hctx.ctx, epi, P(dA), K, P(dB), N, M, N, K, P(z), P(y), P(db), P(dzp), N,
+                                     None))
+    torch.cuda.synchronize()
+    ref = A.astype(np.float64) @ B.astype(np.float64)
+    scale = np.abs(A).astype(np.float64) @ np.abs(B).astype(np.float64)
+    if epi in (0, 2):
+        r = ref + (bias if epi == 2 else 0.0)
+        assert np.all(np.abs(z.cpu().numpy() - r) <= 1e-5 * (scale + np.abs(bias)) + 1e-6)
+    elif epi == 1:
+        r = ref + bias
+        zz = z.cpu().numpy()
+        assert np.all(np.abs(zz - r) <= 1e-5 * (scale + np.abs(bias)) + 1e-6)
+        yy = _bf16(y)
+        expect = mlp.silu(zz.astype(np.float64))
+        assert np.all(np.abs(yy - expect) <= 2.0 ** -8 * np.abs(expect) + 1e-6)
+    else:
+        yy = _bf16(y)
+        expect = ref * mlp.silu_grad(zprev.astype(np.float64))
+        tol = 2.0 ** -8 * np.abs(expect) + 2e-5 * scale * np.abs(mlp.silu_grad(zprev.astype(np.float64)))
+        assert np.all(np.abs(yy - expect) <= tol + 1e-6)
+
+
+def test_gemm_rejects_unaligned_shapes(hctx):
+    a = torch.zeros((64, 64), dtype=torch.bfloat16, device="cuda")
+    z = torch.zeros((64, 64), dtype=torch.float32, device="cuda")
+    P = S._ptr
+    st = hctx.lib.hydro_nn_gemm(hctx.ctx, 0, P(a), 64, P(a), 64, 64, 64, 48, P(z), None, None, None, 64, None)
+    assert st == abi.HYDRO_ERR_INVALID_ARG
+    st = hctx.lib.hydro_nn_gemm(hctx.ctx, 1, P(a), 64, P(a), 64, 64, 64, 64, P(z), None, None, None, 64, None)
+    assert st == abi.HYDRO_ERR_INVALID_ARG   # no y / bias
+
+
+def test_training_gradients_match_oracle(hctx):
+    """One forward/backward pass of the full network on the GPU against the
+    CPU restatement with the same bfloat16 rounding points."""
+    rng = np.random.default_rng(5)
+    B = 256
+    sur = S.Surrogate(hctx, hidden=256, seed=3, batch=B)
+    feats = _dev(rng.normal(size=(4 * B, S.N_FEAT)) * 2.0 + 1.0)
+    targ = _dev(rng.normal(size=(4 * B, S.N_OUT)) * 50.0)
+    sur.fit_normalisation(feats, targ)
+    X = sur.prepare_inputs(feats)[:B]
+    T = targ[:B]
+    sur.forward_backward(X, T)
+    torch.cuda.synchronize()
+    x0 = _bf16(X).astype(np.float64)
+    Ws = [_bf16(L["w16"]).astype(np.float64) for L in sur.layers]
+    bs = [L["b"].cpu().numpy().astype(np.float64) for L in sur.layers]
+    t = T.cpu().numpy()
+    tn = ((t - sur.t_mean.cpu().numpy()) * sur.t_istd.cpu().numpy()).astype(np.float32).astype(np.float64)
+    dWs, dbs = mlp.backward(x0, Ws, bs, tn, S.N_OUT, bf16=True)
+    for l, L in enumerate(sur.layers):
+        gw = L["gw"].cpu().numpy()
+        gb = L["gb"].cpu().numpy()
+        ew = np.linalg.norm(gw - dWs[l]) / max(np.linalg.norm(dWs[l]), 1e-30)
+        eb = np.linalg.norm(gb - dbs[l]) / max(np.linalg.norm(dbs[l]), 1e-30)
+        assert ew < 5e-3 and eb < 5e-3, (l, ew, eb)
+    # and the bf16-free FP64 gradients agree to bfloat16 accuracy
+    dW64, _ = mlp.backward(x0, Ws, bs, tn, S.N_OUT, bf16=False)
+    for l in range(4):
+        e = np.linalg.norm(sur.layers[l]["gw"].cpu().numpy() - dW64[l]) / np.linalg.norm(dW64[l])
+        assert e < 5e-2, (l, e)
+
+
+def test_adamw_step(hctx):
+    rng = np.random.default_rng(2)
+    rows, cols = 3, 70
+    w = rng.normal(size=(rows, cols)).astype(np.float32)
+    m = rng.normal(size=(rows, cols)).astype(np.float32) * 0.1
+    v = np.abs(rng.normal(size=(rows, cols))).astype(np.float32) * 0.01
+    g = rng.normal(size=(rows, cols)).astype(np.float32)
+    dw, dm, dv, dg = _dev(w), _dev(m), _dev(v), _dev(g)
+    w16 = torch.zeros((rows, cols), dtype=torch.bfloat16, device="cuda")
+    wt16 = torch.zeros((cols, rows), dtype=torch.bfloat16, device="cuda")
+    lr, b1, b2, eps, wd, step = 1e-2, 0.9, 0.999, 1e-8, 0.01, 7
+    P = S._ptr
+    _ck(hctx, hctx.lib.hydro_nn_adamw(hctx.ctx, P(dw), P(dm), P(dv), P(dg), rows, cols, cols, lr, b1, b2, eps, wd,
+                                      step, P(w16), P(wt16), None))
+    torch.cuda.synchronize()
+    m1 = b1 * m + (1 - b1) * g
+    v1 = b2 * v + (1 - b2) * g * g
+    mh = m1 / (1 - b1 ** step)
+    vh = v1 / (1 - b2 ** step)
+    w1 = w * (1 - lr * wd) - lr * mh / (np.sqrt(vh) + eps)
+    assert np.allclose(dw.cpu().numpy(), w1, rtol=1e-5, atol=1e-6)
+    assert np.allclose(dm.cpu().numpy(), m1, rtol=1e-6, atol=1e-7)
+    assert np.array_equal(_bf16(w16), mlp.bf16_round(dw.cpu().numpy()))
+    assert np.array_equal(_bf16(wt16), mlp.bf16_round(dw.cpu().numpy()).T)
+
+
+def test_features_flat_ocean(hctx):
+    rng = np.random.default_rng(8)
+    n = 300
+    bodies = S.sample_states(rng, n)
+    ocean = scenarios.flat_ocean(current=(0.2, -0.1, 0.05))
+    d_b = torch.from_numpy(np.frombuffer(bodies.tobytes(), dtype=np.uint8).copy()).cuda()
+    f = torch.zeros((n, 16), dtype=torch.float32, device="cuda")
+    _ck(hctx, hctx.lib.hydro_nn_features(hctx.ctx, S._ptr(d_b), n, C.byref(ocean), S._ptr(f), None))
+    torch.cuda.synchronize()
+    f = f.cpu().numpy()
+    R = bodies["T_CG"]["basis"].reshape(n, 3, 3)
+    z = bodies["T_CG"]["origin"][:, 2]
+    assert np.allclose(f[:, 0], z, atol=1e-6)
+    assert np.allclose(f[:, 1], np.arctan2(R[:, 2, 1], R[:, 2, 2]), atol=1e-5)
+    assert np.allclose(f[:, 2], np.arcsin(np.clip(-R[:, 2, 0], -1, 1)), atol=1e-5)
+    vb = np.einsum("nji,nj->ni", R, bodies["v"])
+    wb = np.einsum("nji,nj->ni", R, bodies["omega"])
+    cb = np.einsum("nji,j->ni", R, np.array([0.2, -0.1, 0.05]))
+    assert np.allclose(f[:, 3:6], vb, atol=1e-5)
+    assert np.allclose(f[:, 6:9], wb, atol=1e-5)
+    assert np.allclose(f[:, 9:12], cb, atol=1e-6)
+    assert np.all(f[:, 12:] == 0.0)
+
+
+def test_gate_and_routing(hctx):
+    rng = np.random.default_rng(9)
+    n = 1000
+    feats = rng.normal(size=(n, 16)).astype(np.float32)
+    feats[::7, 3] = 9.0                       # outside the box
+    lo = np.full(16, -4.0, np.float32)
+    hi = np.full(16, 4.0, np.float32)
+    mean = np.zeros(16, np.float32)
+    Pm = np.eye(16, dtype=np.float32)
+    thr = 30.0
+    mask = torch.zeros(n, dtype=torch.uint8, device="cuda")
+    df = _dev(feats)
+    P = S._ptr
+    keep = [_dev(lo), _dev(hi), _dev(mean), _dev(Pm)]   # referenced until the kernel has run
+    _ck(hctx, hctx.lib.hydro_nn_gate(hctx.ctx, P(df), n, *[P(t) for t in keep], thr, P(mask), None))
+    torch.cuda.synchronize()
+    inbox = np.all((feats >= lo) & (feats <= hi), axis=1)
+    q = np.sum(feats.astype(np.float64) ** 2, axis=1)
+    expect = inbox & (q <= thr)
+    near = np.abs(q - thr) < 1e-3
+    got = mask.cpu().numpy().astype(bool)
+    assert np.array_equal(got[~near], expect[~near])
+    assert (~got).sum() > n // 7
+
+    # routing: rejected bodies packed in order, the rest of the slots off
+    bodies = S.sample_states(rng, n)
+    bodies["reserved"] = np.arange(n)
+    d_b = torch.from_numpy(np.frombuffer(bodies.tobytes(), dtype=np.uint8).copy()).cuda()
+    counts = torch.zeros((n + 255) // 256, dtype=torch.int32, device="cuda")
+    packed = torch.zeros(n * abi.BODY_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    pos = torch.zeros(n, dtype=torch.int32, device="cuda")
+    npk = torch.zeros(1, dtype=torch.int32, device="cuda")
+    _ck(hctx, hctx.lib.hydro_nn_route(hctx.ctx, P(d_b), P(mask), n, P(counts), P(packed), P(pos), P(npk), None))
+    torch.cuda.synchronize()
+    rej = np.nonzero(~got)[0]
+    k = int(npk.item())
+    assert k == rej.size
+    pk = np.frombuffer(packed.cpu().numpy().tobytes(), dtype=abi.BODY_DTYPE)
+    assert np.array_equal(pk["reserved"][:k], rej)
+    assert np.all(pk["mode"][k:] == abi.MODE_DISABLED)
+    p = pos.cpu().numpy()
+    assert np.array_equal(p[rej], np.arange(k))
+    assert np.all(p[got] == -1)
+
+    # merge: surrogate rows for accepted bodies, rotated exact wrench for the rest
+    z = rng.normal(size=(n, 64)).astype(np.float32)
+    ex = np.zeros(n, dtype=abi.WRENCH_DTYPE)
+    for key in ("Fb", "Tb", "Fdq", "Tdq", "Fdf", "Tdf"):
+        ex[key] = rng.normal(size=(n, 3))
+    d_ex = torch.from_numpy(np.frombuffer(ex.tobytes(), dtype=np.uint8).copy()).cuda()
+    out = torch.zeros((n, 6), dtype=torch.float32, device="cuda")
+    dz = _dev(z)
+    _ck(hctx, hctx.lib.hydro_nn_merge(hctx.ctx, P(d_b), P(dz), 64, P(pos), P(d_ex), n, P(out), None))
+    torch.cuda.synchronize()
+    o = out.cpu().numpy()
+    assert np.array_equal(o[got], z[got, :6])
+    R = bodies["T_CG"]["basis"].reshape(n, 3, 3)
+    F = ex["Fb"] + ex["Fdq"] + ex["Fdf"]
+    T = ex["Tb"] + ex["Tdq"] + ex["Tdf"]
+    Fb = np.einsum("nji,nj->ni", R[rej], F[p[rej]])
+    Tb = np.einsum("nji,nj->ni", R[rej], T[p[rej]])
+    assert np.allclose(o[rej, :3], Fb, rtol=1e-6, atol=1e-5)
+    assert np.allclose(o[rej, 3:], Tb, rtol=1e-6, atol=1e-5)
+
+
+def test_surrogate_learns_and_beats_exact_step(built_library):
+    """Trains a network on 1M states labelled by the exact step, then
+    shows the gain: its wrench error is far below a constant predictor's,
+    and its gated evaluation is much faster than the exact step."""
+    from stonefish_gb300.hydro import HydroContext
+
+    h64 = HydroContext(0, cut_precision=abi.CUT_FP64)
+    h32 = HydroContext(0)
+    xyz, fc = S.hull_mesh()
+    waves = scenarios.wave_grid()
+    m64, m32 = h64.upload_mesh(xyz, fc), h32.upload_mesh(xyz, fc)
+    h64.set_wave_grid(waves)
+    h32.set_wave_grid(waves)
+    ocean, st = S.wave_ocean(), scenarios.settings()
+    lab = S.Labeller(h64, m64, ocean, st)
+    F, T = S.generate(lab, 1 << 20, seed=21)
+    n_test = 8192
+    rng = np.random.default_rng(22)
+    test_bodies = S.sample_states(rng, n_test)
+    Ft = torch.empty((n_test, 16), dtype=torch.float32, device="cuda")
+    Tt = torch.empty((n_test, 6), dtype=torch.float32, device="cuda")
+    lab.label(test_bodies, Ft, Tt)
+    sur = S.Surrogate(h32, batch=1024)
+    info = sur.fit(F, T, epochs=4, lr=1e-3)
+    assert info["loss"][-1] < 0.2 * info["loss"][0]
+    tt = Tt.cpu().numpy()
+    gp = S.GatedPredictor(sur, h32, m32, n_test, ocean, st)
+    test_bodies["mesh"] = m32
+    d_b = torch.from_numpy(np.frombuffer(test_bodies.tobytes(), dtype=np.uint8).copy()).cuda()
+    out = gp.predict(d_b).cpu().numpy()
+    err = S.wrench_errors(out, tt, ocean)
+    const = S.wrench_errors(np.tile(tt.mean(0), (n_test, 1)), tt, ocean)
+    assert err["wrench_median"] < 0.15 * const["wrench_median"], (err, const)
+    assert err["wrench_median"] < 2.5e-2, err
+    assert gp.rejected() < n_test // 20
+
+    def timed(fn, reps):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    bx = h32.batch(np.full(n_test, m32, dtype=np.uint32))
+    io = torch.zeros(n_test * abi.WRENCH_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    t_exact = timed(lambda: bx.compute_device(d_b.data_ptr(), ocean, st, io.data_ptr(), s), 5)
+    t_sur = timed(lambda: gp.predict(d_b), 10)
+    assert t_sur * 5 < t_exact, (t_sur, t_exact)
+    for o in (bx, gp, lab):
+        o.close()
+    h32.close()
+    h64.close()
