@@ -334,6 +334,88 @@ def surrogate_bench(args, device: int) -> dict:
     return res
 
 
+# --------------------------------------------------------------- rollout
+def rollout_bench(args, device: int) -> dict:
+    """16384 hulls (8000-face torpedo, 50 kg, four fixed body-frame thrusts
+    U(-20,20) N) over the wave field, 1000 steps of dt = 0.01 s by
+    semi-implicit Euler, captured as one CUDA graph per rollout: once with
+    the exact step and once with the surrogate (trained here on the same
+    hull) behind its gate.  Reports env-steps/s of each and how far the two
+    trajectories drift apart."""
+    import torch
+
+    from stonefish_gb300 import abi, scenarios
+    from stonefish_gb300 import rollout as RO
+    from stonefish_gb300 import surrogate as S
+    from stonefish_gb300.hydro import HydroContext
+
+    n, steps, faces = args.roll_envs, args.roll_steps, 8000
+    t_setup = time.perf_counter()
+    h64 = HydroContext(device, cut_precision=abi.CUT_FP64)
+    h32 = HydroContext(device)
+    xyz, fc = S.hull_mesh(faces)
+    waves = scenarios.wave_grid()
+    m64, m32 = h64.upload_mesh(xyz, fc), h32.upload_mesh(xyz, fc)
+    h64.set_wave_grid(waves)
+    h32.set_wave_grid(waves)
+    ocean, st = S.wave_ocean(), scenarios.settings()
+    lab = S.Labeller(h64, m64, ocean, st)
+    surf = RO.surface_z(h32, ocean)
+    # training envelope of the floating hulls: CG within 0.6 m below to 0.5 m
+    # above the local surface, |v| components to 2 m/s, |omega| to 1 rad/s
+    F, T = S.generate(lab, args.roll_train, seed=303, depth=(-0.5, 0.6), v_range=2.0, w_range=1.0,
+                      surface=surf)
+    sur = S.Surrogate(h32, batch=args.sur_batch)
+    sur.fit(F, T, epochs=args.sur_epochs, lr=args.sur_lr)
+    del F, T
+    lab.close()
+    init = RO.initial_states(np.random.default_rng(404), n, surface=surf)
+    ex = RO.Rollout(h32, m32, n, ocean, st, "exact")
+    ex.reset(init)
+    k_ex = ex.capture(steps)
+    gp = S.GatedPredictor(sur, h32, m32, n, ocean, st)
+    su = RO.Rollout(h32, m32, n, ocean, st, "surrogate", predictor=gp)
+    su.reset(init)
+    k_su = su.capture(steps)
+    # the same exact rollout with FP64 cut points: how far two exact
+    # evaluations that differ only in rounding drift apart (chaos floor)
+    e64 = RO.Rollout(h64, m64, n, ocean, st, "exact")
+    e64.reset(init)
+    k_64 = e64.capture(steps)
+    setup_s = time.perf_counter() - t_setup
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    res = {}
+    for name, ro, k in (("exact", ex, k_ex), ("surrogate", su, k_su), ("exact_fp64_cut", e64, k_64)):
+        ro.reset(init)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        ro.replay()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        res[name] = {"env_steps_per_s": n * steps / (ms / 1e3), "ms_per_step": ms / steps,
+                     "rollout_s": ms / 1e3, "gpu_launches_per_step": k / steps}
+    res["surrogate"]["gate_rejected_last_step"] = gp.rejected()
+    a, b, c = ex.snapshots(), su.snapshots(), e64.snapshots()
+    res["divergence"] = {f"step_{(i + 1) * 100}": RO.divergence(a[i], b[i], init) for i in range(len(a))}
+    res["divergence_exact_fp32_vs_fp64_cut"] = {f"step_{(i + 1) * 100}": RO.divergence(a[i], c[i], init)
+                                                for i in range(len(a))}
+    res["exact"]["states"] = {f"step_{(i + 1) * 100}": RO.state_stats(a[i]) for i in range(len(a))}
+    res["surrogate"]["states"] = {f"step_{(i + 1) * 100}": RO.state_stats(b[i]) for i in range(len(b))}
+    res["finite"] = bool(all(np.all(np.isfinite(r.host_states()["p"])) for r in (ex, su, e64)))
+    res["speedup_surrogate_vs_exact"] = res["exact"]["rollout_s"] / res["surrogate"]["rollout_s"]
+    res["workload"] = (f"{n} torpedo hulls x {faces} faces, 50 kg, 4 thrusters U(-20,20) N, dt 0.01 s, "
+                       f"{steps} steps in one CUDA graph, 1024x1024 wave grid; surrogate trained on "
+                       f"{args.roll_train} exact-labelled states of the same hull")
+    res["setup_s"] = setup_s
+    for o in (ex, su, gp, e64):
+        o.close()
+    h32.close()
+    h64.close()
+    return res
+
+
 # ---------------------------------------------------------------- GPU arm
 def run_gpu(args, rank: int, world: int, local_rank: int, dist):
     import torch
@@ -454,6 +536,8 @@ def run_gpu(args, rank: int, world: int, local_rank: int, dist):
     if not args.no_surrogate and world == 1:
         batch.close()
         result["surrogate"] = surrogate_bench(args, local_rank)
+    if not args.no_rollout and world == 1:
+        result["rollout"] = rollout_bench(args, local_rank)
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         cpu_s, n = cpu_baseline(sc, threads)
@@ -510,6 +594,10 @@ def main():
     ap.add_argument("--chunk-faces", type=int, default=0)
     ap.add_argument("--ctas-per-sm", type=int, default=0)
     ap.add_argument("--no-surrogate", action="store_true")
+    ap.add_argument("--no-rollout", action="store_true")
+    ap.add_argument("--roll-envs", type=int, default=16384)
+    ap.add_argument("--roll-steps", type=int, default=1000)
+    ap.add_argument("--roll-train", type=int, default=4_000_000)
     ap.add_argument("--sur-train", type=int, default=10_000_000)
     ap.add_argument("--sur-epochs", type=int, default=6)
     ap.add_argument("--sur-batch", type=int, default=1024)

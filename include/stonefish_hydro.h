@@ -461,6 +461,53 @@ hydro_status hydro_nn_wrench_body(hydro_ctx* ctx, const hydro_body* d_bodies,
                                   const hydro_wrench* d_wrenches, uint32_t n, float* d_out,
                                   void* stream);
 
+/* ------------------------------------------------------------------------
+ * Device-resident rigid-body rollout (no counterpart in the reference,
+ * which integrates bodies with Bullet on the CPU).
+ *
+ * State of one free hull, integrated without contacts the way Bullet
+ * integrates a Stonefish rigid body (btRigidBody with the implicit
+ * gyroscopic term, which SolidEntity::BuildRigidBody enables,
+ * SolidEntity.cpp:1076-1086): semi-implicit Euler for the velocities, one
+ * Newton step of implicit Euler for the gyroscopic term, positions from the
+ * new velocities and orientation by the exponential map.  q is the
+ * body-to-world rotation as a unit quaternion (w, x, y, z); p, v, w are the
+ * CG position, linear and angular velocity in the world frame (NED); the
+ * thrust wrench is fixed in the body frame (about the CG).  mass weighs the
+ * hull (gravity = mass g); inertial_mass divides the force and inertia is
+ * the diagonal body-frame inertia about the CG -- for a SUBMERGED body the
+ * reference uses mass + added mass and Ipri + added inertia there
+ * (SolidEntity::getAugmentedMass/getAugmentedInertia, :657-670).
+ * half_extents is the collision-shape AABB half size in the body frame (the
+ * body record's AABB is its rotation).
+ * ---------------------------------------------------------------------- */
+typedef struct hydro_rigid_state {
+    double p[3];
+    double q[4];
+    double v[3];
+    double w[3];
+    double thrust_force[3];
+    double thrust_torque[3];
+    double mass;
+    double inertial_mass;
+    double inertia[3];
+    double half_extents[3];
+} hydro_rigid_state;
+
+/* One step of dt seconds for n hulls.  The hydrodynamic wrench comes from
+ * d_exact (world-frame hydro_wrench results of a step on d_bodies) or, when
+ * d_exact is NULL, from d_body_wrench (body-frame F[3], T[3] per hull, e.g.
+ * the surrogate's output); both NULL integrates thrust and gravity only.
+ * gravity is g along +z.  Updates d_states and rewrites the pose, velocity
+ * and AABB fields of d_bodies (other fields are left as they are). */
+hydro_status hydro_rigid_step(hydro_ctx* ctx, hydro_rigid_state* d_states, hydro_body* d_bodies,
+                              const hydro_wrench* d_exact, const float* d_body_wrench, uint32_t n,
+                              double dt, double gravity, void* stream);
+
+/* Writes the pose, velocity and AABB fields of d_bodies from d_states. */
+hydro_status hydro_rigid_write_bodies(hydro_ctx* ctx, const hydro_rigid_state* d_states,
+                                      hydro_body* d_bodies, uint32_t n, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

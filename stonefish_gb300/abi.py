@@ -80,6 +80,12 @@ class Wrench(C.Structure):
                 ("position", C.c_int32), ("status", C.c_int32)]
 
 
+class RigidState(C.Structure):
+    _fields_ = [("p", _d3), ("q", C.c_double * 4), ("v", _d3), ("w", _d3),
+                ("thrust_force", _d3), ("thrust_torque", _d3), ("mass", C.c_double),
+                ("inertial_mass", C.c_double), ("inertia", _d3), ("half_extents", _d3)]
+
+
 class Config(C.Structure):
     _fields_ = [("device", C.c_int32), ("cut_precision", C.c_int32),
                 ("tile_faces", C.c_uint32), ("ctas_per_sm", C.c_uint32),
@@ -111,6 +117,7 @@ BODY_DTYPE = _dtype_of(Body)
 WRENCH_DTYPE = _dtype_of(Wrench)
 OCEAN_DTYPE = _dtype_of(Ocean)
 CURRENT_DTYPE = _dtype_of(Current)
+RIGID_DTYPE = _dtype_of(RigidState)
 
 WRENCH_VECTORS = ("Fb", "Tb", "Fdq", "Tdq", "Fdf", "Tdf")
 
@@ -187,6 +194,8 @@ def _declare(lib: C.CDLL) -> None:
         "hydro_nn_route": (i32, [vp, vp, vp, u32, vp, vp, vp, vp, vp]),
         "hydro_nn_merge": (i32, [vp, vp, vp, i32, vp, vp, u32, vp, vp]),
         "hydro_nn_wrench_body": (i32, [vp, vp, vp, u32, vp, vp]),
+        "hydro_rigid_step": (i32, [vp, vp, vp, vp, vp, u32, C.c_double, C.c_double, vp]),
+        "hydro_rigid_write_bodies": (i32, [vp, vp, vp, u32, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -1000,6 +1000,26 @@ extern "C" hydro_status hydro_nn_merge(hydro_ctx* ctx, const hydro_body* d_bodie
            "nn merge");
 }
 
+// ====================================================== rigid-body rollout
+extern "C" hydro_status hydro_rigid_step(hydro_ctx* ctx, hydro_rigid_state* d_states, hydro_body* d_bodies,
+                                         const hydro_wrench* d_exact, const float* d_body_wrench, uint32_t n,
+                                         double dt, double gravity, void* stream)
+{
+    NN_CTX_CHECK();
+    if (!d_states || !d_bodies || !(dt > 0.0)) return fail(ctx, HYDRO_ERR_INVALID_ARG, "rigid step");
+    NN_RET(launch_rigid_step(d_states, d_bodies, d_exact, d_body_wrench, n, dt, gravity,
+                             static_cast<cudaStream_t>(stream)), "rigid step");
+}
+
+extern "C" hydro_status hydro_rigid_write_bodies(hydro_ctx* ctx, const hydro_rigid_state* d_states,
+                                                 hydro_body* d_bodies, uint32_t n, void* stream)
+{
+    NN_CTX_CHECK();
+    if (!d_states || !d_bodies) return fail(ctx, HYDRO_ERR_INVALID_ARG, "rigid write bodies");
+    NN_RET(launch_rigid_write_bodies(d_states, d_bodies, n, static_cast<cudaStream_t>(stream)),
+           "rigid write bodies");
+}
+
 // ====================================================== allocation-free step
 // Some callers cannot allocate device memory while they run: a simulator
 // that evaluates the hydrodynamics inside its real-time tick (cudaMalloc

@@ -102,4 +102,9 @@ cudaError_t launch_merge(const hydro_body* bodies, const float* z, int ld, const
 cudaError_t launch_wrench_body(const hydro_body* bodies, const hydro_wrench* w, uint32_t n, float* out,
                                cudaStream_t s);
 
+cudaError_t launch_rigid_step(hydro_rigid_state* states, hydro_body* bodies, const hydro_wrench* exact,
+                              const float* body_wrench, uint32_t n, double dt, double gravity, cudaStream_t s);
+cudaError_t launch_rigid_write_bodies(const hydro_rigid_state* states, hydro_body* bodies, uint32_t n,
+                                      cudaStream_t s);
+
 }  // namespace sfh

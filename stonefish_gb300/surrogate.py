@@ -63,17 +63,20 @@ def hull_scales(ocean: abi.Ocean) -> tuple[float, float]:
 
 
 def sample_states(rng: np.random.Generator, n: int, depth=(-1.0, 0.3), extent: float = 102.4,
-                  v_range: float = 1.0, w_range: float = 0.5) -> np.ndarray:
-    """Hull states drawn uniformly: CG x, y over the wave grid, CG depth in
-    ``depth``, uniform random orientation, v in [-v_range, v_range]^3,
-    omega in [-w_range, w_range]^3 (the single-body and wave workloads'
-    ranges).  Returns a hydro_body array with mesh id 0."""
+                  v_range: float = 1.0, w_range: float = 0.5, surface=None) -> np.ndarray:
+    """Hull states drawn uniformly: CG x, y over the wave grid, CG z in
+    ``depth`` (below the local surface when ``surface(xy) -> z`` is given,
+    else absolute), uniform random orientation, v in [-v_range, v_range]^3,
+    omega in [-w_range, w_range]^3 (the defaults are the single-body and
+    wave workloads' ranges).  Returns a hydro_body array with mesh id 0."""
     q = scenarios.random_quaternions(rng, n)
     R = scenarios.quat_to_matrix(q)
     pos = np.empty((n, 3))
     pos[:, 0] = rng.uniform(0.0, extent, n)
     pos[:, 1] = rng.uniform(0.0, extent, n)
     pos[:, 2] = rng.uniform(depth[0], depth[1], n)
+    if surface is not None:
+        pos[:, 2] += surface(pos[:, :2])
     v = rng.uniform(-v_range, v_range, (n, 3))
     w = rng.uniform(-w_range, w_range, (n, 3))
     half = np.tile([0.5 * HULL_LENGTH + HULL_RADIUS, HULL_RADIUS, HULL_RADIUS], (n, 1))

@@ -17,7 +17,9 @@ LAYOUT_C = r"""
 #define S(T) printf(#T " %zu\n", sizeof(T))
 int main(void) {
   S(hydro_transform); S(hydro_settings); S(hydro_current); S(hydro_ocean);
-  S(hydro_body); S(hydro_wrench); S(hydro_config);
+  S(hydro_body); S(hydro_wrench); S(hydro_config); S(hydro_rigid_state);
+  P(hydro_rigid_state, q); P(hydro_rigid_state, thrust_torque); P(hydro_rigid_state, mass); P(hydro_rigid_state, inertial_mass);
+  P(hydro_rigid_state, half_extents);
   P(hydro_body, T_C); P(hydro_body, R_O); P(hydro_body, v); P(hydro_body, omega);
   P(hydro_body, Cd); P(hydro_body, Cf); P(hydro_body, P_CB); P(hydro_body, volume);
   P(hydro_body, surface); P(hydro_body, aabb_min); P(hydro_body, aabb_max);
@@ -40,7 +42,8 @@ def test_struct_layout_matches_header(tmp_path):
     got = {k: int(v) for k, v in got.items()}
     sizes = {"hydro_transform": abi.Transform, "hydro_settings": abi.Settings,
              "hydro_current": abi.Current, "hydro_ocean": abi.Ocean, "hydro_body": abi.Body,
-             "hydro_wrench": abi.Wrench, "hydro_config": abi.Config}
+             "hydro_wrench": abi.Wrench, "hydro_config": abi.Config,
+             "hydro_rigid_state": abi.RigidState}
     for name, st in sizes.items():
         assert got[name] == C.sizeof(st), name
     for key, off in got.items():
@@ -48,7 +51,7 @@ def test_struct_layout_matches_header(tmp_path):
             continue
         t, f = key.split(".")
         st = {"hydro_body": abi.Body, "hydro_wrench": abi.Wrench, "hydro_ocean": abi.Ocean,
-              "hydro_current": abi.Current}[t]
+              "hydro_current": abi.Current, "hydro_rigid_state": abi.RigidState}[t]
         assert getattr(st, f).offset == off, key
     assert abi.BODY_DTYPE.itemsize == got["hydro_body"]
     assert abi.WRENCH_DTYPE.itemsize == got["hydro_wrench"]
