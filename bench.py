@@ -125,8 +125,23 @@ def profile_traffic(workload: str):
     return None
 
 
+def hull_states_workload(faces: int, n_bodies: int, seed: int = 505):
+    """The surrogate's torpedo hull (``faces`` faces) at n seeded states over
+    the wave field, as an exact-step workload (the CPU reference arm of the
+    surrogate and rollout lines)."""
+    from stonefish_gb300 import scenarios
+    from stonefish_gb300 import surrogate as S
+    xyz, fc = S.hull_mesh(faces)
+    bodies = S.sample_states(np.random.default_rng(seed), n_bodies)
+    return {"meshes": [(xyz, fc)], "bodies": bodies, "ocean": S.wave_ocean(), "waves": scenarios.wave_grid()}
+
+
 def build_workload(name: str, n_bodies: int | None):
     from stonefish_gb300 import scenarios
+    if name == "surrogate":
+        return hull_states_workload(12000, n_bodies or 512)
+    if name == "rollout":
+        return hull_states_workload(8000, n_bodies or 512)
     if name == "batch":
         return scenarios.mixed_batch(n_bodies=n_bodies or 4096)
     if name == "waves":
@@ -141,7 +156,9 @@ def workload_config(name: str, sc) -> dict:
     per_body_faces = np.array([len(sc["meshes"][m][1]) for m in sc["bodies"]["mesh"]])
     cfg = {"workload": {"batch": "mixed_batch_4096_bodies_distinct_meshes",
                         "waves": "torpedo_hulls_on_1024x1024_wave_grid",
-                        "sphere": "single_icosphere_1280_faces_1000_states"}[name],
+                        "sphere": "single_icosphere_1280_faces_1000_states",
+                        "surrogate": "exact step on the 12000-face torpedo, seeded states over the wave grid",
+                        "rollout": "exact step on the 8000-face torpedo, seeded states over the wave grid"}[name],
            "bodies": int(len(sc["bodies"])), "faces_per_step": int(per_body_faces.sum()),
            "distinct_mesh_faces": nf, "surface": "waves" if sc["ocean"].waves else "flat",
            "current_mps": [0.2, 0.0, 0.0], "density": 1025.0,
@@ -416,6 +433,34 @@ def rollout_bench(args, device: int) -> dict:
     return res
 
 
+def section_line(args, rank: int, world: int, local_rank: int, dist):
+    """``--workload surrogate|rollout``: that section alone, as the line's
+    headline (one replica per rank; rank 0 reports its own replica)."""
+    if args.workload == "surrogate":
+        sec = surrogate_bench(args, local_rank)
+        value, unit, ms = sec["value"], UNIT, sec["ms_per_step"]
+        launches, e2e = sec["gpu_launches_per_step"], sec["e2e"]
+        roof = sec["roofline"]
+        cfg = {"workload": sec["workload"], "states_per_step": sec["states_per_step"]}
+        dtype = "bf16 MLP (fp32 accumulate), f32 exact fallback"
+    else:
+        sec = rollout_bench(args, local_rank)
+        value, unit = sec["surrogate"]["env_steps_per_s"], "env-steps/s"
+        ms = sec["surrogate"]["ms_per_step"]
+        launches = sec["surrogate"]["gpu_launches_per_step"]
+        e2e = None
+        roof = None
+        cfg = {"workload": sec["workload"]}
+        dtype = "f64 rigid state, f32 faces / bf16 MLP wrench"
+    if rank != 0:
+        return None
+    return {"metric": METRIC, "value": value * world, "unit": unit, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": dtype, "data": "synthetic (seeded states)",
+            "config": dict(cfg, parallelism=f"replicas x{world}" if world > 1 else "single GPU"),
+            "e2e": e2e, "roofline": roof, "gpu_launches": launches * args.steps, args.workload: sec}
+
+
 # ---------------------------------------------------------------- GPU arm
 def run_gpu(args, rank: int, world: int, local_rank: int, dist):
     import torch
@@ -424,6 +469,8 @@ def run_gpu(args, rank: int, world: int, local_rank: int, dist):
     from stonefish_gb300.hydro import HydroContext
 
     torch.cuda.set_device(local_rank)
+    if args.workload in ("surrogate", "rollout"):
+        return section_line(args, rank, world, local_rank, dist)
     t0 = time.perf_counter()
     sc = build_workload(args.workload, args.n_bodies)
     cfg, per_body_faces = workload_config(args.workload, sc)
@@ -570,14 +617,15 @@ def run_reference(args, rank: int):
                          waves=sc.get("waves"))
     nb = len(sc["bodies"])
     value = nb * steps / total
-    return {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": 1,
+    unit = "env-steps/s" if args.workload == "rollout" else UNIT
+    return {"metric": METRIC, "value": value, "unit": unit, "impl": "reference", "n_gpus": 1,
             "steps": steps, "warmup": min(args.warmup, 1), "ms_per_step": 1e3 * total / steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 faces (reference arithmetic)", "data": "synthetic", "config": cfg,
             "faces_per_s": int(per_body_faces.sum()) * steps / total,
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+            "cpu_baseline": {"value": value, "unit": unit, "cores": threads, "kind": "port",
                              "sample": f"{steps} full steps of the workload, capped at 10"},
-            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
 def main():
@@ -586,7 +634,7 @@ def main():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="batch", choices=["batch", "waves", "sphere"])
+    ap.add_argument("--workload", default="batch", choices=["batch", "waves", "sphere", "surrogate", "rollout"])
     ap.add_argument("--n-bodies", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-error", action="store_true")

@@ -232,16 +232,33 @@ hydro_status hydro_depth(hydro_ctx* ctx, const hydro_ocean* ocean,
  * (Ocean.cpp:219-268). */
 hydro_status hydro_batch_create(hydro_ctx* ctx, const hydro_mesh_id* mesh_of_body,
                                 uint32_t n_bodies, hydro_batch** out);
+
+/* As hydro_batch_create, with the work-chunk size of this batch in faces
+ * (rounded up to whole 384-face tiles, at most 16 tiles; 0 = the context's
+ * setting).  Small chunks suit batches of which only a few bodies are
+ * active at a time (no counterpart in the reference). */
+hydro_status hydro_batch_create_ex(hydro_ctx* ctx, const hydro_mesh_id* mesh_of_body,
+                                   uint32_t n_bodies, uint32_t chunk_faces, hydro_batch** out);
 void hydro_batch_destroy(hydro_batch* batch);
 
 /* Device-resident step: d_bodies and d_inout are device pointers; the call
  * enqueues on `stream` (a cudaStream_t, NULL = legacy default) and returns
- * without synchronising.  One launch per step (captured in a CUDA graph by
- * the library after its first call). */
+ * without synchronising.  Three kernel launches per step (per-body setup,
+ * the persistent face kernel, per-body finalisation); the call allocates
+ * nothing after the batch exists and may be captured into a CUDA graph. */
 hydro_status hydro_batch_compute_device(hydro_batch* batch, const hydro_body* d_bodies,
                                         const hydro_ocean* ocean,
                                         const hydro_settings* settings,
                                         hydro_wrench* d_inout, void* stream);
+
+/* As hydro_batch_compute_device for the first *d_count bodies only, the
+ * count read on the device when the step runs (e.g. written by an earlier
+ * kernel on the same stream); the other bodies' results are left as they
+ * are and cost nothing (no counterpart in the reference). */
+hydro_status hydro_batch_compute_device_prefix(hydro_batch* batch, const hydro_body* d_bodies,
+                                               const uint32_t* d_count, const hydro_ocean* ocean,
+                                               const hydro_settings* settings,
+                                               hydro_wrench* d_inout, void* stream);
 
 /* Host-buffer step: copies bodies and in-out wrenches host->device, runs the
  * step, copies the wrenches back and synchronises.  With pinned host memory

@@ -167,6 +167,9 @@ def _declare(lib: C.CDLL) -> None:
         "hydro_batch_create": (i32, [vp, vp, u32, C.POINTER(vp)]),
         "hydro_batch_destroy": (None, [vp]),
         "hydro_batch_compute_device": (i32, [vp, vp, C.POINTER(Ocean), C.POINTER(Settings), vp, vp]),
+        "hydro_batch_create_ex": (i32, [vp, vp, u32, u32, C.POINTER(vp)]),
+        "hydro_batch_compute_device_prefix": (i32, [vp, vp, vp, C.POINTER(Ocean), C.POINTER(Settings), vp,
+                                                    vp]),
         "hydro_batch_compute": (i32, [vp, vp, C.POINTER(Ocean), C.POINTER(Settings), vp]),
         "hydro_batch_last_launches": (u32, [vp]),
         "hydro_body_forces": (i32, [vp, vp, C.POINTER(Ocean), C.POINTER(Settings), vp]),

@@ -201,9 +201,9 @@ OceanDev make_ocean(const hydro_ctx* ctx, const hydro_ocean* o)
     return d;
 }
 
-uint32_t tiles_per_chunk(const hydro_ctx* ctx)
+uint32_t tiles_per_chunk(const hydro_ctx* ctx, uint32_t chunk_faces = 0)
 {
-    uint32_t faces = ctx->cfg.tile_faces ? ctx->cfg.tile_faces : 4096u;
+    uint32_t faces = chunk_faces ? chunk_faces : ctx->cfg.tile_faces ? ctx->cfg.tile_faces : 4096u;
     return std::min<uint32_t>((uint32_t)kMaxTilesPerChunk,
                               std::max<uint32_t>(1u, (faces + kTileFaces - 1) / kTileFaces));
 }
@@ -224,7 +224,7 @@ void batch_free(hydro_batch* b)
 }
 
 hydro_status batch_build(hydro_ctx* ctx, const hydro_mesh_id* mesh_of_body, uint32_t n,
-                         hydro_batch** out)
+                         hydro_batch** out, uint32_t chunk_faces = 0)
 {
     for (uint32_t i = 0; i < n; ++i) {
         if (mesh_of_body[i] != HYDRO_NO_MESH && mesh_of_body[i] >= ctx->meshes.size())
@@ -232,7 +232,7 @@ hydro_status batch_build(hydro_ctx* ctx, const hydro_mesh_id* mesh_of_body, uint
     }
     hydro_status st = sync_tiles(ctx);
     if (st != HYDRO_OK) return st;
-    const uint32_t tpc = tiles_per_chunk(ctx);
+    const uint32_t tpc = tiles_per_chunk(ctx, chunk_faces);
     std::vector<ChunkDesc> chunks;
     std::vector<BodyInfo> info(n);
     for (uint32_t i = 0; i < n; ++i) {
@@ -287,7 +287,7 @@ hydro_status batch_build(hydro_ctx* ctx, const hydro_mesh_id* mesh_of_body, uint
 
 hydro_status batch_launch(hydro_batch* b, const hydro_body* d_bodies, const hydro_ocean* ocean,
                           const hydro_settings* settings, hydro_wrench* d_io, cudaStream_t s,
-                          int op)
+                          int op, const uint32_t* d_count = nullptr)
 {
     hydro_ctx* ctx = b->ctx;
     hydro_status st = sync_tiles(ctx);
@@ -303,6 +303,7 @@ hydro_status batch_launch(hydro_batch* b, const hydro_body* d_bodies, const hydr
     P.err = b->err_d;
     P.work = b->err_d + 32;
     P.active_end = b->err_d + 48;
+    P.n_active = d_count;
     P.chunk_active = b->chunk_active_d;
     P.n_bodies = b->n_bodies;
     P.n_chunks = b->n_chunks;
@@ -610,6 +611,18 @@ hydro_status hydro_batch_create(hydro_ctx* ctx, const hydro_mesh_id* mesh_of_bod
     return batch_build(ctx, mesh_of_body, n_bodies, out);
 }
 
+hydro_status hydro_batch_create_ex(hydro_ctx* ctx, const hydro_mesh_id* mesh_of_body, uint32_t n_bodies,
+                                   uint32_t chunk_faces, hydro_batch** out)
+{
+    if (!ctx) return HYDRO_ERR_INVALID_ARG;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (!out || !mesh_of_body || n_bodies == 0)
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "batch: null pointer or no bodies");
+    *out = nullptr;
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, HYDRO_ERR_DEVICE, "cudaSetDevice");
+    return batch_build(ctx, mesh_of_body, n_bodies, out, chunk_faces);
+}
+
 void hydro_batch_destroy(hydro_batch* b)
 {
     if (!b) return;
@@ -629,6 +642,20 @@ hydro_status hydro_batch_compute_device(hydro_batch* b, const hydro_body* d_bodi
     if (!d_bodies || !d_inout || !settings || !valid_ocean(ocean))
         return fail(ctx, HYDRO_ERR_INVALID_ARG, "batch compute: bad arguments");
     return batch_launch(b, d_bodies, ocean, settings, d_inout, static_cast<cudaStream_t>(stream), OP_BODY);
+}
+
+hydro_status hydro_batch_compute_device_prefix(hydro_batch* b, const hydro_body* d_bodies,
+                                               const uint32_t* d_count, const hydro_ocean* ocean,
+                                               const hydro_settings* settings, hydro_wrench* d_inout,
+                                               void* stream)
+{
+    if (!b) return HYDRO_ERR_INVALID_ARG;
+    hydro_ctx* ctx = b->ctx;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (!d_bodies || !d_inout || !d_count || !settings || !valid_ocean(ocean))
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "batch compute prefix: bad arguments");
+    return batch_launch(b, d_bodies, ocean, settings, d_inout, static_cast<cudaStream_t>(stream), OP_BODY,
+                        d_count);
 }
 
 hydro_status hydro_batch_compute(hydro_batch* b, const hydro_body* bodies, const hydro_ocean* ocean,
@@ -912,7 +939,8 @@ extern "C" hydro_status hydro_nn_mse_grad(hydro_ctx* ctx, const float* z, const 
                                           void* dz, double* loss, void* stream)
 {
     NN_CTX_CHECK();
-    if (!z || !target || !dz || rows <= 0 || n_out <= 0 || ld < n_out || (!tmean) != (!tistd))
+    if (!z || !target || !dz || rows <= 0 || n_out <= 0 || ld < n_out || (!tmean) != (!tistd) ||
+        (uint64_t)rows * (uint64_t)ld >= (1ull << 32))
         return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn mse");
     NN_RET(launch_mse_grad(z, target, rows, ld, n_out, tmean, tistd, dz, loss, static_cast<cudaStream_t>(stream)),
            "nn mse");
@@ -942,7 +970,8 @@ extern "C" hydro_status hydro_nn_to_bf16(hydro_ctx* ctx, const float* x, int32_t
                                          const float* mean, const float* istd, void* y, void* stream)
 {
     NN_CTX_CHECK();
-    if (!x || !y || rows <= 0 || n_in <= 0 || ld < n_in || (!mean) != (!istd))
+    if (!x || !y || rows <= 0 || n_in <= 0 || ld < n_in || (!mean) != (!istd) ||
+        (uint64_t)rows * (uint64_t)ld >= (1ull << 32))
         return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn to_bf16");
     NN_RET(launch_to_bf16(x, rows, n_in, ld, mean, istd, y, static_cast<cudaStream_t>(stream)), "nn to_bf16");
 }
@@ -962,8 +991,8 @@ extern "C" hydro_status hydro_nn_gate(hydro_ctx* ctx, const float* d_features, u
                                       float threshold, uint8_t* d_mask, void* stream)
 {
     NN_CTX_CHECK();
-    if (!d_features || !lo || !hi || !mean || !precision || !d_mask)
-        return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn gate");
+    if (!d_features || !lo || !hi || !mean || !precision || !d_mask || (reinterpret_cast<uintptr_t>(d_features) & 15))
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn gate (features must be 16-byte aligned)");
     NN_RET(launch_gate(d_features, n, lo, hi, mean, precision, threshold, d_mask,
                        static_cast<cudaStream_t>(stream)), "nn gate");
 }

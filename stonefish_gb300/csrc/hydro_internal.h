@@ -19,6 +19,7 @@ struct KParams {
     unsigned* err;           // per-launch error word (bit 0: a bounded wait timed out)
     unsigned* work;          // chunk counter of the persistent kernel
     unsigned* active_end;    // 1 + last chunk with a face loop (atomicMax in prep, reset by finalize)
+    const uint32_t* n_active;  // optional (device): only bodies [0, *n_active) are evaluated
     uint8_t* chunk_active;   // per chunk: 1 when its body runs a face loop
     uint32_t n_bodies;
     uint32_t n_chunks;

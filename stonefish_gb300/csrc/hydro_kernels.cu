@@ -415,6 +415,7 @@ __global__ void prep_kernel(const KParams P)
         *P.work = 0u;
     }
     if (b >= P.n_bodies) return;
+    if (P.n_active && b >= *P.n_active) return;
     BodyParams B;
     const BodyInfo bi = P.binfo[b];
     body_prologue(P.bodies + b, bi.mesh, P.op, P.ocean, P.st, B);
@@ -704,6 +705,7 @@ __global__ void finalize_kernel(const KParams P)
     const uint32_t body = blockIdx.x * kWarps + warp;
     if (body == 0 && lane == 0) *P.active_end = 0u;   // the chunk kernel has finished with it
     if (body >= P.n_bodies) return;
+    if (P.n_active && body >= *P.n_active) return;
     const BodyParams B = P.bparams[body];
     const BodyInfo bi = P.binfo[body];
     double s = 0.0;

@@ -199,14 +199,14 @@ __global__ void mse_grad_kernel(const float* __restrict__ z, const float* __rest
                                 bf16* __restrict__ dz, double* loss)
 {
     __shared__ float red[256];
-    const size_t n = (size_t)rows * ld;
+    const uint32_t n = (uint32_t)rows * (uint32_t)ld;   // < 2^32, checked by the host
     const float scale = 1.f / (float)((size_t)rows * n_out);
     float acc = 0.f;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        const int c = (int)(i % ld);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t r = i / (uint32_t)ld, c = i - r * (uint32_t)ld;
         float g = 0.f;
-        if (c < n_out) {
-            float tv = t[(i / ld) * n_out + c];
+        if (c < (uint32_t)n_out) {
+            float tv = t[(size_t)r * n_out + c];
             if (tmean) tv = (tv - tmean[c]) * tistd[c];
             const float d = z[i] - tv;
             acc += d * d;
@@ -298,12 +298,13 @@ __global__ void to_bf16_kernel(const float* __restrict__ x, int rows, int n_in, 
                                const float* __restrict__ mean, const float* __restrict__ istd,
                                bf16* __restrict__ y)
 {
-    const size_t n = (size_t)rows * ld;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        const int c = (int)(i % ld);
+    // rows x ld < 2^32 (checked by the host), so 32-bit index arithmetic
+    const uint32_t n = (uint32_t)rows * (uint32_t)ld;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t r = i / (uint32_t)ld, c = i - r * (uint32_t)ld;
         float v = 0.f;
-        if (c < n_in) {
-            v = x[(i / ld) * n_in + c];
+        if (c < (uint32_t)n_in) {
+            v = x[(size_t)r * n_in + c];
             if (mean) v = (v - mean[c]) * istd[c];
         }
         y[i] = __float2bfloat16(v);
@@ -335,19 +336,20 @@ __global__ void features_kernel(const hydro_body* __restrict__ bodies, uint32_t 
     const hydro_body& b = bodies[i];
     const double* R = b.T_CG.basis;
     const double x = b.T_CG.origin[0], y = b.T_CG.origin[1], z = b.T_CG.origin[2];
-    double hx = R[0], hy = R[3];
-    const double hn = sqrt(hx * hx + hy * hy);
-    if (hn > 1e-9) {
-        hx /= hn;
-        hy /= hn;
+    // heading (unit horizontal projection of the body x axis), FP32
+    float ux = (float)R[0], uy = (float)R[3];
+    const float hn = sqrtf(ux * ux + uy * uy);
+    if (hn > 1e-6f) {
+        ux /= hn;
+        uy /= hn;
     } else {   // body x axis vertical: any heading
-        hx = 1.0;
-        hy = 0.0;
+        ux = 1.f;
+        uy = 0.f;
     }
     float h = 0.f, s_al = 0.f, s_ac = 0.f, k_al = 0.f;
     if (o.waves) {
         const float a = kWaveReach;
-        const float fx = (float)x, fy = (float)y, ux = (float)hx, uy = (float)hy;
+        const float fx = (float)x, fy = (float)y;
         h = -wave_height(o, fx, fy);
         const float ef = -wave_height(o, fx + a * ux, fy + a * uy);
         const float eb = -wave_height(o, fx - a * ux, fy - a * uy);
@@ -364,9 +366,9 @@ __global__ void features_kernel(const hydro_body* __restrict__ bodies, uint32_t 
         out[2] = (float)(R[2] * u[0] + R[5] * u[1] + R[8] * u[2]);
     };
     float* o16 = f + (size_t)i * 16;
-    o16[0] = (float)z + h;                 // depth below the local surface (NED: surface at -h)
-    o16[1] = (float)atan2(R[7], R[8]);     // roll
-    o16[2] = (float)asin(fmax(-1.0, fmin(1.0, -R[6])));   // pitch
+    o16[0] = (float)z + h;                          // depth below the local surface (NED: surface at -h)
+    o16[1] = atan2f((float)R[7], (float)R[8]);      // roll
+    o16[2] = asinf(fmaxf(-1.f, fminf(1.f, (float)-R[6])));   // pitch
     tb(b.v, o16 + 3);
     tb(b.omega, o16 + 6);
     double u[3] = {o.U[0], o.U[1], o.U[2]};
@@ -392,19 +394,36 @@ __global__ void gate_kernel(const float* __restrict__ f, uint32_t n, const float
                             const float* __restrict__ hi, const float* __restrict__ mean,
                             const float* __restrict__ P, float thresh, uint8_t* __restrict__ mask)
 {
+    __shared__ float Ps[256], ls[16], hs[16], ms[16];
+    for (int k = threadIdx.x; k < 256; k += blockDim.x) Ps[k] = P[k];
+    if (threadIdx.x < 16) {
+        ls[threadIdx.x] = lo[threadIdx.x];
+        hs[threadIdx.x] = hi[threadIdx.x];
+        ms[threadIdx.x] = mean[threadIdx.x];
+    }
+    __syncthreads();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float d[16];
     bool in = true;
-    for (int k = 0; k < 16; ++k) {
-        const float x = f[(size_t)i * 16 + k];
-        in = in && (x >= lo[k]) && (x <= hi[k]);
-        d[k] = x - mean[k];
+    const float4* f4 = reinterpret_cast<const float4*>(f + (size_t)i * 16);
+#pragma unroll
+    for (int k4 = 0; k4 < 4; ++k4) {
+        const float4 v = f4[k4];
+        const float xs[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int k = 4 * k4 + j;
+            in = in && (xs[j] >= ls[k]) && (xs[j] <= hs[k]);
+            d[k] = xs[j] - ms[k];
+        }
     }
     float q = 0.f;
+#pragma unroll
     for (int r = 0; r < 16; ++r) {
         float s = 0.f;
-        for (int c = 0; c < 16; ++c) s += P[r * 16 + c] * d[c];
+#pragma unroll
+        for (int c = 0; c < 16; ++c) s += Ps[r * 16 + c] * d[c];
         q += d[r] * s;
     }
     mask[i] = (in && q <= thresh) ? 1 : 0;

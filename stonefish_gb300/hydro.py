@@ -210,21 +210,21 @@ class HydroContext:
                                                         C.byref(ocean), C.byref(settings), d_io,
                                                         stream or None))
 
-    def batch(self, mesh_of_body) -> "Batch":
-        return Batch(self, mesh_of_body)
+    def batch(self, mesh_of_body, chunk_faces: int = 0) -> "Batch":
+        return Batch(self, mesh_of_body, chunk_faces)
 
 
 class Batch:
     """A fixed set of bodies (mesh per body) stepped together."""
 
-    def __init__(self, hctx: HydroContext, mesh_of_body):
+    def __init__(self, hctx: HydroContext, mesh_of_body, chunk_faces: int = 0):
         self.h = hctx
         self.lib = hctx.lib
         ids = np.ascontiguousarray(mesh_of_body, dtype=np.uint32)
         self.n = ids.size
         b = C.c_void_p()
-        _check(self.lib, hctx.ctx, self.lib.hydro_batch_create(hctx.ctx, ids.ctypes.data, ids.size,
-                                                               C.byref(b)))
+        _check(self.lib, hctx.ctx, self.lib.hydro_batch_create_ex(hctx.ctx, ids.ctypes.data, ids.size,
+                                                                  chunk_faces, C.byref(b)))
         self.b = b
 
     def close(self) -> None:
@@ -256,6 +256,12 @@ class Batch:
         """Device pointers in/out; enqueued on ``stream`` (cudaStream_t as int)."""
         _check(self.lib, self.h.ctx, self.lib.hydro_batch_compute_device(
             self.b, d_bodies, C.byref(ocean), C.byref(settings), d_io, stream or None))
+
+    def compute_device_prefix(self, d_bodies: int, d_count: int, ocean, settings, d_io: int,
+                              stream: int = 0) -> None:
+        """As compute_device for the first *d_count bodies (device uint32)."""
+        _check(self.lib, self.h.ctx, self.lib.hydro_batch_compute_device_prefix(
+            self.b, d_bodies, d_count, C.byref(ocean), C.byref(settings), d_io, stream or None))
 
     def last_launches(self) -> int:
         return int(self.lib.hydro_batch_last_launches(self.b))

@@ -409,7 +409,8 @@ class GatedPredictor:
         self.settings = settings
         dev = sur.dev
         self.bufs = sur._infer_bufs(self.n_pad)
-        self.batch = hctx_exact.batch(np.full(n, mesh_id, dtype=np.uint32))
+        # one-tile chunks: only the few gated-out hulls are active per call
+        self.batch = hctx_exact.batch(np.full(n, mesh_id, dtype=np.uint32), chunk_faces=384)
         self.mesh_id = mesh_id
         self.counts = torch.zeros((n + 255) // 256, dtype=torch.int32, device=dev)
         self.packed = torch.zeros(n * abi.BODY_DTYPE.itemsize, dtype=torch.uint8, device=dev)
@@ -438,7 +439,8 @@ class GatedPredictor:
         self._ck(self.lib.hydro_nn_route(ctx, _ptr(d_bodies), _ptr(b["mask"]), n, _ptr(self.counts),
                                          _ptr(self.packed), _ptr(self.pos), _ptr(self.n_packed), st))
         self.exact_io.zero_()
-        self.batch.compute_device(self.packed.data_ptr(), self.ocean, self.settings, self.exact_io.data_ptr(), st)
+        self.batch.compute_device_prefix(self.packed.data_ptr(), self.n_packed.data_ptr(), self.ocean,
+                                         self.settings, self.exact_io.data_ptr(), st)
         self._ck(self.lib.hydro_nn_merge(ctx, _ptr(d_bodies), _ptr(b["z"]), OUT_PAD, _ptr(self.pos),
                                          _ptr(self.exact_io), n, _ptr(self.out), st))
         # features, gate, to_bf16, 4 GEMMs, 2 route, exact step, merge

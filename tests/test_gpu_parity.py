@@ -297,6 +297,43 @@ def test_host_and_device_entry_points_agree(hctx):
     bt.close()
 
 
+@pytest.mark.parametrize("chunk_faces", [384, 1536])
+def test_prefix_entry_and_chunk_size(hctx, chunk_faces):
+    """hydro_batch_compute_device_prefix evaluates exactly the first *count
+    bodies (bit-identical to a full step of those bodies) and leaves the rest
+    of the in-out array untouched; the chunk size does not change results
+    beyond the FP32 summation order."""
+    torch = pytest.importorskip("torch")
+    sc = upload(hctx, scenarios.mixed_batch(n_bodies=80, seed=13, scale_faces=0.05))
+    ids = np.asarray(sc["_ids"], dtype=np.uint32)[sc["bodies"]["mesh"]]
+    bodies = sc["bodies"].copy()
+    bodies["mesh"] = ids
+    full = scenarios.new_wrenches(len(bodies))
+    bf = hctx.batch(ids, chunk_faces=chunk_faces)
+    bf.compute(bodies, sc["ocean"], scenarios.settings(), full)
+    ref = scenarios.new_wrenches(len(bodies))
+    b0 = hctx.batch(ids)
+    b0.compute(bodies, sc["ocean"], scenarios.settings(), ref)
+    e = scaled_errors(full, ref, body_lengths(sc))
+    act = ref["position"] != abi.OUTSIDE
+    for k, v in e.items():
+        assert np.max(v[act]) < TOL_MIRROR, (k, float(np.max(v[act])))
+    k = 37
+    sentinel = scenarios.new_wrenches(len(bodies))
+    sentinel["Swet"] = -7.0
+    d_b = torch.from_numpy(bodies.view(np.uint8).copy()).cuda()
+    d_w = torch.from_numpy(sentinel.view(np.uint8).copy()).cuda()
+    d_k = torch.tensor([k], dtype=torch.int32, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    bf.compute_device_prefix(d_b.data_ptr(), d_k.data_ptr(), sc["ocean"], scenarios.settings(), d_w.data_ptr(), s)
+    torch.cuda.synchronize()
+    got = d_w.cpu().numpy().view(abi.WRENCH_DTYPE)
+    assert got[:k].tobytes() == full[:k].tobytes()
+    assert got[k:].tobytes() == sentinel[k:].tobytes()
+    bf.close()
+    b0.close()
+
+
 @pytest.mark.parametrize("cut", ["fp64", "fp32"])
 def test_waves_batch(oracle, hctx, hctx64, cut):
     h = hctx64 if cut == "fp64" else hctx
