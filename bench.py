@@ -497,10 +497,34 @@ def run_gpu(args, rank: int, world: int, local_rank: int, dist):
     def step():
         batch.compute_device(d_bodies.data_ptr(), ocean, settings, d_io.data_ptr(), sptr)
 
+    tune = None
+    if not args.no_autotune:
+        d_scratch = torch.zeros_like(d_io)
+        tune = batch.autotune(d_bodies.data_ptr(), ocean, settings, d_scratch.data_ptr(), sptr, reps=5)
+        del d_scratch
+        log(f"[rank {rank}] autotune: {tune}")
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
             step()
     torch.cuda.synchronize()
+    graph = None
+    if not args.no_graph:
+        # the whole step (three kernels) as one CUDA graph, replayed per step
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=stream):
+            step()
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            for _ in range(args.warmup):
+                graph.replay()
+        torch.cuda.synchronize()
+
+    def timed_step():
+        if graph is not None:
+            graph.replay()
+        else:
+            step()
+
     gpu_io = d_io.cpu().numpy().view(abi.WRENCH_DTYPE).copy()
     active = (gpu_io["position"] == abi.CROSSING_SURFACE) | (gpu_io["position"] == abi.INSIDE)
     processed_faces = int(per_body_faces[active].sum())
@@ -514,8 +538,9 @@ def run_gpu(args, rank: int, world: int, local_rank: int, dist):
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
-    for _ in range(args.steps):
-        step()
+    with torch.cuda.stream(stream):
+        for _ in range(args.steps):
+            timed_step()
     ev1.record(stream)
     torch.cuda.synchronize()
     if dist is not None:
@@ -574,8 +599,10 @@ def run_gpu(args, rank: int, world: int, local_rank: int, dist):
                      "note": "whole step (prep + chunk + finalise kernels) timed; the chunk kernel "
                              "is issue-bound (profiles/chunk_kernel_batch.txt)"},
         "gpu_launches": args.steps * batch.last_launches(),
-        "kernel_config": {"cut": args.cut, "chunk_faces": args.chunk_faces or 4096,
-                          "ctas_per_sm": args.ctas_per_sm or 2},
+        "kernel_config": {"cut": args.cut,
+                          "chunk_faces": tune["chunk_faces"] if tune else (args.chunk_faces or 4096),
+                          "ctas_per_sm": tune["ctas_per_sm"] if tune else (args.ctas_per_sm or 2),
+                          "autotune": tune, "cuda_graph": graph is not None},
         "clocks": clocks,
     }
     if not args.no_error:
@@ -641,6 +668,8 @@ def main():
     ap.add_argument("--cut", default="fp32", choices=["fp64", "fp32"])
     ap.add_argument("--chunk-faces", type=int, default=0)
     ap.add_argument("--ctas-per-sm", type=int, default=0)
+    ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--no-rollout", action="store_true")
     ap.add_argument("--roll-envs", type=int, default=16384)

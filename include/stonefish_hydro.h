@@ -173,13 +173,15 @@ typedef struct hydro_wrench {
 typedef struct hydro_config {
     int32_t device;              /* CUDA device ordinal */
     int32_t cut_precision;       /* HYDRO_CUT_FP32 (default) or HYDRO_CUT_FP64 */
-    uint32_t tile_faces;         /* faces per work tile; 0 = autotune */
-    uint32_t ctas_per_sm;        /* resident CTAs per SM; 0 = autotune */
-    const char* tune_cache_path; /* autotuner cache file, NULL = none */
+    uint32_t tile_faces;         /* faces per work chunk; 0 = 4096 (hydro_batch_autotune
+                                    picks per batch) */
+    uint32_t ctas_per_sm;        /* resident CTAs per SM; 0 = 2 (or the autotuner's) */
+    const char* tune_cache_path; /* autotuner cache file (copied), NULL = none */
 } hydro_config;
 
 /* -------------------------------------------------------------- lifecycle */
-/* Fills *cfg with defaults (device 0, FP32 cut points, autotuned tiles). */
+/* Fills *cfg with defaults (device 0, FP32 cut points, 4096-face chunks,
+ * 2 CTAs per SM, no tuning cache). */
 void hydro_config_default(hydro_config* cfg);
 
 hydro_status hydro_create(hydro_ctx** ctx, const hydro_config* cfg);
@@ -267,6 +269,30 @@ hydro_status hydro_batch_compute(hydro_batch* batch, const hydro_body* bodies,
                                  const hydro_ocean* ocean,
                                  const hydro_settings* settings,
                                  hydro_wrench* inout);
+
+/* Autotuner (no counterpart in the reference).  Times the step on this
+ * batch's own bodies for every work-chunk size in {768, 1536, 3072, 4224,
+ * 6144} faces and 1 or 2 resident CTAs per SM (reps timed steps each, after
+ * one warm-up step), keeps the fastest, and appends it to the context's
+ * tune_cache_path (if set) under a key made of the GPU name, SM count, cut
+ * precision, surface kind and the batch's face-count histogram.  A later
+ * call with a cached key applies the cached choice without timing
+ * (from_cache = 1).  d_scratch receives the results of the timing steps
+ * (n_bodies hydro_wrench of device scratch).  Synchronises the stream; not
+ * for use inside a stream capture. */
+typedef struct hydro_tune_result {
+    uint32_t chunk_faces;
+    uint32_t ctas_per_sm;
+    float ms_per_step;
+    int32_t from_cache;
+    uint32_t n_candidates;
+    float candidate_ms[16];   /* in the order chunk size (outer) x CTAs per SM */
+} hydro_tune_result;
+
+hydro_status hydro_batch_autotune(hydro_batch* batch, const hydro_body* d_bodies,
+                                  const hydro_ocean* ocean, const hydro_settings* settings,
+                                  hydro_wrench* d_scratch, void* stream, uint32_t reps,
+                                  hydro_tune_result* result);
 
 /* Number of kernel launches the last compute call enqueued. */
 uint32_t hydro_batch_last_launches(const hydro_batch* batch);

@@ -86,6 +86,11 @@ class RigidState(C.Structure):
                 ("inertial_mass", C.c_double), ("inertia", _d3), ("half_extents", _d3)]
 
 
+class TuneResult(C.Structure):
+    _fields_ = [("chunk_faces", C.c_uint32), ("ctas_per_sm", C.c_uint32), ("ms_per_step", C.c_float),
+                ("from_cache", C.c_int32), ("n_candidates", C.c_uint32), ("candidate_ms", C.c_float * 16)]
+
+
 class Config(C.Structure):
     _fields_ = [("device", C.c_int32), ("cut_precision", C.c_int32),
                 ("tile_faces", C.c_uint32), ("ctas_per_sm", C.c_uint32),
@@ -168,6 +173,8 @@ def _declare(lib: C.CDLL) -> None:
         "hydro_batch_destroy": (None, [vp]),
         "hydro_batch_compute_device": (i32, [vp, vp, C.POINTER(Ocean), C.POINTER(Settings), vp, vp]),
         "hydro_batch_create_ex": (i32, [vp, vp, u32, u32, C.POINTER(vp)]),
+        "hydro_batch_autotune": (i32, [vp, vp, C.POINTER(Ocean), C.POINTER(Settings), vp, vp, u32,
+                                       C.POINTER(TuneResult)]),
         "hydro_batch_compute_device_prefix": (i32, [vp, vp, vp, C.POINTER(Ocean), C.POINTER(Settings), vp,
                                                     vp]),
         "hydro_batch_compute": (i32, [vp, vp, C.POINTER(Ocean), C.POINTER(Settings), vp]),

@@ -59,6 +59,8 @@ struct hydro_ctx {
     std::unordered_map<uint32_t, hydro_batch*> single;
     void* small_d = nullptr;   // scratch for the small entry points
     size_t small_cap = 0;
+    std::string tune_path;     // autotuner cache file ("" = none)
+    char gpu_name[256] = {0};
 };
 
 struct hydro_batch {
@@ -76,6 +78,8 @@ struct hydro_batch {
     hydro_wrench* io_d = nullptr;
     cudaStream_t stream = nullptr;
     uint32_t last_launches = 0;
+    uint32_t chunk_tiles = 0;    // tiles per work chunk of this batch
+    uint32_t ctas_per_sm = 0;    // 0 = the context's setting
 };
 
 namespace {
@@ -223,22 +227,17 @@ void batch_free(hydro_batch* b)
     delete b;
 }
 
-hydro_status batch_build(hydro_ctx* ctx, const hydro_mesh_id* mesh_of_body, uint32_t n,
-                         hydro_batch** out, uint32_t chunk_faces = 0)
+// (Re)builds a batch's work list: chunks of at most tpc tiles, body by body,
+// with their per-chunk scratch.
+hydro_status build_work(hydro_ctx* ctx, hydro_batch* b, uint32_t tpc)
 {
-    for (uint32_t i = 0; i < n; ++i) {
-        if (mesh_of_body[i] != HYDRO_NO_MESH && mesh_of_body[i] >= ctx->meshes.size())
-            return fail(ctx, HYDRO_ERR_NOT_FOUND, "body %u: unknown mesh %u", i, mesh_of_body[i]);
-    }
-    hydro_status st = sync_tiles(ctx);
-    if (st != HYDRO_OK) return st;
-    const uint32_t tpc = tiles_per_chunk(ctx, chunk_faces);
+    const uint32_t n = b->n_bodies;
     std::vector<ChunkDesc> chunks;
     std::vector<BodyInfo> info(n);
     for (uint32_t i = 0; i < n; ++i) {
         BodyInfo& bi = info[i];
         bi.first_chunk = (uint32_t)chunks.size();
-        bi.mesh = mesh_of_body[i];
+        bi.mesh = b->mesh_of_body[i];
         uint32_t first = 0, nt = 0;
         if (bi.mesh != HYDRO_NO_MESH) {
             const MeshRec& m = ctx->meshes[bi.mesh];
@@ -254,11 +253,39 @@ hydro_status batch_build(hydro_ctx* ctx, const hydro_mesh_id* mesh_of_body, uint
         if (k == 0) chunks.push_back(ChunkDesc{i, first, 0u, 0u});   // finaliser only
         bi.n_chunks = (uint32_t)chunks.size() - bi.first_chunk;
     }
+    cudaFree(b->chunks_d);
+    cudaFree(b->binfo_d);
+    cudaFree(b->partials_d);
+    cudaFree(b->chunk_active_d);
+    b->chunks_d = nullptr;
+    b->binfo_d = nullptr;
+    b->partials_d = nullptr;
+    b->chunk_active_d = nullptr;
+    b->n_chunks = (uint32_t)chunks.size();
+    b->chunk_tiles = tpc;
+    CK(ctx, cudaMalloc(&b->chunks_d, chunks.size() * sizeof(ChunkDesc)));
+    CK(ctx, cudaMalloc(&b->binfo_d, n * sizeof(BodyInfo)));
+    CK(ctx, cudaMalloc(&b->partials_d, chunks.size() * kPartialStride * sizeof(double)));
+    CK(ctx, cudaMalloc(&b->chunk_active_d, chunks.size()));
+    CK(ctx, cudaMemcpy(b->chunks_d, chunks.data(), chunks.size() * sizeof(ChunkDesc), cudaMemcpyHostToDevice));
+    CK(ctx, cudaMemcpy(b->binfo_d, info.data(), n * sizeof(BodyInfo), cudaMemcpyHostToDevice));
+    CK(ctx, cudaMemset(b->partials_d, 0, chunks.size() * kPartialStride * sizeof(double)));
+    return HYDRO_OK;
+}
+
+hydro_status batch_build(hydro_ctx* ctx, const hydro_mesh_id* mesh_of_body, uint32_t n,
+                         hydro_batch** out, uint32_t chunk_faces = 0)
+{
+    for (uint32_t i = 0; i < n; ++i) {
+        if (mesh_of_body[i] != HYDRO_NO_MESH && mesh_of_body[i] >= ctx->meshes.size())
+            return fail(ctx, HYDRO_ERR_NOT_FOUND, "body %u: unknown mesh %u", i, mesh_of_body[i]);
+    }
+    hydro_status st = sync_tiles(ctx);
+    if (st != HYDRO_OK) return st;
     hydro_batch* b = new (std::nothrow) hydro_batch();
     if (!b) return fail(ctx, HYDRO_ERR_OOM, "host allocation");
     b->ctx = ctx;
     b->n_bodies = n;
-    b->n_chunks = (uint32_t)chunks.size();
     b->mesh_of_body.assign(mesh_of_body, mesh_of_body + n);
     cudaError_t e;
 #define BK(call)                                              \
@@ -270,17 +297,15 @@ hydro_status batch_build(hydro_ctx* ctx, const hydro_mesh_id* mesh_of_body, uint
         }                                                     \
     } while (0)
     BK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
-    BK(cudaMalloc(&b->chunks_d, chunks.size() * sizeof(ChunkDesc)));
-    BK(cudaMalloc(&b->binfo_d, n * sizeof(BodyInfo)));
-    BK(cudaMalloc(&b->partials_d, chunks.size() * kPartialStride * sizeof(double)));
     BK(cudaMalloc(&b->bparams_d, n * sizeof(BodyParams)));
     BK(cudaMalloc(&b->err_d, 256));
-    BK(cudaMalloc(&b->chunk_active_d, chunks.size()));
-    BK(cudaMemcpy(b->chunks_d, chunks.data(), chunks.size() * sizeof(ChunkDesc), cudaMemcpyHostToDevice));
-    BK(cudaMemcpy(b->binfo_d, info.data(), n * sizeof(BodyInfo), cudaMemcpyHostToDevice));
     BK(cudaMemset(b->err_d, 0, 256));
-    BK(cudaMemset(b->partials_d, 0, chunks.size() * kPartialStride * sizeof(double)));
 #undef BK
+    st = build_work(ctx, b, tiles_per_chunk(ctx, chunk_faces));
+    if (st != HYDRO_OK) {
+        batch_free(b);
+        return st;
+    }
     *out = b;
     return HYDRO_OK;
 }
@@ -315,7 +340,7 @@ hydro_status batch_launch(hydro_batch* b, const hydro_body* d_bodies, const hydr
         return fail(ctx, HYDRO_ERR_INVALID_ARG, "ocean.waves set but no wave grid was given");
     const int cut64 = ctx->cfg.cut_precision == HYDRO_CUT_FP64;
     LaunchShape shape{};
-    const int want = ctx->cfg.ctas_per_sm ? (int)ctx->cfg.ctas_per_sm : 2;
+    const int want = b->ctas_per_sm ? (int)b->ctas_per_sm : ctx->cfg.ctas_per_sm ? (int)ctx->cfg.ctas_per_sm : 2;
     shape.ctas_per_sm = std::max(1, std::min(want, chunk_kernel_occupancy(cut64, P.ocean.waves, want)));
     shape.grid = ctx->sm_count * shape.ctas_per_sm;
     uint32_t launches = 0;
@@ -422,7 +447,13 @@ hydro_status hydro_create(hydro_ctx** out, const hydro_config* cfg)
     ctx->cfg = c;
     if (cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, c.device) != cudaSuccess)
         ctx->sm_count = 1;
+    if (c.tune_cache_path) ctx->tune_path = c.tune_cache_path;
     ctx->cfg.tune_cache_path = nullptr;
+    {
+        cudaDeviceProp prop;
+        if (cudaGetDeviceProperties(&prop, c.device) == cudaSuccess)
+            snprintf(ctx->gpu_name, sizeof(ctx->gpu_name), "%s", prop.name);
+    }
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
         delete ctx;
         return HYDRO_ERR_DEVICE;
@@ -896,6 +927,140 @@ extern "C" hydro_status hydro_debug_wait_timeout(hydro_ctx* ctx, uint32_t limit_
     CK(ctx, cudaMemcpyAsync(&h, d, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     CK(ctx, cudaStreamSynchronize(ctx->stream));
     *status = h;
+    return HYDRO_OK;
+}
+
+// ============================================================ autotuner
+namespace {
+
+// Cache key: the GPU, the arithmetic variant and the batch's shape (body
+// count per power-of-two face-count bin, total faces).
+std::string tune_key(const hydro_ctx* ctx, const hydro_batch* b, int waves)
+{
+    uint32_t bins[32] = {0};
+    uint64_t total = 0;
+    for (uint32_t i = 0; i < b->n_bodies; ++i) {
+        const uint32_t m = b->mesh_of_body[i];
+        const uint32_t f = m == HYDRO_NO_MESH ? 0u : ctx->meshes[m].n_faces;
+        total += f;
+        int k = 0;
+        while (k < 31 && (1u << (k + 1)) <= f) ++k;
+        ++bins[f ? k + 1 : 0];
+    }
+    std::string key = std::string(ctx->gpu_name) + "|sm" + std::to_string(ctx->sm_count) + "|cut" +
+                      std::to_string(ctx->cfg.cut_precision) + "|waves" + std::to_string(waves) + "|n" +
+                      std::to_string(b->n_bodies) + "|f" + std::to_string(total) + "|h";
+    for (int k = 0; k < 32; ++k)
+        if (bins[k]) key += std::to_string(k) + ":" + std::to_string(bins[k]) + ",";
+    for (char& c : key)
+        if (c == ' ' || c == '\n' || c == '\t') c = '_';
+    return key;
+}
+
+bool tune_lookup(const std::string& path, const std::string& key, uint32_t* faces, uint32_t* ctas, float* ms)
+{
+    if (path.empty()) return false;
+    FILE* f = fopen(path.c_str(), "r");
+    if (!f) return false;
+    char line[2048];
+    bool found = false;
+    while (fgets(line, sizeof(line), f)) {
+        char k[1800];
+        unsigned a = 0, c = 0;
+        float t = 0.f;
+        if (sscanf(line, "%1799s %u %u %f", k, &a, &c, &t) == 4 && key == k) {
+            *faces = a;
+            *ctas = c;
+            *ms = t;
+            found = true;   // the last entry for a key wins
+        }
+    }
+    fclose(f);
+    return found;
+}
+
+}  // namespace
+
+extern "C" hydro_status hydro_batch_autotune(hydro_batch* b, const hydro_body* d_bodies,
+                                             const hydro_ocean* ocean, const hydro_settings* settings,
+                                             hydro_wrench* d_scratch, void* stream, uint32_t reps,
+                                             hydro_tune_result* out)
+{
+    if (!b) return HYDRO_ERR_INVALID_ARG;
+    hydro_ctx* ctx = b->ctx;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (!d_bodies || !d_scratch || !settings || !valid_ocean(ocean) || !out)
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "autotune: bad arguments");
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, HYDRO_ERR_DEVICE, "cudaSetDevice");
+    if (reps == 0) reps = 5;
+    memset(out, 0, sizeof(*out));
+    const std::string key = tune_key(ctx, b, ocean->waves);
+    uint32_t faces = 0, ctas = 0;
+    float ms = 0.f;
+    if (tune_lookup(ctx->tune_path, key, &faces, &ctas, &ms)) {
+        hydro_status st = build_work(ctx, b, tiles_per_chunk(ctx, faces));
+        if (st != HYDRO_OK) return st;
+        b->ctas_per_sm = ctas;
+        out->chunk_faces = b->chunk_tiles * kTileFaces;
+        out->ctas_per_sm = ctas;
+        out->ms_per_step = ms;
+        out->from_cache = 1;
+        return HYDRO_OK;
+    }
+    static const uint32_t kTiles[] = {2, 4, 8, 11, 16};
+    static const uint32_t kCtas[] = {1, 2};
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CK(ctx, cudaEventCreate(&e0));
+    CK(ctx, cudaEventCreate(&e1));
+    float best = 1e30f;
+    uint32_t best_t = kTiles[0], best_c = kCtas[0], n = 0;
+    hydro_status st = HYDRO_OK;
+    for (uint32_t t : kTiles) {
+        if ((st = build_work(ctx, b, t)) != HYDRO_OK) break;
+        for (uint32_t c : kCtas) {
+            b->ctas_per_sm = c;
+            if ((st = batch_launch(b, d_bodies, ocean, settings, d_scratch, s, OP_BODY)) != HYDRO_OK) break;
+            cudaEventRecord(e0, s);
+            for (uint32_t r = 0; r < reps && st == HYDRO_OK; ++r)
+                st = batch_launch(b, d_bodies, ocean, settings, d_scratch, s, OP_BODY);
+            cudaEventRecord(e1, s);
+            cudaError_t e = cudaEventSynchronize(e1);
+            if (st != HYDRO_OK) break;
+            if (e != cudaSuccess) {
+                st = cuda_fail(ctx, e, "autotune timing");
+                break;
+            }
+            float t_ms = 0.f;
+            cudaEventElapsedTime(&t_ms, e0, e1);
+            t_ms /= (float)reps;
+            if (n < 16) out->candidate_ms[n] = t_ms;
+            ++n;
+            if (t_ms < best) {
+                best = t_ms;
+                best_t = t;
+                best_c = c;
+            }
+        }
+        if (st != HYDRO_OK) break;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st != HYDRO_OK) return st;
+    if ((st = build_work(ctx, b, best_t)) != HYDRO_OK) return st;
+    b->ctas_per_sm = best_c;
+    out->chunk_faces = best_t * kTileFaces;
+    out->ctas_per_sm = best_c;
+    out->ms_per_step = best;
+    out->from_cache = 0;
+    out->n_candidates = n;
+    if (!ctx->tune_path.empty()) {
+        FILE* f = fopen(ctx->tune_path.c_str(), "a");
+        if (f) {
+            fprintf(f, "%s %u %u %.6f\n", key.c_str(), out->chunk_faces, best_c, best);
+            fclose(f);
+        }
+    }
     return HYDRO_OK;
 }
 

@@ -48,7 +48,8 @@ class HydroContext:
     """Owns a hydro_ctx: device meshes, the wave grid and small buffers."""
 
     def __init__(self, device: int = 0, cut_precision: int = abi.CUT_FP32,
-                 tile_faces: int = 0, ctas_per_sm: int = 0, lib_path: str | None = None):
+                 tile_faces: int = 0, ctas_per_sm: int = 0, lib_path: str | None = None,
+                 tune_cache_path: str | None = None):
         self.lib = abi.load_library(lib_path)
         lib = self.lib
         if not hasattr(lib, "_debug_declared"):
@@ -62,6 +63,8 @@ class HydroContext:
         cfg.cut_precision = cut_precision
         cfg.tile_faces = tile_faces
         cfg.ctas_per_sm = ctas_per_sm
+        self._tune_path = tune_cache_path.encode() if tune_cache_path else None
+        cfg.tune_cache_path = self._tune_path
         h = C.c_void_p()
         st = lib.hydro_create(C.byref(h), C.byref(cfg))
         if st != abi.HYDRO_OK:
@@ -262,6 +265,16 @@ class Batch:
         """As compute_device for the first *d_count bodies (device uint32)."""
         _check(self.lib, self.h.ctx, self.lib.hydro_batch_compute_device_prefix(
             self.b, d_bodies, d_count, C.byref(ocean), C.byref(settings), d_io, stream or None))
+
+    def autotune(self, d_bodies: int, ocean, settings, d_scratch: int, stream: int = 0, reps: int = 5) -> dict:
+        """hydro_batch_autotune: picks chunk size and CTAs per SM for this batch."""
+        r = abi.TuneResult()
+        _check(self.lib, self.h.ctx, self.lib.hydro_batch_autotune(self.b, d_bodies, C.byref(ocean),
+                                                                   C.byref(settings), d_scratch,
+                                                                   stream or None, reps, C.byref(r)))
+        return {"chunk_faces": r.chunk_faces, "ctas_per_sm": r.ctas_per_sm, "ms_per_step": r.ms_per_step,
+                "from_cache": bool(r.from_cache),
+                "candidate_ms": [float(x) for x in r.candidate_ms[: r.n_candidates]]}
 
     def last_launches(self) -> int:
         return int(self.lib.hydro_batch_last_launches(self.b))
