@@ -24,9 +24,11 @@
  *   ORACLE_REF64      the same algorithm entirely in FP64 (no FP32 casts of
  *                     transforms, velocities or depths);
  *   ORACLE_MIRROR64   FP32 faces as REF32 but cut points in FP64 and sums in
- *                     FP64: the arithmetic of the GPU kernel's default mode;
+ *                     FP64: the arithmetic of the GPU kernel's HYDRO_CUT_FP64
+ *                     mode;
  *   ORACLE_MIRROR32   FP32 faces and cut points as REF32, sums in FP64: the
- *                     GPU kernel's HYDRO_CUT_FP32 mode.
+ *                     arithmetic of the GPU kernel's default HYDRO_CUT_FP32
+ *                     mode.
  */
 #ifndef HYDRO_ORACLE_H
 #define HYDRO_ORACLE_H

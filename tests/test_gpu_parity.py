@@ -376,3 +376,9 @@ def test_argument_errors(hctx):
     with pytest.raises(abi.HydroError) as ei:
         hctx.batch(np.array([10 ** 6], np.uint32))
     assert ei.value.status == abi.HYDRO_ERR_NOT_FOUND
+    with pytest.raises(abi.HydroError) as ei:
+        hctx.batch(np.array([], np.uint32))          # empty batch
+    assert ei.value.status == abi.HYDRO_ERR_INVALID_ARG
+    with pytest.raises(abi.HydroError) as ei:
+        hctx.upload_mesh(np.zeros((0, 3), np.float32), np.zeros((0, 3), np.uint32))   # empty mesh
+    assert ei.value.status == abi.HYDRO_ERR_INVALID_ARG
