@@ -40,6 +40,9 @@ BYTES_PER_FACE = 18.0      # indexed mesh: 12 B of indices + 0.5 x 12 B of posit
 BYTES_PER_BODY = 200.0     # FP64 pose/velocity/coefficients in, 6 vec3 + 2 scalars out
 
 
+from stonefish_gb300.replicas import max_over_ranks, whole_job_rate  # noqa: E402
+
+
 def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
@@ -546,14 +549,10 @@ def run_gpu(args, rank: int, world: int, local_rank: int, dist):
     if dist is not None:
         dist.barrier()
     clocks = sampler.stop()
-    ms = ev0.elapsed_time(ev1)
-    if dist is not None:
-        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ev0.elapsed_time(ev1), dist, "cuda")
     ms_per_step = ms / args.steps
-    value = world * nb * args.steps / (ms / 1e3)
-    faces_per_s = world * int(per_body_faces.sum()) * args.steps / (ms / 1e3)
+    value = whole_job_rate(nb * args.steps, world, ms / 1e3)
+    faces_per_s = whole_job_rate(int(per_body_faces.sum()) * args.steps, world, ms / 1e3)
 
     # end to end through the host-buffer call, pinned host memory
     h_bodies = torch.from_numpy(bodies.view(np.uint8).copy()).pin_memory()
@@ -566,12 +565,8 @@ def run_gpu(args, rank: int, world: int, local_rank: int, dist):
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         batch.compute_ptr(h_bodies.data_ptr(), ocean, settings, h_io.data_ptr())
-    e2e_s = time.perf_counter() - t0
-    if dist is not None:
-        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = world * nb * e2e_steps / e2e_s
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dist, "cuda")
+    e2e_value = whole_job_rate(nb * e2e_steps, world, e2e_s)
     host_io = h_io.numpy().view(abi.WRENCH_DTYPE)
     assert host_io.tobytes() == gpu_io.tobytes(), "host-buffer and device-buffer results differ"
 
