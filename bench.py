@@ -287,7 +287,17 @@ def surrogate_bench(args, device: int) -> dict:
     e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / steps
-    # the MLP alone (four GEMMs), for the tensor-core roofline
+    # the network alone (the fused tcgen05 kernel predict() launches), for
+    # the tensor-core roofline; and the four mma.sync GEMMs for comparison
+    feats_d = gp.bufs["feats"]
+    for _ in range(3):
+        sur.infer_tc(feats_d, gp.z16, gp.tcw)
+    e0.record(stream)
+    for _ in range(steps):
+        sur.infer_tc(feats_d, gp.z16, gp.tcw)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_mlp = e0.elapsed_time(e1) / steps
     bufs = sur._infer_bufs(nB)
     for _ in range(3):
         sur._mlp(bufs, nB)
@@ -296,7 +306,7 @@ def surrogate_bench(args, device: int) -> dict:
         sur._mlp(bufs, nB)
     e1.record(stream)
     torch.cuda.synchronize()
-    ms_mlp = e0.elapsed_time(e1) / steps
+    ms_mma = e0.elapsed_time(e1) / steps
     # the exact FP32 step on the same states
     bx = h32.batch(np.full(nB, m32, dtype=np.uint32))
     io = torch.zeros(nB * abi.WRENCH_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
@@ -342,8 +352,12 @@ def surrogate_bench(args, device: int) -> dict:
                 "d2h_bytes_per_step": int(nB * 6 * 4)},
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "peak_source": kind, "traffic": None,
-                     "kernel": "four BF16 GEMMs of the MLP (mma.sync m16n8k16), timed together",
-                     "flop_rule": f"{MLP_FLOP_PER_EVAL:.0f} FLOP per state (unpadded layers)"},
+                     "kernel": "mlp_tc_kernel: the whole 16-256-256-256-6 network fused, tcgen05.mma "
+                               "kind::f16 M128 with TMEM accumulators, weights by bulk copy",
+                     "kernel_us": ms_mlp * 1e3,
+                     "flop_rule": f"{MLP_FLOP_PER_EVAL:.0f} FLOP per state (unpadded layers)",
+                     "mma_sync_gemms_us": ms_mma * 1e3,
+                     "mma_sync_tflops": MLP_FLOP_PER_EVAL * nB / (ms_mma / 1e3) / 1e12},
         "gpu_launches_per_step": gp.launches,
         "setup_s": setup_s,
     }

@@ -483,6 +483,27 @@ hydro_status hydro_nn_gate(hydro_ctx* ctx, const float* d_features, uint32_t n, 
                            const float* hi, const float* mean, const float* precision,
                            float threshold, uint8_t* d_mask, void* stream);
 
+/* Fused inference of the whole network on the 5th-generation tensor cores
+ * (tcgen05 MMAs, FP32 accumulators in tensor memory, activations kept in
+ * shared memory): d_out[i][16] = layer-3 output (bias added; columns 0..5
+ * are the wrench) of the 16 features d_features[i] normalised as
+ * (f - fmean) * fistd.  d_image holds HYDRO_NN_TC_IMAGE_BYTES of weights in
+ * the kernels' shared-memory layout, written by hydro_nn_pack_sw128 at the
+ * offsets 0 (W0^T, 256 x 64, K 16 used), 32768 (W1^T, 256 x 256), 163840
+ * (W2^T) and 294912 (W3^T, 16 x 256); b0..b2 have 256 entries, b3 16.
+ * *d_err gets bit 0 if a bounded wait ran out. */
+#define HYDRO_NN_TC_IMAGE_BYTES 303104u
+hydro_status hydro_nn_mlp_tc(hydro_ctx* ctx, const float* d_features, uint32_t n, const float* fmean,
+                             const float* fistd, const void* d_image, const float* b0, const float* b1,
+                             const float* b2, const float* b3, float* d_out, uint32_t* d_err, void* stream);
+
+/* Writes src[rows][K] (bf16, row stride ld) into dst as the tensor-core
+ * operand image: K-major, K zero-padded to kpad (a multiple of 64), each
+ * [rows x 64] block in 8-row x 128-byte atoms with 16-byte chunk c of row r
+ * stored at chunk c ^ (r % 8) (128-byte swizzle). */
+hydro_status hydro_nn_pack_sw128(hydro_ctx* ctx, const void* src, int32_t rows, int32_t K, int32_t ld,
+                                 int32_t kpad, void* dst, void* stream);
+
 /* Packs the bodies with d_mask[i] == 0, in index order, to the front of
  * d_packed (n entries) and switches the rest of d_packed off (mode
  * HYDRO_MODE_DISABLED), so an exact step over d_packed integrates only the

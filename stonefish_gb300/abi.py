@@ -204,6 +204,8 @@ def _declare(lib: C.CDLL) -> None:
         "hydro_nn_route": (i32, [vp, vp, vp, u32, vp, vp, vp, vp, vp]),
         "hydro_nn_merge": (i32, [vp, vp, vp, i32, vp, vp, u32, vp, vp]),
         "hydro_nn_wrench_body": (i32, [vp, vp, vp, u32, vp, vp]),
+        "hydro_nn_pack_sw128": (i32, [vp, vp, i32, i32, i32, i32, vp, vp]),
+        "hydro_nn_mlp_tc": (i32, [vp, vp, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
         "hydro_rigid_step": (i32, [vp, vp, vp, vp, vp, u32, C.c_double, C.c_double, vp]),
         "hydro_rigid_write_bodies": (i32, [vp, vp, vp, u32, vp]),
     }

@@ -1172,6 +1172,29 @@ extern "C" hydro_status hydro_nn_wrench_body(hydro_ctx* ctx, const hydro_body* d
            "nn wrench_body");
 }
 
+extern "C" hydro_status hydro_nn_pack_sw128(hydro_ctx* ctx, const void* src, int32_t rows, int32_t K, int32_t ld,
+                                            int32_t kpad, void* dst, void* stream)
+{
+    NN_CTX_CHECK();
+    if (!src || !dst || rows <= 0 || K <= 0 || kpad % 64 || K > kpad || ld < K ||
+        (reinterpret_cast<uintptr_t>(dst) & 15))
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn pack_sw128");
+    NN_RET(launch_pack_sw128(src, rows, K, ld, kpad, dst, static_cast<cudaStream_t>(stream)), "nn pack_sw128");
+}
+
+extern "C" hydro_status hydro_nn_mlp_tc(hydro_ctx* ctx, const float* d_features, uint32_t n, const float* fmean,
+                                        const float* fistd, const void* d_image, const float* b0, const float* b1,
+                                        const float* b2, const float* b3, float* d_out, uint32_t* d_err,
+                                        void* stream)
+{
+    NN_CTX_CHECK();
+    if (!d_features || !fmean || !fistd || !d_image || !b0 || !b1 || !b2 || !b3 || !d_out || !d_err ||
+        (reinterpret_cast<uintptr_t>(d_image) & 15) || (reinterpret_cast<uintptr_t>(d_out) & 15))
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn mlp_tc");
+    NN_RET(launch_mlp_tc(d_features, n, fmean, fistd, d_image, b0, b1, b2, b3, d_out, d_err,
+                         static_cast<cudaStream_t>(stream)), "nn mlp_tc");
+}
+
 extern "C" hydro_status hydro_nn_route(hydro_ctx* ctx, const hydro_body* d_bodies, const uint8_t* d_mask,
                                        uint32_t n, uint32_t* d_counts, hydro_body* d_packed, int32_t* d_pos,
                                        uint32_t* d_n_packed, void* stream)

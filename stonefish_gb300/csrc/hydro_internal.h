@@ -108,4 +108,10 @@ cudaError_t launch_rigid_step(hydro_rigid_state* states, hydro_body* bodies, con
 cudaError_t launch_rigid_write_bodies(const hydro_rigid_state* states, hydro_body* bodies, uint32_t n,
                                       cudaStream_t s);
 
+cudaError_t launch_pack_sw128(const void* src, int rows, int K, int ld, int kpad, void* dst, cudaStream_t s);
+size_t mlp_tc_image_bytes();
+cudaError_t launch_mlp_tc(const float* feats, uint32_t n, const float* fmean, const float* fistd,
+                          const void* wimg, const float* b0, const float* b1, const float* b2, const float* b3,
+                          float* out, unsigned* err, cudaStream_t s);
+
 }  // namespace sfh

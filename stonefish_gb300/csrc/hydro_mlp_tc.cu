@@ -1,0 +1,391 @@
+// hydro_mlp_tc.cu -- fused inference of the wrench surrogate on the 5th-
+// generation tensor cores: one CTA takes 128 states through all four layers
+// (16 -> 256 -> 256 -> 256 -> 16) with the activations kept in shared memory
+// and the accumulators in tensor memory.
+//
+//   * operands are K-major BF16 in the 128-byte-swizzled canonical layout
+//     (8-row x 128-byte atoms, 16-byte chunk c of row r stored at chunk
+//     c ^ (r % 8)); each [rows x 64] K-block is contiguous, blocks follow
+//     each other;
+//   * the weights are packed once into that image in global memory
+//     (pack_sw128_kernel), so each layer's weights arrive with one 1-D bulk
+//     copy (cp.async.bulk, mbarrier complete_tx) while the previous layer's
+//     epilogue runs;
+//   * one thread issues tcgen05.mma (M = 128, N = 256 or 16, K = 16 per
+//     instruction, FP32 accumulate in 256 TMEM columns) and commits to an
+//     mbarrier; eight warps read the accumulator with tcgen05.ld (warp w
+//     reads TMEM lanes 32 (w % 4) .. +31, half the columns), add the bias,
+//     apply SiLU, round to BF16 and write the next layer's A operand;
+//   * the input features are normalised and rounded in the kernel, the
+//     output (bias added) is written as FP32 rows of 16.
+//
+// Every mbarrier wait is bounded (%globaltimer); a timeout sets *err, the
+// CTA stops issuing work, waits (bounded) for its tensor-core work to
+// retire, frees its tensor memory and returns.
+#include <cstdint>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "hydro_internal.h"
+
+namespace sfh {
+
+typedef __nv_bfloat16 bf16;
+
+namespace tc {
+
+constexpr int kRows = 128;      // states per CTA = UMMA M
+constexpr int kHid = 256;
+constexpr int kIn = 16;         // features = layer-0 K
+constexpr int kOut = 16;        // output columns (6 used)
+constexpr int kThreads = 256;   // 8 warps
+constexpr uint32_t kTmemCols = 256;
+
+// shared-memory image (offsets from a 1024-byte-aligned base)
+constexpr uint32_t kOffA = 0;                        // 128 x 256 bf16, 4 K-blocks of 16 KB
+constexpr uint32_t kOffW = kOffA + 4 * 16384;        // 256 x 256 bf16, 4 K-blocks of 32 KB
+constexpr uint32_t kOffW3 = kOffW + 4 * 32768;       // 16 x 256 bf16, 4 K-blocks of 2 KB
+constexpr uint32_t kOffBias = kOffW3 + 4 * 2048;     // 3 x 256 + 16 floats
+constexpr uint32_t kOffBar = kOffBias + (3 * kHid + kOut) * 4;
+constexpr uint32_t kOffTmem = kOffBar + 4 * 8;
+constexpr uint32_t kSmemBytes = kOffTmem + 16 + 1024; // + alignment slack
+
+// global weight image (bytes)
+constexpr uint32_t kImgW0 = 0;                       // 256 x 64 (K 16 used) = 32 KB
+constexpr uint32_t kImgW1 = kImgW0 + 32768;
+constexpr uint32_t kImgW2 = kImgW1 + 131072;
+constexpr uint32_t kImgW3 = kImgW2 + 131072;         // 16 x 256 = 8 KB
+constexpr uint32_t kImgBytes = kImgW3 + 8192;
+
+__device__ __forceinline__ uint32_t sw128_offset(uint32_t rows, uint32_t r, uint32_t k)
+{
+    // byte offset of element (r, k) of a [rows x K] bf16 operand
+    const uint32_t blk = k >> 6, kk = k & 63;
+    return blk * rows * 128u + r * 128u + ((((kk >> 3) ^ (r & 7u)) & 7u) << 4) + ((kk & 7u) << 1);
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// tcgen05 shared-memory matrix descriptor: K-major, 128-byte swizzle,
+// 8-row groups 1024 bytes apart (SBO), descriptor version 1.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr)
+{
+    uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)1u << 16;                 // leading byte offset (unused by swizzled K-major)
+    d |= (uint64_t)(1024u >> 4) << 32;       // stride byte offset
+    d |= (uint64_t)1u << 46;                 // version
+    d |= (uint64_t)2u << 61;                 // SWIZZLE_128B
+    return d;
+}
+
+// instruction descriptor, kind::f16: BF16 A and B, FP32 D, both K-major
+__host__ __device__ constexpr uint32_t idesc_bf16(uint32_t M, uint32_t N)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((N >> 3) << 17) | ((M >> 4) << 24);
+}
+
+__device__ __forceinline__ uint64_t globaltimer()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+    return ok != 0;
+}
+
+// bounded wait: gives up after limit_ns
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint64_t limit_ns)
+{
+    if (mbar_try(bar, parity)) return true;
+    const uint64_t t0 = globaltimer();
+    while (!mbar_try(bar, parity)) {
+        if (globaltimer() - t0 > limit_ns) return false;
+        __nanosleep(64);
+    }
+    return true;
+}
+
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 :: "r"(dst), "l"(src), "r"(bytes), "r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void expect_tx(uint32_t bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void mma(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc)
+{
+    asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                 " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+                 :: "r"(tmem_d), "l"(a), "l"(b), "r"(idesc), "r"(acc) : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                 :: "r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
+{
+    uint32_t r[16];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+                 "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                   "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                   "=r"(r[14]), "=r"(r[15])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// SiLU with the fast exponential and division: their relative error (about
+// 1e-6) is far below the BF16 rounding of the activation that follows
+__device__ __forceinline__ float silu_fast(float z) { return __fdividef(z, 1.f + __expf(-z)); }
+
+__device__ __forceinline__ uint32_t pack2(float a, float b)
+{
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+
+// Epilogue of a hidden layer: D (TMEM, 128 x 256 FP32) + bias -> SiLU ->
+// BF16 -> A operand (row = TMEM lane).  Warp w: lanes 32 (w % 4).., columns
+// (w / 4) * 128 ..
+__device__ __forceinline__ void hidden_epilogue(uint32_t tmem, unsigned char* base, const float* bias)
+{
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t q = (uint32_t)(warp & 3), half = (uint32_t)(warp >> 2);
+    const uint32_t row = 32u * q + (uint32_t)lane;
+#pragma unroll 1
+    for (uint32_t g = 0; g < 8; ++g) {
+        const uint32_t col = half * 128u + g * 16u;
+        float v[16];
+        tmem_ld16(tmem + ((32u * q) << 16) + col, v);
+        uint32_t w[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+            w[i] = pack2(silu_fast(v[2 * i] + bias[col + 2 * i]), silu_fast(v[2 * i + 1] + bias[col + 2 * i + 1]));
+        uint4* d0 = reinterpret_cast<uint4*>(base + kOffA + sw128_offset(kRows, row, col));
+        uint4* d1 = reinterpret_cast<uint4*>(base + kOffA + sw128_offset(kRows, row, col + 8));
+        *d0 = make_uint4(w[0], w[1], w[2], w[3]);
+        *d1 = make_uint4(w[4], w[5], w[6], w[7]);
+    }
+}
+
+}  // namespace tc
+
+__global__ void __launch_bounds__(tc::kThreads, 1)
+mlp_tc_kernel(const float* __restrict__ feats, uint32_t n, const float* __restrict__ fmean,
+              const float* __restrict__ fistd, const unsigned char* __restrict__ wimg,
+              const float* __restrict__ b0, const float* __restrict__ b1, const float* __restrict__ b2,
+              const float* __restrict__ b3, float* __restrict__ out, unsigned* __restrict__ err)
+{
+    using namespace tc;
+    extern __shared__ unsigned char smem_raw[];
+    const uint32_t raw = smem_u32(smem_raw);
+    unsigned char* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
+    const uint32_t sb = smem_u32(base);
+    const uint32_t barW = sb + kOffBar, barM = sb + kOffBar + 8;
+    float* bias = reinterpret_cast<float*>(base + kOffBias);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(base + kOffTmem);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const uint32_t row0 = blockIdx.x * (uint32_t)kRows;
+    const uint64_t kLimit = 1000000000ull;   // 1 s per wait
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     :: "r"(smem_u32(tmem_slot)), "r"(kTmemCols) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(barW) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(barM) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    // weights of layers 0 and 3 (40 KB)
+    if (tid == 0) {
+        expect_tx(barW, 32768u + 8192u);
+        bulk_load(sb + kOffW, wimg + kImgW0, 32768u, barW);
+        bulk_load(sb + kOffW3, wimg + kImgW3, 8192u, barW);
+    }
+    for (int i = tid; i < kHid; i += kThreads) {
+        bias[i] = b0[i];
+        bias[kHid + i] = b1[i];
+        bias[2 * kHid + i] = b2[i];
+    }
+    if (tid < kOut) bias[3 * kHid + tid] = b3[tid];
+    // normalised BF16 inputs: thread -> (row, 8 features)
+    {
+        const uint32_t r = (uint32_t)(tid & (kRows - 1)), h = (uint32_t)(tid >> 7);
+        const uint32_t gr = row0 + r;
+        float x[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int k = (int)h * 8 + j;
+            x[j] = gr < n ? (feats[(size_t)gr * kIn + k] - fmean[k]) * fistd[k] : 0.f;
+        }
+        *reinterpret_cast<uint4*>(base + kOffA + sw128_offset(kRows, r, h * 8)) =
+            make_uint4(pack2(x[0], x[1]), pack2(x[2], x[3]), pack2(x[4], x[5]), pack2(x[6], x[7]));
+    }
+    fence_async_smem();
+    __syncthreads();
+
+    bool ok = true;
+    uint32_t phaseW = 0, phaseM = 0;
+    // ---- layers 0..2: hidden, N = 256
+#pragma unroll 1
+    for (int layer = 0; layer < 3 && ok; ++layer) {
+        if (tid == 0) {
+            ok = mbar_wait(barW, phaseW, kLimit);
+            if (ok) {
+                fence_after();
+                const uint32_t idesc = idesc_bf16(128, 256);
+                const int ksteps = layer == 0 ? 1 : kHid / 16;
+                for (int j = 0; j < ksteps; ++j) {
+                    const uint32_t off_a = kOffA + (uint32_t)(j >> 2) * (kRows * 128u) + (uint32_t)(j & 3) * 32u;
+                    const uint32_t off_b = kOffW + (uint32_t)(j >> 2) * (kHid * 128u) + (uint32_t)(j & 3) * 32u;
+                    mma(tmem, sw128_desc(sb + off_a), sw128_desc(sb + off_b), idesc, j > 0 ? 1u : 0u);
+                }
+                mma_commit(barM);
+            }
+        }
+        phaseW ^= 1u;
+        ok = __syncthreads_and(ok) != 0;
+        if (!ok) break;
+        ok = mbar_wait(barM, phaseM, kLimit);
+        phaseM ^= 1u;
+        ok = __syncthreads_and(ok) != 0;
+        if (!ok) break;
+        fence_after();
+        // the weight buffer is free again: stream the next layer's weights
+        if (tid == 0 && layer < 2) {
+            expect_tx(barW, 131072u);
+            bulk_load(sb + kOffW, wimg + (layer == 0 ? kImgW1 : kImgW2), 131072u, barW);
+        }
+        hidden_epilogue(tmem, base, bias + layer * kHid);
+        fence_before();
+        fence_async_smem();
+        __syncthreads();
+    }
+    // ---- layer 3: N = 16, bias, FP32 rows of 16
+    if (ok) {
+        if (tid == 0) {
+            fence_after();
+            const uint32_t idesc = idesc_bf16(128, kOut);
+            for (int j = 0; j < kHid / 16; ++j) {
+                const uint32_t off_a = kOffA + (uint32_t)(j >> 2) * (kRows * 128u) + (uint32_t)(j & 3) * 32u;
+                const uint32_t off_b = kOffW3 + (uint32_t)(j >> 2) * (kOut * 128u) + (uint32_t)(j & 3) * 32u;
+                mma(tmem, sw128_desc(sb + off_a), sw128_desc(sb + off_b), idesc, j > 0 ? 1u : 0u);
+            }
+            mma_commit(barM);
+        }
+        ok = mbar_wait(barM, phaseM, kLimit);
+        phaseM ^= 1u;
+        ok = __syncthreads_and(ok) != 0;
+        if (ok) {
+            fence_after();
+            if (warp < 4) {
+                const int lane = tid & 31;
+                float v[16];
+                tmem_ld16(tmem + ((32u * (uint32_t)warp) << 16), v);
+                const uint32_t gr = row0 + 32u * (uint32_t)warp + (uint32_t)lane;
+                if (gr < n) {
+                    float4* o = reinterpret_cast<float4*>(out + (size_t)gr * kOut);
+                    const float* bb = bias + 3 * kHid;
+#pragma unroll
+                    for (int i = 0; i < 4; ++i)
+                        o[i] = make_float4(v[4 * i] + bb[4 * i], v[4 * i + 1] + bb[4 * i + 1],
+                                           v[4 * i + 2] + bb[4 * i + 2], v[4 * i + 3] + bb[4 * i + 3]);
+                }
+            }
+        }
+    }
+    if (!ok) {
+        // let issued tensor-core work and weight copies retire before the
+        // tensor memory is freed and the CTA exits (bounded)
+        if (tid == 0) {
+            atomicOr(err, 1u);
+            mma_commit(barM);
+            mbar_wait(barM, phaseM, kLimit);
+            mbar_wait(barW, phaseW, kLimit);
+        }
+    }
+    fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(kTmemCols) : "memory");
+    }
+}
+
+// dst = 128-byte-swizzled K-major image of src[rows][K] (row stride ld),
+// K padded with zeros to kpad (a multiple of 64); one thread per 16 bytes.
+__global__ void pack_sw128_kernel(const bf16* __restrict__ src, int rows, int K, int ld, int kpad,
+                                  unsigned char* __restrict__ dst)
+{
+    const uint32_t chunks = (uint32_t)rows * (uint32_t)(kpad / 8);
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= chunks) return;
+    const uint32_t r = i / (uint32_t)(kpad / 8), k0 = (i % (uint32_t)(kpad / 8)) * 8u;
+    uint16_t v[8];
+    const uint16_t* s = reinterpret_cast<const uint16_t*>(src);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) v[j] = (k0 + j < (uint32_t)K) ? s[(size_t)r * ld + k0 + j] : (uint16_t)0;
+    uint4 w;
+    w.x = v[0] | ((uint32_t)v[1] << 16);
+    w.y = v[2] | ((uint32_t)v[3] << 16);
+    w.z = v[4] | ((uint32_t)v[5] << 16);
+    w.w = v[6] | ((uint32_t)v[7] << 16);
+    *reinterpret_cast<uint4*>(dst + tc::sw128_offset((uint32_t)rows, r, k0)) = w;
+}
+
+cudaError_t launch_pack_sw128(const void* src, int rows, int K, int ld, int kpad, void* dst, cudaStream_t s)
+{
+    if (rows <= 0 || K <= 0 || kpad % 64 || K > kpad || ld < K) return cudaErrorInvalidValue;
+    const uint32_t chunks = (uint32_t)rows * (uint32_t)(kpad / 8);
+    pack_sw128_kernel<<<(chunks + 255) / 256, 256, 0, s>>>(static_cast<const bf16*>(src), rows, K, ld, kpad,
+                                                           static_cast<unsigned char*>(dst));
+    return cudaGetLastError();
+}
+
+size_t mlp_tc_image_bytes() { return tc::kImgBytes; }
+
+cudaError_t launch_mlp_tc(const float* feats, uint32_t n, const float* fmean, const float* fistd,
+                          const void* wimg, const float* b0, const float* b1, const float* b2, const float* b3,
+                          float* out, unsigned* err, cudaStream_t s)
+{
+    if (n == 0) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(mlp_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)tc::kSmemBytes);
+    if (e != cudaSuccess) return e;
+    const uint32_t grid = (n + tc::kRows - 1) / tc::kRows;
+    mlp_tc_kernel<<<grid, tc::kThreads, tc::kSmemBytes, s>>>(feats, n, fmean, fistd,
+                                                            static_cast<const unsigned char*>(wimg), b0, b1, b2,
+                                                            b3, out, err);
+    return cudaGetLastError();
+}
+
+}  // namespace sfh

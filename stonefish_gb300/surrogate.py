@@ -37,6 +37,7 @@ from .hydro import HydroContext, _check
 N_FEAT = 16
 N_OUT = 6
 IN_PAD = 64          # input columns (features padded; GEMM tiles are 64 wide)
+TC_IMAGE_BYTES = 303104   # HYDRO_NN_TC_IMAGE_BYTES
 OUT_PAD = 64         # output columns (6 used)
 
 # the training hull: the torpedo of the wave workload at 12000 faces
@@ -383,6 +384,42 @@ class Surrogate:
         self._mlp(bufs, n_pad)
         return bufs["z"]
 
+    def tc_weights(self) -> dict:
+        """Weights of the fused tensor-core kernel (hydro_nn_mlp_tc): the four
+        layers' transposes in the 128-byte-swizzled operand image, the last
+        layer with the target de-normalisation folded in and its output
+        padded to 16 columns, and the biases."""
+        L = self.layers
+        img = torch.zeros(TC_IMAGE_BYTES, dtype=torch.uint8, device=self.dev)
+        st = self._s()
+        offs = (0, 32768, 163840)
+        for l in range(3):
+            self._ck(self.lib.hydro_nn_pack_sw128(self.h.ctx, _ptr(L[l]["wt16"]), L[l]["n"], L[l]["k"], L[l]["k"],
+                                                  L[l]["k"], C.c_void_p(img.data_ptr() + offs[l]), st))
+        w = L[3]["w"].cpu().numpy().astype(np.float64)
+        b = L[3]["b"].cpu().numpy().astype(np.float64)
+        std, mean = self.stats["t_std"], self.stats["t_mean"]
+        w[:, :N_OUT] *= std
+        b[:N_OUT] = b[:N_OUT] * std + mean
+        w3t = torch.tensor(np.ascontiguousarray(w[:, :16].T), dtype=torch.float32, device=self.dev)
+        w3t16 = torch.empty((16, self.hidden), dtype=torch.bfloat16, device=self.dev)
+        self.to_bf16(w3t, 16, self.hidden, self.hidden, w3t16)
+        self._ck(self.lib.hydro_nn_pack_sw128(self.h.ctx, _ptr(w3t16), 16, self.hidden, self.hidden, self.hidden,
+                                              C.c_void_p(img.data_ptr() + 294912), st))
+        torch.cuda.synchronize(self.dev)
+        return {"image": img, "b": [L[0]["b"].clone(), L[1]["b"].clone(), L[2]["b"].clone(),
+                                    torch.tensor(b[:16], dtype=torch.float32, device=self.dev)],
+                "err": torch.zeros(1, dtype=torch.int32, device=self.dev)}
+
+    def infer_tc(self, feats: torch.Tensor, out: torch.Tensor, tcw: dict) -> torch.Tensor:
+        """Fused tensor-core inference: out[n, 16] (columns 0..5 the wrench)."""
+        n = feats.shape[0]
+        b = tcw["b"]
+        self._ck(self.lib.hydro_nn_mlp_tc(self.h.ctx, _ptr(feats), n, _ptr(self.f_mean), _ptr(self.f_istd),
+                                          _ptr(tcw["image"]), _ptr(b[0]), _ptr(b[1]), _ptr(b[2]), _ptr(b[3]),
+                                          _ptr(out), _ptr(tcw["err"]), self._s()))
+        return out
+
     def _mlp(self, bufs, n_pad):
         H = self.hidden
         Ls = self.layers
@@ -399,7 +436,7 @@ class GatedPredictor:
     past the rejected count are switched off and cost nothing)."""
 
     def __init__(self, sur: Surrogate, hctx_exact: HydroContext, mesh_id: int, n: int,
-                 ocean: abi.Ocean, settings: abi.Settings):
+                 ocean: abi.Ocean, settings: abi.Settings, tensor_cores: str = "tcgen05"):
         self.s = sur
         self.h = hctx_exact
         self.lib = hctx_exact.lib
@@ -419,6 +456,13 @@ class GatedPredictor:
         self.exact_io = torch.zeros(n * abi.WRENCH_DTYPE.itemsize, dtype=torch.uint8, device=dev)
         self.out = torch.zeros((n, N_OUT), dtype=torch.float32, device=dev)
         self.launches = 0
+        # "tcgen05": one fused kernel for the whole network; "mma": the four
+        # mma.sync GEMMs of the training path
+        assert tensor_cores in ("tcgen05", "mma")
+        self.mode = tensor_cores
+        if tensor_cores == "tcgen05":
+            self.tcw = sur.tc_weights()
+            self.z16 = torch.zeros((self.n_pad, 16), dtype=torch.float32, device=dev)
 
     def _ck(self, st):
         _check(self.lib, self.h.ctx, st)
@@ -434,17 +478,22 @@ class GatedPredictor:
         self._ck(self.lib.hydro_nn_features(ctx, _ptr(d_bodies), n, C.byref(self.ocean), _ptr(b["feats"]), st))
         self._ck(self.lib.hydro_nn_gate(ctx, _ptr(b["feats"]), n, _ptr(g["lo"]), _ptr(g["hi"]), _ptr(g["mean"]),
                                         _ptr(g["P"]), g["thr"], _ptr(b["mask"]), st))
-        s.to_bf16(b["feats"], self.n_pad, N_FEAT, IN_PAD, b["X0"], s.f_mean, s.f_istd)
-        s._mlp(b, self.n_pad)
+        if self.mode == "tcgen05":
+            s.infer_tc(b["feats"], self.z16, self.tcw)
+            z, ldz, mlp_launches = self.z16, 16, 1
+        else:
+            s.to_bf16(b["feats"], self.n_pad, N_FEAT, IN_PAD, b["X0"], s.f_mean, s.f_istd)
+            s._mlp(b, self.n_pad)
+            z, ldz, mlp_launches = b["z"], OUT_PAD, 5
         self._ck(self.lib.hydro_nn_route(ctx, _ptr(d_bodies), _ptr(b["mask"]), n, _ptr(self.counts),
                                          _ptr(self.packed), _ptr(self.pos), _ptr(self.n_packed), st))
         self.exact_io.zero_()
         self.batch.compute_device_prefix(self.packed.data_ptr(), self.n_packed.data_ptr(), self.ocean,
                                          self.settings, self.exact_io.data_ptr(), st)
-        self._ck(self.lib.hydro_nn_merge(ctx, _ptr(d_bodies), _ptr(b["z"]), OUT_PAD, _ptr(self.pos),
+        self._ck(self.lib.hydro_nn_merge(ctx, _ptr(d_bodies), _ptr(z), ldz, _ptr(self.pos),
                                          _ptr(self.exact_io), n, _ptr(self.out), st))
-        # features, gate, to_bf16, 4 GEMMs, 2 route, exact step, merge
-        self.launches = 1 + 1 + 1 + 4 + 2 + self.batch.last_launches() + 1
+        # features, gate, network, 2 route, exact step, merge
+        self.launches = 1 + 1 + mlp_launches + 2 + self.batch.last_launches() + 1
         return self.out
 
     def rejected(self) -> int:

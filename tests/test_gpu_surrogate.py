@@ -278,3 +278,28 @@ def test_surrogate_learns_and_beats_exact_step(built_library):
         o.close()
     h32.close()
     h64.close()
+
+
+@pytest.mark.parametrize("n", [1000, 4096])
+def test_fused_tensor_core_inference_matches_gemm_path(hctx, n):
+    """hydro_nn_mlp_tc (tcgen05, one kernel) against the four mma.sync GEMMs:
+    same BF16 weights and activations, so only the FP32 accumulation order
+    and the SiLU evaluation differ."""
+    rng = np.random.default_rng(31)
+    sur = S.Surrogate(hctx, hidden=256, seed=7, batch=256)
+    feats = _dev(rng.normal(size=(n, S.N_FEAT)) * 1.5 + 0.5)
+    targ = _dev(rng.normal(size=(n, S.N_OUT)) * 40.0 + 5.0)
+    sur.fit_normalisation(feats, targ)
+    # a few training steps so that every layer has non-trivial weights
+    sur.fit(feats[: 4 * 256].contiguous(), targ[: 4 * 256].contiguous(), epochs=2, lr=3e-3, warmup=1)
+    ref = sur.infer_features(feats)[:n, :6].cpu().numpy()
+    tcw = sur.tc_weights()
+    out = torch.zeros(((n + 127) // 128 * 128, 16), dtype=torch.float32, device="cuda")
+    got = sur.infer_tc(feats, out, tcw)[:n, :6].cpu().numpy()
+    assert int(tcw["err"].item()) == 0
+    scale = np.max(np.abs(ref), axis=0)
+    err = np.max(np.abs(got - ref), axis=0) / scale
+    assert np.all(err < 1e-2), err
+    med = np.median(np.abs(got - ref), axis=0) / scale
+    assert np.all(med < 1e-3), med
+    assert np.all(out[n:].cpu().numpy() == 0.0)      # rows past n are not written
