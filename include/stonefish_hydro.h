@@ -138,6 +138,39 @@ typedef struct hydro_ocean {
     hydro_current currents[HYDRO_MAX_CURRENTS];
 } hydro_ocean;
 
+/* The Atmosphere as seen by the aerodynamic path (Atmosphere.cpp:146-157):
+ * gas density and the wind fields, all of which are summed (the atmosphere
+ * has no per-field or global enable switch). */
+typedef struct hydro_atmosphere {
+    double density;              /* Atmosphere::getGas().density */
+    uint32_t n_winds;
+    uint32_t reserved;
+    hydro_current winds[HYDRO_MAX_CURRENTS];
+} hydro_atmosphere;
+
+/* GeometryApproxType, Library/include/entities/SolidEntity.h:39 */
+enum {
+    HYDRO_APPROX_AUTO = 0,
+    HYDRO_APPROX_SPHERE = 1,
+    HYDRO_APPROX_CYLINDER = 2,
+    HYDRO_APPROX_ELLIPSOID = 3
+};
+
+/* Per-body inputs of CorrectAerodynamicForces (SolidEntity.cpp:1925-1956). */
+typedef struct hydro_aero_params {
+    int32_t approx_type;         /* fdApproxType */
+    int32_t reserved;
+    double R_CG2H[9];            /* T_CG2H.getBasis(), rows */
+    double approx_params[3];     /* fdApproxParams[0..2] (ellipsoid semi-axes) */
+} hydro_aero_params;
+
+/* Results of the aerodynamic path: the SolidEntity members Fda, Tda. */
+typedef struct hydro_aero_wrench {
+    double Fda[3], Tda[3];
+    int32_t status;              /* per-body error word, 0 = ok */
+    int32_t reserved;
+} hydro_aero_wrench;
+
 /* Per-body state read by SolidEntity::ComputeHydrodynamicForces
  * (SolidEntity.cpp:1799-1850) and its accessors (:215-226, :410-459). */
 typedef struct hydro_body {
@@ -368,6 +401,34 @@ hydro_status hydro_correct_forces(hydro_ctx* ctx, const hydro_ocean* ocean,
 hydro_status hydro_fluid_position(hydro_ctx* ctx, const hydro_ocean* ocean,
                                   const double aabb_min[3],
                                   const double aabb_max[3], int32_t* position);
+
+/* ---------------------------------------------------------- aerodynamics */
+/* SolidEntity::ComputeAerodynamicForces(mesh, atm, T_CG, T_C, v, omega,
+ * Fda, Tda) (SolidEntity.cpp:1865-1923): quadratic-law drag of the faces
+ * whose normal velocity points into them, about the CG, for one body.  As in
+ * the reference, each face's term is vn * 3 * A (glm's vec3::length() is the
+ * component count, not the norm).  mesh HYDRO_NO_MESH gives zeros. */
+hydro_status hydro_aero_forces(hydro_ctx* ctx, hydro_mesh_id mesh, const hydro_atmosphere* atm,
+                               const hydro_transform* T_CG, const hydro_transform* T_C,
+                               const double v[3], const double omega[3], double Fda[3], double Tda[3]);
+
+/* SolidEntity::CorrectAerodynamicForces (SolidEntity.cpp:1925-1956). */
+hydro_status hydro_aero_correct(hydro_ctx* ctx, const hydro_aero_params* params, double Fda[3],
+                                double Tda[3]);
+
+/* SolidEntity::ComputeAerodynamicForces(Atmosphere*) (SolidEntity.cpp:1852-1863)
+ * for every body of the batch: bodies whose mode is not
+ * HYDRO_MODE_AERODYNAMIC are left untouched; the others get the face loop
+ * and the correction.  Device pointers, enqueued on `stream`. */
+hydro_status hydro_batch_compute_aero_device(hydro_batch* batch, const hydro_body* d_bodies,
+                                             const hydro_aero_params* d_params,
+                                             const hydro_atmosphere* atm, hydro_aero_wrench* d_out,
+                                             void* stream);
+
+/* Host-buffer version of hydro_batch_compute_aero_device (synchronises). */
+hydro_status hydro_batch_compute_aero(hydro_batch* batch, const hydro_body* bodies,
+                                      const hydro_aero_params* params, const hydro_atmosphere* atm,
+                                      hydro_aero_wrench* out);
 
 /* ------------------------------------------------------------ diagnostics */
 /* Per-face contributions of the surface loop (ComputeHydrodynamicForcesSurface,

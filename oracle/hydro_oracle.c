@@ -365,6 +365,93 @@ void oracle_correct_forces(const hydro_ocean* ocean, double Fdq[3], double Tdq[3
     correct_one(inv, Tdf, Cf, ocean->density);
 }
 
+/* ----------------------------------------------------------- aerodynamics */
+/* Atmosphere::GetFluidVelocity sums every wind field (Atmosphere.cpp:146-152):
+ * the winds as enabled currents of an ocean descriptor. */
+static void atmosphere_ocean(const hydro_atmosphere* a, hydro_ocean* o)
+{
+    memset(o, 0, sizeof(*o));
+    o->density = a->density;
+    o->currents_enabled = 1;
+    o->n_currents = a->n_winds < HYDRO_MAX_CURRENTS ? a->n_winds : HYDRO_MAX_CURRENTS;
+    for (uint32_t i = 0; i < o->n_currents; ++i) {
+        o->currents[i] = a->winds[i];
+        o->currents[i].enabled = 1;
+    }
+}
+
+/* SolidEntity::ComputeAerodynamicForces(mesh, atm, T_CG, T_C, v, omega, Fda, Tda)
+ * (SolidEntity.cpp:1865-1923). */
+void oracle_aero_forces(int variant, const oracle_mesh* mesh, const hydro_atmosphere* atm,
+                        const hydro_transform* T_CG, const hydro_transform* T_C, const double v[3],
+                        const double omega[3], double Fda[3], double Tda[3])
+{
+    if (mesh == NULL) { zero3(Fda); zero3(Tda); return; }  /* :1868-1873 */
+    hydro_ocean o;
+    atmosphere_ocean(atm, &o);
+    double F[3] = {0, 0, 0}, Tq[3] = {0, 0, 0};
+    if (variant == ORACLE_REF32) {
+        job_f32 J;
+        v3_f32 f = {0, 0, 0}, t = {0, 0, 0};
+        job_init_f32(&J, mesh, &o, NULL, T_CG, T_C, v, omega, 0, 0);
+        for (uint32_t i = 0; i < mesh->n_faces; ++i) face_aero_f32(&J, i, &f, &t);
+        set3(F, f.x, f.y, f.z);
+        set3(Tq, t.x, t.y, t.z);
+    } else if (variant == ORACLE_REF64) {
+        job_f64 J;
+        v3_f64 f = {0, 0, 0}, t = {0, 0, 0};
+        job_init_f64(&J, mesh, &o, NULL, T_CG, T_C, v, omega, 0, 0);
+        for (uint32_t i = 0; i < mesh->n_faces; ++i) face_aero_f64(&J, i, &f, &t);
+        set3(F, f.x, f.y, f.z);
+        set3(Tq, t.x, t.y, t.z);
+    } else {
+        /* FP32 face terms summed in double: the GPU kernel's arithmetic */
+        job_f32 J;
+        job_init_f32(&J, mesh, &o, NULL, T_CG, T_C, v, omega, 0, 0);
+        for (uint32_t i = 0; i < mesh->n_faces; ++i) {
+            v3_f32 f = {0, 0, 0}, t = {0, 0, 0};
+            face_aero_f32(&J, i, &f, &t);
+            F[0] += (double)f.x; F[1] += (double)f.y; F[2] += (double)f.z;
+            Tq[0] += (double)t.x; Tq[1] += (double)t.y; Tq[2] += (double)t.z;
+        }
+    }
+    const double k = 0.5 * atm->density;                    /* :1918-1922 */
+    set3(Fda, k * F[0], k * F[1], k * F[2]);
+    set3(Tda, k * Tq[0], k * Tq[1], k * Tq[2]);
+}
+
+/* SolidEntity::CorrectAerodynamicForces (SolidEntity.cpp:1925-1956). */
+void oracle_aero_correct(const hydro_aero_params* p, double Fda[3], double Tda[3])
+{
+    double inv[9];
+    binverse(p->R_CG2H, inv);
+    double n[3] = {inv[0] * Fda[0] + inv[1] * Fda[1] + inv[2] * Fda[2],
+                   inv[3] * Fda[0] + inv[4] * Fda[1] + inv[5] * Fda[2],
+                   inv[6] * Fda[0] + inv[7] * Fda[1] + inv[8] * Fda[2]};
+    /* btVector3::safeNormalize; operator/= multiplies by the reciprocal */
+    double l2 = bdot(n, n);
+    if (l2 >= DBL_EPSILON * DBL_EPSILON) {
+        double s = 1.0 / sqrt(l2);
+        n[0] *= s; n[1] *= s; n[2] *= s;
+    } else {
+        n[0] = 1.0; n[1] = 0.0; n[2] = 0.0;
+    }
+    double cor = 1.0;
+    if (p->approx_type == HYDRO_APPROX_CYLINDER) {
+        double cd[3] = {0.5, 0.5, 1.0};
+        cor = bdot(cd, n);
+    } else if (p->approx_type == HYDRO_APPROX_ELLIPSOID) {
+        double cd[3] = {1.0 / p->approx_params[0], 1.0 / p->approx_params[1], 1.0 / p->approx_params[2]};
+        double mx = cd[0] > cd[1] ? cd[0] : cd[1];
+        mx = mx > cd[2] ? mx : cd[2];
+        double s = 1.0 / mx;
+        cd[0] *= s; cd[1] *= s; cd[2] *= s;
+        cor = bdot(cd, n);
+    }
+    cor = fabs(cor);
+    for (int k = 0; k < 3; ++k) { Fda[k] *= cor; Tda[k] *= cor; }
+}
+
 /* SolidEntity::ComputeHydrodynamicForces (SolidEntity.cpp:1799-1850). */
 void oracle_body_forces(int variant, const hydro_body* b, const oracle_mesh* mesh,
                         const hydro_ocean* ocean, const oracle_waves* waves,

@@ -117,6 +117,13 @@ double oracle_batch(int variant, int threads, const hydro_body* bodies,
 
 int oracle_hardware_threads(void);
 
+/* SolidEntity::ComputeAerodynamicForces (static form, SolidEntity.cpp:1865-1923)
+ * and CorrectAerodynamicForces (:1925-1956). */
+void oracle_aero_forces(int variant, const oracle_mesh* mesh, const hydro_atmosphere* atm,
+                        const hydro_transform* T_CG, const hydro_transform* T_C, const double v[3],
+                        const double omega[3], double Fda[3], double Tda[3]);
+void oracle_aero_correct(const hydro_aero_params* params, double Fda[3], double Tda[3]);
+
 #ifdef __cplusplus
 }
 #endif

@@ -79,6 +79,11 @@ class Oracle:
                                    P(abi.Settings), vp]
         L.oracle_hardware_threads.restype = i32
         L.oracle_hardware_threads.argtypes = []
+        L.oracle_aero_forces.restype = None
+        L.oracle_aero_forces.argtypes = [i32, vp, P(abi.Atmosphere), P(abi.Transform), P(abi.Transform),
+                                         d, d, d, d]
+        L.oracle_aero_correct.restype = None
+        L.oracle_aero_correct.argtypes = [P(abi.AeroParams), d, d]
         self._keep = []
 
     # ------------------------------------------------------------ helpers
@@ -185,6 +190,24 @@ class Oracle:
         ptrs = [io[k].ctypes.data_as(C.POINTER(C.c_double)) for k in ("Fdq", "Tdq", "Fdf", "Tdf")]
         self.lib.oracle_correct_forces(C.byref(ocean), *ptrs, pcd, pcf, pro)
         return io
+
+    def aero_forces(self, variant, mesh, atm, T_CG, T_C, v, omega):
+        """SolidEntity::ComputeAerodynamicForces (static form): (Fda, Tda)."""
+        m = None if mesh is None else self.make_mesh(*mesh)
+        vv, pv = self._vec(v)
+        ww, pw = self._vec(omega)
+        F = np.zeros(3)
+        T = np.zeros(3)
+        self.lib.oracle_aero_forces(variant, self._p(m), C.byref(atm), C.byref(T_CG), C.byref(T_C), pv, pw,
+                                    F.ctypes.data_as(C.POINTER(C.c_double)), T.ctypes.data_as(C.POINTER(C.c_double)))
+        return F, T
+
+    def aero_correct(self, params, Fda, Tda):
+        F = np.array(Fda, dtype=np.float64)
+        T = np.array(Tda, dtype=np.float64)
+        self.lib.oracle_aero_correct(C.byref(params), F.ctypes.data_as(C.POINTER(C.c_double)),
+                                     T.ctypes.data_as(C.POINTER(C.c_double)))
+        return F, T
 
     def face_terms(self, variant, settings, mesh, ocean, T_CG, T_C, v, omega, waves=None):
         m = self.make_mesh(*mesh)

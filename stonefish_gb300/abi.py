@@ -66,6 +66,20 @@ class Ocean(C.Structure):
                 ("currents", Current * MAX_CURRENTS)]
 
 
+class Atmosphere(C.Structure):
+    _fields_ = [("density", C.c_double), ("n_winds", C.c_uint32), ("reserved", C.c_uint32),
+                ("winds", Current * MAX_CURRENTS)]
+
+
+class AeroParams(C.Structure):
+    _fields_ = [("approx_type", C.c_int32), ("reserved", C.c_int32), ("R_CG2H", C.c_double * 9),
+                ("approx_params", _d3)]
+
+
+class AeroWrench(C.Structure):
+    _fields_ = [("Fda", _d3), ("Tda", _d3), ("status", C.c_int32), ("reserved", C.c_int32)]
+
+
 class Body(C.Structure):
     _fields_ = [("T_CG", Transform), ("T_C", Transform), ("R_O", C.c_double * 9),
                 ("v", _d3), ("omega", _d3), ("Cd", _d3), ("Cf", _d3), ("P_CB", _d3),
@@ -123,6 +137,9 @@ WRENCH_DTYPE = _dtype_of(Wrench)
 OCEAN_DTYPE = _dtype_of(Ocean)
 CURRENT_DTYPE = _dtype_of(Current)
 RIGID_DTYPE = _dtype_of(RigidState)
+AERO_PARAMS_DTYPE = _dtype_of(AeroParams)
+AERO_WRENCH_DTYPE = _dtype_of(AeroWrench)
+APPROX_AUTO, APPROX_SPHERE, APPROX_CYLINDER, APPROX_ELLIPSOID = range(4)
 
 WRENCH_VECTORS = ("Fb", "Tb", "Fdq", "Tdq", "Fdf", "Tdf")
 
@@ -206,6 +223,11 @@ def _declare(lib: C.CDLL) -> None:
         "hydro_nn_wrench_body": (i32, [vp, vp, vp, u32, vp, vp]),
         "hydro_nn_pack_sw128": (i32, [vp, vp, i32, i32, i32, i32, vp, vp]),
         "hydro_nn_mlp_tc": (i32, [vp, vp, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
+        "hydro_aero_forces": (i32, [vp, u32, C.POINTER(Atmosphere), C.POINTER(Transform), C.POINTER(Transform),
+                                    d, d, d, d]),
+        "hydro_aero_correct": (i32, [vp, C.POINTER(AeroParams), d, d]),
+        "hydro_batch_compute_aero_device": (i32, [vp, vp, vp, C.POINTER(Atmosphere), vp, vp]),
+        "hydro_batch_compute_aero": (i32, [vp, vp, vp, C.POINTER(Atmosphere), vp]),
         "hydro_rigid_step": (i32, [vp, vp, vp, vp, vp, u32, C.c_double, C.c_double, vp]),
         "hydro_rigid_write_bodies": (i32, [vp, vp, vp, u32, vp]),
     }

@@ -80,6 +80,8 @@ struct hydro_batch {
     uint32_t last_launches = 0;
     uint32_t chunk_tiles = 0;    // tiles per work chunk of this batch
     uint32_t ctas_per_sm = 0;    // 0 = the context's setting
+    hydro_aero_params* aparams_d = nullptr;   // staging for the host-buffer aerodynamic call
+    hydro_aero_wrench* aio_d = nullptr;
 };
 
 namespace {
@@ -167,6 +169,29 @@ bool valid_ocean(const hydro_ocean* o)
     return o && o->n_currents <= HYDRO_MAX_CURRENTS;
 }
 
+bool valid_atmosphere(const hydro_atmosphere* a)
+{
+    return a && a->n_winds <= HYDRO_MAX_CURRENTS;
+}
+
+// The atmosphere in the ocean descriptor the kernels read: gas density and
+// every wind field as an enabled current (Atmosphere::GetFluidVelocity sums
+// all fields, Atmosphere.cpp:146-152); no waves.
+hydro_ocean atmosphere_ocean(const hydro_atmosphere* a)
+{
+    hydro_ocean o{};
+    o.density = a->density;
+    o.gravity = 0.0;
+    o.waves = 0;
+    o.currents_enabled = 1;
+    o.n_currents = a->n_winds;
+    for (uint32_t i = 0; i < a->n_winds && i < HYDRO_MAX_CURRENTS; ++i) {
+        o.currents[i] = a->winds[i];
+        o.currents[i].enabled = 1;
+    }
+    return o;
+}
+
 // The kernels' view of the ocean: the position-independent currents are
 // summed in FP64 in the reference's order and cast once (Ocean.cpp:183-201).
 OceanDev make_ocean(const hydro_ctx* ctx, const hydro_ocean* o)
@@ -223,6 +248,8 @@ void batch_free(hydro_batch* b)
     cudaFree(b->chunk_active_d);
     cudaFree(b->bodies_d);
     cudaFree(b->io_d);
+    cudaFree(b->aparams_d);
+    cudaFree(b->aio_d);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
 }
@@ -312,7 +339,8 @@ hydro_status batch_build(hydro_ctx* ctx, const hydro_mesh_id* mesh_of_body, uint
 
 hydro_status batch_launch(hydro_batch* b, const hydro_body* d_bodies, const hydro_ocean* ocean,
                           const hydro_settings* settings, hydro_wrench* d_io, cudaStream_t s,
-                          int op, const uint32_t* d_count = nullptr)
+                          int op, const uint32_t* d_count = nullptr, hydro_aero_wrench* d_aero = nullptr,
+                          const hydro_aero_params* d_aero_params = nullptr)
 {
     hydro_ctx* ctx = b->ctx;
     hydro_status st = sync_tiles(ctx);
@@ -329,6 +357,8 @@ hydro_status batch_launch(hydro_batch* b, const hydro_body* d_bodies, const hydr
     P.work = b->err_d + 32;
     P.active_end = b->err_d + 48;
     P.n_active = d_count;
+    P.aero_io = d_aero;
+    P.aero_params = d_aero_params;
     P.chunk_active = b->chunk_active_d;
     P.n_bodies = b->n_bodies;
     P.n_chunks = b->n_chunks;
@@ -812,6 +842,112 @@ hydro_status hydro_correct_forces(hydro_ctx* ctx, const hydro_ocean* ocean, doub
     CK(ctx, cudaMemcpyAsync(h, d, 12 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     CK(ctx, cudaStreamSynchronize(ctx->stream));
     copy3(Fdq, h); copy3(Tdq, h + 3); copy3(Fdf, h + 6); copy3(Tdf, h + 9);
+    return HYDRO_OK;
+}
+
+// ------------------------------------------------------------ aerodynamics
+hydro_status hydro_aero_forces(hydro_ctx* ctx, hydro_mesh_id mesh, const hydro_atmosphere* atm,
+                               const hydro_transform* T_CG, const hydro_transform* T_C, const double v[3],
+                               const double omega[3], double Fda[3], double Tda[3])
+{
+    if (!ctx) return HYDRO_ERR_INVALID_ARG;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (!valid_atmosphere(atm) || !T_CG || !T_C || !v || !omega || !Fda || !Tda)
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "aero forces: null argument");
+    if (mesh != HYDRO_NO_MESH && mesh >= ctx->meshes.size())
+        return fail(ctx, HYDRO_ERR_NOT_FOUND, "unknown mesh %u", mesh);
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, HYDRO_ERR_DEVICE, "cudaSetDevice");
+    hydro_batch* b = nullptr;
+    hydro_status st = single_batch(ctx, mesh, &b);
+    if (st != HYDRO_OK) return st;
+    if ((st = ensure_small(ctx, sizeof(hydro_aero_wrench))) != HYDRO_OK) return st;
+    hydro_body body{};
+    body.T_CG = *T_CG;
+    body.T_C = *T_C;
+    copy3(body.v, v);
+    copy3(body.omega, omega);
+    body.mesh = mesh;
+    body.mode = HYDRO_MODE_AERODYNAMIC;
+    hydro_aero_wrench w{};
+    hydro_aero_wrench* d = static_cast<hydro_aero_wrench*>(ctx->small_d);
+    const hydro_ocean o = atmosphere_ocean(atm);
+    const hydro_settings none{0, 0};
+    CK(ctx, cudaMemcpyAsync(b->bodies_d, &body, sizeof(body), cudaMemcpyHostToDevice, ctx->stream));
+    CK(ctx, cudaMemcpyAsync(d, &w, sizeof(w), cudaMemcpyHostToDevice, ctx->stream));
+    st = batch_launch(b, b->bodies_d, &o, &none, nullptr, ctx->stream, OP_AERO, nullptr, d, nullptr);
+    if (st != HYDRO_OK) return st;
+    CK(ctx, cudaMemcpyAsync(&w, d, sizeof(w), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(ctx, cudaStreamSynchronize(ctx->stream));
+    copy3(Fda, w.Fda);
+    copy3(Tda, w.Tda);
+    return HYDRO_OK;
+}
+
+hydro_status hydro_aero_correct(hydro_ctx* ctx, const hydro_aero_params* params, double Fda[3], double Tda[3])
+{
+    if (!ctx) return HYDRO_ERR_INVALID_ARG;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (!params || !Fda || !Tda) return fail(ctx, HYDRO_ERR_INVALID_ARG, "aero correct: null argument");
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, HYDRO_ERR_DEVICE, "cudaSetDevice");
+    hydro_status st = ensure_small(ctx, 256 + sizeof(hydro_aero_params));
+    if (st != HYDRO_OK) return st;
+    double h[6];
+    copy3(h, Fda);
+    copy3(h + 3, Tda);
+    unsigned char* base = static_cast<unsigned char*>(ctx->small_d);
+    double* d = reinterpret_cast<double*>(base);
+    hydro_aero_params* dp = reinterpret_cast<hydro_aero_params*>(base + 256);
+    CK(ctx, cudaMemcpyAsync(d, h, sizeof(h), cudaMemcpyHostToDevice, ctx->stream));
+    CK(ctx, cudaMemcpyAsync(dp, params, sizeof(*params), cudaMemcpyHostToDevice, ctx->stream));
+    cudaError_t e = launch_aero_correct(dp, d, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "aero correct kernel");
+    CK(ctx, cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(ctx, cudaStreamSynchronize(ctx->stream));
+    copy3(Fda, h);
+    copy3(Tda, h + 3);
+    return HYDRO_OK;
+}
+
+hydro_status hydro_batch_compute_aero_device(hydro_batch* b, const hydro_body* d_bodies,
+                                             const hydro_aero_params* d_params, const hydro_atmosphere* atm,
+                                             hydro_aero_wrench* d_out, void* stream)
+{
+    if (!b) return HYDRO_ERR_INVALID_ARG;
+    hydro_ctx* ctx = b->ctx;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (!d_bodies || !d_params || !d_out || !valid_atmosphere(atm))
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "aero batch: bad arguments");
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, HYDRO_ERR_DEVICE, "cudaSetDevice");
+    const hydro_ocean o = atmosphere_ocean(atm);
+    const hydro_settings none{0, 0};
+    return batch_launch(b, d_bodies, &o, &none, nullptr, static_cast<cudaStream_t>(stream), OP_AERO_BODY, nullptr,
+                        d_out, d_params);
+}
+
+hydro_status hydro_batch_compute_aero(hydro_batch* b, const hydro_body* bodies, const hydro_aero_params* params,
+                                      const hydro_atmosphere* atm, hydro_aero_wrench* out)
+{
+    if (!b) return HYDRO_ERR_INVALID_ARG;
+    hydro_ctx* ctx = b->ctx;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (!bodies || !params || !out || !valid_atmosphere(atm))
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "aero batch: bad arguments");
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, HYDRO_ERR_DEVICE, "cudaSetDevice");
+    const size_t nb = (size_t)b->n_bodies;
+    if (!b->bodies_d) CK(ctx, cudaMalloc(&b->bodies_d, nb * sizeof(hydro_body)));
+    if (!b->aparams_d) CK(ctx, cudaMalloc(&b->aparams_d, nb * sizeof(hydro_aero_params)));
+    if (!b->aio_d) CK(ctx, cudaMalloc(&b->aio_d, nb * sizeof(hydro_aero_wrench)));
+    CK(ctx, cudaMemcpyAsync(b->bodies_d, bodies, nb * sizeof(hydro_body), cudaMemcpyHostToDevice, b->stream));
+    CK(ctx, cudaMemcpyAsync(b->aparams_d, params, nb * sizeof(hydro_aero_params), cudaMemcpyHostToDevice,
+                            b->stream));
+    CK(ctx, cudaMemcpyAsync(b->aio_d, out, nb * sizeof(hydro_aero_wrench), cudaMemcpyHostToDevice, b->stream));
+    const hydro_ocean o = atmosphere_ocean(atm);
+    const hydro_settings none{0, 0};
+    hydro_status st = batch_launch(b, b->bodies_d, &o, &none, nullptr, b->stream, OP_AERO_BODY, nullptr, b->aio_d,
+                                   b->aparams_d);
+    if (st != HYDRO_OK) return st;
+    CK(ctx, cudaMemcpyAsync(out, b->aio_d, nb * sizeof(hydro_aero_wrench), cudaMemcpyDeviceToHost, b->stream));
+    CK(ctx, cudaStreamSynchronize(b->stream));
     return HYDRO_OK;
 }
 

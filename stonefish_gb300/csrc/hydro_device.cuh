@@ -34,9 +34,9 @@ enum : int {
 };
 
 // loop kinds of a body in one launch
-enum : int { LOOP_NONE = 0, LOOP_SURFACE = 1, LOOP_SUBMERGED = 2 };
+enum : int { LOOP_NONE = 0, LOOP_SURFACE = 1, LOOP_SUBMERGED = 2, LOOP_AERO = 3 };
 // launch operations
-enum : int { OP_BODY = 0, OP_SURFACE = 1, OP_SUBMERGED = 2 };
+enum : int { OP_BODY = 0, OP_SURFACE = 1, OP_SUBMERGED = 2, OP_AERO = 3, OP_AERO_BODY = 4 };
 
 // ------------------------------------------------------------- data layout
 // One tile of a mesh: nv vertices stored as x[nvp], y[nvp], z[nvp] floats
@@ -369,6 +369,27 @@ __device__ __forceinline__ bool tri_props(v3 p1, v3 p2, v3 p3, v3& fc, v3& fn1, 
     fn1 = dvs_rcp(fn, len);
     A = len * 0.5f;
     return true;
+}
+
+// One face of SolidEntity::ComputeAerodynamicForces (SolidEntity.cpp:1885-1915):
+// wind (the atmosphere's fields, passed as currents) relative to the face
+// centroid, its normal part vn, and for faces it flows into the term
+// vn * vn.length() * A, where glm's vec3::length() is the component count 3.
+// Force and torque go to the Q_FDQ / Q_TDQ accumulators.
+__device__ __forceinline__ void face_aero(const OceanDev& o, const BodyParams& B, Acc& a, v3 p1, v3 p2, v3 p3)
+{
+    v3 fc, fn1;
+    float A;
+    if (!tri_props(p1, p2, p3, fc, fn1, A)) return;
+    const v3 r = sub(fc, B.p);
+    const v3 vc = sub(fluid_velocity(o, fc), add(B.v, cross(B.omega, r)));
+    const float s = dot(vc, fn1);
+    const v3 vn = mk(s * fn1.x, s * fn1.y, s * fn1.z);
+    if (dot(fn1, vn) < -1e-12f) {
+        const v3 q = mul(mul(vn, 3.f), A);
+        acc_add3(a, Q_FDQ, q);
+        acc_add3(a, Q_TDQ, cross(r, q));
+    }
 }
 
 // The part of a surface-loop face after its polygon is known (:1650-1686).

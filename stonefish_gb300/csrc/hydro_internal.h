@@ -20,6 +20,8 @@ struct KParams {
     unsigned* work;          // chunk counter of the persistent kernel
     unsigned* active_end;    // 1 + last chunk with a face loop (atomicMax in prep, reset by finalize)
     const uint32_t* n_active;  // optional (device): only bodies [0, *n_active) are evaluated
+    hydro_aero_wrench* aero_io;            // OP_AERO / OP_AERO_BODY outputs
+    const hydro_aero_params* aero_params;  // OP_AERO_BODY correction inputs
     uint8_t* chunk_active;   // per chunk: 1 when its body runs a face loop
     uint32_t n_bodies;
     uint32_t n_chunks;
@@ -113,5 +115,7 @@ size_t mlp_tc_image_bytes();
 cudaError_t launch_mlp_tc(const float* feats, uint32_t n, const float* fmean, const float* fistd,
                           const void* wimg, const float* b0, const float* b1, const float* b2, const float* b3,
                           float* out, unsigned* err, cudaStream_t s);
+
+cudaError_t launch_aero_correct(const hydro_aero_params* p, double* io6, cudaStream_t s);
 
 }  // namespace sfh

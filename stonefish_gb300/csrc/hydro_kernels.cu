@@ -156,6 +156,17 @@ __device__ void body_prologue(const hydro_body* b, uint32_t batch_mesh, int op, 
                 buoy = buoy && (b->buoyancy != 0);
             }
         }
+    } else if (op == OP_AERO_BODY) {
+        // SolidEntity::ComputeAerodynamicForces(Atmosphere*) (:1852-1863)
+        if (!mismatch && b->mode == HYDRO_MODE_AERODYNAMIC) {
+            loop = LOOP_AERO;
+            pos = HYDRO_OUTSIDE;   // any value but SKIPPED: outputs are written
+        }
+    } else if (op == OP_AERO) {
+        if (!mismatch) {
+            loop = LOOP_AERO;
+            pos = HYDRO_OUTSIDE;
+        }
     } else if (!mismatch) {
         loop = (op == OP_SURFACE) ? LOOP_SURFACE : LOOP_SUBMERGED;
         pos = (op == OP_SURFACE) ? HYDRO_CROSSING_SURFACE : HYDRO_INSIDE;
@@ -178,10 +189,75 @@ __device__ void body_prologue(const hydro_body* b, uint32_t batch_mesh, int op, 
     B.pad[0] = B.pad[1] = B.pad[2] = 0;
 }
 
+// CorrectAerodynamicForces (SolidEntity.cpp:1925-1956): both vectors scaled
+// by |Cd . n|, n the force's direction in the proxy frame, Cd per
+// approximation type.
+__device__ void aero_correct(const hydro_aero_params& ap, double* Fda, double* Tda)
+{
+    double inv[9];
+    binverse(ap.R_CG2H, inv);
+    double n[3] = {inv[0] * Fda[0] + inv[1] * Fda[1] + inv[2] * Fda[2],
+                   inv[3] * Fda[0] + inv[4] * Fda[1] + inv[5] * Fda[2],
+                   inv[6] * Fda[0] + inv[7] * Fda[1] + inv[8] * Fda[2]};
+    // btVector3::safeNormalize; btVector3::operator/= multiplies by 1 / s
+    const double l2 = n[0] * n[0] + n[1] * n[1] + n[2] * n[2];
+    const double eps = 2.220446049250313080847e-16;   // DBL_EPSILON
+    if (l2 >= eps * eps) {
+        const double s = 1.0 / sqrt(l2);
+        n[0] *= s;
+        n[1] *= s;
+        n[2] *= s;
+    } else {
+        n[0] = 1.0;
+        n[1] = 0.0;
+        n[2] = 0.0;
+    }
+    double cor = 1.0;
+    if (ap.approx_type == HYDRO_APPROX_CYLINDER) {
+        cor = 0.5 * n[0] + 0.5 * n[1] + 1.0 * n[2];
+    } else if (ap.approx_type == HYDRO_APPROX_ELLIPSOID) {
+        double cd[3] = {1.0 / ap.approx_params[0], 1.0 / ap.approx_params[1], 1.0 / ap.approx_params[2]};
+        const double mx = fmax(fmax(cd[0], cd[1]), cd[2]);   // btMax
+        const double s = 1.0 / mx;
+        cd[0] *= s;
+        cd[1] *= s;
+        cd[2] *= s;
+        cor = cd[0] * n[0] + cd[1] * n[1] + cd[2] * n[2];
+    }
+    cor = fabs(cor);
+    for (int k = 0; k < 3; ++k) {
+        Fda[k] *= cor;
+        Tda[k] *= cor;
+    }
+}
+
+// Finalisation of the aerodynamic ops: Fda = 0.5 rho sum, Tda likewise
+// (SolidEntity.cpp:1918-1922), then the correction for OP_AERO_BODY.
+__device__ void aero_finalize(const KParams& P, uint32_t body, const BodyParams& B, const double* S, int status)
+{
+    hydro_aero_wrench w = P.aero_io[body];
+    if (B.mismatch) {
+        w.status = HYDRO_ERR_MISMATCH;
+    } else if (B.position != HYDRO_SKIPPED) {
+        const double k = 0.5 * P.ocean.density;
+        for (int c = 0; c < 3; ++c) {
+            w.Fda[c] = k * S[Q_FDQ + c];
+            w.Tda[c] = k * S[Q_TDQ + c];
+        }
+        if (P.op == OP_AERO_BODY) aero_correct(P.aero_params[body], w.Fda, w.Tda);
+        w.status = status;
+    }
+    P.aero_io[body] = w;
+}
+
 // Finalisation of one body from its FP64 sums S (kQ values).
 __device__ void body_finalize(const KParams& P, uint32_t body, const BodyParams& B,
                               const double* S, int status)
 {
+    if (P.op == OP_AERO || P.op == OP_AERO_BODY) {
+        aero_finalize(P, body, B, S, status);
+        return;
+    }
     const hydro_body* b = P.bodies + body;
     hydro_wrench w = P.io[body];
     const BodyInfo bi = P.binfo[body];
@@ -555,6 +631,21 @@ __device__ __forceinline__ void tile_faces(const KParams& P, const StageBuf& st,
     Bl.loop = B.loop; Bl.buoyancy = B.buoyancy; Bl.damping = B.damping;
     const int nf = m.nf, nvp = (m.nv + 3) & ~3;
     const uint32_t* idx = reinterpret_cast<const uint32_t*>(reinterpret_cast<const float*>(st.raw) + 3 * nvp);
+    if (Bl.loop == LOOP_AERO) {
+        // every face, one per lane, on the scalar path (no clipping)
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const int f = (k * 32 + lane) * kWarps + warp;
+            if (f < nf) {
+                const uint32_t w = idx[f];
+                const float4 q1 = verts[w & 511u];
+                const float4 q2 = verts[(w >> 9) & 511u];
+                const float4 q3 = verts[w >> 18];
+                face_aero(P.ocean, Bl, acc, mk(q1.x, q1.y, q1.z), mk(q2.x, q2.y, q2.z), mk(q3.x, q3.y, q3.z));
+            }
+        }
+        return;
+    }
     // Warp w takes faces (k*32 + lane)*kWarps + w, k = 0, 1: a spread sample
     // of the tile, so that the warps get similar work.  Its faces are
     // compacted (deterministically, by ballot) into a list of fully
@@ -845,6 +936,17 @@ __global__ void correct_kernel(double density, double* io, const double* Cd, con
 {
     if (threadIdx.x == 0 && blockIdx.x == 0)
         correct4(density, io, io + 3, io + 6, io + 9, Cd, Cf, R_O);
+}
+
+__global__ void aero_correct_kernel(const hydro_aero_params* p, double* io6)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) aero_correct(*p, io6, io6 + 3);
+}
+
+cudaError_t launch_aero_correct(const hydro_aero_params* p, double* io6, cudaStream_t s)
+{
+    aero_correct_kernel<<<1, 32, 0, s>>>(p, io6);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_correct(double density, double* io12, const double* Cd, const double* Cf,

@@ -173,6 +173,26 @@ class HydroContext:
                                                ro.ctypes.data_as(P)))
         return io
 
+    def aero_forces(self, mesh, atm, T_CG, T_C, v, omega):
+        """SolidEntity::ComputeAerodynamicForces (static form,
+        SolidEntity.cpp:1865-1923): returns (Fda, Tda)."""
+        F = np.zeros(3)
+        T = np.zeros(3)
+        vv, pv = _d3(v)
+        wv, pw = _d3(omega)
+        self._ck(self.lib.hydro_aero_forces(self.ctx, mesh, C.byref(atm), C.byref(T_CG), C.byref(T_C), pv, pw,
+                                            F.ctypes.data_as(C.POINTER(C.c_double)),
+                                            T.ctypes.data_as(C.POINTER(C.c_double))))
+        return F, T
+
+    def aero_correct(self, params, Fda, Tda):
+        """SolidEntity::CorrectAerodynamicForces (SolidEntity.cpp:1925-1956)."""
+        F = np.array(Fda, dtype=np.float64)
+        T = np.array(Tda, dtype=np.float64)
+        self._ck(self.lib.hydro_aero_correct(self.ctx, C.byref(params), F.ctypes.data_as(C.POINTER(C.c_double)),
+                                             T.ctypes.data_as(C.POINTER(C.c_double))))
+        return F, T
+
     def face_terms(self, body: np.ndarray, ocean, settings, packed: bool = True) -> np.ndarray:
         """Per-face surface-loop terms (n_faces, 23) float32 of one body; packed
         evaluates pairs of submerged faces on the packed FP32 path."""
@@ -259,6 +279,19 @@ class Batch:
         """Device pointers in/out; enqueued on ``stream`` (cudaStream_t as int)."""
         _check(self.lib, self.h.ctx, self.lib.hydro_batch_compute_device(
             self.b, d_bodies, C.byref(ocean), C.byref(settings), d_io, stream or None))
+
+    def compute_aero(self, bodies: np.ndarray, params: np.ndarray, atm, out: np.ndarray) -> np.ndarray:
+        """SolidEntity::ComputeAerodynamicForces(Atmosphere*) for every body
+        (host buffers; bodies not in AERODYNAMIC mode are left untouched)."""
+        assert bodies.dtype == abi.BODY_DTYPE and params.dtype == abi.AERO_PARAMS_DTYPE
+        assert out.dtype == abi.AERO_WRENCH_DTYPE and bodies.size == params.size == out.size == self.n
+        _check(self.lib, self.h.ctx, self.lib.hydro_batch_compute_aero(self.b, bodies.ctypes.data, params.ctypes.data,
+                                                                       C.byref(atm), out.ctypes.data))
+        return out
+
+    def compute_aero_device(self, d_bodies: int, d_params: int, atm, d_out: int, stream: int = 0) -> None:
+        _check(self.lib, self.h.ctx, self.lib.hydro_batch_compute_aero_device(self.b, d_bodies, d_params,
+                                                                              C.byref(atm), d_out, stream or None))
 
     def compute_device_prefix(self, d_bodies: int, d_count: int, ocean, settings, d_io: int,
                               stream: int = 0) -> None:
