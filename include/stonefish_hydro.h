@@ -402,6 +402,49 @@ hydro_status hydro_fluid_position(hydro_ctx* ctx, const hydro_ocean* ocean,
                                   const double aabb_min[3],
                                   const double aabb_max[3], int32_t* position);
 
+/* ------------------------------------------------------------- compounds */
+/* One part of a Compound (Library/src/entities/solids/Compound.cpp:291-436).
+ * The compound itself is described by a hydro_body (T_CG, v, omega, the
+ * compound's AABB, volume, surface, P_CB, mode and buoyancy; its mesh, T_C,
+ * R_O, Cd and Cf are not used). */
+typedef struct hydro_compound_part {
+    hydro_transform T_C;         /* getOTransform() * parts[i].origin * solid->getO2CTransform() */
+    double R_O[9];               /* basis of getOTransform() * parts[i].origin (correction frame) */
+    double Cd[3];                /* solid->getHydrodynamicCoefficients() */
+    double Cf[3];
+    hydro_mesh_id mesh;          /* solid->getPhysicsMesh(); HYDRO_NO_MESH = nullptr */
+    int32_t mode;                /* solid->getPhysicsMode() */
+    int32_t buoyant;             /* solid->isBuoyant() */
+    int32_t external;            /* parts[i].isExternal */
+} hydro_compound_part;
+
+typedef struct hydro_compound_batch hydro_compound_batch;
+
+/* A set of compounds with a fixed list of parts: compound c owns the
+ * parts_per_compound[c] consecutive entries of part_mesh (and of the part
+ * array given at compute time), in the reference's part order. */
+hydro_status hydro_compound_batch_create(hydro_ctx* ctx, const hydro_mesh_id* part_mesh,
+                                         const uint32_t* parts_per_compound, uint32_t n_compounds,
+                                         hydro_compound_batch** out);
+void hydro_compound_batch_destroy(hydro_compound_batch* batch);
+
+/* Compound::ComputeHydrodynamicForces (Compound.cpp:291-436) for every
+ * compound: classification by the compound's AABB; INSIDE: buoyancy from the
+ * compound's volume and P_CB, damping summed over the external fluid parts
+ * (each part's submerged loop about the compound's CG, corrected with the
+ * part's Cd/Cf in the part frame); CROSSING: each fluid part's surface loop
+ * (buoyancy only for internal parts), corrected and summed, the per-part
+ * in-out values carried from part to part as the reference's loop does.
+ * Device pointers (d_io: one hydro_wrench per compound, in-out). */
+hydro_status hydro_compound_compute_device(hydro_compound_batch* batch, const hydro_body* d_compounds,
+                                           const hydro_compound_part* d_parts, const hydro_ocean* ocean,
+                                           const hydro_settings* settings, hydro_wrench* d_io, void* stream);
+
+/* Host-buffer version (synchronises). */
+hydro_status hydro_compound_compute(hydro_compound_batch* batch, const hydro_body* compounds,
+                                    const hydro_compound_part* parts, const hydro_ocean* ocean,
+                                    const hydro_settings* settings, hydro_wrench* io);
+
 /* ---------------------------------------------------------- aerodynamics */
 /* SolidEntity::ComputeAerodynamicForces(mesh, atm, T_CG, T_C, v, omega,
  * Fda, Tda) (SolidEntity.cpp:1865-1923): quadratic-law drag of the faces

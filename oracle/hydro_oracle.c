@@ -365,6 +365,92 @@ void oracle_correct_forces(const hydro_ocean* ocean, double Fdq[3], double Tdq[3
     correct_one(inv, Tdf, Cf, ocean->density);
 }
 
+/* ------------------------------------------------------------- compounds */
+static int fluid_mode(int m) { return m == HYDRO_MODE_FLOATING || m == HYDRO_MODE_SUBMERGED; }
+
+/* Compound::ComputeHydrodynamicForces (Library/src/entities/solids/Compound.cpp:291-436). */
+void oracle_compound_forces(int variant, const hydro_body* cb, const hydro_compound_part* parts,
+                            uint32_t n_parts, const oracle_mesh* const* part_meshes,
+                            const hydro_ocean* ocean, const oracle_waves* waves,
+                            const hydro_settings* settings, hydro_wrench* io)
+{
+    if (!fluid_mode(cb->mode)) {                                   /* :293 */
+        io->position = HYDRO_SKIPPED;
+        return;
+    }
+    int bf = oracle_fluid_position(ocean, waves, cb->aabb_min, cb->aabb_max);   /* :299 */
+    io->position = bf;
+    if (bf == HYDRO_OUTSIDE) {                                     /* :302-314 */
+        zero3(io->Fb); zero3(io->Tb); zero3(io->Fdq); zero3(io->Tdq);
+        zero3(io->Fdf); zero3(io->Tdf);
+        io->Swet = 0.0;
+        io->Vsub = 0.0;
+        return;
+    }
+    if (bf == HYDRO_INSIDE) {                                      /* :316-357 */
+        if (cb->buoyancy) {
+            double k = -cb->volume * ocean->density;
+            double f[3] = {0.0 * k, 0.0 * k, ocean->gravity * k};
+            const double* R = cb->T_CG.basis;
+            const double* o = cb->T_CG.origin;
+            double c[3] = {(R[0] * cb->P_CB[0] + R[1] * cb->P_CB[1] + R[2] * cb->P_CB[2]) + o[0],
+                           (R[3] * cb->P_CB[0] + R[4] * cb->P_CB[1] + R[5] * cb->P_CB[2]) + o[1],
+                           (R[6] * cb->P_CB[0] + R[7] * cb->P_CB[1] + R[8] * cb->P_CB[2]) + o[2]};
+            double r[3] = {c[0] - o[0], c[1] - o[1], c[2] - o[2]};
+            set3(io->Fb, f[0], f[1], f[2]);
+            bcross(r, f, io->Tb);
+        }
+        if (settings->damping_forces) {
+            zero3(io->Fdq); zero3(io->Tdq); zero3(io->Fdf); zero3(io->Tdf);
+            double Fq[3] = {0, 0, 0}, Tq[3] = {0, 0, 0}, Ff[3] = {0, 0, 0}, Tf[3] = {0, 0, 0};
+            for (uint32_t i = 0; i < n_parts; ++i) {
+                const hydro_compound_part* pt = &parts[i];
+                if (!(pt->external && fluid_mode(pt->mode))) continue;
+                oracle_submerged_forces(variant, part_meshes[i], ocean, &cb->T_CG, &pt->T_C, cb->v, cb->omega,
+                                        Fq, Tq, Ff, Tf);
+                oracle_correct_forces(ocean, Fq, Tq, Ff, Tf, pt->Cd, pt->Cf, pt->R_O);
+                for (int k = 0; k < 3; ++k) {
+                    io->Fdq[k] += Fq[k]; io->Tdq[k] += Tq[k]; io->Fdf[k] += Ff[k]; io->Tdf[k] += Tf[k];
+                }
+            }
+        }
+        io->Swet = cb->surface;
+        io->Vsub = cb->volume;
+        return;
+    }
+    if (!(settings->realistic_buoyancy || settings->damping_forces)) return;   /* :361 */
+    if (settings->realistic_buoyancy) { zero3(io->Fb); zero3(io->Tb); }
+    if (settings->damping_forces) { zero3(io->Fdq); zero3(io->Tdq); zero3(io->Fdf); zero3(io->Tdf); }
+    io->Swet = 0.0;
+    io->Vsub = 0.0;
+    /* the per-part in-out values live across the loop (:379-386) */
+    double Fbp[3] = {0, 0, 0}, Tbp[3] = {0, 0, 0}, Fqp[3] = {0, 0, 0}, Tqp[3] = {0, 0, 0};
+    double Ffp[3] = {0, 0, 0}, Tfp[3] = {0, 0, 0}, Swetp = 0.0, Vsubp = 0.0;
+    for (uint32_t i = 0; i < n_parts; ++i) {
+        const hydro_compound_part* pt = &parts[i];
+        if (!fluid_mode(pt->mode)) continue;
+        hydro_settings ps = *settings;
+        ps.realistic_buoyancy = ps.realistic_buoyancy && pt->buoyant;
+        if (pt->external) {
+            oracle_surface_forces(variant, &ps, part_meshes[i], ocean, waves, &cb->T_CG, &pt->T_C, cb->v,
+                                  cb->omega, Fbp, Tbp, Fqp, Tqp, Ffp, Tfp, &Swetp, &Vsubp);
+            oracle_correct_forces(ocean, Fqp, Tqp, Ffp, Tfp, pt->Cd, pt->Cf, pt->R_O);
+            for (int k = 0; k < 3; ++k) {
+                io->Fb[k] += Fbp[k]; io->Tb[k] += Tbp[k]; io->Fdq[k] += Fqp[k]; io->Tdq[k] += Tqp[k];
+                io->Fdf[k] += Ffp[k]; io->Tdf[k] += Tfp[k];
+            }
+            io->Swet += Swetp;
+            io->Vsub += Vsubp;
+        } else if (ps.realistic_buoyancy) {
+            ps.damping_forces = 0;
+            oracle_surface_forces(variant, &ps, part_meshes[i], ocean, waves, &cb->T_CG, &pt->T_C, cb->v,
+                                  cb->omega, Fbp, Tbp, Fqp, Tqp, Ffp, Tfp, &Swetp, &Vsubp);
+            for (int k = 0; k < 3; ++k) { io->Fb[k] += Fbp[k]; io->Tb[k] += Tbp[k]; }
+            io->Vsub += Vsubp;
+        }
+    }
+}
+
 /* ----------------------------------------------------------- aerodynamics */
 /* Atmosphere::GetFluidVelocity sums every wind field (Atmosphere.cpp:146-152):
  * the winds as enabled currents of an ocean descriptor. */

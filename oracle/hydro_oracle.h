@@ -117,6 +117,13 @@ double oracle_batch(int variant, int threads, const hydro_body* bodies,
 
 int oracle_hardware_threads(void);
 
+/* Compound::ComputeHydrodynamicForces (Library/src/entities/solids/Compound.cpp:291-436):
+ * part_meshes[i] is part i's mesh (NULL = nullptr). */
+void oracle_compound_forces(int variant, const hydro_body* compound, const hydro_compound_part* parts,
+                            uint32_t n_parts, const oracle_mesh* const* part_meshes,
+                            const hydro_ocean* ocean, const oracle_waves* waves,
+                            const hydro_settings* settings, hydro_wrench* io);
+
 /* SolidEntity::ComputeAerodynamicForces (static form, SolidEntity.cpp:1865-1923)
  * and CorrectAerodynamicForces (:1925-1956). */
 void oracle_aero_forces(int variant, const oracle_mesh* mesh, const hydro_atmosphere* atm,

@@ -79,6 +79,8 @@ class Oracle:
                                    P(abi.Settings), vp]
         L.oracle_hardware_threads.restype = i32
         L.oracle_hardware_threads.argtypes = []
+        L.oracle_compound_forces.restype = None
+        L.oracle_compound_forces.argtypes = [i32, vp, vp, u32, vp, P(abi.Ocean), vp, P(abi.Settings), vp]
         L.oracle_aero_forces.restype = None
         L.oracle_aero_forces.argtypes = [i32, vp, P(abi.Atmosphere), P(abi.Transform), P(abi.Transform),
                                          d, d, d, d]
@@ -189,6 +191,19 @@ class Oracle:
         ro, pro = self._vec(R_O)
         ptrs = [io[k].ctypes.data_as(C.POINTER(C.c_double)) for k in ("Fdq", "Tdq", "Fdf", "Tdf")]
         self.lib.oracle_correct_forces(C.byref(ocean), *ptrs, pcd, pcf, pro)
+        return io
+
+    def compound_forces(self, variant, compound, parts, part_meshes, ocean, settings, io, waves=None):
+        """Compound::ComputeHydrodynamicForces: compound = hydro_body[1],
+        parts = hydro_compound_part[n], part_meshes = [(xyz, faces) or None];
+        io = hydro_wrench[1], in place."""
+        ms = [None if m is None else self.make_mesh(*m) for m in part_meshes]
+        ptrs = (C.c_void_p * max(1, len(ms)))(*[self._p(m) for m in ms])
+        w = self.make_waves(waves)
+        parts = np.ascontiguousarray(parts)
+        self.lib.oracle_compound_forces(variant, compound.ctypes.data, parts.ctypes.data if len(parts) else None,
+                                        len(parts), C.cast(ptrs, C.c_void_p), C.byref(ocean), self._p(w),
+                                        C.byref(settings), io.ctypes.data)
         return io
 
     def aero_forces(self, variant, mesh, atm, T_CG, T_C, v, omega):

@@ -66,6 +66,11 @@ class Ocean(C.Structure):
                 ("currents", Current * MAX_CURRENTS)]
 
 
+class CompoundPart(C.Structure):
+    _fields_ = [("T_C", Transform), ("R_O", C.c_double * 9), ("Cd", _d3), ("Cf", _d3),
+                ("mesh", C.c_uint32), ("mode", C.c_int32), ("buoyant", C.c_int32), ("external", C.c_int32)]
+
+
 class Atmosphere(C.Structure):
     _fields_ = [("density", C.c_double), ("n_winds", C.c_uint32), ("reserved", C.c_uint32),
                 ("winds", Current * MAX_CURRENTS)]
@@ -138,6 +143,7 @@ OCEAN_DTYPE = _dtype_of(Ocean)
 CURRENT_DTYPE = _dtype_of(Current)
 RIGID_DTYPE = _dtype_of(RigidState)
 AERO_PARAMS_DTYPE = _dtype_of(AeroParams)
+COMPOUND_PART_DTYPE = _dtype_of(CompoundPart)
 AERO_WRENCH_DTYPE = _dtype_of(AeroWrench)
 APPROX_AUTO, APPROX_SPHERE, APPROX_CYLINDER, APPROX_ELLIPSOID = range(4)
 
@@ -223,6 +229,10 @@ def _declare(lib: C.CDLL) -> None:
         "hydro_nn_wrench_body": (i32, [vp, vp, vp, u32, vp, vp]),
         "hydro_nn_pack_sw128": (i32, [vp, vp, i32, i32, i32, i32, vp, vp]),
         "hydro_nn_mlp_tc": (i32, [vp, vp, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
+        "hydro_compound_batch_create": (i32, [vp, vp, vp, u32, C.POINTER(vp)]),
+        "hydro_compound_batch_destroy": (None, [vp]),
+        "hydro_compound_compute_device": (i32, [vp, vp, vp, C.POINTER(Ocean), C.POINTER(Settings), vp, vp]),
+        "hydro_compound_compute": (i32, [vp, vp, vp, C.POINTER(Ocean), C.POINTER(Settings), vp]),
         "hydro_aero_forces": (i32, [vp, u32, C.POINTER(Atmosphere), C.POINTER(Transform), C.POINTER(Transform),
                                     d, d, d, d]),
         "hydro_aero_correct": (i32, [vp, C.POINTER(AeroParams), d, d]),

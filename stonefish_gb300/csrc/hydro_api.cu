@@ -84,6 +84,19 @@ struct hydro_batch {
     hydro_aero_wrench* aio_d = nullptr;
 };
 
+struct hydro_compound_batch {
+    hydro_ctx* ctx = nullptr;
+    hydro_batch* parts = nullptr;          // work list over the parts' meshes
+    uint32_t n_compounds = 0;
+    uint32_t n_parts = 0;
+    CompoundInfo* cinfo_d = nullptr;
+    uint32_t* part_compound_d = nullptr;
+    hydro_body* compounds_d = nullptr;     // staging for the host-buffer call
+    hydro_compound_part* parts_d = nullptr;
+    hydro_wrench* io_d = nullptr;
+    uint32_t last_launches = 0;
+};
+
 namespace {
 
 hydro_status fail(hydro_ctx* ctx, hydro_status s, const char* fmt, ...)
@@ -842,6 +855,169 @@ hydro_status hydro_correct_forces(hydro_ctx* ctx, const hydro_ocean* ocean, doub
     CK(ctx, cudaMemcpyAsync(h, d, 12 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     CK(ctx, cudaStreamSynchronize(ctx->stream));
     copy3(Fdq, h); copy3(Tdq, h + 3); copy3(Fdf, h + 6); copy3(Tdf, h + 9);
+    return HYDRO_OK;
+}
+
+// -------------------------------------------------------------- compounds
+void compound_free(hydro_compound_batch* cb)
+{
+    if (!cb) return;
+    if (cb->parts) batch_free(cb->parts);
+    cudaFree(cb->cinfo_d);
+    cudaFree(cb->part_compound_d);
+    cudaFree(cb->compounds_d);
+    cudaFree(cb->parts_d);
+    cudaFree(cb->io_d);
+    delete cb;
+}
+
+hydro_status hydro_compound_batch_create(hydro_ctx* ctx, const hydro_mesh_id* part_mesh,
+                                         const uint32_t* parts_per_compound, uint32_t n_compounds,
+                                         hydro_compound_batch** out)
+{
+    if (!ctx) return HYDRO_ERR_INVALID_ARG;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (!out || !parts_per_compound || n_compounds == 0)
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "compound batch: null pointer or no compounds");
+    *out = nullptr;
+    uint64_t total = 0;
+    for (uint32_t c = 0; c < n_compounds; ++c) total += parts_per_compound[c];
+    if (total > 0xFFFFFFFull || (total && !part_mesh))
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "compound batch: bad part list");
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, HYDRO_ERR_DEVICE, "cudaSetDevice");
+    hydro_compound_batch* cb = new (std::nothrow) hydro_compound_batch();
+    if (!cb) return fail(ctx, HYDRO_ERR_OOM, "host allocation");
+    cb->ctx = ctx;
+    cb->n_compounds = n_compounds;
+    cb->n_parts = (uint32_t)total;
+    std::vector<CompoundInfo> info(n_compounds);
+    std::vector<uint32_t> owner((size_t)total);
+    uint32_t first = 0;
+    for (uint32_t c = 0; c < n_compounds; ++c) {
+        info[c] = CompoundInfo{first, parts_per_compound[c]};
+        for (uint32_t k = 0; k < parts_per_compound[c]; ++k) owner[first + k] = c;
+        first += parts_per_compound[c];
+    }
+    hydro_status st = HYDRO_OK;
+    if (total) st = batch_build(ctx, part_mesh, (uint32_t)total, &cb->parts);
+    if (st != HYDRO_OK) {
+        compound_free(cb);
+        return st;
+    }
+    cudaError_t e = cudaMalloc(&cb->cinfo_d, n_compounds * sizeof(CompoundInfo));
+    if (e == cudaSuccess) e = cudaMalloc(&cb->part_compound_d, std::max<size_t>(1, total) * sizeof(uint32_t));
+    if (e == cudaSuccess)
+        e = cudaMemcpy(cb->cinfo_d, info.data(), n_compounds * sizeof(CompoundInfo), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && total)
+        e = cudaMemcpy(cb->part_compound_d, owner.data(), total * sizeof(uint32_t), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        compound_free(cb);
+        return cuda_fail(ctx, e, "compound batch allocation");
+    }
+    *out = cb;
+    return HYDRO_OK;
+}
+
+void hydro_compound_batch_destroy(hydro_compound_batch* cb)
+{
+    if (!cb) return;
+    hydro_ctx* ctx = cb->ctx;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    compound_free(cb);
+}
+
+hydro_status compound_launch(hydro_compound_batch* cb, const hydro_body* d_compounds,
+                             const hydro_compound_part* d_parts, const hydro_ocean* ocean,
+                             const hydro_settings* settings, hydro_wrench* d_io, cudaStream_t s)
+{
+    hydro_ctx* ctx = cb->ctx;
+    hydro_status st = sync_tiles(ctx);
+    if (st != HYDRO_OK) return st;
+    if (ocean->waves && !ctx->wave_d)
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "ocean.waves set but no wave grid was given");
+    KParams P{};
+    hydro_batch* b = cb->parts;
+    unsigned* err = nullptr;
+    if (b) {
+        P.chunks = b->chunks_d;
+        P.binfo = b->binfo_d;
+        P.partials = b->partials_d;
+        P.bparams = b->bparams_d;
+        P.chunk_active = b->chunk_active_d;
+        P.n_bodies = b->n_bodies;
+        P.n_chunks = b->n_chunks;
+        err = b->err_d;
+    } else {
+        // no parts at all: a scratch error word from the context
+        if ((st = ensure_small(ctx, 256)) != HYDRO_OK) return st;
+        err = static_cast<unsigned*>(ctx->small_d);
+        CK(ctx, cudaMemsetAsync(err, 0, 256, s));
+    }
+    P.tiles = ctx->tiles_d;
+    P.err = err;
+    P.work = err + 32;
+    P.active_end = err + 48;
+    P.ocean = make_ocean(ctx, ocean);
+    P.st.damping = settings->damping_forces ? 1 : 0;
+    P.st.buoyancy = settings->realistic_buoyancy ? 1 : 0;
+    P.op = OP_SURFACE;
+    CompoundParams C{};
+    C.compounds = d_compounds;
+    C.parts = d_parts;
+    C.cinfo = cb->cinfo_d;
+    C.part_compound = cb->part_compound_d;
+    C.io = d_io;
+    C.n_compounds = cb->n_compounds;
+    const int cut64 = ctx->cfg.cut_precision == HYDRO_CUT_FP64;
+    LaunchShape shape{};
+    const int want = (b && b->ctas_per_sm) ? (int)b->ctas_per_sm : ctx->cfg.ctas_per_sm ? (int)ctx->cfg.ctas_per_sm : 2;
+    shape.ctas_per_sm = std::max(1, std::min(want, chunk_kernel_occupancy(cut64, P.ocean.waves, want)));
+    shape.grid = ctx->sm_count * shape.ctas_per_sm;
+    uint32_t launches = 0;
+    cudaError_t e = launch_compound_step(P, C, shape, cut64, s, &launches);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "compound step launch");
+    cb->last_launches = launches;
+    return HYDRO_OK;
+}
+
+hydro_status hydro_compound_compute_device(hydro_compound_batch* cb, const hydro_body* d_compounds,
+                                           const hydro_compound_part* d_parts, const hydro_ocean* ocean,
+                                           const hydro_settings* settings, hydro_wrench* d_io, void* stream)
+{
+    if (!cb) return HYDRO_ERR_INVALID_ARG;
+    hydro_ctx* ctx = cb->ctx;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (!d_compounds || (!d_parts && cb->n_parts) || !d_io || !settings || !valid_ocean(ocean))
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "compound compute: bad arguments");
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, HYDRO_ERR_DEVICE, "cudaSetDevice");
+    return compound_launch(cb, d_compounds, d_parts, ocean, settings, d_io, static_cast<cudaStream_t>(stream));
+}
+
+hydro_status hydro_compound_compute(hydro_compound_batch* cb, const hydro_body* compounds,
+                                    const hydro_compound_part* parts, const hydro_ocean* ocean,
+                                    const hydro_settings* settings, hydro_wrench* io)
+{
+    if (!cb) return HYDRO_ERR_INVALID_ARG;
+    hydro_ctx* ctx = cb->ctx;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (!compounds || (!parts && cb->n_parts) || !io || !settings || !valid_ocean(ocean))
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "compound compute: bad arguments");
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, HYDRO_ERR_DEVICE, "cudaSetDevice");
+    const size_t nc = cb->n_compounds, np = std::max<uint32_t>(cb->n_parts, 1u);
+    if (!cb->compounds_d) CK(ctx, cudaMalloc(&cb->compounds_d, nc * sizeof(hydro_body)));
+    if (!cb->parts_d) CK(ctx, cudaMalloc(&cb->parts_d, np * sizeof(hydro_compound_part)));
+    if (!cb->io_d) CK(ctx, cudaMalloc(&cb->io_d, nc * sizeof(hydro_wrench)));
+    cudaStream_t s = ctx->stream;
+    CK(ctx, cudaMemcpyAsync(cb->compounds_d, compounds, nc * sizeof(hydro_body), cudaMemcpyHostToDevice, s));
+    if (cb->n_parts)
+        CK(ctx, cudaMemcpyAsync(cb->parts_d, parts, cb->n_parts * sizeof(hydro_compound_part),
+                                cudaMemcpyHostToDevice, s));
+    CK(ctx, cudaMemcpyAsync(cb->io_d, io, nc * sizeof(hydro_wrench), cudaMemcpyHostToDevice, s));
+    hydro_status st = compound_launch(cb, cb->compounds_d, cb->parts_d, ocean, settings, cb->io_d, s);
+    if (st != HYDRO_OK) return st;
+    CK(ctx, cudaMemcpyAsync(io, cb->io_d, nc * sizeof(hydro_wrench), cudaMemcpyDeviceToHost, s));
+    CK(ctx, cudaStreamSynchronize(s));
     return HYDRO_OK;
 }
 

@@ -30,6 +30,21 @@ struct KParams {
     int op;                  // OP_BODY / OP_SURFACE / OP_SUBMERGED
 };
 
+// Compounds: the KParams bodies are the parts; these describe the grouping.
+struct CompoundInfo {
+    uint32_t first_part;
+    uint32_t n_parts;
+};
+
+struct CompoundParams {
+    const hydro_body* compounds;         // n_compounds
+    const hydro_compound_part* parts;    // one per KParams body
+    const CompoundInfo* cinfo;           // n_compounds
+    const uint32_t* part_compound;       // part -> compound
+    hydro_wrench* io;                    // per compound, in-out
+    uint32_t n_compounds;
+};
+
 // Launch shape of the persistent chunk kernel.
 struct LaunchShape {
     int grid;                // CTAs (a multiple of the SM count when work allows)
@@ -116,6 +131,8 @@ cudaError_t launch_mlp_tc(const float* feats, uint32_t n, const float* fmean, co
                           const void* wimg, const float* b0, const float* b1, const float* b2, const float* b3,
                           float* out, unsigned* err, cudaStream_t s);
 
+cudaError_t launch_compound_step(const KParams& P, const CompoundParams& C, LaunchShape shape, int cut64,
+                                 cudaStream_t s, uint32_t* launches);
 cudaError_t launch_aero_correct(const hydro_aero_params* p, double* io6, cudaStream_t s);
 
 }  // namespace sfh

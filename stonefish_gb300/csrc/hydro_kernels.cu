@@ -6,17 +6,18 @@
 //   prep      one thread per body: fluid position (CheckBodyFluidPosition,
 //             SolidEntity.cpp:1239-1261), loop kind and the body's FP32
 //             parameters (the glm casts of ComputeHydrodynamicForcesSurface);
-//   chunk     persistent CTAs.  One producer lane streams the CTA's tiles
-//             (runs of <= 512 faces with their <= 512 distinct vertices,
-//             contiguous in HBM) into a 4-stage shared-memory ring with 1-D
-//             TMA bulk copies signalled on mbarriers; 8 consumer warps
-//             transform each vertex once (with its depth, Ocean::GetDepth)
-//             and evaluate the faces (surface loop :1337-1687 or submerged
-//             loop :1748-1789) from shared memory.  Per-face quantities are
-//             summed in FP32 over at most kFlushFaces faces per thread, then
-//             by a butterfly reduce-scatter across the warp into a two-sum
-//             (float-float) accumulator per lane, combined across warps and
-//             stored as one FP64 partial per chunk;
+//   chunk     persistent CTAs.  One producer lane claims chunks (runs of up
+//             to 16 tiles of <= 384 faces with their <= 384 distinct
+//             vertices, contiguous in HBM) and streams their tiles into an
+//             8-stage shared-memory ring with 1-D TMA bulk copies signalled
+//             on mbarriers; 6 consumer warps transform each vertex once
+//             (with its depth, Ocean::GetDepth) and evaluate the faces
+//             (surface loop :1337-1687, submerged loop :1748-1789, or the
+//             aerodynamic loop :1885-1915) from shared memory.  Per-face
+//             quantities are summed in FP32 over at most kFlushFaces faces
+//             per thread, then by a butterfly reduce-scatter across the warp
+//             into a two-sum (float-float) accumulator per lane, combined
+//             across warps and stored as one FP64 partial per chunk;
 //   finalise  one warp per body: the body's chunk partials are added in
 //             chunk order in FP64 and the FP64 finalisation is applied:
 //             buoyancy (:1689-1720, :1828-1836), the stale-output rules and
@@ -855,6 +856,214 @@ cudaError_t launch_step(const KParams& P, LaunchShape shape, int cut64, cudaStre
     finalize_kernel<<<(P.n_bodies + kWarps - 1) / kWarps, kBlock, 0, s>>>(P);
     if ((e = cudaGetLastError())) return e;
     *launches = 3;
+    return cudaSuccess;
+}
+
+// ------------------------------------------------------------- compounds
+// Compound::ComputeHydrodynamicForces (Compound.cpp:291-436).  The parts are
+// the bodies of the chunk kernel: each part's faces are integrated about the
+// compound's CG with the compound's velocities, in the part's mesh frame.
+
+__device__ __forceinline__ bool fluid_mode(int m) { return m == HYDRO_MODE_FLOATING || m == HYDRO_MODE_SUBMERGED; }
+
+// Loop kind and flags of one part for the compound's fluid position.
+__device__ void compound_part_loop(int pos, const hydro_compound_part& pt, SettingsDev st, int& loop, int& buoy,
+                                   int& damp)
+{
+    loop = LOOP_NONE;
+    buoy = 0;
+    damp = 0;
+    if (!fluid_mode(pt.mode)) return;
+    if (pos == HYDRO_INSIDE) {                                   // :331-353
+        if (st.damping && pt.external) {
+            loop = LOOP_SUBMERGED;
+            damp = 1;
+        }
+    } else if (pos == HYDRO_CROSSING_SURFACE && (st.buoyancy || st.damping)) {   // :359-434
+        const int pb = st.buoyancy && pt.buoyant;
+        if (pt.external) {
+            loop = LOOP_SURFACE;
+            buoy = pb;
+            damp = st.damping;
+        } else if (pb) {
+            loop = LOOP_SURFACE;
+            buoy = 1;
+        }
+    }
+}
+
+__global__ void compound_prep_kernel(const KParams P, const CompoundParams C)
+{
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p == 0) {
+        *P.err = 0u;
+        *P.work = 0u;
+    }
+    if (p >= P.n_bodies) return;
+    const hydro_compound_part& pt = C.parts[p];
+    const hydro_body& cb = C.compounds[C.part_compound[p]];
+    int pos = HYDRO_SKIPPED;
+    if (fluid_mode(cb.mode)) pos = classify(P.ocean, cb.aabb_min, cb.aabb_max);   // :293, :299
+    int loop, buoy, damp;
+    compound_part_loop(pos, pt, P.st, loop, buoy, damp);
+    const BodyInfo bi = P.binfo[p];
+    BodyParams B;
+    for (int r = 0; r < 3; ++r) {
+        for (int c = 0; c < 3; ++c) B.TC[4 * r + c] = (float)pt.T_C.basis[3 * r + c];
+        B.TC[4 * r + 3] = (float)pt.T_C.origin[r];
+    }
+    B.p = mk((float)cb.T_CG.origin[0], (float)cb.T_CG.origin[1], (float)cb.T_CG.origin[2]);
+    B.p0 = mk(B.p.x, B.p.y, 0.f);
+    B.v = mk((float)cb.v[0], (float)cb.v[1], (float)cb.v[2]);
+    B.omega = mk((float)cb.omega[0], (float)cb.omega[1], (float)cb.omega[2]);
+    B.mismatch = (pt.mesh != bi.mesh);
+    B.loop = (B.mismatch || bi.mesh == HYDRO_NO_MESH) ? LOOP_NONE : loop;
+    B.buoyancy = buoy;
+    B.damping = damp;
+    B.position = pos;
+    B.pad[0] = B.pad[1] = B.pad[2] = 0;
+    P.bparams[p] = B;
+    const uint8_t active = (B.loop != LOOP_NONE) ? 1 : 0;
+    for (uint32_t c = 0; c < bi.n_chunks; ++c) P.chunk_active[bi.first_chunk + c] = active;
+    if (active && bi.n_chunks) atomicMax(P.active_end, bi.first_chunk + bi.n_chunks);
+}
+
+__device__ __forceinline__ void add3(double* a, const double* b)
+{
+    a[0] += b[0];
+    a[1] += b[1];
+    a[2] += b[2];
+}
+
+// One warp per compound: lanes sum each part's chunk partials (FP64, chunk
+// order), lane 0 applies the compound's rules part by part.
+__global__ void compound_finalize_kernel(const KParams P, const CompoundParams C)
+{
+    __shared__ double sums[kWarps][32];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const uint32_t c = blockIdx.x * kWarps + warp;
+    if (c == 0 && lane == 0) *P.active_end = 0u;
+    if (c >= C.n_compounds) return;
+    const hydro_body& cb = C.compounds[c];
+    const CompoundInfo ci = C.cinfo[c];
+    const int status = (*P.err & 1u) ? HYDRO_ERR_TIMEOUT : 0;
+    int pos = HYDRO_SKIPPED;
+    if (fluid_mode(cb.mode)) pos = classify(P.ocean, cb.aabb_min, cb.aabb_max);
+    hydro_wrench w = C.io[c];
+    hydro_wrench cw{};            // the per-part in-out values of the reference's loop (:379-386)
+    int mismatch = 0;
+    if (pos == HYDRO_INSIDE) {                                   // :316-356
+        if (cb.buoyancy) {
+            const double k = -cb.volume * P.ocean.density;
+            double f[3] = {0.0 * k, 0.0 * k, P.ocean.gravity * k};
+            const double* R = cb.T_CG.basis;
+            const double* og = cb.T_CG.origin;
+            const double* pc = cb.P_CB;
+            double q[3] = {(R[0] * pc[0] + R[1] * pc[1] + R[2] * pc[2]) + og[0],
+                           (R[3] * pc[0] + R[4] * pc[1] + R[5] * pc[2]) + og[1],
+                           (R[6] * pc[0] + R[7] * pc[1] + R[8] * pc[2]) + og[2]};
+            double r[3] = {q[0] - og[0], q[1] - og[1], q[2] - og[2]};
+            copy3(w.Fb, f);
+            bcross(r, f, w.Tb);
+        }
+        if (P.st.damping) {
+            zero3(w.Fdq); zero3(w.Tdq); zero3(w.Fdf); zero3(w.Tdf);
+        }
+    } else if (pos == HYDRO_CROSSING_SURFACE && (P.st.buoyancy || P.st.damping)) {   // :359-381
+        if (P.st.buoyancy) { zero3(w.Fb); zero3(w.Tb); }
+        if (P.st.damping) { zero3(w.Fdq); zero3(w.Tdq); zero3(w.Fdf); zero3(w.Tdf); }
+        w.Swet = 0.0;
+        w.Vsub = 0.0;
+    }
+    for (uint32_t k = 0; k < ci.n_parts; ++k) {
+        const uint32_t p = ci.first_part + k;
+        const BodyParams B = P.bparams[p];
+        const BodyInfo bi = P.binfo[p];
+        double s = 0.0;
+        if (B.loop != LOOP_NONE && lane < kQ) {
+            const double* q = P.partials + (size_t)bi.first_chunk * kPartialStride + lane;
+            for (uint32_t j = 0; j < bi.n_chunks; ++j) s += q[(size_t)j * kPartialStride];
+        }
+        sums[warp][lane] = s;
+        __syncwarp();
+        if (lane == 0) {
+            const hydro_compound_part& pt = C.parts[p];
+            mismatch |= B.mismatch;
+            const double* S = sums[warp];
+            const bool null_mesh = (bi.mesh == HYDRO_NO_MESH);
+            if (pos == HYDRO_INSIDE && P.st.damping && pt.external && fluid_mode(pt.mode)) {
+                // ComputeHydrodynamicForcesSubmerged then the part's correction (:337-352)
+                double Fq[3], Tq[3], Ff[3], Tf[3];
+                copy3(Fq, S + Q_FDQ); copy3(Tq, S + Q_TDQ); copy3(Ff, S + Q_FDF); copy3(Tf, S + Q_TDF);
+                correct4(P.ocean.density, Fq, Tq, Ff, Tf, pt.Cd, pt.Cf, pt.R_O);
+                add3(w.Fdq, Fq); add3(w.Tdq, Tq); add3(w.Fdf, Ff); add3(w.Tdf, Tf);
+            } else if (pos == HYDRO_CROSSING_SURFACE && (P.st.buoyancy || P.st.damping) && fluid_mode(pt.mode)) {
+                const int pb = P.st.buoyancy && pt.buoyant;
+                if (pt.external || pb) {
+                    const int dmp = pt.external ? P.st.damping : 0;
+                    // ComputeHydrodynamicForcesSurface on the carried in-out values
+                    if (null_mesh) {
+                        if (pb) { zero3(cw.Fb); zero3(cw.Tb); }
+                        if (dmp) { zero3(cw.Fdq); zero3(cw.Tdq); zero3(cw.Fdf); zero3(cw.Tdf); }
+                        cw.Swet = 0.0;
+                        cw.Vsub = 0.0;
+                    } else {
+                        finalize_surface(P.ocean, pb, dmp, cb.T_CG.origin, (double)B.p0.x, (double)B.p0.y, S,
+                                         cw);
+                    }
+                    if (pt.external) {                           // :411-422
+                        correct4(P.ocean.density, cw.Fdq, cw.Tdq, cw.Fdf, cw.Tdf, pt.Cd, pt.Cf, pt.R_O);
+                        add3(w.Fb, cw.Fb); add3(w.Tb, cw.Tb);
+                        add3(w.Fdq, cw.Fdq); add3(w.Tdq, cw.Tdq); add3(w.Fdf, cw.Fdf); add3(w.Tdf, cw.Tdf);
+                        w.Swet += cw.Swet;
+                        w.Vsub += cw.Vsub;
+                    } else {                                     // :424-431
+                        add3(w.Fb, cw.Fb); add3(w.Tb, cw.Tb);
+                        w.Vsub += cw.Vsub;
+                    }
+                }
+            }
+        }
+        __syncwarp();
+    }
+    if (lane == 0) {
+        if (pos == HYDRO_OUTSIDE) {                                  // :302-314
+            zero3(w.Fb); zero3(w.Tb); zero3(w.Fdq); zero3(w.Tdq); zero3(w.Fdf); zero3(w.Tdf);
+            w.Swet = 0.0;
+            w.Vsub = 0.0;
+        } else if (pos == HYDRO_INSIDE) {
+            w.Swet = cb.surface;                                     // :355-356
+            w.Vsub = cb.volume;
+        }
+        w.position = pos;
+        w.status = mismatch ? HYDRO_ERR_MISMATCH : status;
+        C.io[c] = w;
+    }
+}
+
+cudaError_t launch_compound_step(const KParams& P, const CompoundParams& C, LaunchShape shape, int cut64,
+                                 cudaStream_t s, uint32_t* launches)
+{
+    *launches = 0;
+    if (C.n_compounds == 0) return cudaSuccess;
+    cudaError_t e;
+    if (P.n_bodies) {
+        compound_prep_kernel<<<(P.n_bodies + 127) / 128, 128, 0, s>>>(P, C);
+        if ((e = cudaGetLastError())) return e;
+        int grid = shape.grid;
+        if (grid > (int)P.n_chunks) grid = (int)P.n_chunks;
+        if (grid < 1) grid = 1;
+        const void* k = chunk_kernel_for(cut64, P.ocean.waves != 0, shape.ctas_per_sm);
+        if ((e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ChunkSmem))))
+            return e;
+        void* args[] = {const_cast<KParams*>(&P)};
+        if ((e = cudaLaunchKernel(k, dim3(grid), dim3(kThreads), args, sizeof(ChunkSmem), s))) return e;
+        *launches = 2;
+    }
+    compound_finalize_kernel<<<(C.n_compounds + kWarps - 1) / kWarps, kBlock, 0, s>>>(P, C);
+    if ((e = cudaGetLastError())) return e;
+    *launches += 1;
     return cudaSuccess;
 }
 

@@ -311,3 +311,47 @@ class Batch:
 
     def last_launches(self) -> int:
         return int(self.lib.hydro_batch_last_launches(self.b))
+
+
+class CompoundBatch:
+    """Compounds with fixed part lists (hydro_compound_batch): compound c owns
+    parts_per_compound[c] consecutive parts, in the reference's part order."""
+
+    def __init__(self, hctx: HydroContext, part_mesh, parts_per_compound):
+        self.h = hctx
+        self.lib = hctx.lib
+        pm = np.ascontiguousarray(part_mesh, dtype=np.uint32)
+        ppc = np.ascontiguousarray(parts_per_compound, dtype=np.uint32)
+        self.n = ppc.size
+        self.n_parts = int(ppc.sum())
+        b = C.c_void_p()
+        _check(self.lib, hctx.ctx, self.lib.hydro_compound_batch_create(hctx.ctx, pm.ctypes.data if pm.size else None,
+                                                                        ppc.ctypes.data, ppc.size, C.byref(b)))
+        self.b = b
+
+    def close(self) -> None:
+        if self.b:
+            self.lib.hydro_compound_batch_destroy(self.b)
+            self.b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def compute(self, compounds: np.ndarray, parts: np.ndarray, ocean, settings, io: np.ndarray) -> np.ndarray:
+        """Compound::ComputeHydrodynamicForces for every compound (host buffers)."""
+        assert compounds.dtype == abi.BODY_DTYPE and io.dtype == abi.WRENCH_DTYPE
+        assert parts.dtype == abi.COMPOUND_PART_DTYPE and parts.size == self.n_parts
+        assert compounds.size == io.size == self.n
+        _check(self.lib, self.h.ctx, self.lib.hydro_compound_compute(self.b, compounds.ctypes.data,
+                                                                     parts.ctypes.data if parts.size else None,
+                                                                     C.byref(ocean), C.byref(settings),
+                                                                     io.ctypes.data))
+        return io
+
+    def compute_device(self, d_compounds: int, d_parts: int, ocean, settings, d_io: int, stream: int = 0) -> None:
+        _check(self.lib, self.h.ctx, self.lib.hydro_compound_compute_device(self.b, d_compounds, d_parts,
+                                                                            C.byref(ocean), C.byref(settings),
+                                                                            d_io, stream or None))

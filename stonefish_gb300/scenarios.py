@@ -266,3 +266,67 @@ def torpedo_waves(n_bodies: int = 1024, seed: int = 2, depth=(-0.5, 0.2), faces=
     ocean = flat_ocean()
     ocean.waves = 1
     return {"meshes": [(xyz, fc)], "bodies": bodies, "ocean": ocean, "waves": waves}
+
+
+def compound_batch(n_compounds: int = 64, seed: int = 5, depth=(-0.8, 0.8), faces_scale: float = 1.0):
+    """Seeded AUV-like compounds for Compound::ComputeHydrodynamicForces
+    (Compound.cpp:291-436): an external buoyant hull (capped cylinder), two
+    external pontoons (boxes), an internal buoyant ballast block and, on
+    every third compound, a part whose mode takes it out of the fluid
+    computation.  The compound's origin frame is its CG frame; each part
+    sits at a fixed offset (origin) in it.  Returns meshes, compounds
+    (hydro_body, one per compound), parts (hydro_compound_part) with mesh
+    indices into meshes, parts_per_compound and a flat ocean."""
+    rng = np.random.default_rng(seed)
+    hull = meshes.capped_cylinder_for_faces(0.2, 1.2, max(200, int(3000 * faces_scale)))
+    pontoon = meshes.build_box((0.5, 0.08, 0.06), 2 if faces_scale < 1 else 3)
+    ballast = meshes.build_box((0.3, 0.1, 0.05), 1)
+    mesh_list = [hull, pontoon, ballast]
+    vol = (meshes.capped_cylinder_volume(0.2, 1.2), 8 * 0.5 * 0.08 * 0.06, 8 * 0.3 * 0.1 * 0.05)
+    area = (meshes.capped_cylinder_surface(0.2, 1.2), 8 * (0.5 * 0.08 + 0.5 * 0.06 + 0.08 * 0.06),
+            8 * (0.3 * 0.1 + 0.3 * 0.05 + 0.1 * 0.05))
+    R, pos, v, w = random_states(rng, n_compounds, depth)
+    compounds = np.zeros(n_compounds, dtype=abi.BODY_DTYPE)
+    half_c = np.array([0.9, 0.45, 0.25])
+    parts = []
+    counts = []
+    for c in range(n_compounds):
+        Rc = R[c]
+        layout = [  # (mesh, offset, external, buoyant, mode, Cd, Cf)
+            (0, (0.0, 0.0, 0.0), 1, 1, abi.MODE_SUBMERGED, (1.0, 0.5, 0.5), (0.1, 0.05, 0.05)),
+            (1, (0.0, 0.35, 0.15), 1, 1, abi.MODE_SUBMERGED, (0.3, 1.0, 1.0), (0.03, 0.1, 0.1)),
+            (1, (0.0, -0.35, 0.15), 1, 1, abi.MODE_FLOATING, (0.3, 1.0, 1.0), (0.03, 0.1, 0.1)),
+            (2, (0.1, 0.0, -0.05), 0, 1, abi.MODE_SUBMERGED, (1.0, 1.0, 1.0), (0.1, 0.1, 0.1)),
+        ]
+        if c % 3 == 0:
+            layout.append((1, (0.0, 0.0, -0.3), 1, 1, abi.MODE_DISABLED, (1.0, 1.0, 1.0), (0.1, 0.1, 0.1)))
+        for mi, off, ext, buoy, mode, cd, cf in layout:
+            p = np.zeros(1, dtype=abi.COMPOUND_PART_DTYPE)
+            p["T_C"]["basis"] = Rc.reshape(9)
+            p["T_C"]["origin"] = pos[c] + Rc @ np.asarray(off)
+            p["R_O"] = Rc.reshape(9)
+            p["Cd"] = cd
+            p["Cf"] = cf
+            p["mesh"] = mi
+            p["mode"] = mode
+            p["buoyant"] = buoy
+            p["external"] = ext
+            parts.append(p)
+        counts.append(len(layout))
+    compounds["T_CG"]["basis"] = R.reshape(n_compounds, 9)
+    compounds["T_CG"]["origin"] = pos
+    compounds["T_C"] = compounds["T_CG"]
+    compounds["R_O"] = R.reshape(n_compounds, 9)
+    compounds["v"] = v
+    compounds["omega"] = w
+    compounds["volume"] = vol[0] + 2 * vol[1] + vol[2]
+    compounds["surface"] = area[0] + 2 * area[1] + area[2]
+    compounds["P_CB"] = (0.0, 0.0, 0.02)
+    mn, mx = compound_aabb(R, pos, np.tile(half_c, (n_compounds, 1)))
+    compounds["aabb_min"] = mn
+    compounds["aabb_max"] = mx
+    compounds["mesh"] = abi.NO_MESH
+    compounds["mode"] = np.where(np.arange(n_compounds) % 11 == 10, abi.MODE_DISABLED, abi.MODE_SUBMERGED)
+    compounds["buoyancy"] = 1
+    return {"meshes": mesh_list, "compounds": compounds, "parts": np.concatenate(parts),
+            "parts_per_compound": np.asarray(counts, dtype=np.uint32), "ocean": flat_ocean()}
