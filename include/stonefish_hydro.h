@@ -445,6 +445,43 @@ hydro_status hydro_compound_compute(hydro_compound_batch* batch, const hydro_bod
                                     const hydro_compound_part* parts, const hydro_ocean* ocean,
                                     const hydro_settings* settings, hydro_wrench* io);
 
+/* ---------------------------------------------------------------- cables */
+/* One CableEntity: nodes first_node .. first_node + n_nodes - 1 of the
+ * node arrays (Bullet soft-body nodes m_x, m_v), cylinder radius, physics
+ * mode and PhysicsSettings::buoyancy. */
+typedef struct hydro_cable {
+    uint32_t first_node;
+    uint32_t n_nodes;
+    double radius;
+    int32_t mode;
+    int32_t buoyancy;
+} hydro_cable;
+
+/* The nodal forces of CableEntity (CableEntity.h:42-54). */
+typedef struct hydro_cable_node_forces {
+    double Fb[3];
+    double Fdq[3];
+    double Fdf[3];
+} hydro_cable_node_forces;
+
+/* CableEntity::ComputeHydrodynamicForces (CableEntity.cpp:240-376) for
+ * n_cables cables: per segment the submerged volume of its cylinder, the
+ * buoyancy and the form and skin drag from the segment's mean velocity
+ * relative to the current, split between its nodes; the end nodes' forces
+ * doubled.  Cables whose mode is neither FLOATING nor SUBMERGED, and cables
+ * whose node range does not lie within n_nodes_total, are left untouched.
+ * x and v are [n_nodes_total][3] FP64.  Device pointers on `stream`; the
+ * call keeps n_nodes_total x 72 bytes of scratch per context. */
+hydro_status hydro_cable_forces_device(hydro_ctx* ctx, const hydro_cable* d_cables, uint32_t n_cables,
+                                       const double* d_x, const double* d_v, uint32_t n_nodes_total,
+                                       const hydro_ocean* ocean, const hydro_settings* settings,
+                                       hydro_cable_node_forces* d_out, void* stream);
+
+/* Host-buffer version (synchronises). */
+hydro_status hydro_cable_forces(hydro_ctx* ctx, const hydro_cable* cables, uint32_t n_cables, const double* x,
+                                const double* v, uint32_t n_nodes_total, const hydro_ocean* ocean,
+                                const hydro_settings* settings, hydro_cable_node_forces* out);
+
 /* ---------------------------------------------------------- aerodynamics */
 /* SolidEntity::ComputeAerodynamicForces(mesh, atm, T_CG, T_C, v, omega,
  * Fda, Tda) (SolidEntity.cpp:1865-1923): quadratic-law drag of the faces

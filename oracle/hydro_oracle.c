@@ -451,6 +451,115 @@ void oracle_compound_forces(int variant, const hydro_body* cb, const hydro_compo
     }
 }
 
+/* ---------------------------------------------------------------- cables */
+/* CableEntity::circularSegmentArea (CableEntity.cpp:218-238) with btAcos's clamp */
+static double cable_acos(double x) { if (x < -1.0) x = -1.0; if (x > 1.0) x = 1.0; return acos(x); }
+
+static double circular_segment_area(double h, double r)
+{
+    if (h <= 0.0) return 0.0;
+    if (h >= 2.0 * r) return M_PI * r * r;
+    if (h > r) {
+        h = 2.0 * r - h;
+        double theta = 2.0 * cable_acos((r - h) / r);
+        return r * r * (M_PI - (theta - sin(theta)) / 2.0);
+    }
+    double theta = 2.0 * cable_acos((r - h) / r);
+    return (r * r / 2.0) * (theta - sin(theta));
+}
+
+/* CableEntity::ComputeHydrodynamicForces (CableEntity.cpp:240-376). */
+void oracle_cable_forces(const hydro_cable* cables, uint32_t n_cables, const double* x, const double* v,
+                         uint32_t n_nodes_total, const hydro_ocean* ocean, const oracle_waves* waves,
+                         const hydro_settings* settings, hydro_cable_node_forces* out)
+{
+    for (uint32_t c = 0; c < n_cables; ++c) {
+        const hydro_cable* cb = &cables[c];
+        if (cb->mode != HYDRO_MODE_FLOATING && cb->mode != HYDRO_MODE_SUBMERGED) continue;   /* :242 */
+        uint32_t n = cb->n_nodes, f = cb->first_node;
+        if (n == 0 || (uint64_t)f + n > n_nodes_total) continue;
+        double r = cb->radius;
+        for (uint32_t i = 0; i < n; ++i) memset(&out[f + i], 0, sizeof(out[f + i]));      /* :245-246 */
+        for (uint32_t i = 0; i + 1 < n; ++i) {
+            double p1[3], p2[3];
+            memcpy(p1, x + 3 * (size_t)(f + i), sizeof(p1));
+            memcpy(p2, x + 3 * (size_t)(f + i + 1), sizeof(p2));
+            double d1 = (double)oracle_depth(ORACLE_REF32, ocean, waves, (float)p1[0], (float)p1[1], (float)p1[2]);
+            double d2 = (double)oracle_depth(ORACLE_REF32, ocean, waves, (float)p2[0], (float)p2[1], (float)p2[2]);
+            if (d1 > d2) {
+                double t[3];
+                memcpy(t, p1, sizeof(t)); memcpy(p1, p2, sizeof(t)); memcpy(p2, t, sizeof(t));
+                double td = d1; d1 = d2; d2 = td;
+            }
+            double dz = d2 - d1;
+            double hx = p2[0] - p1[0], hy = p2[1] - p1[1];
+            double h2 = hx * hx + hy * hy + 0.0 * 0.0;          /* btVector3::safeNorm */
+            double dxy = h2 > DBL_EPSILON ? sqrt(h2) : 0.0;
+            double sv[3] = {p2[0] - p1[0], p2[1] - p1[1], p2[2] - p1[2]};
+            double L = sqrt(sv[0] * sv[0] + sv[1] * sv[1] + sv[2] * sv[2]);
+            double alpha = atan(dz / dxy);
+            double margin = fabs(dxy) < DBL_EPSILON ? 0.0 : r * cos(alpha);
+            double V = 0.0;
+            if (d2 < -margin) continue;
+            else if (d1 > margin) V = M_PI * r * r * L;
+            else if (fabs(dxy) < DBL_EPSILON) V = M_PI * r * r * (d2 < dz ? d2 : dz);
+            else if (fabs(dz) < DBL_EPSILON) V = circular_segment_area(d1 + r, r) * L;
+            else if (fabs(d1) <= margin && fabs(d2) <= margin) {
+                double A1 = circular_segment_area(d1 / cos(alpha) + r, r);
+                double A2 = circular_segment_area(d2 / cos(alpha) + r, r);
+                V = (A1 + A2) / 2.0 * L;
+            } else if (d1 < -margin && d2 > margin) {
+                double l1 = (d2 - r * cos(alpha)) / sin(alpha);
+                double l2 = 2.0 * r * cos(alpha);
+                V = M_PI * r * r * (l1 + l2 / 2.0);
+            } else if (d2 <= margin) {
+                double a = r + d2 / cos(alpha);
+                double l = a / sin(alpha);
+                V = circular_segment_area(a, r) * l / 2.0;
+            } else if (d1 >= -margin) {
+                double a = r - d1 / cos(alpha);
+                double l = a / sin(alpha);
+                V = M_PI * r * r * L - circular_segment_area(a, r) * l / 2.0;
+            }
+            if (cb->buoyancy && settings->realistic_buoyancy) {
+                double k = -V * ocean->density;
+                double b[3] = {k * 0.0, k * 0.0, k * ocean->gravity};
+                for (int q = 0; q < 3; ++q) {
+                    out[f + i].Fb[q] += b[q] / 2.0;
+                    out[f + i + 1].Fb[q] += b[q] / 2.0;
+                }
+            }
+            if (settings->damping_forces && V > 0.0) {
+                double p[3] = {(p1[0] + p2[0]) / 2.0, (p1[1] + p2[1]) / 2.0, (p1[2] + p2[2]) / 2.0};
+                const double* va = v + 3 * (size_t)(f + i);
+                const double* vb = v + 3 * (size_t)(f + i + 1);
+                double vm[3] = {(va[0] + vb[0]) / 2.0, (va[1] + vb[1]) / 2.0, (va[2] + vb[2]) / 2.0};
+                double wv[3];
+                current_velocity(ocean, p[0], p[1], p[2], wv);
+                double rv[3] = {vm[0] - wv[0], vm[1] - wv[1], vm[2] - wv[2]};
+                double f1 = fabs(sv[0] * rv[0] + sv[1] * rv[1] + sv[2] * rv[2]);
+                double f2 = V / (M_PI * r * r * L);
+                double rl = sqrt(rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2]);
+                double S = 2.0 * r * L;
+                double qd = -(1.0 - f1) * f2 * 0.5 * ocean->density * 0.5 * S * rl;
+                double Sf = f2 * ((2.0 * M_PI) * r * L);
+                for (int q = 0; q < 3; ++q) {
+                    double fq = qd * rv[q], ff = -Sf * rv[q];
+                    out[f + i].Fdq[q] += fq / 2.0;
+                    out[f + i + 1].Fdq[q] += fq / 2.0;
+                    out[f + i].Fdf[q] += ff / 2.0;
+                    out[f + i + 1].Fdf[q] += ff / 2.0;
+                }
+            }
+        }
+        for (int q = 0; q < 3; ++q) {                          /* :367-373 */
+            out[f].Fb[q] *= 2.0; out[f + n - 1].Fb[q] *= 2.0;
+            out[f].Fdq[q] *= 2.0; out[f + n - 1].Fdq[q] *= 2.0;
+            out[f].Fdf[q] *= 2.0; out[f + n - 1].Fdf[q] *= 2.0;
+        }
+    }
+}
+
 /* ----------------------------------------------------------- aerodynamics */
 /* Atmosphere::GetFluidVelocity sums every wind field (Atmosphere.cpp:146-152):
  * the winds as enabled currents of an ocean descriptor. */

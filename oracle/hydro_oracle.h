@@ -117,6 +117,11 @@ double oracle_batch(int variant, int threads, const hydro_body* bodies,
 
 int oracle_hardware_threads(void);
 
+/* CableEntity::ComputeHydrodynamicForces (Library/src/entities/CableEntity.cpp:240-376). */
+void oracle_cable_forces(const hydro_cable* cables, uint32_t n_cables, const double* x, const double* v,
+                         uint32_t n_nodes_total, const hydro_ocean* ocean, const oracle_waves* waves,
+                         const hydro_settings* settings, hydro_cable_node_forces* out);
+
 /* Compound::ComputeHydrodynamicForces (Library/src/entities/solids/Compound.cpp:291-436):
  * part_meshes[i] is part i's mesh (NULL = nullptr). */
 void oracle_compound_forces(int variant, const hydro_body* compound, const hydro_compound_part* parts,

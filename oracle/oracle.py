@@ -79,6 +79,8 @@ class Oracle:
                                    P(abi.Settings), vp]
         L.oracle_hardware_threads.restype = i32
         L.oracle_hardware_threads.argtypes = []
+        L.oracle_cable_forces.restype = None
+        L.oracle_cable_forces.argtypes = [vp, u32, vp, vp, u32, P(abi.Ocean), vp, P(abi.Settings), vp]
         L.oracle_compound_forces.restype = None
         L.oracle_compound_forces.argtypes = [i32, vp, vp, u32, vp, P(abi.Ocean), vp, P(abi.Settings), vp]
         L.oracle_aero_forces.restype = None
@@ -192,6 +194,17 @@ class Oracle:
         ptrs = [io[k].ctypes.data_as(C.POINTER(C.c_double)) for k in ("Fdq", "Tdq", "Fdf", "Tdf")]
         self.lib.oracle_correct_forces(C.byref(ocean), *ptrs, pcd, pcf, pro)
         return io
+
+    def cable_forces(self, cables, x, v, ocean, settings, out, waves=None):
+        """CableEntity::ComputeHydrodynamicForces for every cable; out
+        (CABLE_FORCES_DTYPE per node) updated in place."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        w = self.make_waves(waves)
+        self.lib.oracle_cable_forces(cables.ctypes.data if len(cables) else None, len(cables), x.ctypes.data,
+                                     v.ctypes.data, len(x), C.byref(ocean), self._p(w), C.byref(settings),
+                                     out.ctypes.data)
+        return out
 
     def compound_forces(self, variant, compound, parts, part_meshes, ocean, settings, io, waves=None):
         """Compound::ComputeHydrodynamicForces: compound = hydro_body[1],

@@ -71,6 +71,15 @@ class CompoundPart(C.Structure):
                 ("mesh", C.c_uint32), ("mode", C.c_int32), ("buoyant", C.c_int32), ("external", C.c_int32)]
 
 
+class Cable(C.Structure):
+    _fields_ = [("first_node", C.c_uint32), ("n_nodes", C.c_uint32), ("radius", C.c_double),
+                ("mode", C.c_int32), ("buoyancy", C.c_int32)]
+
+
+class CableNodeForces(C.Structure):
+    _fields_ = [("Fb", _d3), ("Fdq", _d3), ("Fdf", _d3)]
+
+
 class Atmosphere(C.Structure):
     _fields_ = [("density", C.c_double), ("n_winds", C.c_uint32), ("reserved", C.c_uint32),
                 ("winds", Current * MAX_CURRENTS)]
@@ -144,6 +153,8 @@ CURRENT_DTYPE = _dtype_of(Current)
 RIGID_DTYPE = _dtype_of(RigidState)
 AERO_PARAMS_DTYPE = _dtype_of(AeroParams)
 COMPOUND_PART_DTYPE = _dtype_of(CompoundPart)
+CABLE_DTYPE = _dtype_of(Cable)
+CABLE_FORCES_DTYPE = _dtype_of(CableNodeForces)
 AERO_WRENCH_DTYPE = _dtype_of(AeroWrench)
 APPROX_AUTO, APPROX_SPHERE, APPROX_CYLINDER, APPROX_ELLIPSOID = range(4)
 
@@ -233,6 +244,9 @@ def _declare(lib: C.CDLL) -> None:
         "hydro_compound_batch_destroy": (None, [vp]),
         "hydro_compound_compute_device": (i32, [vp, vp, vp, C.POINTER(Ocean), C.POINTER(Settings), vp, vp]),
         "hydro_compound_compute": (i32, [vp, vp, vp, C.POINTER(Ocean), C.POINTER(Settings), vp]),
+        "hydro_cable_forces_device": (i32, [vp, vp, u32, vp, vp, u32, C.POINTER(Ocean), C.POINTER(Settings), vp,
+                                            vp]),
+        "hydro_cable_forces": (i32, [vp, vp, u32, vp, vp, u32, C.POINTER(Ocean), C.POINTER(Settings), vp]),
         "hydro_aero_forces": (i32, [vp, u32, C.POINTER(Atmosphere), C.POINTER(Transform), C.POINTER(Transform),
                                     d, d, d, d]),
         "hydro_aero_correct": (i32, [vp, C.POINTER(AeroParams), d, d]),

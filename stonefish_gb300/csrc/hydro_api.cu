@@ -60,6 +60,10 @@ struct hydro_ctx {
     void* small_d = nullptr;   // scratch for the small entry points
     size_t small_cap = 0;
     std::string tune_path;     // autotuner cache file ("" = none)
+    double* cable_seg = nullptr;   // cable segment scratch (9 doubles per node)
+    size_t cable_cap = 0;
+    void* cable_stage = nullptr;   // host-buffer cable call staging
+    size_t cable_stage_cap = 0;
     char gpu_name[256] = {0};
 };
 
@@ -515,6 +519,8 @@ void hydro_destroy(hydro_ctx* ctx)
     cudaFree(ctx->tiles_d);
     cudaFree(ctx->wave_d);
     cudaFree(ctx->small_d);
+    cudaFree(ctx->cable_seg);
+    cudaFree(ctx->cable_stage);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -1017,6 +1023,85 @@ hydro_status hydro_compound_compute(hydro_compound_batch* cb, const hydro_body* 
     hydro_status st = compound_launch(cb, cb->compounds_d, cb->parts_d, ocean, settings, cb->io_d, s);
     if (st != HYDRO_OK) return st;
     CK(ctx, cudaMemcpyAsync(io, cb->io_d, nc * sizeof(hydro_wrench), cudaMemcpyDeviceToHost, s));
+    CK(ctx, cudaStreamSynchronize(s));
+    return HYDRO_OK;
+}
+
+// ----------------------------------------------------------------- cables
+// Segment scratch (9 doubles per node) followed by one error word.
+hydro_status cable_scratch(hydro_ctx* ctx, uint32_t n_nodes)
+{
+    const size_t need = (size_t)std::max<uint32_t>(n_nodes, 1u) * 9 + 32;
+    if (ctx->cable_cap >= need) return HYDRO_OK;
+    cudaFree(ctx->cable_seg);
+    ctx->cable_seg = nullptr;
+    ctx->cable_cap = 0;
+    CK(ctx, cudaMalloc(&ctx->cable_seg, need * sizeof(double)));
+    ctx->cable_cap = need;
+    return HYDRO_OK;
+}
+
+hydro_status hydro_cable_forces_device(hydro_ctx* ctx, const hydro_cable* d_cables, uint32_t n_cables,
+                                       const double* d_x, const double* d_v, uint32_t n_nodes_total,
+                                       const hydro_ocean* ocean, const hydro_settings* settings,
+                                       hydro_cable_node_forces* d_out, void* stream)
+{
+    if (!ctx) return HYDRO_ERR_INVALID_ARG;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if ((n_cables && (!d_cables || !d_x || !d_v || !d_out)) || !settings || !valid_ocean(ocean))
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "cable forces: bad arguments");
+    if (ocean->waves && !ctx->wave_d) return fail(ctx, HYDRO_ERR_INVALID_ARG, "no wave grid");
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, HYDRO_ERR_DEVICE, "cudaSetDevice");
+    hydro_status st = cable_scratch(ctx, n_nodes_total);
+    if (st != HYDRO_OK) return st;
+    SettingsDev sd;
+    sd.damping = settings->damping_forces ? 1 : 0;
+    sd.buoyancy = settings->realistic_buoyancy ? 1 : 0;
+    unsigned* bad = reinterpret_cast<unsigned*>(ctx->cable_seg + ctx->cable_cap - 32);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    CK(ctx, cudaMemsetAsync(bad, 0, sizeof(unsigned), s));
+    cudaError_t e = launch_cable(d_cables, n_cables, n_nodes_total, d_x, d_v, make_ocean(ctx, ocean), sd,
+                                 ctx->cable_seg, d_out, bad, s);
+    return e == cudaSuccess ? HYDRO_OK : cuda_fail(ctx, e, "cable kernel");
+}
+
+hydro_status hydro_cable_forces(hydro_ctx* ctx, const hydro_cable* cables, uint32_t n_cables, const double* x,
+                                const double* v, uint32_t n_nodes_total, const hydro_ocean* ocean,
+                                const hydro_settings* settings, hydro_cable_node_forces* out)
+{
+    if (!ctx) return HYDRO_ERR_INVALID_ARG;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if ((n_cables && (!cables || !x || !v || !out)) || !settings || !valid_ocean(ocean))
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "cable forces: bad arguments");
+    for (uint32_t c = 0; c < n_cables; ++c)
+        if ((uint64_t)cables[c].first_node + cables[c].n_nodes > n_nodes_total)
+            return fail(ctx, HYDRO_ERR_INDEX_RANGE, "cable %u: nodes beyond n_nodes_total", c);
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, HYDRO_ERR_DEVICE, "cudaSetDevice");
+    const size_t bc = (size_t)n_cables * sizeof(hydro_cable), bx = (size_t)n_nodes_total * 3 * sizeof(double);
+    const size_t bo = (size_t)n_nodes_total * sizeof(hydro_cable_node_forces);
+    const size_t o1 = (bc + 255) & ~size_t(255), o2 = o1 + ((bx + 255) & ~size_t(255));
+    const size_t o3 = o2 + ((bx + 255) & ~size_t(255)), need = o3 + bo + 256;
+    if (ctx->cable_stage_cap < need) {
+        cudaFree(ctx->cable_stage);
+        ctx->cable_stage = nullptr;
+        ctx->cable_stage_cap = 0;
+        CK(ctx, cudaMalloc(&ctx->cable_stage, need));
+        ctx->cable_stage_cap = need;
+    }
+    char* base = static_cast<char*>(ctx->cable_stage);
+    cudaStream_t s = ctx->stream;
+    if (bc) CK(ctx, cudaMemcpyAsync(base, cables, bc, cudaMemcpyHostToDevice, s));
+    if (bx) {
+        CK(ctx, cudaMemcpyAsync(base + o1, x, bx, cudaMemcpyHostToDevice, s));
+        CK(ctx, cudaMemcpyAsync(base + o2, v, bx, cudaMemcpyHostToDevice, s));
+        CK(ctx, cudaMemcpyAsync(base + o3, out, bo, cudaMemcpyHostToDevice, s));
+    }
+    hydro_status st = hydro_cable_forces_device(ctx, reinterpret_cast<const hydro_cable*>(base), n_cables,
+                                                reinterpret_cast<const double*>(base + o1),
+                                                reinterpret_cast<const double*>(base + o2), n_nodes_total, ocean,
+                                                settings, reinterpret_cast<hydro_cable_node_forces*>(base + o3), s);
+    if (st != HYDRO_OK) return st;
+    if (bo) CK(ctx, cudaMemcpyAsync(out, base + o3, bo, cudaMemcpyDeviceToHost, s));
     CK(ctx, cudaStreamSynchronize(s));
     return HYDRO_OK;
 }

@@ -25,7 +25,7 @@ constexpr int kTileFaces = 384;      // max faces per tile (64 per compute warp)
 constexpr int kTileVerts = 384;      // max distinct vertices per tile (< 512: 9-bit indices)
 constexpr int kQ = 23;               // accumulated quantities per body
 constexpr int kPartialStride = 24;   // doubles per chunk partial (23 + status)
-constexpr int kFlushFaces = 8;       // faces a thread sums in FP32 before a flush
+constexpr int kFlushFaces = 16;      // faces a thread sums in FP32 before a flush
 
 // indices of the accumulated quantities
 enum : int {

@@ -133,6 +133,9 @@ cudaError_t launch_mlp_tc(const float* feats, uint32_t n, const float* fmean, co
 
 cudaError_t launch_compound_step(const KParams& P, const CompoundParams& C, LaunchShape shape, int cut64,
                                  cudaStream_t s, uint32_t* launches);
+cudaError_t launch_cable(const hydro_cable* cables, uint32_t n_cables, uint32_t n_nodes_total, const double* x,
+                         const double* v, OceanDev o, SettingsDev st, double* seg, hydro_cable_node_forces* out,
+                         unsigned* bad, cudaStream_t s);
 cudaError_t launch_aero_correct(const hydro_aero_params* p, double* io6, cudaStream_t s);
 
 }  // namespace sfh

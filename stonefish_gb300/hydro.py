@@ -173,6 +173,18 @@ class HydroContext:
                                                ro.ctypes.data_as(P)))
         return io
 
+    def cable_forces(self, cables: np.ndarray, x, v, ocean, settings, out: np.ndarray) -> np.ndarray:
+        """CableEntity::ComputeHydrodynamicForces (CableEntity.cpp:240-376) for
+        every cable (host buffers): out = nodal forces, in place."""
+        assert cables.dtype == abi.CABLE_DTYPE and out.dtype == abi.CABLE_FORCES_DTYPE
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        assert x.shape == v.shape and x.shape[0] == out.size
+        self._ck(self.lib.hydro_cable_forces(self.ctx, cables.ctypes.data if cables.size else None, cables.size,
+                                             x.ctypes.data, v.ctypes.data, x.shape[0], C.byref(ocean),
+                                             C.byref(settings), out.ctypes.data))
+        return out
+
     def aero_forces(self, mesh, atm, T_CG, T_C, v, omega):
         """SolidEntity::ComputeAerodynamicForces (static form,
         SolidEntity.cpp:1865-1923): returns (Fda, Tda)."""

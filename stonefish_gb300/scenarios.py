@@ -330,3 +330,46 @@ def compound_batch(n_compounds: int = 64, seed: int = 5, depth=(-0.8, 0.8), face
     compounds["buoyancy"] = 1
     return {"meshes": mesh_list, "compounds": compounds, "parts": np.concatenate(parts),
             "parts_per_compound": np.asarray(counts, dtype=np.uint32), "ocean": flat_ocean()}
+
+
+def cable_set(n_cables: int = 48, seed: int = 6, max_nodes: int = 120):
+    """Seeded cables for CableEntity::ComputeHydrodynamicForces
+    (CableEntity.cpp:240-376): sagging catenary-like chains across the
+    surface, plus cables built to hit each submersion case exactly -- a
+    horizontal cable on the waterline (dz = 0), a vertical one through it
+    (dxy = 0), fully submerged and fully dry ones -- and one cable in a mode
+    outside the fluid computation.  Returns cables, node positions and
+    velocities (FP64) and a flat ocean with a uniform current."""
+    rng = np.random.default_rng(seed)
+    cables = np.zeros(n_cables, dtype=abi.CABLE_DTYPE)
+    xs, vs = [], []
+    first = 0
+    for c in range(n_cables):
+        kind = c % 6
+        n = int(rng.integers(2, max_nodes)) if kind not in (1, 2) else int(rng.integers(2, 20))
+        t = np.linspace(0.0, 1.0, n)
+        x0 = rng.uniform(-5, 5, 3)
+        if kind == 1:        # horizontal on the waterline
+            pts = np.stack([x0[0] + 3 * t, np.full(n, x0[1]), np.full(n, rng.uniform(-0.02, 0.02))], axis=1)
+        elif kind == 2:      # vertical through the surface
+            pts = np.stack([np.full(n, x0[0]), np.full(n, x0[1]), -1.0 + 2.5 * t], axis=1)
+        elif kind == 3:      # fully submerged
+            pts = np.stack([x0[0] + 4 * t, x0[1] + t, 2.0 + np.sin(3 * t)], axis=1)
+        elif kind == 4:      # dry
+            pts = np.stack([x0[0] + 4 * t, x0[1] - t, -3.0 - t], axis=1)
+        else:                # sagging chain across the surface
+            span = rng.uniform(2, 10)
+            sag = rng.uniform(0.2, 3.0)
+            pts = np.stack([x0[0] + span * t, x0[1] + rng.uniform(-1, 1) * t,
+                            rng.uniform(-1.0, 0.3) + sag * (1 - (2 * t - 1) ** 2)], axis=1)
+        xs.append(pts)
+        vs.append(rng.uniform(-1.0, 1.0, (n, 3)))
+        cables[c]["first_node"] = first
+        cables[c]["n_nodes"] = n
+        cables[c]["radius"] = rng.uniform(0.01, 0.08)
+        cables[c]["mode"] = abi.MODE_DISABLED if c == n_cables - 1 else (abi.MODE_FLOATING if c % 2 else
+                                                                          abi.MODE_SUBMERGED)
+        cables[c]["buoyancy"] = 0 if c % 7 == 5 else 1
+        first += n
+    return {"cables": cables, "x": np.concatenate(xs), "v": np.concatenate(vs),
+            "ocean": flat_ocean(current=(0.3, -0.1, 0.0))}
