@@ -445,6 +445,45 @@ hydro_status hydro_compound_compute(hydro_compound_batch* batch, const hydro_bod
                                     const hydro_compound_part* parts, const hydro_ocean* ocean,
                                     const hydro_settings* settings, hydro_wrench* io);
 
+/* ------------------------------------------------------------- FFT ocean */
+/* The reference's GPU ocean (OpenGLOcean, Library/src/graphics/OpenGLOcean.cpp)
+ * as CUDA kernels writing this context's wave grid: Elfouhaily spectrum for
+ * four grid sizes with the reference's random phases (host, once), then per
+ * update h(k,t) (oceanInit.frag) and the log2(N)-pass inverse FFTs along x
+ * and y (oceanFFTX/Y.frag) with the reference's binary16 butterfly table.
+ * After an update the wave grid holds N x N texels of four heights and the
+ * depth queries read channels 0 and 1 at grid sizes 0 and 1, as
+ * OpenGLRealOcean::ComputeWaveHeight does (OpenGLRealOcean.cpp:321-331). */
+typedef struct hydro_fft_ocean_params {
+    float wind;                  /* params.wind, U10 [m/s] */
+    float omega;                 /* params.omega, inverse wave age */
+    float amplitude;             /* params.A */
+    float km;                    /* params.km (370) */
+    float cm;                    /* params.cm (0.23) */
+    float grid_sizes[4];         /* params.gridSizes (893, 101, 21, 11) [m] */
+    uint32_t passes;             /* params.passes: N = 2^passes texels per side (8) */
+    int32_t propagate;           /* params.propagate (1) */
+} hydro_fft_ocean_params;
+
+/* The parameters OpenGLRealOcean uses for a sea state (OpenGLRealOcean.cpp:40-45,
+ * OpenGLOcean.cpp:63-70): wind = 5 state + 2, omega = 5 exp(-state) + 0.2. */
+void hydro_fft_ocean_params_for_state(float state, hydro_fft_ocean_params* params);
+
+typedef struct hydro_fft_ocean hydro_fft_ocean;
+
+/* Builds the spectrum (seed 1234 of the reference's generator) and the
+ * butterfly table and makes the context's wave grid N x N x 4. */
+hydro_status hydro_fft_ocean_create(hydro_ctx* ctx, const hydro_fft_ocean_params* params, hydro_fft_ocean** out);
+void hydro_fft_ocean_destroy(hydro_fft_ocean* ocean);
+
+/* The wave field at time t [s] into the context's wave grid (three kernel
+ * launches on `stream`; later hydrodynamics calls on the same stream see
+ * it). */
+hydro_status hydro_fft_ocean_update(hydro_fft_ocean* ocean, float t, void* stream);
+
+/* Copies the current wave grid (N x N x 4 floats) to host memory (synchronises). */
+hydro_status hydro_fft_ocean_read(hydro_fft_ocean* ocean, float* out);
+
 /* ---------------------------------------------------------------- cables */
 /* One CableEntity: nodes first_node .. first_node + n_nodes - 1 of the
  * node arrays (Bullet soft-body nodes m_x, m_v), cylinder radius, physics

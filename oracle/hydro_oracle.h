@@ -117,6 +117,10 @@ double oracle_batch(int variant, int threads, const hydro_body* bodies,
 
 int oracle_hardware_threads(void);
 
+/* The reference's FFT ocean at time t (oracle/fft_ocean.c): N x N x 4 heights. */
+void oracle_fft_ocean(const hydro_fft_ocean_params* params, float t, float* out);
+void oracle_fft_ocean_init_only(const hydro_fft_ocean_params* params, float t, float* out);
+
 /* CableEntity::ComputeHydrodynamicForces (Library/src/entities/CableEntity.cpp:240-376). */
 void oracle_cable_forces(const hydro_cable* cables, uint32_t n_cables, const double* x, const double* v,
                          uint32_t n_nodes_total, const hydro_ocean* ocean, const oracle_waves* waves,

@@ -26,7 +26,8 @@ def oracle_lib_path() -> str:
 def build_oracle(force: bool = False) -> str:
     """Compiles the oracle with its Makefile (gcc, no -march, no FMA contraction)."""
     path = oracle_lib_path()
-    srcs = [os.path.join(HERE, f) for f in ("hydro_oracle.c", "hydro_oracle_core.inc", "hydro_oracle.h")]
+    srcs = [os.path.join(HERE, f) for f in ("hydro_oracle.c", "hydro_oracle_core.inc", "hydro_oracle.h",
+                                            "fft_ocean.c", "Makefile")]
     srcs.append(os.path.join(abi.INCLUDE_DIR, "stonefish_hydro.h"))
     stale = force or not os.path.exists(path) or any(
         os.path.getmtime(s) > os.path.getmtime(path) for s in srcs)
@@ -79,6 +80,10 @@ class Oracle:
                                    P(abi.Settings), vp]
         L.oracle_hardware_threads.restype = i32
         L.oracle_hardware_threads.argtypes = []
+        L.oracle_fft_ocean.restype = None
+        L.oracle_fft_ocean.argtypes = [P(abi.FftOceanParams), C.c_float, vp]
+        L.oracle_fft_ocean_init_only.restype = None
+        L.oracle_fft_ocean_init_only.argtypes = [P(abi.FftOceanParams), C.c_float, vp]
         L.oracle_cable_forces.restype = None
         L.oracle_cable_forces.argtypes = [vp, u32, vp, vp, u32, P(abi.Ocean), vp, P(abi.Settings), vp]
         L.oracle_compound_forces.restype = None
@@ -194,6 +199,15 @@ class Oracle:
         ptrs = [io[k].ctypes.data_as(C.POINTER(C.c_double)) for k in ("Fdq", "Tdq", "Fdf", "Tdf")]
         self.lib.oracle_correct_forces(C.byref(ocean), *ptrs, pcd, pcf, pro)
         return io
+
+    def fft_ocean(self, params, t: float, init_only: bool = False) -> np.ndarray:
+        """The reference's FFT ocean at time t: [N, N, 4] float32 (heights of
+        the four grids), or the h(k,t) field before the FFTs."""
+        N = 1 << params.passes
+        out = np.zeros((N, N, 4), dtype=np.float32)
+        fn = self.lib.oracle_fft_ocean_init_only if init_only else self.lib.oracle_fft_ocean
+        fn(C.byref(params), t, out.ctypes.data)
+        return out
 
     def cable_forces(self, cables, x, v, ocean, settings, out, waves=None):
         """CableEntity::ComputeHydrodynamicForces for every cable; out

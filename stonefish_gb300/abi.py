@@ -71,6 +71,11 @@ class CompoundPart(C.Structure):
                 ("mesh", C.c_uint32), ("mode", C.c_int32), ("buoyant", C.c_int32), ("external", C.c_int32)]
 
 
+class FftOceanParams(C.Structure):
+    _fields_ = [("wind", C.c_float), ("omega", C.c_float), ("amplitude", C.c_float), ("km", C.c_float),
+                ("cm", C.c_float), ("grid_sizes", C.c_float * 4), ("passes", C.c_uint32), ("propagate", C.c_int32)]
+
+
 class Cable(C.Structure):
     _fields_ = [("first_node", C.c_uint32), ("n_nodes", C.c_uint32), ("radius", C.c_double),
                 ("mode", C.c_int32), ("buoyancy", C.c_int32)]
@@ -244,6 +249,11 @@ def _declare(lib: C.CDLL) -> None:
         "hydro_compound_batch_destroy": (None, [vp]),
         "hydro_compound_compute_device": (i32, [vp, vp, vp, C.POINTER(Ocean), C.POINTER(Settings), vp, vp]),
         "hydro_compound_compute": (i32, [vp, vp, vp, C.POINTER(Ocean), C.POINTER(Settings), vp]),
+        "hydro_fft_ocean_params_for_state": (None, [C.c_float, C.POINTER(FftOceanParams)]),
+        "hydro_fft_ocean_create": (i32, [vp, C.POINTER(FftOceanParams), C.POINTER(vp)]),
+        "hydro_fft_ocean_destroy": (None, [vp]),
+        "hydro_fft_ocean_update": (i32, [vp, C.c_float, vp]),
+        "hydro_fft_ocean_read": (i32, [vp, vp]),
         "hydro_cable_forces_device": (i32, [vp, vp, u32, vp, vp, u32, C.POINTER(Ocean), C.POINTER(Settings), vp,
                                             vp]),
         "hydro_cable_forces": (i32, [vp, vp, u32, vp, vp, u32, C.POINTER(Ocean), C.POINTER(Settings), vp]),

@@ -101,6 +101,21 @@ struct hydro_compound_batch {
     uint32_t last_launches = 0;
 };
 
+struct hydro_fft_ocean {
+    hydro_ctx* ctx = nullptr;
+    hydro_fft_ocean_params p{};
+    uint32_t N = 0;
+    float4* s12_d = nullptr;
+    float4* s34_d = nullptr;
+    int2* idx_d = nullptr;
+    float2* w_d = nullptr;
+};
+
+namespace sfh {
+void fft_ocean_spectrum(const hydro_fft_ocean_params& p, std::vector<float4>& s12, std::vector<float4>& s34);
+void fft_ocean_butterfly(int passes, std::vector<int2>& idx, std::vector<float2>& w);
+}
+
 namespace {
 
 hydro_status fail(hydro_ctx* ctx, hydro_status s, const char* fmt, ...)
@@ -1024,6 +1039,118 @@ hydro_status hydro_compound_compute(hydro_compound_batch* cb, const hydro_body* 
     if (st != HYDRO_OK) return st;
     CK(ctx, cudaMemcpyAsync(io, cb->io_d, nc * sizeof(hydro_wrench), cudaMemcpyDeviceToHost, s));
     CK(ctx, cudaStreamSynchronize(s));
+    return HYDRO_OK;
+}
+
+// -------------------------------------------------------------- FFT ocean
+void hydro_fft_ocean_params_for_state(float state, hydro_fft_ocean_params* p)
+{
+    if (!p) return;
+    p->wind = state * 5.f + 2.f;
+    p->omega = 5.f * expf(-state) + 0.2f;
+    p->amplitude = 1.f;
+    p->km = 370.f;
+    p->cm = 0.23f;
+    p->grid_sizes[0] = 893.f;
+    p->grid_sizes[1] = 101.f;
+    p->grid_sizes[2] = 21.f;
+    p->grid_sizes[3] = 11.f;
+    p->passes = 8;
+    p->propagate = 1;
+}
+
+void fft_ocean_free(hydro_fft_ocean* o)
+{
+    if (!o) return;
+    cudaFree(o->s12_d);
+    cudaFree(o->s34_d);
+    cudaFree(o->idx_d);
+    cudaFree(o->w_d);
+    delete o;
+}
+
+hydro_status hydro_fft_ocean_create(hydro_ctx* ctx, const hydro_fft_ocean_params* params, hydro_fft_ocean** out)
+{
+    if (!ctx) return HYDRO_ERR_INVALID_ARG;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (!params || !out || params->passes < 2 || params->passes > 10 || !(params->wind > 0.f) ||
+        !(params->omega > 0.f))
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "fft ocean: bad parameters");
+    for (int g = 0; g < 4; ++g)
+        if (!(params->grid_sizes[g] > 0.f)) return fail(ctx, HYDRO_ERR_INVALID_ARG, "fft ocean: bad grid size");
+    *out = nullptr;
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, HYDRO_ERR_DEVICE, "cudaSetDevice");
+    hydro_fft_ocean* o = new (std::nothrow) hydro_fft_ocean();
+    if (!o) return fail(ctx, HYDRO_ERR_OOM, "host allocation");
+    o->ctx = ctx;
+    o->p = *params;
+    o->N = 1u << params->passes;
+    std::vector<float4> s12, s34;
+    std::vector<int2> idx;
+    std::vector<float2> w;
+    fft_ocean_spectrum(o->p, s12, s34);
+    fft_ocean_butterfly((int)o->p.passes, idx, w);
+    const size_t nn = (size_t)o->N * o->N;
+    cudaError_t e = cudaMalloc(&o->s12_d, nn * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMalloc(&o->s34_d, nn * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMalloc(&o->idx_d, idx.size() * sizeof(int2));
+    if (e == cudaSuccess) e = cudaMalloc(&o->w_d, w.size() * sizeof(float2));
+    if (e == cudaSuccess) e = cudaMemcpy(o->s12_d, s12.data(), nn * sizeof(float4), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(o->s34_d, s34.data(), nn * sizeof(float4), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(o->idx_d, idx.data(), idx.size() * sizeof(int2), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(o->w_d, w.data(), w.size() * sizeof(float2), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        fft_ocean_free(o);
+        return cuda_fail(ctx, e, "fft ocean allocation");
+    }
+    // the context's wave grid becomes the N x N x 4 readback, zero until the first update
+    std::vector<float> zero(nn * 4, 0.f);
+    const uint32_t ch[2] = {0, 1};
+    const float gs[2] = {params->grid_sizes[0], params->grid_sizes[1]};
+    hydro_status st = hydro_wave_grid_set(ctx, zero.data(), o->N, 4, 2, ch, gs);
+    if (st != HYDRO_OK) {
+        fft_ocean_free(o);
+        return st;
+    }
+    *out = o;
+    return HYDRO_OK;
+}
+
+void hydro_fft_ocean_destroy(hydro_fft_ocean* o)
+{
+    if (!o) return;
+    std::lock_guard<std::recursive_mutex> lk(o->ctx->mu);
+    cudaSetDevice(o->ctx->device);
+    fft_ocean_free(o);
+}
+
+hydro_status hydro_fft_ocean_update(hydro_fft_ocean* o, float t, void* stream)
+{
+    if (!o) return HYDRO_ERR_INVALID_ARG;
+    hydro_ctx* ctx = o->ctx;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (!ctx->wave_d || ctx->wave_n != o->N || ctx->wave_channels != 4)
+        return fail(ctx, HYDRO_ERR_MISMATCH, "fft ocean: the context's wave grid was replaced");
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, HYDRO_ERR_DEVICE, "cudaSetDevice");
+    // inverseGridSizes = 2 pi N / L, evaluated in double and stored as float (OpenGLOcean.cpp:469-472)
+    const double two_pi = 2.0 * 3.14159265358979323846;
+    const float4 ig = make_float4((float)(two_pi * (float)o->N / o->p.grid_sizes[0]),
+                                  (float)(two_pi * (float)o->N / o->p.grid_sizes[1]),
+                                  (float)(two_pi * (float)o->N / o->p.grid_sizes[2]),
+                                  (float)(two_pi * (float)o->N / o->p.grid_sizes[3]));
+    cudaError_t e = launch_fft_ocean(o->s12_d, o->s34_d, o->idx_d, o->w_d, (int)o->p.passes, ig, t,
+                                     reinterpret_cast<float4*>(ctx->wave_d), static_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? HYDRO_OK : cuda_fail(ctx, e, "fft ocean kernels");
+}
+
+hydro_status hydro_fft_ocean_read(hydro_fft_ocean* o, float* out)
+{
+    if (!o || !out) return HYDRO_ERR_INVALID_ARG;
+    hydro_ctx* ctx = o->ctx;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, HYDRO_ERR_DEVICE, "cudaSetDevice");
+    CK(ctx, cudaDeviceSynchronize());
+    CK(ctx, cudaMemcpy(out, ctx->wave_d, (size_t)o->N * o->N * 4 * sizeof(float), cudaMemcpyDeviceToHost));
     return HYDRO_OK;
 }
 

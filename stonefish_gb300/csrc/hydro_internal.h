@@ -136,6 +136,8 @@ cudaError_t launch_compound_step(const KParams& P, const CompoundParams& C, Laun
 cudaError_t launch_cable(const hydro_cable* cables, uint32_t n_cables, uint32_t n_nodes_total, const double* x,
                          const double* v, OceanDev o, SettingsDev st, double* seg, hydro_cable_node_forces* out,
                          unsigned* bad, cudaStream_t s);
+cudaError_t launch_fft_ocean(const float4* s12, const float4* s34, const int2* idx, const float2* w, int passes,
+                             float4 inv_grid, float t, float4* out, cudaStream_t s);
 cudaError_t launch_aero_correct(const hydro_aero_params* p, double* io6, cudaStream_t s);
 
 }  // namespace sfh

@@ -367,3 +367,45 @@ class CompoundBatch:
         _check(self.lib, self.h.ctx, self.lib.hydro_compound_compute_device(self.b, d_compounds, d_parts,
                                                                             C.byref(ocean), C.byref(settings),
                                                                             d_io, stream or None))
+
+
+def fft_ocean_params(state: float = 1.0, passes: int = 8) -> abi.FftOceanParams:
+    """OpenGLRealOcean's parameters for a sea state (hydro_fft_ocean_params_for_state)."""
+    lib = abi.load_library()
+    p = abi.FftOceanParams()
+    lib.hydro_fft_ocean_params_for_state(state, C.byref(p))
+    p.passes = passes
+    return p
+
+
+class FftOcean:
+    """The reference's FFT ocean on the GPU (hydro_fft_ocean_*): writes the
+    context's wave grid; depth queries and wrench steps with ocean.waves = 1
+    then use it."""
+
+    def __init__(self, hctx: HydroContext, params: abi.FftOceanParams):
+        self.h = hctx
+        self.lib = hctx.lib
+        self.N = 1 << params.passes
+        o = C.c_void_p()
+        _check(self.lib, hctx.ctx, self.lib.hydro_fft_ocean_create(hctx.ctx, C.byref(params), C.byref(o)))
+        self.o = o
+
+    def update(self, t: float, stream: int = 0) -> None:
+        _check(self.lib, self.h.ctx, self.lib.hydro_fft_ocean_update(self.o, t, stream or None))
+
+    def read(self) -> np.ndarray:
+        out = np.zeros((self.N, self.N, 4), dtype=np.float32)
+        _check(self.lib, self.h.ctx, self.lib.hydro_fft_ocean_read(self.o, out.ctypes.data))
+        return out
+
+    def close(self) -> None:
+        if self.o:
+            self.lib.hydro_fft_ocean_destroy(self.o)
+            self.o = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
