@@ -445,6 +445,44 @@ hydro_status hydro_compound_compute(hydro_compound_batch* batch, const hydro_bod
                                     const hydro_compound_part* parts, const hydro_ocean* ocean,
                                     const hydro_settings* settings, hydro_wrench* io);
 
+/* ----------------------------------------------------------- mesh ingest */
+/* Mass properties of a physics mesh (ComputePhysicalProperties,
+ * Library/src/utils/GeometryFileUtil.cpp:335-566): solid (thickness <= 0,
+ * signed tetrahedra) or shell (thickness > 0); CG, volume, surface and mass;
+ * Ipri the principal moments about the CG and Irot (rows) the rotation whose
+ * columns are the principal axes (identity when the tensor is diagonal). */
+typedef struct hydro_mesh_properties {
+    double mass;
+    double volume;
+    double surface;
+    double CG[3];
+    double Ipri[3];
+    double Irot[9];
+} hydro_mesh_properties;
+
+/* The face sums on the GPU over the uploaded mesh (one CTA per tile, FP64),
+ * the rest on the host. */
+hydro_status hydro_mesh_compute_properties(hydro_ctx* ctx, hydro_mesh_id mesh, double thickness, double density,
+                                           hydro_mesh_properties* out);
+
+/* OBJ text to the physics mesh the reference builds from it: positions
+ * times scale, every face of every shape, polygons triangulated as
+ * rapidobj::Triangulate does (quads along the shorter diagonal, larger
+ * polygons by ear slicing; LoadOBJ, GeometryFileUtil.cpp:52-230, physics
+ * part), then, when
+ * refine_threshold > 0, OpenGLContent::Refine (OpenGLContent.cpp:2833-2895;
+ * Polyhedron uses 3).  Host only.  Sets *n_vertices and *n_faces; copies
+ * xyz (n_vertices x 3) and faces (n_faces x 3) when the arrays are given
+ * with enough room (capacities in vertices and faces), so a first call
+ * with NULL arrays sizes them. */
+hydro_status hydro_obj_parse(const char* text, size_t len, float scale, float refine_threshold, float* xyz,
+                             uint32_t xyz_capacity, uint32_t* faces, uint32_t faces_capacity, uint32_t* n_vertices,
+                             uint32_t* n_faces);
+
+/* hydro_obj_parse and hydro_mesh_upload in one call. */
+hydro_status hydro_mesh_upload_obj(hydro_ctx* ctx, const char* text, size_t len, float scale, float refine_threshold,
+                                   hydro_mesh_id* out_id);
+
 /* ------------------------------------------------------------- FFT ocean */
 /* The reference's GPU ocean (OpenGLOcean, Library/src/graphics/OpenGLOcean.cpp)
  * as CUDA kernels writing this context's wave grid: Elfouhaily spectrum for

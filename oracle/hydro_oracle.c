@@ -365,6 +365,104 @@ void oracle_correct_forces(const hydro_ocean* ocean, double Fdq[3], double Tdq[3
     correct_one(inv, Tdf, Cf, ocean->density);
 }
 
+/* ---------------------------------------------------------- mesh ingest */
+/* ComputePhysicalProperties (Library/src/utils/GeometryFileUtil.cpp:335-566),
+ * serial FP64 sums as the reference; btVector3's "/ s" multiplies by 1 / s. */
+static void pterms(const double* v1, const double* v2, const double* v3, double* P)
+{
+    double c[3];
+    bcross(v2, v3, c);
+    const double V6 = bdot(v1, c);
+#define SQ(k) (v1[k] * v1[k] + v2[k] * v2[k] + v3[k] * v3[k] + v1[k] * v2[k] + v1[k] * v3[k] + v2[k] * v3[k])
+#define PR(j, k) (2 * (v1[j] * v1[k] + v2[j] * v2[k] + v3[j] * v3[k]) + v1[j] * v2[k] + v1[k] * v2[j] + \
+                  v1[j] * v3[k] + v1[k] * v3[j] + v2[j] * v3[k] + v2[k] * v3[j])
+    P[0] += V6 * 2 * SQ(0);
+    P[1] += V6 * 2 * SQ(1);
+    P[2] += V6 * 2 * SQ(2);
+    P[3] += V6 * PR(0, 1);
+    P[4] += V6 * PR(0, 2);
+    P[5] += V6 * PR(1, 2);
+#undef SQ
+#undef PR
+}
+
+void oracle_mesh_properties(const oracle_mesh* mesh, double thickness, double density, double out[7])
+{
+    double surface = 0.0, volume = 0.0, cg[3] = {0, 0, 0};
+    for (uint32_t i = 0; i < mesh->n_faces; ++i) {
+        double v[3][3];
+        for (int a = 0; a < 3; ++a) {
+            const float* q = mesh->xyz + (size_t)mesh->idx[3 * i + a] * mesh->stride;
+            v[a][0] = q[0]; v[a][1] = q[1]; v[a][2] = q[2];
+        }
+        double e1[3] = {v[1][0] - v[0][0], v[1][1] - v[0][1], v[1][2] - v[0][2]};
+        double e2[3] = {v[2][0] - v[0][0], v[2][1] - v[0][1], v[2][2] - v[0][2]};
+        double n[3];
+        bcross(e1, e2, n);
+        const double A = sqrt(bdot(n, n)) / 2.0;
+        surface += A;
+        if (thickness > 0.0) {
+            const double V = A * thickness;
+            for (int k = 0; k < 3; ++k) cg[k] += ((v[0][k] + v[1][k]) + v[2][k]) * (1.0 / 3.0) * V;
+            volume += V;
+        } else {
+            double c[3];
+            bcross(v[1], v[2], c);
+            const double V6 = bdot(v[0], c);
+            for (int k = 0; k < 3; ++k) cg[k] += ((v[0][k] + v[1][k]) + v[2][k]) * 0.25 * V6;
+            volume += V6;
+        }
+    }
+    if (volume > 0.0) {
+        const double iv = 1.0 / volume;
+        for (int k = 0; k < 3; ++k) cg[k] *= iv;
+    } else {
+        cg[0] = cg[1] = cg[2] = 0.0;
+    }
+    if (!(thickness > 0.0)) volume /= 6.0;
+    double P[6] = {0, 0, 0, 0, 0, 0}, Pi[6] = {0, 0, 0, 0, 0, 0};
+    for (uint32_t i = 0; i < mesh->n_faces; ++i) {
+        double v[3][3];
+        for (int a = 0; a < 3; ++a) {
+            const float* q = mesh->xyz + (size_t)mesh->idx[3 * i + a] * mesh->stride;
+            v[a][0] = q[0]; v[a][1] = q[1]; v[a][2] = q[2];
+        }
+        if (thickness > 0.0) {
+            double e1[3] = {v[1][0] - v[0][0], v[1][1] - v[0][1], v[1][2] - v[0][2]};
+            double e2[3] = {v[2][0] - v[0][0], v[2][1] - v[0][1], v[2][2] - v[0][2]};
+            double n[3];
+            bcross(e1, e2, n);
+            const double il = 1.0 / sqrt(bdot(n, n));
+            const double u[3] = {n[0] * il, n[1] * il, n[2] * il};
+            double o[3][3], in[3][3];
+            for (int a = 0; a < 3; ++a)
+                for (int k = 0; k < 3; ++k) {
+                    o[a][k] = v[a][k] + u[k] * thickness / 2.0 - cg[k];
+                    in[a][k] = v[a][k] - u[k] * thickness / 2.0 - cg[k];
+                }
+            pterms(o[0], o[1], o[2], P);
+            pterms(in[0], in[1], in[2], Pi);
+        } else {
+            double r[3][3];
+            for (int a = 0; a < 3; ++a)
+                for (int k = 0; k < 3; ++k) r[a][k] = v[a][k] - cg[k];
+            pterms(r[0], r[1], r[2], P);
+        }
+    }
+    const double k = density / 120.0;
+    double Ixx = (P[1] * k + P[2] * k), Iyy = (P[0] * k + P[2] * k), Izz = (P[0] * k + P[1] * k);
+    if (thickness > 0.0) {
+        Ixx -= (Pi[1] * k + Pi[2] * k);
+        Iyy -= (Pi[0] * k + Pi[2] * k);
+        Izz -= (Pi[0] * k + Pi[1] * k);
+    }
+    out[0] = volume * density;   /* mass */
+    out[1] = volume;
+    out[2] = surface;
+    out[3] = cg[0]; out[4] = cg[1]; out[5] = cg[2];
+    out[6] = Ixx + Iyy + Izz;    /* trace of the inertia tensor (invariant of the principal axes) */
+}
+
 /* ------------------------------------------------------------- compounds */
 static int fluid_mode(int m) { return m == HYDRO_MODE_FLOATING || m == HYDRO_MODE_SUBMERGED; }
 

@@ -117,6 +117,10 @@ double oracle_batch(int variant, int threads, const hydro_body* bodies,
 
 int oracle_hardware_threads(void);
 
+/* ComputePhysicalProperties (GeometryFileUtil.cpp:335-566): out = mass,
+ * volume, surface, CG[3], trace of the inertia tensor about the CG. */
+void oracle_mesh_properties(const oracle_mesh* mesh, double thickness, double density, double out[7]);
+
 /* The reference's FFT ocean at time t (oracle/fft_ocean.c): N x N x 4 heights. */
 void oracle_fft_ocean(const hydro_fft_ocean_params* params, float t, float* out);
 void oracle_fft_ocean_init_only(const hydro_fft_ocean_params* params, float t, float* out);

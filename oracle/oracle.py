@@ -80,6 +80,8 @@ class Oracle:
                                    P(abi.Settings), vp]
         L.oracle_hardware_threads.restype = i32
         L.oracle_hardware_threads.argtypes = []
+        L.oracle_mesh_properties.restype = None
+        L.oracle_mesh_properties.argtypes = [vp, C.c_double, C.c_double, vp]
         L.oracle_fft_ocean.restype = None
         L.oracle_fft_ocean.argtypes = [P(abi.FftOceanParams), C.c_float, vp]
         L.oracle_fft_ocean_init_only.restype = None
@@ -199,6 +201,14 @@ class Oracle:
         ptrs = [io[k].ctypes.data_as(C.POINTER(C.c_double)) for k in ("Fdq", "Tdq", "Fdf", "Tdf")]
         self.lib.oracle_correct_forces(C.byref(ocean), *ptrs, pcd, pcf, pro)
         return io
+
+    def mesh_properties(self, mesh, thickness: float, density: float) -> dict:
+        """ComputePhysicalProperties: mass, volume, surface, CG and the trace
+        of the inertia tensor about the CG."""
+        m = self.make_mesh(*mesh)
+        out = np.zeros(7)
+        self.lib.oracle_mesh_properties(self._p(m), thickness, density, out.ctypes.data)
+        return {"mass": out[0], "volume": out[1], "surface": out[2], "CG": out[3:6].copy(), "trace": out[6]}
 
     def fft_ocean(self, params, t: float, init_only: bool = False) -> np.ndarray:
         """The reference's FFT ocean at time t: [N, N, 4] float32 (heights of

@@ -71,6 +71,11 @@ class CompoundPart(C.Structure):
                 ("mesh", C.c_uint32), ("mode", C.c_int32), ("buoyant", C.c_int32), ("external", C.c_int32)]
 
 
+class MeshProperties(C.Structure):
+    _fields_ = [("mass", C.c_double), ("volume", C.c_double), ("surface", C.c_double), ("CG", _d3),
+                ("Ipri", _d3), ("Irot", C.c_double * 9)]
+
+
 class FftOceanParams(C.Structure):
     _fields_ = [("wind", C.c_float), ("omega", C.c_float), ("amplitude", C.c_float), ("km", C.c_float),
                 ("cm", C.c_float), ("grid_sizes", C.c_float * 4), ("passes", C.c_uint32), ("propagate", C.c_int32)]
@@ -249,6 +254,10 @@ def _declare(lib: C.CDLL) -> None:
         "hydro_compound_batch_destroy": (None, [vp]),
         "hydro_compound_compute_device": (i32, [vp, vp, vp, C.POINTER(Ocean), C.POINTER(Settings), vp, vp]),
         "hydro_compound_compute": (i32, [vp, vp, vp, C.POINTER(Ocean), C.POINTER(Settings), vp]),
+        "hydro_mesh_compute_properties": (i32, [vp, u32, C.c_double, C.c_double, C.POINTER(MeshProperties)]),
+        "hydro_obj_parse": (i32, [C.c_char_p, C.c_size_t, C.c_float, C.c_float, vp, u32, vp, u32, C.POINTER(u32),
+                                  C.POINTER(u32)]),
+        "hydro_mesh_upload_obj": (i32, [vp, C.c_char_p, C.c_size_t, C.c_float, C.c_float, C.POINTER(u32)]),
         "hydro_fft_ocean_params_for_state": (None, [C.c_float, C.POINTER(FftOceanParams)]),
         "hydro_fft_ocean_create": (i32, [vp, C.POINTER(FftOceanParams), C.POINTER(vp)]),
         "hydro_fft_ocean_destroy": (None, [vp]),
@@ -278,3 +287,20 @@ def exported_symbols_from_header(header: str | None = None) -> list[str]:
     text = open(path).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     return sorted(set(re.findall(r"\b(hydro_[a-z0-9_]+)\s*\(", text)))
+
+
+def obj_parse(text: str, scale: float = 1.0, refine_threshold: float = 0.0, lib_path: str | None = None):
+    """hydro_obj_parse (host only): OBJ text -> (xyz float32 [V,3], faces uint32 [F,3])."""
+    lib = load_library(lib_path)
+    b = text.encode()
+    nv, nf = C.c_uint32(), C.c_uint32()
+    st = lib.hydro_obj_parse(b, len(b), scale, refine_threshold, None, 0, None, 0, C.byref(nv), C.byref(nf))
+    if st != HYDRO_OK:
+        raise HydroError(st, "hydro_obj_parse")
+    xyz = np.zeros((nv.value, 3), dtype=np.float32)
+    faces = np.zeros((nf.value, 3), dtype=np.uint32)
+    st = lib.hydro_obj_parse(b, len(b), scale, refine_threshold, xyz.ctypes.data, nv.value, faces.ctypes.data,
+                             nf.value, C.byref(nv), C.byref(nf))
+    if st != HYDRO_OK:
+        raise HydroError(st, "hydro_obj_parse")
+    return xyz, faces

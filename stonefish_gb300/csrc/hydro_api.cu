@@ -112,6 +112,11 @@ struct hydro_fft_ocean {
 };
 
 namespace sfh {
+bool parse_obj(const char* text, size_t len, float scale, std::vector<float>& xyz, std::vector<uint32_t>& faces,
+               std::string& err);
+void refine_mesh(std::vector<float>& xyz, std::vector<uint32_t>& faces, float threshold);
+void finish_properties(double thickness, double density, const double* s0, const double* s1,
+                       hydro_mesh_properties* out);
 void fft_ocean_spectrum(const hydro_fft_ocean_params& p, std::vector<float4>& s12, std::vector<float4>& s34);
 void fft_ocean_butterfly(int passes, std::vector<int2>& idx, std::vector<float2>& w);
 }
@@ -1039,6 +1044,89 @@ hydro_status hydro_compound_compute(hydro_compound_batch* cb, const hydro_body* 
     if (st != HYDRO_OK) return st;
     CK(ctx, cudaMemcpyAsync(io, cb->io_d, nc * sizeof(hydro_wrench), cudaMemcpyDeviceToHost, s));
     CK(ctx, cudaStreamSynchronize(s));
+    return HYDRO_OK;
+}
+
+// ------------------------------------------------------------ mesh ingest
+hydro_status hydro_obj_parse(const char* text, size_t len, float scale, float refine_threshold, float* xyz,
+                             uint32_t xyz_capacity, uint32_t* faces, uint32_t faces_capacity, uint32_t* n_vertices,
+                             uint32_t* n_faces)
+{
+    if (!text || !n_vertices || !n_faces) return HYDRO_ERR_INVALID_ARG;
+    std::vector<float> v;
+    std::vector<uint32_t> f;
+    std::string err;
+    try {
+        if (!parse_obj(text, len, scale, v, f, err)) return HYDRO_ERR_INVALID_ARG;
+        if (refine_threshold > 0.f) refine_mesh(v, f, refine_threshold);
+    } catch (...) {
+        return HYDRO_ERR_OOM;
+    }
+    if (v.size() / 3 > 0xFFFFFFFFull || f.size() / 3 > 0xFFFFFFFFull) return HYDRO_ERR_INVALID_ARG;
+    *n_vertices = (uint32_t)(v.size() / 3);
+    *n_faces = (uint32_t)(f.size() / 3);
+    if (xyz) {
+        if (xyz_capacity < *n_vertices) return HYDRO_ERR_INVALID_ARG;
+        memcpy(xyz, v.data(), v.size() * sizeof(float));
+    }
+    if (faces) {
+        if (faces_capacity < *n_faces) return HYDRO_ERR_INVALID_ARG;
+        memcpy(faces, f.data(), f.size() * sizeof(uint32_t));
+    }
+    return HYDRO_OK;
+}
+
+hydro_status hydro_mesh_upload_obj(hydro_ctx* ctx, const char* text, size_t len, float scale, float refine_threshold,
+                                   hydro_mesh_id* out_id)
+{
+    if (!ctx) return HYDRO_ERR_INVALID_ARG;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (!text || !out_id) return fail(ctx, HYDRO_ERR_INVALID_ARG, "obj upload: null argument");
+    std::vector<float> v;
+    std::vector<uint32_t> f;
+    std::string err;
+    try {
+        if (!parse_obj(text, len, scale, v, f, err)) return fail(ctx, HYDRO_ERR_INVALID_ARG, "obj: %s", err.c_str());
+        if (refine_threshold > 0.f) refine_mesh(v, f, refine_threshold);
+    } catch (...) {
+        return fail(ctx, HYDRO_ERR_OOM, "obj: host allocation");
+    }
+    return hydro_mesh_upload(ctx, v.data(), 3 * sizeof(float), (uint32_t)(v.size() / 3), f.data(),
+                             (uint32_t)(f.size() / 3), out_id);
+}
+
+hydro_status hydro_mesh_compute_properties(hydro_ctx* ctx, hydro_mesh_id mesh, double thickness, double density,
+                                           hydro_mesh_properties* out)
+{
+    if (!ctx) return HYDRO_ERR_INVALID_ARG;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (!out) return fail(ctx, HYDRO_ERR_INVALID_ARG, "mesh properties: null argument");
+    if (mesh >= ctx->meshes.size()) return fail(ctx, HYDRO_ERR_NOT_FOUND, "unknown mesh %u", mesh);
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, HYDRO_ERR_DEVICE, "cudaSetDevice");
+    hydro_status st = sync_tiles(ctx);
+    if (st != HYDRO_OK) return st;
+    const MeshRec& m = ctx->meshes[mesh];
+    const size_t bytes = (size_t)std::max<uint32_t>(m.n_tiles, 1u) * 12 * sizeof(double);
+    if ((st = ensure_small(ctx, bytes)) != HYDRO_OK) return st;
+    double* d = static_cast<double*>(ctx->small_d);
+    std::vector<double> part((size_t)m.n_tiles * 12);
+    double s0[12] = {0}, s1[12] = {0};
+    for (int pass = 0; pass < 2; ++pass) {
+        double3 cg = make_double3(0.0, 0.0, 0.0);
+        if (pass == 1) {
+            hydro_mesh_properties tmp{};
+            finish_properties(thickness, density, s0, s1, &tmp);
+            cg = make_double3(tmp.CG[0], tmp.CG[1], tmp.CG[2]);
+        }
+        cudaError_t e = launch_mesh_props(ctx->tiles_d, m.first_tile, m.n_tiles, pass, thickness, cg, d, ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "mesh properties kernel");
+        CK(ctx, cudaMemcpyAsync(part.data(), d, part.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(ctx, cudaStreamSynchronize(ctx->stream));
+        double* acc = pass == 0 ? s0 : s1;
+        for (uint32_t t = 0; t < m.n_tiles; ++t)
+            for (int k = 0; k < 12; ++k) acc[k] += part[(size_t)t * 12 + k];
+    }
+    finish_properties(thickness, density, s0, s1, out);
     return HYDRO_OK;
 }
 

@@ -138,6 +138,8 @@ cudaError_t launch_cable(const hydro_cable* cables, uint32_t n_cables, uint32_t 
                          unsigned* bad, cudaStream_t s);
 cudaError_t launch_fft_ocean(const float4* s12, const float4* s34, const int2* idx, const float2* w, int passes,
                              float4 inv_grid, float t, float4* out, cudaStream_t s);
+cudaError_t launch_mesh_props(const TileDesc* tiles, uint32_t first_tile, uint32_t n_tiles, int pass, double thickness,
+                              double3 cg, double* out, cudaStream_t s);
 cudaError_t launch_aero_correct(const hydro_aero_params* p, double* io6, cudaStream_t s);
 
 }  // namespace sfh

@@ -106,6 +106,20 @@ class HydroContext:
         self.mesh_faces[int(mid.value)] = faces.size // 3
         return int(mid.value)
 
+    def upload_obj(self, text: str, scale: float = 1.0, refine_threshold: float = 3.0) -> int:
+        """hydro_mesh_upload_obj: OBJ text -> refined physics mesh on the device."""
+        b = text.encode()
+        mid = C.c_uint32()
+        self._ck(self.lib.hydro_mesh_upload_obj(self.ctx, b, len(b), scale, refine_threshold, C.byref(mid)))
+        return int(mid.value)
+
+    def mesh_properties(self, mesh: int, thickness: float = 0.0, density: float = 1000.0) -> dict:
+        """hydro_mesh_compute_properties (ComputePhysicalProperties)."""
+        p = abi.MeshProperties()
+        self._ck(self.lib.hydro_mesh_compute_properties(self.ctx, mesh, thickness, density, C.byref(p)))
+        return {"mass": p.mass, "volume": p.volume, "surface": p.surface, "CG": np.array(p.CG[:]),
+                "Ipri": np.array(p.Ipri[:]), "Irot": np.array(p.Irot[:]).reshape(3, 3)}
+
     def mesh_info(self, mesh: int) -> tuple[int, int, int]:
         nv, nf, nt = C.c_uint32(), C.c_uint32(), C.c_uint32()
         self._ck(self.lib.hydro_mesh_info(self.ctx, mesh, C.byref(nv), C.byref(nf), C.byref(nt)))
