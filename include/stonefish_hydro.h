@@ -91,6 +91,9 @@ enum {
 #define HYDRO_MAX_CURRENTS 8
 #define HYDRO_MAX_WAVE_LAYERS 4
 #define HYDRO_NO_MESH 0xFFFFFFFFu   /* stands for the reference's mesh == nullptr */
+/* Faces per mesh tile: work chunks (hydro_config.tile_faces, the chunk_faces
+ * of hydro_batch_create_ex and of the autotuner) are whole tiles. */
+#define HYDRO_TILE_FACES 448
 
 typedef uint32_t hydro_mesh_id;
 typedef struct hydro_ctx hydro_ctx;
@@ -206,8 +209,8 @@ typedef struct hydro_wrench {
 typedef struct hydro_config {
     int32_t device;              /* CUDA device ordinal */
     int32_t cut_precision;       /* HYDRO_CUT_FP32 (default) or HYDRO_CUT_FP64 */
-    uint32_t tile_faces;         /* faces per work chunk; 0 = 4096 (hydro_batch_autotune
-                                    picks per batch) */
+    uint32_t tile_faces;         /* faces per work chunk, rounded up to whole tiles;
+                                    0 = 4096 (hydro_batch_autotune picks per batch) */
     uint32_t ctas_per_sm;        /* resident CTAs per SM; 0 = 2 (or the autotuner's) */
     const char* tune_cache_path; /* autotuner cache file (copied), NULL = none */
 } hydro_config;
@@ -329,6 +332,15 @@ hydro_status hydro_batch_autotune(hydro_batch* batch, const hydro_body* d_bodies
 
 /* Number of kernel launches the last compute call enqueued. */
 uint32_t hydro_batch_last_launches(const hydro_batch* batch);
+
+/* Per-kernel device times of a batch's steps (the reference's hydrodynamics
+ * timer, PerformanceMonitor.cpp:80-88, at kernel granularity).  With
+ * profiling on, each hydro_batch_compute(_device) call outside stream
+ * capture records CUDA events around its three kernels on the launch
+ * stream; hydro_batch_kernel_ms waits for the last recorded step and
+ * returns its prep, chunk (face loop) and finalize durations. */
+hydro_status hydro_batch_profile(hydro_batch* batch, int enable);
+hydro_status hydro_batch_kernel_ms(hydro_batch* batch, float* prep_ms, float* chunk_ms, float* finalize_ms);
 
 /* Allocation-free step (no counterpart in the reference).  For callers that
  * cannot allocate device memory while they run: a simulator evaluating the

@@ -15,6 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
 LIB_DIR = os.path.join(HERE, "lib")
 LIB_PATH = os.path.join(LIB_DIR, "libstonefish_hydro.so")
+TILE_FACES = 448   # HYDRO_TILE_FACES: faces per mesh tile, the unit of work chunks
 INCLUDE_DIR = os.path.join(REPO, "include")
 
 # status codes
@@ -223,6 +224,8 @@ def _declare(lib: C.CDLL) -> None:
                                                     vp]),
         "hydro_batch_compute": (i32, [vp, vp, C.POINTER(Ocean), C.POINTER(Settings), vp]),
         "hydro_batch_last_launches": (u32, [vp]),
+        "hydro_batch_profile": (i32, [vp, C.c_int]),
+        "hydro_batch_kernel_ms": (i32, [vp, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float)]),
         "hydro_body_forces": (i32, [vp, vp, C.POINTER(Ocean), C.POINTER(Settings), vp]),
         "hydro_surface_forces": (i32, [vp, C.POINTER(Settings), u32, C.POINTER(Ocean),
                                        C.POINTER(Transform), C.POINTER(Transform), d, d,

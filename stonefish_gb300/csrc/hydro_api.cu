@@ -86,6 +86,8 @@ struct hydro_batch {
     uint32_t ctas_per_sm = 0;    // 0 = the context's setting
     hydro_aero_params* aparams_d = nullptr;   // staging for the host-buffer aerodynamic call
     hydro_aero_wrench* aio_d = nullptr;
+    cudaEvent_t prof_ev[4] = {nullptr, nullptr, nullptr, nullptr};   // per-kernel timing, when enabled
+    bool prof_recorded = false;
 };
 
 struct hydro_compound_batch {
@@ -287,6 +289,8 @@ void batch_free(hydro_batch* b)
     cudaFree(b->io_d);
     cudaFree(b->aparams_d);
     cudaFree(b->aio_d);
+    for (cudaEvent_t ev : b->prof_ev)
+        if (ev) cudaEventDestroy(ev);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
 }
@@ -411,9 +415,16 @@ hydro_status batch_launch(hydro_batch* b, const hydro_body* d_bodies, const hydr
     shape.ctas_per_sm = std::max(1, std::min(want, chunk_kernel_occupancy(cut64, P.ocean.waves, want)));
     shape.grid = ctx->sm_count * shape.ctas_per_sm;
     uint32_t launches = 0;
-    cudaError_t e = launch_step(P, shape, cut64, s, &launches);
+    // kernel timing events (hydro_batch_profile) outside stream capture only
+    cudaEvent_t* ev = nullptr;
+    if (b->prof_ev[0]) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusNone) ev = b->prof_ev;
+    }
+    cudaError_t e = launch_step(P, shape, cut64, s, &launches, ev);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "wrench step launch");
     b->last_launches = launches;
+    if (ev) b->prof_recorded = true;
     return HYDRO_OK;
 }
 
@@ -780,6 +791,43 @@ hydro_status hydro_batch_compute(hydro_batch* b, const hydro_body* bodies, const
 }
 
 uint32_t hydro_batch_last_launches(const hydro_batch* b) { return b ? b->last_launches : 0u; }
+
+hydro_status hydro_batch_profile(hydro_batch* b, int enable)
+{
+    if (!b) return HYDRO_ERR_INVALID_ARG;
+    hydro_ctx* ctx = b->ctx;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, HYDRO_ERR_DEVICE, "cudaSetDevice");
+    if (enable && !b->prof_ev[0]) {
+        for (cudaEvent_t& ev : b->prof_ev) {
+            cudaError_t e = cudaEventCreate(&ev);
+            if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaEventCreate");
+        }
+    } else if (!enable) {
+        for (cudaEvent_t& ev : b->prof_ev) {
+            if (ev) cudaEventDestroy(ev);
+            ev = nullptr;
+        }
+    }
+    b->prof_recorded = false;
+    return HYDRO_OK;
+}
+
+hydro_status hydro_batch_kernel_ms(hydro_batch* b, float* prep_ms, float* chunk_ms, float* finalize_ms)
+{
+    if (!b || !prep_ms || !chunk_ms || !finalize_ms) return HYDRO_ERR_INVALID_ARG;
+    hydro_ctx* ctx = b->ctx;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (!b->prof_ev[0] || !b->prof_recorded)
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "kernel times: profiling off or no step recorded");
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, HYDRO_ERR_DEVICE, "cudaSetDevice");
+    cudaError_t e = cudaEventSynchronize(b->prof_ev[3]);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(prep_ms, b->prof_ev[0], b->prof_ev[1]);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(chunk_ms, b->prof_ev[1], b->prof_ev[2]);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(finalize_ms, b->prof_ev[2], b->prof_ev[3]);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "kernel times");
+    return HYDRO_OK;
+}
 
 hydro_status hydro_body_forces(hydro_ctx* ctx, const hydro_body* body, const hydro_ocean* ocean,
                                const hydro_settings* settings, hydro_wrench* io)

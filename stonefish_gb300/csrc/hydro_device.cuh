@@ -19,10 +19,12 @@
 namespace sfh {
 
 // ------------------------------------------------------------ constants
-constexpr int kBlock = 192;          // compute threads per CTA
+constexpr int kBlock = 224;          // compute threads per CTA (seven warps)
 constexpr int kWarps = kBlock / 32;
-constexpr int kTileFaces = 384;      // max faces per tile (64 per compute warp)
-constexpr int kTileVerts = 384;      // max distinct vertices per tile (< 512: 9-bit indices)
+constexpr int kTileFaces = HYDRO_TILE_FACES;   // max faces per tile (64 per compute warp)
+constexpr int kTileVerts = 448;      // max distinct vertices per tile (< 512: 9-bit indices)
+static_assert(kTileFaces == 64 * kWarps, "a tile gives each compute warp 64 faces");
+static_assert(kTileVerts < 512, "vertex indices are packed in 9 bits");
 constexpr int kQ = 23;               // accumulated quantities per body
 constexpr int kPartialStride = 24;   // doubles per chunk partial (23 + status)
 constexpr int kFlushFaces = 16;      // faces a thread sums in FP32 before a flush

@@ -61,8 +61,10 @@ int chunk_kernel_occupancy(int cut64, int waves, int ctas_per_sm);
 // The batched wrench step: prep (per body), persistent chunk kernel with a
 // TMA-fed tile pipeline, finalise (per body).  `cut64` selects FP64 cut
 // points.  Returns the number of kernels launched in *launches.
+// ev (optional): four events recorded before prep, after prep, after the
+// chunk kernel and after finalize.
 cudaError_t launch_step(const KParams& P, LaunchShape shape, int cut64, cudaStream_t s,
-                        uint32_t* launches);
+                        uint32_t* launches, cudaEvent_t* ev = nullptr);
 
 // Per-face surface-loop terms of one body for the parity tests: out holds
 // n_faces * kQ floats in uploaded face order.  packed = 1 sends pairs of

@@ -774,7 +774,11 @@ __device__ __forceinline__ void consumer(const KParams& P, ChunkSmem& S)
 }
 
 template <bool CUT64, bool WAVES, int MINB>
-__global__ void __launch_bounds__(kThreads, MINB) chunk_kernel(const KParams P)
+// MINB = 2: two CTAs of seven warps per SM put four warps on some SM
+// sub-partition, whose 16K registers then allow 128 per thread.  The cap is
+// given as a register limit rather than a minimum block count, with which
+// ptxas allocates the flat-surface variants without spills.
+__global__ void __launch_bounds__(kThreads) __maxnreg__(MINB == 2 ? 128 : 255) chunk_kernel(const KParams P)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     ChunkSmem& S = *reinterpret_cast<ChunkSmem*>(smem_raw);
@@ -795,30 +799,33 @@ __global__ void __launch_bounds__(kThreads, MINB) chunk_kernel(const KParams P)
 }
 
 // ----------------------------------------------------------- finalise kernel
-// One warp per body: lanes 0..22 add the body's chunk partials in chunk
-// order (FP64), lane 0 finalises.
-__global__ void finalize_kernel(const KParams P)
+// One thread per body: it adds the body's chunk partials in chunk order
+// (FP64, quantity by quantity) and finalises.  GB300 executes FP64 at about
+// two lanes per clock per SM, and a warp instruction costs the same with one
+// active lane as with 32, so the finalisation runs 32 bodies per warp and
+// one warp per CTA, which spreads the bodies over all SMs.
+constexpr int kBodyThreads = 32;
+
+__global__ void __launch_bounds__(kBodyThreads) finalize_kernel(const KParams P)
 {
-    __shared__ double sums[kWarps][32];
-    const int lane = threadIdx.x & 31;
-    const int warp = threadIdx.x >> 5;
-    const uint32_t body = blockIdx.x * kWarps + warp;
-    if (body == 0 && lane == 0) *P.active_end = 0u;   // the chunk kernel has finished with it
+    const uint32_t body = blockIdx.x * kBodyThreads + threadIdx.x;
+    if (body == 0) *P.active_end = 0u;   // the chunk kernel has finished with it
     if (body >= P.n_bodies) return;
     if (P.n_active && body >= *P.n_active) return;
     const BodyParams B = P.bparams[body];
     const BodyInfo bi = P.binfo[body];
-    double s = 0.0;
-    if (B.loop != LOOP_NONE && lane < kQ) {
-        const double* p = P.partials + (size_t)bi.first_chunk * kPartialStride + lane;
-        for (uint32_t c = 0; c < bi.n_chunks; ++c) s += p[(size_t)c * kPartialStride];
+    double S[kQ];
+#pragma unroll
+    for (int k = 0; k < kQ; ++k) S[k] = 0.0;
+    if (B.loop != LOOP_NONE) {
+        const double* p = P.partials + (size_t)bi.first_chunk * kPartialStride;
+        for (uint32_t c = 0; c < bi.n_chunks; ++c, p += kPartialStride) {
+#pragma unroll
+            for (int k = 0; k < kQ; ++k) S[k] += p[k];
+        }
     }
-    sums[warp][lane] = s;
-    __syncwarp();
-    if (lane == 0) {
-        const int status = (*P.err & 1u) ? HYDRO_ERR_TIMEOUT : 0;
-        body_finalize(P, body, B, sums[warp], status);
-    }
+    const int status = (*P.err & 1u) ? HYDRO_ERR_TIMEOUT : 0;
+    body_finalize(P, body, B, S, status);
 }
 
 template <int MINB>
@@ -846,13 +853,15 @@ int chunk_kernel_occupancy(int cut64, int waves, int ctas_per_sm)
 }
 
 cudaError_t launch_step(const KParams& P, LaunchShape shape, int cut64, cudaStream_t s,
-                        uint32_t* launches)
+                        uint32_t* launches, cudaEvent_t* ev)
 {
     *launches = 0;
     if (P.n_bodies == 0) return cudaSuccess;
     cudaError_t e;
-    prep_kernel<<<(P.n_bodies + 127) / 128, 128, 0, s>>>(P);
+    if (ev && (e = cudaEventRecord(ev[0], s))) return e;
+    prep_kernel<<<(P.n_bodies + kBodyThreads - 1) / kBodyThreads, kBodyThreads, 0, s>>>(P);
     if ((e = cudaGetLastError())) return e;
+    if (ev && (e = cudaEventRecord(ev[1], s))) return e;
     int grid = shape.grid;
     if (grid > (int)P.n_chunks) grid = (int)P.n_chunks;
     if (grid < 1) grid = 1;
@@ -861,8 +870,10 @@ cudaError_t launch_step(const KParams& P, LaunchShape shape, int cut64, cudaStre
         return e;
     void* args[] = {const_cast<KParams*>(&P)};
     if ((e = cudaLaunchKernel(k, dim3(grid), dim3(kThreads), args, sizeof(ChunkSmem), s))) return e;
-    finalize_kernel<<<(P.n_bodies + kWarps - 1) / kWarps, kBlock, 0, s>>>(P);
+    if (ev && (e = cudaEventRecord(ev[2], s))) return e;
+    finalize_kernel<<<(P.n_bodies + kBodyThreads - 1) / kBodyThreads, kBodyThreads, 0, s>>>(P);
     if ((e = cudaGetLastError())) return e;
+    if (ev && (e = cudaEventRecord(ev[3], s))) return e;
     *launches = 3;
     return cudaSuccess;
 }
@@ -943,15 +954,13 @@ __device__ __forceinline__ void add3(double* a, const double* b)
     a[2] += b[2];
 }
 
-// One warp per compound: lanes sum each part's chunk partials (FP64, chunk
-// order), lane 0 applies the compound's rules part by part.
-__global__ void compound_finalize_kernel(const KParams P, const CompoundParams C)
+// One thread per compound (FP64 work, as in finalize_kernel): it sums each
+// part's chunk partials (chunk order) and applies the compound's rules part
+// by part.
+__global__ void __launch_bounds__(kBodyThreads) compound_finalize_kernel(const KParams P, const CompoundParams C)
 {
-    __shared__ double sums[kWarps][32];
-    const int lane = threadIdx.x & 31;
-    const int warp = threadIdx.x >> 5;
-    const uint32_t c = blockIdx.x * kWarps + warp;
-    if (c == 0 && lane == 0) *P.active_end = 0u;
+    const uint32_t c = blockIdx.x * kBodyThreads + threadIdx.x;
+    if (c == 0) *P.active_end = 0u;
     if (c >= C.n_compounds) return;
     const hydro_body& cb = C.compounds[c];
     const CompoundInfo ci = C.cinfo[c];
@@ -988,17 +997,19 @@ __global__ void compound_finalize_kernel(const KParams P, const CompoundParams C
         const uint32_t p = ci.first_part + k;
         const BodyParams B = P.bparams[p];
         const BodyInfo bi = P.binfo[p];
-        double s = 0.0;
-        if (B.loop != LOOP_NONE && lane < kQ) {
-            const double* q = P.partials + (size_t)bi.first_chunk * kPartialStride + lane;
-            for (uint32_t j = 0; j < bi.n_chunks; ++j) s += q[(size_t)j * kPartialStride];
+        double S[kQ];
+#pragma unroll
+        for (int q = 0; q < kQ; ++q) S[q] = 0.0;
+        if (B.loop != LOOP_NONE) {
+            const double* pp = P.partials + (size_t)bi.first_chunk * kPartialStride;
+            for (uint32_t j = 0; j < bi.n_chunks; ++j, pp += kPartialStride) {
+#pragma unroll
+                for (int q = 0; q < kQ; ++q) S[q] += pp[q];
+            }
         }
-        sums[warp][lane] = s;
-        __syncwarp();
-        if (lane == 0) {
+        {
             const hydro_compound_part& pt = C.parts[p];
             mismatch |= B.mismatch;
-            const double* S = sums[warp];
             const bool null_mesh = (bi.mesh == HYDRO_NO_MESH);
             if (pos == HYDRO_INSIDE && P.st.damping && pt.external && fluid_mode(pt.mode)) {
                 // ComputeHydrodynamicForcesSubmerged then the part's correction (:337-352)
@@ -1033,9 +1044,8 @@ __global__ void compound_finalize_kernel(const KParams P, const CompoundParams C
                 }
             }
         }
-        __syncwarp();
     }
-    if (lane == 0) {
+    {
         if (pos == HYDRO_OUTSIDE) {                                  // :302-314
             zero3(w.Fb); zero3(w.Tb); zero3(w.Fdq); zero3(w.Tdq); zero3(w.Fdf); zero3(w.Tdf);
             w.Swet = 0.0;
@@ -1057,7 +1067,7 @@ cudaError_t launch_compound_step(const KParams& P, const CompoundParams& C, Laun
     if (C.n_compounds == 0) return cudaSuccess;
     cudaError_t e;
     if (P.n_bodies) {
-        compound_prep_kernel<<<(P.n_bodies + 127) / 128, 128, 0, s>>>(P, C);
+        compound_prep_kernel<<<(P.n_bodies + kBodyThreads - 1) / kBodyThreads, kBodyThreads, 0, s>>>(P, C);
         if ((e = cudaGetLastError())) return e;
         int grid = shape.grid;
         if (grid > (int)P.n_chunks) grid = (int)P.n_chunks;
@@ -1069,7 +1079,8 @@ cudaError_t launch_compound_step(const KParams& P, const CompoundParams& C, Laun
         if ((e = cudaLaunchKernel(k, dim3(grid), dim3(kThreads), args, sizeof(ChunkSmem), s))) return e;
         *launches = 2;
     }
-    compound_finalize_kernel<<<(C.n_compounds + kWarps - 1) / kWarps, kBlock, 0, s>>>(P, C);
+    compound_finalize_kernel<<<(C.n_compounds + kBodyThreads - 1) / kBodyThreads, kBodyThreads, 0, s>>>(
+        P, C);
     if ((e = cudaGetLastError())) return e;
     *launches += 1;
     return cudaSuccess;

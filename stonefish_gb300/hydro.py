@@ -338,6 +338,16 @@ class Batch:
     def last_launches(self) -> int:
         return int(self.lib.hydro_batch_last_launches(self.b))
 
+    def profile(self, enable: bool = True) -> None:
+        """hydro_batch_profile: record per-kernel events on later steps."""
+        _check(self.lib, self.h.ctx, self.lib.hydro_batch_profile(self.b, int(enable)))
+
+    def kernel_ms(self) -> dict:
+        """hydro_batch_kernel_ms: prep, chunk and finalize times of the last step."""
+        a, b, c = C.c_float(), C.c_float(), C.c_float()
+        _check(self.lib, self.h.ctx, self.lib.hydro_batch_kernel_ms(self.b, C.byref(a), C.byref(b), C.byref(c)))
+        return {"prep": a.value, "chunk": b.value, "finalize": c.value}
+
 
 class CompoundBatch:
     """Compounds with fixed part lists (hydro_compound_batch): compound c owns

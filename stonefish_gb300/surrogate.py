@@ -447,7 +447,7 @@ class GatedPredictor:
         dev = sur.dev
         self.bufs = sur._infer_bufs(self.n_pad)
         # one-tile chunks: only the few gated-out hulls are active per call
-        self.batch = hctx_exact.batch(np.full(n, mesh_id, dtype=np.uint32), chunk_faces=384)
+        self.batch = hctx_exact.batch(np.full(n, mesh_id, dtype=np.uint32), chunk_faces=abi.TILE_FACES)
         self.mesh_id = mesh_id
         self.counts = torch.zeros((n + 255) // 256, dtype=torch.int32, device=dev)
         self.packed = torch.zeros(n * abi.BODY_DTYPE.itemsize, dtype=torch.uint8, device=dev)

@@ -118,3 +118,10 @@ def test_product_does_not_reference_oracle():
                 assert "import oracle" not in text and "from oracle" not in text, f
                 assert "hydro_oracle" not in text, f
     assert os.path.isdir(os.path.join(root, "oracle"))
+
+
+def test_tile_size_constant_matches_header():
+    import re
+    with open(os.path.join(abi.INCLUDE_DIR, "stonefish_hydro.h")) as fh:
+        m = re.search(r"#define HYDRO_TILE_FACES (\d+)", fh.read())
+    assert m and int(m.group(1)) == abi.TILE_FACES

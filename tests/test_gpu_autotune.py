@@ -31,7 +31,7 @@ def test_autotune_picks_a_candidate_and_caches_it(built_library, tmp_path):
     d_s = torch.zeros(len(bodies) * abi.WRENCH_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
     r = b.autotune(d_b.data_ptr(), sc["ocean"], st, d_s.data_ptr(), reps=2)
     assert not r["from_cache"]
-    assert r["chunk_faces"] in (768, 1536, 3072, 4224, 6144)
+    assert r["chunk_faces"] in tuple(t * abi.TILE_FACES for t in (2, 4, 8, 11, 16))
     assert r["ctas_per_sm"] in (1, 2)
     assert len(r["candidate_ms"]) == 10 and min(r["candidate_ms"]) == pytest.approx(r["ms_per_step"])
     after = scenarios.new_wrenches(len(bodies))
@@ -51,4 +51,33 @@ def test_autotune_picks_a_candidate_and_caches_it(built_library, tmp_path):
     assert again.tobytes() == after.tobytes()
     b.close()
     b2.close()
+    h.close()
+
+
+def test_kernel_timing_events_leave_results_unchanged(built_library):
+    from stonefish_gb300.hydro import HydroContext
+
+    h = HydroContext(0)
+    sc = scenarios.mixed_batch(n_bodies=48, seed=5, scale_faces=0.05)
+    ids = np.asarray([h.upload_mesh(x, f) for x, f in sc["meshes"]], dtype=np.uint32)[sc["bodies"]["mesh"]]
+    bodies = sc["bodies"].copy()
+    bodies["mesh"] = ids
+    st = scenarios.settings()
+    b = h.batch(ids)
+    with pytest.raises(abi.HydroError):
+        b.kernel_ms()                       # profiling off
+    plain = scenarios.new_wrenches(len(bodies))
+    b.compute(bodies, sc["ocean"], st, plain)
+    b.profile(True)
+    with pytest.raises(abi.HydroError):
+        b.kernel_ms()                       # no step recorded yet
+    timed = scenarios.new_wrenches(len(bodies))
+    b.compute(bodies, sc["ocean"], st, timed)
+    t = b.kernel_ms()
+    assert t["prep"] > 0 and t["chunk"] > 0 and t["finalize"] > 0
+    assert timed.tobytes() == plain.tobytes()
+    b.profile(False)
+    with pytest.raises(abi.HydroError):
+        b.kernel_ms()
+    b.close()
     h.close()

@@ -297,7 +297,7 @@ def test_host_and_device_entry_points_agree(hctx):
     bt.close()
 
 
-@pytest.mark.parametrize("chunk_faces", [384, 1536])
+@pytest.mark.parametrize("chunk_faces", [abi.TILE_FACES, 4 * abi.TILE_FACES])
 def test_prefix_entry_and_chunk_size(hctx, chunk_faces):
     """hydro_batch_compute_device_prefix evaluates exactly the first *count
     bodies (bit-identical to a full step of those bodies) and leaves the rest
