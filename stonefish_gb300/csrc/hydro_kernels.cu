@@ -539,6 +539,8 @@ struct __align__(128) StageBuf {
 struct __align__(128) ChunkSmem {
     StageBuf stage[kStages];
     float4 verts[2][kTileVerts];      // transformed vertices, double-buffered
+    uint32_t tflags[2][8];            // per-warp vertex votes of each vertex buffer (bit 0 above, bit 1 under)
+    static_assert(kWarps <= 8, "one vote slot per compute warp");
     float2 red[kWarps][32];
     uint16_t flist[kWarps][64];       // per-warp compacted face lists
     ItemMeta meta[kStages];
@@ -609,28 +611,34 @@ __device__ __forceinline__ void producer(const KParams& P, ChunkSmem& S)
 }
 
 // Transforms the vertices of the tile in stage `st` into `out` (x, y, z,
-// depth), each vertex once.
+// depth), each vertex once, and records per warp whether any of its
+// vertices is above water (depth < 0, bit 0) or not (bit 1).
 template <bool WAVES>
 __device__ __forceinline__ void transform_tile(const KParams& P, const StageBuf& st, const ItemMeta& m,
-                                               float4* out)
+                                               float4* out, uint32_t* flags)
 {
     const float* raw = reinterpret_cast<const float*>(st.raw);
     const int nv = m.nv, nvp = (nv + 3) & ~3;
     float TC[12];
 #pragma unroll
     for (int k = 0; k < 12; ++k) TC[k] = st.bp.TC[k];
+    bool above = false, under = false;
     for (int v = threadIdx.x; v < nv; v += kBlock) {
         v3 p = xform(TC, raw[v], raw[nvp + v], raw[2 * nvp + v]);
         float d = WAVES ? depth_at(P.ocean, p.x, p.y, p.z) : p.z;
         out[v] = make_float4(p.x, p.y, p.z, d);
+        above |= d < 0.f;
+        under |= !(d < 0.f);
     }
+    const unsigned a = __ballot_sync(0xffffffffu, above), u = __ballot_sync(0xffffffffu, under);
+    if ((threadIdx.x & 31) == 0) flags[threadIdx.x >> 5] = (a ? 1u : 0u) | (u ? 2u : 0u);
 }
 
 // Faces of one tile: per-warp compaction, then the packed path for pairs of
 // fully submerged faces and the scalar path for straddling faces.
 template <bool CUT64, bool WAVES>
 __device__ __forceinline__ void tile_faces(const KParams& P, const StageBuf& st, const ItemMeta& m,
-                                           const float4* verts, uint16_t* list, Acc& acc)
+                                           const float4* verts, const uint32_t* flags, uint16_t* list, Acc& acc)
 {
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
@@ -655,38 +663,56 @@ __device__ __forceinline__ void tile_faces(const KParams& P, const StageBuf& st,
         }
         return;
     }
+    // Tiles of the surface loop wholly on one side of the surface: above
+    // water every face is skipped (:1353-1354), under water every face is
+    // fully submerged, as in the submerged loop.
+    bool all_under = Bl.loop != LOOP_SURFACE;
+    if (!all_under) {
+        const uint4 f0 = *reinterpret_cast<const uint4*>(flags);
+        const uint4 f1 = *reinterpret_cast<const uint4*>(flags + 4);
+        const uint32_t tf = f0.x | f0.y | f0.z | f0.w | f1.x | f1.y | f1.z | f1.w;
+        if (!(tf & 2u)) return;
+        all_under = !(tf & 1u);
+    }
     // Warp w takes faces (k*32 + lane)*kWarps + w, k = 0, 1: a spread sample
-    // of the tile, so that the warps get similar work.  Its faces are
-    // compacted (deterministically, by ballot) into a list of fully
-    // submerged faces and a list of straddling faces.  The first list is
-    // evaluated two faces per lane on the packed FP32 pipe (faces
-    // list[lane] and list[lane + 32]), the second face by face.
+    // of the tile, so that the warps get similar work.  Unless they are all
+    // under water, its faces are compacted (deterministically, by ballot)
+    // into a list of fully submerged faces and a list of straddling faces.
+    // The fully submerged faces are evaluated two per lane on the packed
+    // FP32 pipe (faces list[lane] and list[lane + 32]), the straddling ones
+    // face by face.
     int nfull = 0, ncut = 0;
-    const unsigned lt = (1u << lane) - 1u;
+    int fa = lane * kWarps + warp, fb = (lane + 32) * kWarps + warp;
+    if (all_under) {
+        // faces j * kWarps + warp, j < nfull, exist: fa for lane < nfull, fb for lane + 32 < nfull
+        nfull = nf > warp ? min(64, (nf - warp + kWarps - 1) / kWarps) : 0;
+    } else {
+        const unsigned lt = (1u << lane) - 1u;
 #pragma unroll
-    for (int k = 0; k < 2; ++k) {
-        const int f = (k * 32 + lane) * kWarps + warp;
-        int cls = 0;
-        if (f < nf) {
-            if (Bl.loop == LOOP_SURFACE) {
+        for (int k = 0; k < 2; ++k) {
+            const int f = k == 0 ? fa : fb;
+            int cls = 0;
+            if (f < nf) {
                 const uint32_t w = idx[f];
                 cls = face_class(verts[w & 511u].w, verts[(w >> 9) & 511u].w, verts[w >> 18].w);
-            } else {
-                cls = 1;
             }
+            const unsigned mf = __ballot_sync(0xffffffffu, cls == 1);
+            const unsigned mc = __ballot_sync(0xffffffffu, cls == 2);
+            if (cls == 1) list[nfull + __popc(mf & lt)] = (uint16_t)f;
+            if (cls == 2) list[63 - (ncut + __popc(mc & lt))] = (uint16_t)f;
+            nfull += __popc(mf);
+            ncut += __popc(mc);
         }
-        const unsigned mf = __ballot_sync(0xffffffffu, cls == 1);
-        const unsigned mc = __ballot_sync(0xffffffffu, cls == 2);
-        if (cls == 1) list[nfull + __popc(mf & lt)] = (uint16_t)f;
-        if (cls == 2) list[63 - (ncut + __popc(mc & lt))] = (uint16_t)f;
-        nfull += __popc(mf);
-        ncut += __popc(mc);
+        __syncwarp();
+        if (lane < nfull) {
+            fa = list[lane];
+            fb = list[lane + 32 < nfull ? lane + 32 : lane];
+        }
     }
-    __syncwarp();
     if (lane < nfull) {
         const bool hasB = lane + 32 < nfull;
-        const uint32_t wa = idx[list[lane]];
-        const uint32_t wb = idx[list[hasB ? lane + 32 : lane]];
+        const uint32_t wa = idx[fa];
+        const uint32_t wb = idx[hasB ? fb : fa];
         const P3 p1 = corners(verts[wa & 511u], verts[wb & 511u]);
         const P3 p2 = corners(verts[(wa >> 9) & 511u], verts[(wb >> 9) & 511u]);
         const P3 p3 = corners(verts[wa >> 18], verts[wb >> 18]);
@@ -728,20 +754,21 @@ __device__ __forceinline__ void consumer(const KParams& P, ChunkSmem& S)
     // first tile
     bool ok = mbar_wait(&S.full[0], 0u);
     ItemMeta m = S.meta[0];
-    if (ok && !(m.flags & ITEM_END)) transform_tile<WAVES>(P, S.stage[0], m, S.verts[0]);
+    if (ok && !(m.flags & ITEM_END)) transform_tile<WAVES>(P, S.stage[0], m, S.verts[0], S.tflags[0]);
     if (!consumer_all(ok)) {
         if (tid == 0) atomicOr(P.err, 1u);
         return;
     }
     for (uint32_t item = 0; !(m.flags & ITEM_END); ++item) {
         const int s = (int)(item % kStages);
-        tile_faces<CUT64, WAVES>(P, S.stage[s], m, S.verts[item & 1u], S.flist[warp], acc);
+        tile_faces<CUT64, WAVES>(P, S.stage[s], m, S.verts[item & 1u], S.tflags[item & 1u], S.flist[warp], acc);
         // next tile: wait, read its metadata, transform its vertices
         const uint32_t nx = item + 1u;
         const int sn = (int)(nx % kStages);
         ok = mbar_wait(&S.full[sn], (nx / kStages) & 1u);
         const ItemMeta mn = S.meta[sn];
-        if (ok && !(mn.flags & ITEM_END)) transform_tile<WAVES>(P, S.stage[sn], mn, S.verts[nx & 1u]);
+        if (ok && !(mn.flags & ITEM_END))
+            transform_tile<WAVES>(P, S.stage[sn], mn, S.verts[nx & 1u], S.tflags[nx & 1u]);
         if (!consumer_all(ok)) {
             if (tid == 0) atomicOr(P.err, 1u);
             return;
@@ -773,15 +800,16 @@ __device__ __forceinline__ void consumer(const KParams& P, ChunkSmem& S)
     }
 }
 
-template <bool CUT64, bool WAVES, int MINB>
-// MINB = 2: two CTAs of seven warps per SM put four warps on some SM
+// MINB = 2: two CTAs of eight warps per SM put four warps on each SM
 // sub-partition, whose 16K registers then allow 128 per thread.  The cap is
 // given as a register limit rather than a minimum block count, with which
 // ptxas allocates the flat-surface variants without spills.
+template <bool CUT64, bool WAVES, int MINB>
 __global__ void __launch_bounds__(kThreads) __maxnreg__(MINB == 2 ? 128 : 255) chunk_kernel(const KParams P)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     ChunkSmem& S = *reinterpret_cast<ChunkSmem*>(smem_raw);
+    if (threadIdx.x < 16) (&S.tflags[0][0])[threadIdx.x] = 0u;   // slots of absent warps stay 0
     const int tid = threadIdx.x;
     if (tid == kBlock) {
         for (int s = 0; s < kStages; ++s) {
