@@ -29,13 +29,6 @@
 #include "hydro_internal.h"
 #include "hydro_pair.cuh"
 
-// Tiles between flushes of a thread's FP32 runs: at most 4 faces per tile
-// and thread, so 4 tiles keep every FP32 run at or below 16 faces.  (Runs
-// of 8 faces measured 3 % slower on the mixed batch for a change of 1.6e-7
-// of the force scale.)
-#ifndef HYDRO_FLUSH_TILES
-#define HYDRO_FLUSH_TILES 4
-#endif
 
 namespace sfh {
 
@@ -521,6 +514,16 @@ __global__ void prep_kernel(const KParams P)
 constexpr int kStages = 8;
 constexpr int kStageRaw = kTileVerts * 12 + kTileFaces * 4;   // 6144 bytes
 constexpr int kThreads = kBlock + 32;
+// Straddling faces wait in a per-warp queue until 32 of them (or the end of
+// the chunk) fill one pass of the scalar clipping path: at most 31 wait
+// while a tile adds up to 64.
+constexpr int kCutQueue = 96;
+
+__device__ __forceinline__ int wrap_queue(int x)
+{
+    x = x >= kCutQueue ? x - kCutQueue : x;
+    return x >= kCutQueue ? x - kCutQueue : x;
+}
 
 enum : int { ITEM_FIRST = 1, ITEM_LAST = 2, ITEM_END = 4 };
 
@@ -543,6 +546,7 @@ struct __align__(128) ChunkSmem {
     static_assert(kWarps <= 8, "one vote slot per compute warp");
     float2 red[kWarps][32];
     uint16_t flist[kWarps][64];       // per-warp compacted face lists
+    float4 cutq[kWarps][kCutQueue][3];  // per-warp queues of straddling faces (corners with depth)
     ItemMeta meta[kStages];
     uint64_t full[kStages];
     uint64_t empty[kStages];
@@ -634,11 +638,20 @@ __device__ __forceinline__ void transform_tile(const KParams& P, const StageBuf&
     if ((threadIdx.x & 31) == 0) flags[threadIdx.x >> 5] = (a ? 1u : 0u) | (u ? 2u : 0u);
 }
 
+// Per-warp queue of straddling faces: head slot and length (warp-uniform).
+struct CutQueue {
+    float4 (*q)[3];
+    int head, len;
+};
+
 // Faces of one tile: per-warp compaction, then the packed path for pairs of
-// fully submerged faces and the scalar path for straddling faces.
+// fully submerged faces; straddling faces join the warp's queue, which runs
+// the scalar path 32 at a time (and empties when `drain`).  Returns the
+// number of faces each lane added at most (pairs count two, a pass one).
 template <bool CUT64, bool WAVES>
-__device__ __forceinline__ void tile_faces(const KParams& P, const StageBuf& st, const ItemMeta& m,
-                                           const float4* verts, const uint32_t* flags, uint16_t* list, Acc& acc)
+__device__ __forceinline__ int tile_faces(const KParams& P, const StageBuf& st, const ItemMeta& m,
+                                          const float4* verts, const uint32_t* flags, uint16_t* list,
+                                          CutQueue& cq, bool drain, Acc& acc)
 {
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
@@ -661,74 +674,90 @@ __device__ __forceinline__ void tile_faces(const KParams& P, const StageBuf& st,
                 face_aero(P.ocean, Bl, acc, mk(q1.x, q1.y, q1.z), mk(q2.x, q2.y, q2.z), mk(q3.x, q3.y, q3.z));
             }
         }
-        return;
+        return 2;
     }
+    int added = 0;
     // Tiles of the surface loop wholly on one side of the surface: above
     // water every face is skipped (:1353-1354), under water every face is
     // fully submerged, as in the submerged loop.
-    bool all_under = Bl.loop != LOOP_SURFACE;
+    bool all_under = Bl.loop != LOOP_SURFACE, any_under = true;
     if (!all_under) {
         const uint4 f0 = *reinterpret_cast<const uint4*>(flags);
         const uint4 f1 = *reinterpret_cast<const uint4*>(flags + 4);
         const uint32_t tf = f0.x | f0.y | f0.z | f0.w | f1.x | f1.y | f1.z | f1.w;
-        if (!(tf & 2u)) return;
         all_under = !(tf & 1u);
+        any_under = (tf & 2u) != 0u;
     }
-    // Warp w takes faces (k*32 + lane)*kWarps + w, k = 0, 1: a spread sample
-    // of the tile, so that the warps get similar work.  Unless they are all
-    // under water, its faces are compacted (deterministically, by ballot)
-    // into a list of fully submerged faces and a list of straddling faces.
-    // The fully submerged faces are evaluated two per lane on the packed
-    // FP32 pipe (faces list[lane] and list[lane + 32]), the straddling ones
-    // face by face.
-    int nfull = 0, ncut = 0;
-    int fa = lane * kWarps + warp, fb = (lane + 32) * kWarps + warp;
-    if (all_under) {
-        // faces j * kWarps + warp, j < nfull, exist: fa for lane < nfull, fb for lane + 32 < nfull
-        nfull = nf > warp ? min(64, (nf - warp + kWarps - 1) / kWarps) : 0;
-    } else {
-        const unsigned lt = (1u << lane) - 1u;
+    if (any_under) {
+        // Warp w takes faces (k*32 + lane)*kWarps + w, k = 0, 1: a spread sample
+        // of the tile, so that the warps get similar work.  Unless they are all
+        // under water, its faces are compacted (deterministically, by ballot)
+        // into a list of fully submerged faces and a list of straddling faces.
+        // The fully submerged faces are evaluated two per lane on the packed
+        // FP32 pipe (faces list[lane] and list[lane + 32]), the straddling ones
+        // face by face.
+        int nfull = 0, ncut = 0;
+        int fa = lane * kWarps + warp, fb = (lane + 32) * kWarps + warp;
+        if (all_under) {
+            // faces j * kWarps + warp, j < nfull, exist: fa for lane < nfull, fb for lane + 32 < nfull
+            nfull = nf > warp ? min(64, (nf - warp + kWarps - 1) / kWarps) : 0;
+        } else {
+            const unsigned lt = (1u << lane) - 1u;
 #pragma unroll
-        for (int k = 0; k < 2; ++k) {
-            const int f = k == 0 ? fa : fb;
-            int cls = 0;
-            if (f < nf) {
-                const uint32_t w = idx[f];
-                cls = face_class(verts[w & 511u].w, verts[(w >> 9) & 511u].w, verts[w >> 18].w);
+            for (int k = 0; k < 2; ++k) {
+                const int f = k == 0 ? fa : fb;
+                int cls = 0;
+                uint32_t w = 0;
+                if (f < nf) {
+                    w = idx[f];
+                    cls = face_class(verts[w & 511u].w, verts[(w >> 9) & 511u].w, verts[w >> 18].w);
+                }
+                const unsigned mf = __ballot_sync(0xffffffffu, cls == 1);
+                const unsigned mc = __ballot_sync(0xffffffffu, cls == 2);
+                if (cls == 1) list[nfull + __popc(mf & lt)] = (uint16_t)f;
+                if (cls == 2) {
+                    float4* e = cq.q[wrap_queue(cq.head + cq.len + ncut + __popc(mc & lt))];
+                    e[0] = verts[w & 511u];
+                    e[1] = verts[(w >> 9) & 511u];
+                    e[2] = verts[w >> 18];
+                }
+                nfull += __popc(mf);
+                ncut += __popc(mc);
             }
-            const unsigned mf = __ballot_sync(0xffffffffu, cls == 1);
-            const unsigned mc = __ballot_sync(0xffffffffu, cls == 2);
-            if (cls == 1) list[nfull + __popc(mf & lt)] = (uint16_t)f;
-            if (cls == 2) list[63 - (ncut + __popc(mc & lt))] = (uint16_t)f;
-            nfull += __popc(mf);
-            ncut += __popc(mc);
+            cq.len += ncut;
+            __syncwarp();
+            if (lane < nfull) {
+                fa = list[lane];
+                fb = list[lane + 32 < nfull ? lane + 32 : lane];
+            }
         }
-        __syncwarp();
         if (lane < nfull) {
-            fa = list[lane];
-            fb = list[lane + 32 < nfull ? lane + 32 : lane];
+            const bool hasB = lane + 32 < nfull;
+            const uint32_t wa = idx[fa];
+            const uint32_t wb = idx[hasB ? fb : fa];
+            const P3 p1 = corners(verts[wa & 511u], verts[wb & 511u]);
+            const P3 p2 = corners(verts[(wa >> 9) & 511u], verts[(wb >> 9) & 511u]);
+            const P3 p3 = corners(verts[wa >> 18], verts[wb >> 18]);
+            const BodyPair Bp = body_pair(Bl, P.ocean);
+            if (Bl.loop == LOOP_SURFACE) face_full2<WAVES>(P.ocean, Bl, Bp, acc, p1, p2, p3, hasB);
+            else face_submerged2(P.ocean, Bp, acc, p1, p2, p3, hasB);
         }
+        if (nfull > 0) added = 2;
     }
-    if (lane < nfull) {
-        const bool hasB = lane + 32 < nfull;
-        const uint32_t wa = idx[fa];
-        const uint32_t wb = idx[hasB ? fb : fa];
-        const P3 p1 = corners(verts[wa & 511u], verts[wb & 511u]);
-        const P3 p2 = corners(verts[(wa >> 9) & 511u], verts[(wb >> 9) & 511u]);
-        const P3 p3 = corners(verts[wa >> 18], verts[wb >> 18]);
-        const BodyPair Bp = body_pair(Bl, P.ocean);
-        if (Bl.loop == LOOP_SURFACE) face_full2<WAVES>(P.ocean, Bl, Bp, acc, p1, p2, p3, hasB);
-        else face_submerged2(P.ocean, Bp, acc, p1, p2, p3, hasB);
+    while (cq.len >= 32 || (drain && cq.len > 0)) {
+        const int n = cq.len < 32 ? cq.len : 32;
+        if (lane < n) {
+            const float4* e = cq.q[wrap_queue(cq.head + lane)];
+            const float4 q1 = e[0], q2 = e[1], q3 = e[2];
+            face_cut<CUT64, WAVES>(P.ocean, Bl, acc, mk(q1.x, q1.y, q1.z), mk(q2.x, q2.y, q2.z),
+                                   mk(q3.x, q3.y, q3.z), q1.w, q2.w, q3.w);
+        }
+        cq.head = wrap_queue(cq.head + n);
+        cq.len -= n;
+        ++added;
+        __syncwarp();
     }
-    for (int i = lane; i < ncut; i += 32) {
-        const uint32_t w = idx[list[63 - i]];
-        const float4 q1 = verts[w & 511u];
-        const float4 q2 = verts[(w >> 9) & 511u];
-        const float4 q3 = verts[w >> 18];
-        face_cut<CUT64, WAVES>(P.ocean, Bl, acc, mk(q1.x, q1.y, q1.z), mk(q2.x, q2.y, q2.z),
-                               mk(q3.x, q3.y, q3.z), q1.w, q2.w, q3.w);
-    }
-    __syncwarp();
+    return added;
 }
 
 // Compute warps.  Iteration i evaluates the faces of tile i and transforms
@@ -745,11 +774,12 @@ __device__ __forceinline__ void consumer(const KParams& P, ChunkSmem& S)
 #pragma unroll
     for (int k = 0; k < kQ; ++k) acc.q[k] = 0.f;
     float hi = 0.f, lo = 0.f;
-    int tiles_since_flush = 0;
-    // A thread adds at most two paired faces and two straddling faces per
-    // tile; a flush every kFlushTiles tiles keeps its FP32 runs short (at
-    // most kFlushFaces faces).
-    constexpr int kFlushTiles = HYDRO_FLUSH_TILES;
+    // A tile adds at most five faces to a lane's run (a pair and three
+    // queue passes: up to 95 queued faces, the last one drained), so a
+    // flush once a run has reached kFlushFaces - 4 keeps every FP32 run at
+    // or below kFlushFaces faces.
+    int run = 0;
+    CutQueue cq{S.cutq[warp], 0, 0};
 
     // first tile
     bool ok = mbar_wait(&S.full[0], 0u);
@@ -761,7 +791,9 @@ __device__ __forceinline__ void consumer(const KParams& P, ChunkSmem& S)
     }
     for (uint32_t item = 0; !(m.flags & ITEM_END); ++item) {
         const int s = (int)(item % kStages);
-        tile_faces<CUT64, WAVES>(P, S.stage[s], m, S.verts[item & 1u], S.tflags[item & 1u], S.flist[warp], acc);
+        const bool last = (m.flags & ITEM_LAST) != 0;
+        run += tile_faces<CUT64, WAVES>(P, S.stage[s], m, S.verts[item & 1u], S.tflags[item & 1u], S.flist[warp],
+                                        cq, last, acc);
         // next tile: wait, read its metadata, transform its vertices
         const uint32_t nx = item + 1u;
         const int sn = (int)(nx % kStages);
@@ -774,10 +806,9 @@ __device__ __forceinline__ void consumer(const KParams& P, ChunkSmem& S)
             return;
         }
         if (tid == 0) mbar_arrive(&S.empty[s]);
-        const bool last = (m.flags & ITEM_LAST) != 0;
-        if (last || ++tiles_since_flush == kFlushTiles) {
+        if (last || run > kFlushFaces - 5) {
             flush(acc, hi, lo);
-            tiles_since_flush = 0;
+            run = 0;
         }
         if (last) {
             S.red[warp][lane] = make_float2(hi, lo);
