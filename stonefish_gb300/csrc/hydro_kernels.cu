@@ -253,8 +253,11 @@ __device__ void aero_finalize(const KParams& P, uint32_t body, const BodyParams&
 }
 
 // Finalisation of one body from its FP64 sums S (kQ values).
+// With `defer` set, the four damping vectors are written uncorrected and
+// *correct tells whether CorrectHydrodynamicForces applies to them: each of
+// them is then correct_one of its sum in S (zero sums for a null mesh).
 __device__ void body_finalize(const KParams& P, uint32_t body, const BodyParams& B,
-                              const double* S, int status)
+                              const double* S, int status, bool defer = false, bool* correct = nullptr)
 {
     if (P.op == OP_AERO || P.op == OP_AERO_BODY) {
         aero_finalize(P, body, B, S, status);
@@ -323,8 +326,10 @@ __device__ void body_finalize(const KParams& P, uint32_t body, const BodyParams&
                 finalize_surface(P.ocean, B.buoyancy, B.damping, b->T_CG.origin,
                                  (double)B.p0.x, (double)B.p0.y, S, w);
             }
-            if (B.damping)
-                correct4(P.ocean.density, w.Fdq, w.Tdq, w.Fdf, w.Tdf, b->Cd, b->Cf, b->R_O);
+            if (B.damping) {
+                if (defer) *correct = true;
+                else correct4(P.ocean.density, w.Fdq, w.Tdq, w.Fdf, w.Tdf, b->Cd, b->Cf, b->R_O);
+            }
         }
     }
     w.status = status;
@@ -858,33 +863,56 @@ __global__ void __launch_bounds__(kThreads) __maxnreg__(MINB == 2 ? 128 : 255) c
 }
 
 // ----------------------------------------------------------- finalise kernel
-// One thread per body: it adds the body's chunk partials in chunk order
-// (FP64, quantity by quantity) and finalises.  GB300 executes FP64 at about
-// two lanes per clock per SM, and a warp instruction costs the same with one
-// active lane as with 32, so the finalisation runs 32 bodies per warp and
-// one warp per CTA, which spreads the bodies over all SMs.
+// Four threads per body.  GB300 executes FP64 at about two lanes per clock
+// per SM and the finalisation is a chain of dependent FP64 operations, so
+// the work of a body is split: thread k of the group adds quantities
+// k, k + 4, ... of the chunk partials in chunk order, thread 0 finalises,
+// and threads 0..3 apply CorrectHydrodynamicForces to one damping vector
+// each (SolidEntity.cpp:1263-1287).  Warp-sized CTAs spread the bodies over
+// all SMs.
 constexpr int kBodyThreads = 32;
+constexpr int kFinSub = 4;
 
 __global__ void __launch_bounds__(kBodyThreads) finalize_kernel(const KParams P)
 {
-    const uint32_t body = blockIdx.x * kBodyThreads + threadIdx.x;
-    if (body == 0) *P.active_end = 0u;   // the chunk kernel has finished with it
-    if (body >= P.n_bodies) return;
-    if (P.n_active && body >= *P.n_active) return;
-    const BodyParams B = P.bparams[body];
-    const BodyInfo bi = P.binfo[body];
-    double S[kQ];
-#pragma unroll
-    for (int k = 0; k < kQ; ++k) S[k] = 0.0;
-    if (B.loop != LOOP_NONE) {
-        const double* p = P.partials + (size_t)bi.first_chunk * kPartialStride;
-        for (uint32_t c = 0; c < bi.n_chunks; ++c, p += kPartialStride) {
-#pragma unroll
-            for (int k = 0; k < kQ; ++k) S[k] += p[k];
+    __shared__ double sums[kBodyThreads / kFinSub][kPartialStride];
+    const uint32_t gt = blockIdx.x * kBodyThreads + threadIdx.x;
+    const uint32_t body = gt / kFinSub;
+    const int sub = (int)(gt % kFinSub), slot = (int)(threadIdx.x / kFinSub);
+    if (gt == 0) *P.active_end = 0u;   // the chunk kernel has finished with it
+    const bool live = body < P.n_bodies && !(P.n_active && body >= *P.n_active);
+    BodyParams B{};
+    if (live) {
+        B = P.bparams[body];
+        const BodyInfo bi = P.binfo[body];
+        for (int q = sub; q < kQ; q += kFinSub) {
+            double s = 0.0;
+            if (B.loop != LOOP_NONE) {
+                const double* p = P.partials + (size_t)bi.first_chunk * kPartialStride + q;
+                for (uint32_t c = 0; c < bi.n_chunks; ++c, p += kPartialStride) s += *p;
+            }
+            sums[slot][q] = s;
         }
     }
-    const int status = (*P.err & 1u) ? HYDRO_ERR_TIMEOUT : 0;
-    body_finalize(P, body, B, S, status);
+    __syncwarp();
+    bool correct = false;
+    if (live && sub == 0) {
+        const int status = (*P.err & 1u) ? HYDRO_ERR_TIMEOUT : 0;
+        body_finalize(P, body, B, sums[slot], status, true, &correct);
+    }
+    const int lane = (int)(threadIdx.x & 31u);
+    correct = __shfl_sync(0xffffffffu, correct ? 1 : 0, lane & ~(kFinSub - 1)) != 0;
+    __syncwarp();                      // thread 0's record is written before the corrected vectors
+    if (live && correct) {
+        const hydro_body* b = P.bodies + body;
+        double inv[9], v[3];
+        binverse(b->R_O, inv);
+        copy3(v, sums[slot] + Q_FDQ + 3 * sub);
+        correct_one(inv, v, sub < 2 ? b->Cd : b->Cf, sub < 2 ? 0.5 * P.ocean.density : P.ocean.density);
+        hydro_wrench& w = P.io[body];
+        double* dst = sub == 0 ? w.Fdq : sub == 1 ? w.Tdq : sub == 2 ? w.Fdf : w.Tdf;
+        copy3(dst, v);
+    }
 }
 
 template <int MINB>
@@ -930,7 +958,7 @@ cudaError_t launch_step(const KParams& P, LaunchShape shape, int cut64, cudaStre
     void* args[] = {const_cast<KParams*>(&P)};
     if ((e = cudaLaunchKernel(k, dim3(grid), dim3(kThreads), args, sizeof(ChunkSmem), s))) return e;
     if (ev && (e = cudaEventRecord(ev[2], s))) return e;
-    finalize_kernel<<<(P.n_bodies + kBodyThreads - 1) / kBodyThreads, kBodyThreads, 0, s>>>(P);
+    finalize_kernel<<<(P.n_bodies + kBodyThreads / kFinSub - 1) / (kBodyThreads / kFinSub), kBodyThreads, 0, s>>>(P);
     if ((e = cudaGetLastError())) return e;
     if (ev && (e = cudaEventRecord(ev[3], s))) return e;
     *launches = 3;
