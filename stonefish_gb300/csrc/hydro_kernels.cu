@@ -490,9 +490,21 @@ __device__ __forceinline__ bool consumer_all(bool x)
 }
 
 // ------------------------------------------------------------ prep kernel
+// Requests the 128-byte lines part, part + parts, ... of [p, p + bytes) into
+// L1: the per-body kernels read their records field by field behind
+// branches, and the requests let those reads find the lines on the SM.
+__device__ __forceinline__ void prefetch_lines(const void* p, size_t bytes, int part, int parts)
+{
+    const uintptr_t end = reinterpret_cast<uintptr_t>(p) + bytes;
+    for (uintptr_t a = (reinterpret_cast<uintptr_t>(p) & ~(uintptr_t)127) + 128u * (uintptr_t)part; a < end;
+         a += 128u * (uintptr_t)parts)
+        asm volatile("prefetch.global.L1 [%0];" ::"l"(a));
+}
+
 __global__ void prep_kernel(const KParams P)
 {
     const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b < P.n_bodies) prefetch_lines(P.bodies + b, sizeof(hydro_body), 0, 1);
     if (b == 0) {
         *P.err = 0u;
         *P.work = 0u;
@@ -511,13 +523,13 @@ __global__ void prep_kernel(const KParams P)
 }
 
 // ------------------------------------------------------------ main kernel
-// Persistent CTAs: warps 0..7 compute, warp 8 (one lane) streams the CTA's
+// Persistent CTAs: warps 0..6 compute, warp 7 (one lane) streams the CTA's
 // tiles into a ring of kStages shared-memory stages with 1-D TMA bulk
 // copies.  The producer claims chunks from a global counter (reset by the
 // prep kernel) and skips the chunks of bodies without a face loop; which CTA
 // takes a chunk does not change the chunk's result.
 constexpr int kStages = 8;
-constexpr int kStageRaw = kTileVerts * 12 + kTileFaces * 4;   // 6144 bytes
+constexpr int kStageRaw = kTileVerts * 12 + kTileFaces * 4;   // 7168 bytes
 constexpr int kThreads = kBlock + 32;
 // Straddling faces wait in a per-warp queue until 32 of them (or the end of
 // the chunk) fill one pass of the scalar clipping path: at most 31 wait
@@ -881,6 +893,10 @@ __global__ void __launch_bounds__(kBodyThreads) finalize_kernel(const KParams P)
     const int sub = (int)(gt % kFinSub), slot = (int)(threadIdx.x / kFinSub);
     if (gt == 0) *P.active_end = 0u;   // the chunk kernel has finished with it
     const bool live = body < P.n_bodies && !(P.n_active && body >= *P.n_active);
+    if (live && P.op != OP_AERO && P.op != OP_AERO_BODY) {
+        prefetch_lines(P.bodies + body, sizeof(hydro_body), sub, kFinSub);
+        prefetch_lines(P.io + body, sizeof(hydro_wrench), sub, kFinSub);
+    }
     BodyParams B{};
     if (live) {
         B = P.bparams[body];
