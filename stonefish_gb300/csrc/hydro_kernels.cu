@@ -23,6 +23,7 @@
 //             buoyancy (:1689-1720, :1828-1836), the stale-output rules and
 //             CorrectHydrodynamicForces (:1263-1287).
 // No result depends on scheduling: every sum has a fixed order.
+#include <algorithm>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -501,25 +502,27 @@ __device__ __forceinline__ void prefetch_lines(const void* p, size_t bytes, int 
         asm volatile("prefetch.global.L1 [%0];" ::"l"(a));
 }
 
+// One thread per body, grid-stride over the bodies to evaluate (the first
+// *n_active of them when a device count is given).
 __global__ void prep_kernel(const KParams P)
 {
-    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b < P.n_bodies) prefetch_lines(P.bodies + b, sizeof(hydro_body), 0, 1);
-    if (b == 0) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
         *P.err = 0u;
         *P.work = 0u;
     }
-    if (b >= P.n_bodies) return;
-    if (P.n_active && b >= *P.n_active) return;
-    BodyParams B;
-    const BodyInfo bi = P.binfo[b];
-    body_prologue(P.bodies + b, bi.mesh, P.op, P.ocean, P.st, B);
-    P.bparams[b] = B;
-    const uint8_t active = (B.loop != LOOP_NONE) ? 1 : 0;
-    for (uint32_t c = 0; c < bi.n_chunks; ++c) P.chunk_active[bi.first_chunk + c] = active;
-    // chunks are numbered body by body, so the producers can stop after the
-    // last active one (bodies switched off at the end of a batch cost nothing)
-    if (active && bi.n_chunks) atomicMax(P.active_end, bi.first_chunk + bi.n_chunks);
+    const uint32_t limit = P.n_active ? min(P.n_bodies, *P.n_active) : P.n_bodies;
+    for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < limit; b += gridDim.x * blockDim.x) {
+        prefetch_lines(P.bodies + b, sizeof(hydro_body), 0, 1);
+        BodyParams B;
+        const BodyInfo bi = P.binfo[b];
+        body_prologue(P.bodies + b, bi.mesh, P.op, P.ocean, P.st, B);
+        P.bparams[b] = B;
+        const uint8_t active = (B.loop != LOOP_NONE) ? 1 : 0;
+        for (uint32_t c = 0; c < bi.n_chunks; ++c) P.chunk_active[bi.first_chunk + c] = active;
+        // chunks are numbered body by body, so the producers can stop after the
+        // last active one (bodies switched off at the end of a batch cost nothing)
+        if (active && bi.n_chunks) atomicMax(P.active_end, bi.first_chunk + bi.n_chunks);
+    }
 }
 
 // ------------------------------------------------------------ main kernel
@@ -887,47 +890,52 @@ constexpr int kFinSub = 4;
 
 __global__ void __launch_bounds__(kBodyThreads) finalize_kernel(const KParams P)
 {
-    __shared__ double sums[kBodyThreads / kFinSub][kPartialStride];
-    const uint32_t gt = blockIdx.x * kBodyThreads + threadIdx.x;
-    const uint32_t body = gt / kFinSub;
-    const int sub = (int)(gt % kFinSub), slot = (int)(threadIdx.x / kFinSub);
-    if (gt == 0) *P.active_end = 0u;   // the chunk kernel has finished with it
-    const bool live = body < P.n_bodies && !(P.n_active && body >= *P.n_active);
-    if (live && P.op != OP_AERO && P.op != OP_AERO_BODY) {
-        prefetch_lines(P.bodies + body, sizeof(hydro_body), sub, kFinSub);
-        prefetch_lines(P.io + body, sizeof(hydro_wrench), sub, kFinSub);
-    }
-    BodyParams B{};
-    if (live) {
-        B = P.bparams[body];
-        const BodyInfo bi = P.binfo[body];
-        for (int q = sub; q < kQ; q += kFinSub) {
-            double s = 0.0;
-            if (B.loop != LOOP_NONE) {
-                const double* p = P.partials + (size_t)bi.first_chunk * kPartialStride + q;
-                for (uint32_t c = 0; c < bi.n_chunks; ++c, p += kPartialStride) s += *p;
-            }
-            sums[slot][q] = s;
-        }
-    }
-    __syncwarp();
-    bool correct = false;
-    if (live && sub == 0) {
-        const int status = (*P.err & 1u) ? HYDRO_ERR_TIMEOUT : 0;
-        body_finalize(P, body, B, sums[slot], status, true, &correct);
-    }
+    constexpr uint32_t kPerCta = kBodyThreads / kFinSub;
+    __shared__ double sums[kPerCta][kPartialStride];
+    const int sub = (int)(threadIdx.x % kFinSub), slot = (int)(threadIdx.x / kFinSub);
     const int lane = (int)(threadIdx.x & 31u);
-    correct = __shfl_sync(0xffffffffu, correct ? 1 : 0, lane & ~(kFinSub - 1)) != 0;
-    __syncwarp();                      // thread 0's record is written before the corrected vectors
-    if (live && correct) {
-        const hydro_body* b = P.bodies + body;
-        double inv[9], v[3];
-        binverse(b->R_O, inv);
-        copy3(v, sums[slot] + Q_FDQ + 3 * sub);
-        correct_one(inv, v, sub < 2 ? b->Cd : b->Cf, sub < 2 ? 0.5 * P.ocean.density : P.ocean.density);
-        hydro_wrench& w = P.io[body];
-        double* dst = sub == 0 ? w.Fdq : sub == 1 ? w.Tdq : sub == 2 ? w.Fdf : w.Tdf;
-        copy3(dst, v);
+    if (blockIdx.x == 0 && threadIdx.x == 0) *P.active_end = 0u;   // the chunk kernel has finished with it
+    const uint32_t limit = P.n_active ? min(P.n_bodies, *P.n_active) : P.n_bodies;
+    // grid-stride over groups of kPerCta bodies (uniform across the warp)
+    for (uint32_t base = blockIdx.x * kPerCta; base < limit; base += gridDim.x * kPerCta) {
+        const uint32_t body = base + (uint32_t)slot;
+        const bool live = body < limit;
+        if (live && P.op != OP_AERO && P.op != OP_AERO_BODY) {
+            prefetch_lines(P.bodies + body, sizeof(hydro_body), sub, kFinSub);
+            prefetch_lines(P.io + body, sizeof(hydro_wrench), sub, kFinSub);
+        }
+        BodyParams B{};
+        if (live) {
+            B = P.bparams[body];
+            const BodyInfo bi = P.binfo[body];
+            for (int q = sub; q < kQ; q += kFinSub) {
+                double s = 0.0;
+                if (B.loop != LOOP_NONE) {
+                    const double* p = P.partials + (size_t)bi.first_chunk * kPartialStride + q;
+                    for (uint32_t c = 0; c < bi.n_chunks; ++c, p += kPartialStride) s += *p;
+                }
+                sums[slot][q] = s;
+            }
+        }
+        __syncwarp();
+        bool correct = false;
+        if (live && sub == 0) {
+            const int status = (*P.err & 1u) ? HYDRO_ERR_TIMEOUT : 0;
+            body_finalize(P, body, B, sums[slot], status, true, &correct);
+        }
+        correct = __shfl_sync(0xffffffffu, correct ? 1 : 0, lane & ~(kFinSub - 1)) != 0;
+        __syncwarp();                  // thread 0's record is written before the corrected vectors
+        if (live && correct) {
+            const hydro_body* b = P.bodies + body;
+            double inv[9], v[3];
+            binverse(b->R_O, inv);
+            copy3(v, sums[slot] + Q_FDQ + 3 * sub);
+            correct_one(inv, v, sub < 2 ? b->Cd : b->Cf, sub < 2 ? 0.5 * P.ocean.density : P.ocean.density);
+            hydro_wrench& w = P.io[body];
+            double* dst = sub == 0 ? w.Fdq : sub == 1 ? w.Tdq : sub == 2 ? w.Fdf : w.Tdf;
+            copy3(dst, v);
+        }
+        __syncwarp();                  // sums are reused by the next group
     }
 }
 
@@ -962,7 +970,10 @@ cudaError_t launch_step(const KParams& P, LaunchShape shape, int cut64, cudaStre
     if (P.n_bodies == 0) return cudaSuccess;
     cudaError_t e;
     if (ev && (e = cudaEventRecord(ev[0], s))) return e;
-    prep_kernel<<<(P.n_bodies + kBodyThreads - 1) / kBodyThreads, kBodyThreads, 0, s>>>(P);
+    // per-body kernels: at most eight warp-sized CTAs per SM, grid-stride
+    // beyond (a device count may leave most of a large batch idle)
+    const uint32_t cap = 8u * (uint32_t)std::max(1, shape.grid / std::max(1, shape.ctas_per_sm));
+    prep_kernel<<<std::min((P.n_bodies + kBodyThreads - 1) / kBodyThreads, cap), kBodyThreads, 0, s>>>(P);
     if ((e = cudaGetLastError())) return e;
     if (ev && (e = cudaEventRecord(ev[1], s))) return e;
     int grid = shape.grid;
@@ -974,7 +985,8 @@ cudaError_t launch_step(const KParams& P, LaunchShape shape, int cut64, cudaStre
     void* args[] = {const_cast<KParams*>(&P)};
     if ((e = cudaLaunchKernel(k, dim3(grid), dim3(kThreads), args, sizeof(ChunkSmem), s))) return e;
     if (ev && (e = cudaEventRecord(ev[2], s))) return e;
-    finalize_kernel<<<(P.n_bodies + kBodyThreads / kFinSub - 1) / (kBodyThreads / kFinSub), kBodyThreads, 0, s>>>(P);
+    finalize_kernel<<<std::min((P.n_bodies + kBodyThreads / kFinSub - 1) / (kBodyThreads / kFinSub), cap),
+                      kBodyThreads, 0, s>>>(P);
     if ((e = cudaGetLastError())) return e;
     if (ev && (e = cudaEventRecord(ev[3], s))) return e;
     *launches = 3;
