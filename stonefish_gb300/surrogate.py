@@ -435,8 +435,14 @@ class GatedPredictor:
     rejects routed to the exact step (one exact batch over n slots; slots
     past the rejected count are switched off and cost nothing)."""
 
+    # faces per work chunk of the exact fallback batch: four tiles (measured
+    # against one, two and eight: within 1% for 68 gated-out hulls of 65536,
+    # 27% faster in rollouts that gate out thousands)
+    FALLBACK_CHUNK_FACES = 4 * abi.TILE_FACES
+
     def __init__(self, sur: Surrogate, hctx_exact: HydroContext, mesh_id: int, n: int,
-                 ocean: abi.Ocean, settings: abi.Settings, tensor_cores: str = "tcgen05"):
+                 ocean: abi.Ocean, settings: abi.Settings, tensor_cores: str = "tcgen05",
+                 fallback_chunk_faces: int | None = None):
         self.s = sur
         self.h = hctx_exact
         self.lib = hctx_exact.lib
@@ -446,8 +452,9 @@ class GatedPredictor:
         self.settings = settings
         dev = sur.dev
         self.bufs = sur._infer_bufs(self.n_pad)
-        # one-tile chunks: only the few gated-out hulls are active per call
-        self.batch = hctx_exact.batch(np.full(n, mesh_id, dtype=np.uint32), chunk_faces=abi.TILE_FACES)
+        # small chunks: only the few gated-out hulls are active per call
+        self.batch = hctx_exact.batch(np.full(n, mesh_id, dtype=np.uint32),
+                                      chunk_faces=fallback_chunk_faces or self.FALLBACK_CHUNK_FACES)
         self.mesh_id = mesh_id
         self.counts = torch.zeros((n + 255) // 256, dtype=torch.int32, device=dev)
         self.packed = torch.zeros(n * abi.BODY_DTYPE.itemsize, dtype=torch.uint8, device=dev)
