@@ -531,19 +531,24 @@ __global__ void prep_kernel(const KParams P)
 // copies.  The producer claims chunks from a global counter (reset by the
 // prep kernel) and skips the chunks of bodies without a face loop; which CTA
 // takes a chunk does not change the chunk's result.
-constexpr int kStages = 8;
+constexpr int kStages = 4;
 constexpr int kStageRaw = kTileVerts * 12 + kTileFaces * 4;   // 7168 bytes
 constexpr int kThreads = kBlock + 32;
 // Straddling faces wait in a per-warp queue until 32 of them (or the end of
 // the chunk) fill one pass of the scalar clipping path: at most 31 wait
-// while a tile adds up to 64.
+// while a tile adds up to 64.  The fully submerged faces of tiles that are
+// not wholly under water wait likewise for 64 (one pass of pairs): at most
+// 63 wait while a tile adds up to 64.
 constexpr int kCutQueue = 96;
+constexpr int kPairQueue = 127;
 
 __device__ __forceinline__ int wrap_queue(int x)
 {
     x = x >= kCutQueue ? x - kCutQueue : x;
     return x >= kCutQueue ? x - kCutQueue : x;
 }
+
+__device__ __forceinline__ int wrap_pair_queue(int x) { return x >= kPairQueue ? x - kPairQueue : x; }
 
 enum : int { ITEM_FIRST = 1, ITEM_LAST = 2, ITEM_END = 4 };
 
@@ -565,8 +570,8 @@ struct __align__(128) ChunkSmem {
     uint32_t tflags[2][8];            // per-warp vertex votes of each vertex buffer (bit 0 above, bit 1 under)
     static_assert(kWarps <= 8, "one vote slot per compute warp");
     float2 red[kWarps][32];
-    uint16_t flist[kWarps][64];       // per-warp compacted face lists
     float4 cutq[kWarps][kCutQueue][3];  // per-warp queues of straddling faces (corners with depth)
+    float pairq[kWarps][kPairQueue * 9]; // per-warp queues of fully submerged faces (corner positions)
     ItemMeta meta[kStages];
     uint64_t full[kStages];
     uint64_t empty[kStages];
@@ -658,19 +663,27 @@ __device__ __forceinline__ void transform_tile(const KParams& P, const StageBuf&
     if ((threadIdx.x & 31) == 0) flags[threadIdx.x >> 5] = (a ? 1u : 0u) | (u ? 2u : 0u);
 }
 
-// Per-warp queue of straddling faces: head slot and length (warp-uniform).
+// Per-warp queues: head slot and length (warp-uniform).
 struct CutQueue {
     float4 (*q)[3];
     int head, len;
 };
 
-// Faces of one tile: per-warp compaction, then the packed path for pairs of
-// fully submerged faces; straddling faces join the warp's queue, which runs
-// the scalar path 32 at a time (and empties when `drain`).  Returns the
-// number of faces each lane added at most (pairs count two, a pass one).
+struct PairQueue {
+    float* q;   // kPairQueue entries of 9 floats: x, y, z of the three corners
+    int head, len;
+};
+
+// Faces of one tile.  A tile wholly under water is evaluated directly, two
+// faces per lane on the packed path; in other tiles each face is classified
+// and queued: fully submerged faces in the warp's pair queue, straddling
+// faces in its clipping queue.  The queues run a pass when full enough for
+// all 32 lanes (64 paired faces, 32 straddling faces) or when `drain` (the
+// chunk's last tile).  Returns the number of faces each lane added at most
+// (a pair pass counts two, a clipping pass one).
 template <bool CUT64, bool WAVES>
 __device__ __forceinline__ int tile_faces(const KParams& P, const StageBuf& st, const ItemMeta& m,
-                                          const float4* verts, const uint32_t* flags, uint16_t* list,
+                                          const float4* verts, const uint32_t* flags, PairQueue& pq,
                                           CutQueue& cq, bool drain, Acc& acc)
 {
     const int lane = threadIdx.x & 31;
@@ -708,61 +721,87 @@ __device__ __forceinline__ int tile_faces(const KParams& P, const StageBuf& st, 
         all_under = !(tf & 1u);
         any_under = (tf & 2u) != 0u;
     }
-    if (any_under) {
-        // Warp w takes faces (k*32 + lane)*kWarps + w, k = 0, 1: a spread sample
-        // of the tile, so that the warps get similar work.  Unless they are all
-        // under water, its faces are compacted (deterministically, by ballot)
-        // into a list of fully submerged faces and a list of straddling faces.
-        // The fully submerged faces are evaluated two per lane on the packed
-        // FP32 pipe (faces list[lane] and list[lane + 32]), the straddling ones
-        // face by face.
-        int nfull = 0, ncut = 0;
-        int fa = lane * kWarps + warp, fb = (lane + 32) * kWarps + warp;
-        if (all_under) {
-            // faces j * kWarps + warp, j < nfull, exist: fa for lane < nfull, fb for lane + 32 < nfull
-            nfull = nf > warp ? min(64, (nf - warp + kWarps - 1) / kWarps) : 0;
-        } else {
-            const unsigned lt = (1u << lane) - 1u;
+    // Warp w takes faces (k*32 + lane)*kWarps + w, k = 0, 1: a spread sample
+    // of the tile, so that the warps get similar work.
+    int direct = 0;   // faces of the direct pass: lane l pairs faces l*kWarps + w and (l+32)*kWarps + w
+    if (all_under) {
+        direct = nf > warp ? min(64, (nf - warp + kWarps - 1) / kWarps) : 0;
+    } else if (any_under) {
+        const unsigned lt = (1u << lane) - 1u;
+        int nq = 0, nc = 0;
 #pragma unroll
-            for (int k = 0; k < 2; ++k) {
-                const int f = k == 0 ? fa : fb;
-                int cls = 0;
-                uint32_t w = 0;
-                if (f < nf) {
-                    w = idx[f];
-                    cls = face_class(verts[w & 511u].w, verts[(w >> 9) & 511u].w, verts[w >> 18].w);
-                }
-                const unsigned mf = __ballot_sync(0xffffffffu, cls == 1);
-                const unsigned mc = __ballot_sync(0xffffffffu, cls == 2);
-                if (cls == 1) list[nfull + __popc(mf & lt)] = (uint16_t)f;
-                if (cls == 2) {
-                    float4* e = cq.q[wrap_queue(cq.head + cq.len + ncut + __popc(mc & lt))];
-                    e[0] = verts[w & 511u];
-                    e[1] = verts[(w >> 9) & 511u];
-                    e[2] = verts[w >> 18];
-                }
-                nfull += __popc(mf);
-                ncut += __popc(mc);
+        for (int k = 0; k < 2; ++k) {
+            const int f = (k * 32 + lane) * kWarps + warp;
+            int cls = 0;
+            uint32_t w = 0;
+            if (f < nf) {
+                w = idx[f];
+                cls = face_class(verts[w & 511u].w, verts[(w >> 9) & 511u].w, verts[w >> 18].w);
             }
-            cq.len += ncut;
-            __syncwarp();
-            if (lane < nfull) {
-                fa = list[lane];
-                fb = list[lane + 32 < nfull ? lane + 32 : lane];
+            const unsigned mf = __ballot_sync(0xffffffffu, cls == 1);
+            const unsigned mc = __ballot_sync(0xffffffffu, cls == 2);
+            if (cls == 1) {
+                float* e = pq.q + 9 * wrap_pair_queue(pq.head + pq.len + nq + __popc(mf & lt));
+                const float4 c1 = verts[w & 511u], c2 = verts[(w >> 9) & 511u], c3 = verts[w >> 18];
+                e[0] = c1.x; e[1] = c1.y; e[2] = c1.z;
+                e[3] = c2.x; e[4] = c2.y; e[5] = c2.z;
+                e[6] = c3.x; e[7] = c3.y; e[8] = c3.z;
             }
+            if (cls == 2) {
+                float4* e = cq.q[wrap_queue(cq.head + cq.len + nc + __popc(mc & lt))];
+                e[0] = verts[w & 511u];
+                e[1] = verts[(w >> 9) & 511u];
+                e[2] = verts[w >> 18];
+            }
+            nq += __popc(mf);
+            nc += __popc(mc);
         }
-        if (lane < nfull) {
-            const bool hasB = lane + 32 < nfull;
-            const uint32_t wa = idx[fa];
-            const uint32_t wb = idx[hasB ? fb : fa];
-            const P3 p1 = corners(verts[wa & 511u], verts[wb & 511u]);
-            const P3 p2 = corners(verts[(wa >> 9) & 511u], verts[(wb >> 9) & 511u]);
-            const P3 p3 = corners(verts[wa >> 18], verts[wb >> 18]);
+        pq.len += nq;
+        cq.len += nc;
+        __syncwarp();
+    }
+    // pair passes: the direct pass of a tile wholly under water, then the
+    // queue's passes (one call site for the packed arithmetic)
+    for (;;) {
+        int n;
+        bool from_queue;
+        if (direct > 0) {
+            n = direct;
+            from_queue = false;
+            direct = 0;
+        } else if (pq.len >= 64 || (drain && pq.len > 0)) {
+            n = pq.len < 64 ? pq.len : 64;
+            from_queue = true;
+        } else {
+            break;
+        }
+        if (lane < n) {
+            const bool hasB = lane + 32 < n;
+            P3 p1, p2, p3;
+            if (!from_queue) {
+                const int fa = lane * kWarps + warp, fb = (lane + 32) * kWarps + warp;
+                const uint32_t wa = idx[fa];
+                const uint32_t wb = idx[hasB ? fb : fa];
+                p1 = corners(verts[wa & 511u], verts[wb & 511u]);
+                p2 = corners(verts[(wa >> 9) & 511u], verts[(wb >> 9) & 511u]);
+                p3 = corners(verts[wa >> 18], verts[wb >> 18]);
+            } else {
+                const float* a = pq.q + 9 * wrap_pair_queue(pq.head + lane);
+                const float* b = pq.q + 9 * wrap_pair_queue(pq.head + (hasB ? lane + 32 : lane));
+                p1 = pk(f2(a[0], b[0]), f2(a[1], b[1]), f2(a[2], b[2]));
+                p2 = pk(f2(a[3], b[3]), f2(a[4], b[4]), f2(a[5], b[5]));
+                p3 = pk(f2(a[6], b[6]), f2(a[7], b[7]), f2(a[8], b[8]));
+            }
             const BodyPair Bp = body_pair(Bl, P.ocean);
             if (Bl.loop == LOOP_SURFACE) face_full2<WAVES>(P.ocean, Bl, Bp, acc, p1, p2, p3, hasB);
             else face_submerged2(P.ocean, Bp, acc, p1, p2, p3, hasB);
         }
-        if (nfull > 0) added = 2;
+        if (from_queue) {
+            pq.head = wrap_pair_queue(pq.head + n);
+            pq.len -= n;
+        }
+        added += 2;
+        __syncwarp();
     }
     while (cq.len >= 32 || (drain && cq.len > 0)) {
         const int n = cq.len < 32 ? cq.len : 32;
@@ -794,12 +833,14 @@ __device__ __forceinline__ void consumer(const KParams& P, ChunkSmem& S)
 #pragma unroll
     for (int k = 0; k < kQ; ++k) acc.q[k] = 0.f;
     float hi = 0.f, lo = 0.f;
-    // A tile adds at most five faces to a lane's run (a pair and three
-    // queue passes: up to 95 queued faces, the last one drained), so a
-    // flush once a run has reached kFlushFaces - 4 keeps every FP32 run at
-    // or below kFlushFaces faces.
+    // A tile adds at most seven faces to a lane's run: two pair passes (a
+    // direct or queued pass and the drain) and three clipping passes (up to
+    // 95 queued faces, the last pass a drain), so a flush once a run has
+    // passed kFlushFaces - 7 keeps every FP32 run at or below kFlushFaces
+    // faces.
     int run = 0;
     CutQueue cq{S.cutq[warp], 0, 0};
+    PairQueue pq{S.pairq[warp], 0, 0};
 
     // first tile
     bool ok = mbar_wait(&S.full[0], 0u);
@@ -812,8 +853,8 @@ __device__ __forceinline__ void consumer(const KParams& P, ChunkSmem& S)
     for (uint32_t item = 0; !(m.flags & ITEM_END); ++item) {
         const int s = (int)(item % kStages);
         const bool last = (m.flags & ITEM_LAST) != 0;
-        run += tile_faces<CUT64, WAVES>(P, S.stage[s], m, S.verts[item & 1u], S.tflags[item & 1u], S.flist[warp],
-                                        cq, last, acc);
+        run += tile_faces<CUT64, WAVES>(P, S.stage[s], m, S.verts[item & 1u], S.tflags[item & 1u], pq, cq, last,
+                                        acc);
         // next tile: wait, read its metadata, transform its vertices
         const uint32_t nx = item + 1u;
         const int sn = (int)(nx % kStages);
@@ -826,7 +867,7 @@ __device__ __forceinline__ void consumer(const KParams& P, ChunkSmem& S)
             return;
         }
         if (tid == 0) mbar_arrive(&S.empty[s]);
-        if (last || run > kFlushFaces - 5) {
+        if (last || run > kFlushFaces - 7) {
             flush(acc, hi, lo);
             run = 0;
         }
