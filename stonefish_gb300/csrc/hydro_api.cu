@@ -588,18 +588,36 @@ hydro_status hydro_mesh_upload(hydro_ctx* ctx, const void* vertex_data, size_t v
         if (ti.empty()) return;
         const uint32_t nv = (uint32_t)tv.size(), nf = (uint32_t)ti.size();
         const uint32_t nvp = (nv + 3) & ~3u;
-        const size_t bytes = tile_bytes(nv, nf);
+        const size_t bytes = tile_block_bytes(nv, nf);
         size_t off = host.size();
         host.resize(off + bytes, 0);
         float* f = reinterpret_cast<float*>(host.data() + off);
+        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
         for (uint32_t k = 0; k < nv; ++k) {
             float p[3];
             pos(tv[k], p);
             f[k] = p[0];
             f[nvp + k] = p[1];
             f[2 * nvp + k] = p[2];
+            for (int a = 0; a < 3; ++a) {
+                lo[a] = std::min(lo[a], (double)p[a]);
+                hi[a] = std::max(hi[a], (double)p[a]);
+            }
         }
         std::memcpy(host.data() + off + (size_t)nvp * 12, ti.data(), ti.size() * 4);
+        // bounding sphere: centre of the box, radius to the farthest vertex
+        // from the stored (float) centre, rounded up
+        float c[3];
+        for (int a = 0; a < 3; ++a) c[a] = (float)(0.5 * (lo[a] + hi[a]));
+        double r2 = 0.0;
+        for (uint32_t k = 0; k < nv; ++k) {
+            float p[3];
+            pos(tv[k], p);
+            const double dx = (double)p[0] - c[0], dy = (double)p[1] - c[1], dz = (double)p[2] - c[2];
+            r2 = std::max(r2, dx * dx + dy * dy + dz * dz);
+        }
+        const float sphere[4] = {c[0], c[1], c[2], std::nextafter((float)(std::sqrt(r2) * (1.0 + 1e-6)), 1e30f)};
+        std::memcpy(host.data() + off + tile_bytes(nv, nf), sphere, 16);
         pend.push_back(Pending{off, (uint16_t)nv, (uint16_t)nf, tile_first_face});
         for (uint32_t g : tv) local[g] = -1;
         tv.clear();

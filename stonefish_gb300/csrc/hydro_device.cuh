@@ -60,6 +60,14 @@ __host__ __device__ __forceinline__ uint32_t tile_bytes(uint32_t nv, uint32_t nf
     return (nvp * 12u + nf * 4u + 15u) & ~15u;
 }
 
+// Each tile block is followed in memory (not copied with it) by the tile's
+// bounding sphere in mesh coordinates: float4 (centre x, y, z, radius),
+// radius rounded up so that every vertex of the tile lies inside.
+__host__ __device__ __forceinline__ uint32_t tile_block_bytes(uint32_t nv, uint32_t nf)
+{
+    return tile_bytes(nv, nf) + 16u;
+}
+
 constexpr int kMaxTilesPerChunk = 16;
 
 // One work item: tiles [first_tile, first_tile + n_tiles) of one body.

@@ -579,6 +579,34 @@ struct __align__(128) ChunkSmem {
 
 size_t chunk_kernel_smem() { return sizeof(ChunkSmem); }
 
+// Tiles of a chunk to stream (bit t for tile t).  On a flat surface a tile
+// of a surface-loop body whose bounding sphere lies wholly above the water
+// (every vertex at depth < 0, so every face is skipped, SolidEntity.cpp
+// :1353-1354) is not loaded at all.  The test bounds the consumer's FP32
+// transform of each vertex with a margin far above its rounding error.  A
+// chunk keeps at least one tile, which carries its (zero) partial.
+__device__ __forceinline__ uint32_t tiles_to_issue(const KParams& P, uint32_t body, const TileDesc (&td)[kMaxTilesPerChunk],
+                                                   uint32_t nt)
+{
+    uint32_t keep = (1u << nt) - 1u;
+    if (P.ocean.waves) return keep;
+    const BodyParams& B = P.bparams[body];
+    if (B.loop != LOOP_SURFACE) return keep;
+    const float4 T = *reinterpret_cast<const float4*>(B.TC + 8);   // row giving z
+    const float rsum = fabsf(T.x) + fabsf(T.y) + fabsf(T.z);
+#pragma unroll
+    for (int t = 0; t < kMaxTilesPerChunk; ++t) {
+        if ((uint32_t)t >= nt) break;
+        const float4 c = *reinterpret_cast<const float4*>(reinterpret_cast<const char*>(td[t].block) +
+                                                          tile_bytes(td[t].nv, td[t].nf));
+        const float zc = (T.x * c.x + T.y * c.y) + (T.z * c.z + T.w);
+        const float reach = rsum * c.w;
+        const float margin = 1e-5f * (rsum * (fabsf(c.x) + fabsf(c.y) + fabsf(c.z) + c.w) + fabsf(T.w)) + 1e-6f;
+        if (zc + reach + margin < 0.f) keep &= ~(1u << t);
+    }
+    return keep ? keep : 1u;
+}
+
 __device__ __forceinline__ void producer(const KParams& P, ChunkSmem& S)
 {
     uint32_t item = 0;
@@ -597,8 +625,10 @@ __device__ __forceinline__ void producer(const KParams& P, ChunkSmem& S)
 #pragma unroll
         for (int t = 0; t < kMaxTilesPerChunk; ++t)
             if ((uint32_t)t < nt) td[t] = P.tiles[ch.first_tile + t];
+        const uint32_t keep = tiles_to_issue(P, ch.body, td, nt);
 #pragma unroll 1
-        for (uint32_t t = 0; t < nt; ++t, ++item) {
+        for (uint32_t t = 0; t < nt; ++t) {
+            if (!((keep >> t) & 1u)) continue;
             const int s = (int)(item % kStages);
             if (item >= (uint32_t)kStages && !mbar_wait_sleep(&S.empty[s], ((item / kStages) - 1u) & 1u)) {
                 atomicOr(P.err, 1u);
@@ -612,7 +642,7 @@ __device__ __forceinline__ void producer(const KParams& P, ChunkSmem& S)
             const uint32_t bytes = tile_bytes(d.nv, d.nf);
             ItemMeta m;
             m.chunk = c;
-            m.flags = (t == 0 ? ITEM_FIRST : 0) | (t + 1 == nt ? ITEM_LAST : 0);
+            m.flags = ((keep & ((1u << t) - 1u)) == 0u ? ITEM_FIRST : 0) | ((keep >> (t + 1)) == 0u ? ITEM_LAST : 0);
             m.nv = d.nv;
             m.nf = d.nf;
             m.pad = 0;
@@ -620,6 +650,7 @@ __device__ __forceinline__ void producer(const KParams& P, ChunkSmem& S)
             mbar_arrive_expect_tx(&S.full[s], bytes + (uint32_t)sizeof(BodyParams));
             tma_copy(&S.stage[s].bp, P.bparams + ch.body, (uint32_t)sizeof(BodyParams), &S.full[s]);
             tma_copy(S.stage[s].raw, d.block, bytes, &S.full[s]);
+            ++item;
         }
     }
     // end of stream
