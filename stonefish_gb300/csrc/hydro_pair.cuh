@@ -112,21 +112,29 @@ __device__ __forceinline__ P3 pdvs3(P3 a)
 #endif
 }
 
-// Conditional accumulation of the two halves of a packed term into the
-// thread's scalar running sums (face A first, then face B).
-__device__ __forceinline__ void acc_add2(float& acc, float2 v, bool ca, bool cb)
+// Accumulation of the two halves of a packed term into the thread's scalar
+// running sums (face A first, then face B).  A term the reference does not
+// add (degenerate face, padding half, no drag or no friction on the face)
+// reaches this point as exactly zero: the running sums start at +0 and an
+// IEEE round-to-nearest sum is -0 only when both addends are -0, so a sum is
+// never -0 and adding a zero of either sign leaves its bits unchanged.
+__device__ __forceinline__ void acc_add2(float& acc, float2 v)
 {
-    const float t = acc + v.x;
-    acc = ca ? t : acc;
-    const float u = acc + v.y;
-    acc = cb ? u : acc;
+    acc = acc + v.x;
+    acc = acc + v.y;
 }
 
-__device__ __forceinline__ void acc_add3p(Acc& a, int k, P3 v, bool ca, bool cb)
+__device__ __forceinline__ void acc_add3p(Acc& a, int k, P3 v)
 {
-    acc_add2(a.q[k], v.x, ca, cb);
-    acc_add2(a.q[k + 1], v.y, ca, cb);
-    acc_add2(a.q[k + 2], v.z, ca, cb);
+    acc_add2(a.q[k], v.x);
+    acc_add2(a.q[k + 1], v.y);
+    acc_add2(a.q[k + 2], v.z);
+}
+
+// Per-half zeroing of a scalar pair: (ca ? v.x : 0, cb ? v.y : 0)
+__device__ __forceinline__ float2 keep2(bool ca, bool cb, float2 v)
+{
+    return make_float2(ca ? v.x : 0.f, cb ? v.y : 0.f);
 }
 
 __device__ __forceinline__ P3 corners(float4 qa, float4 qb)
@@ -159,45 +167,47 @@ __device__ __forceinline__ P3 fluid_velocity2(const OceanDev& o, const BodyPair&
     return pk(f2(a.x, b.x), f2(a.y, b.y), f2(a.z, b.z));
 }
 
-// tri_props for two triangles; okA/okB false for a degenerate face
-// (len^2 < 1e-12, :1385-1386).
-__device__ __forceinline__ void tri_props2(P3 p1, P3 p2, P3 p3, P3& fc, P3& fn1, float2& A,
-                                           bool& okA, bool& okB)
+// tri_props for two triangles.  A degenerate face (len^2 < 1e-12,
+// :1385-1386) and the padding half (validB false) get a zero normal and
+// area, which makes every term they would add zero (their corners are
+// finite).
+__device__ __forceinline__ void tri_props2(P3 p1, P3 p2, P3 p3, P3& fc, P3& fn1, float2& A, bool validB)
 {
     P3 fv1 = psub(p2, p1);
     P3 fv2 = psub(p3, p1);
     fc = pdvs3(padd(padd(p1, p2), p3));
     P3 fn = pcross(fv1, fv2);
     float2 len = pdot(fn, fn);
-    okA = !(len.x < 1e-12f);
-    okB = !(len.y < 1e-12f);
+    const bool okA = !(len.x < 1e-12f);
+    const bool okB = !(len.y < 1e-12f) && validB;
     len = f2(sqrtf(len.x), sqrtf(len.y));
     fn1 = pdvs_rcp(fn, len);
-    A = mul2(len, bc(0.5f));
+    fn1 = pk(keep2(okA, okB, fn1.x), keep2(okA, okB, fn1.y), keep2(okA, okB, fn1.z));
+    A = keep2(okA, okB, mul2(len, bc(0.5f)));
 }
 
-// Damping of two faces (:1661-1683).
+// Damping of two faces (:1661-1683).  Drag and skin friction of a face
+// that does not get them are computed with a zero area.
 __device__ __forceinline__ void damping2(const OceanDev& o, const BodyPair& Bp, Acc& a, P3 fc,
-                                         P3 fn1, float2 A, bool okA, bool okB)
+                                         P3 fn1, float2 A)
 {
     P3 r = psub(fc, Bp.p);
     P3 vc = psub(fluid_velocity2(o, Bp, fc), padd(Bp.v, pcross(Bp.omega, r)));
     float2 vc_n = pdot(vc, fn1);
     P3 vn = pk(mul2(vc_n, fn1.x), mul2(vc_n, fn1.y), mul2(vc_n, fn1.z));
     P3 vt = psub(vc, vn);
-    const bool qa = okA && (vc_n.x < -1e-12f), qb = okB && (vc_n.y < -1e-12f);
+    const bool qa = vc_n.x < -1e-12f, qb = vc_n.y < -1e-12f;   // zero normal: false
     if (qa || qb) {
         float2 vmag2 = pdot(vc, vc);
         float2 s = f2(sqrtf(vmag2.x), sqrtf(vmag2.y));
-        P3 q = pmul(pmul(pmul(vc, s), neg2(vc_n)), A);
-        acc_add3p(a, Q_FDQ, q, qa, qb);
-        acc_add3p(a, Q_TDQ, pcross(r, q), qa, qb);
+        P3 q = pmul(pmul(pmul(vc, s), neg2(vc_n)), keep2(qa, qb, A));
+        acc_add3p(a, Q_FDQ, q);
+        acc_add3p(a, Q_TDQ, pcross(r, q));
     }
     float2 vt2 = pdot(vt, vt);
-    const bool sa = okA && (vt2.x > 1e-9f), sb = okB && (vt2.y > 1e-9f);
-    P3 sk = pmul(vt, A);
-    acc_add3p(a, Q_FDF, sk, sa, sb);
-    acc_add3p(a, Q_TDF, pcross(r, sk), sa, sb);
+    P3 sk = pmul(vt, keep2(vt2.x > 1e-9f, vt2.y > 1e-9f, A));
+    acc_add3p(a, Q_FDF, sk);
+    acc_add3p(a, Q_TDF, pcross(r, sk));
 }
 
 // Two fully submerged faces of the surface loop (:1618-1647, :1650-1686).
@@ -209,23 +219,21 @@ __device__ __forceinline__ void face_full2(const OceanDev& o, const BodyParams& 
     {
         const P3 p01 = psub(p1, Bp.p0), p02 = psub(p2, Bp.p0), p03 = psub(p3, Bp.p0);
         P3 cg = pmul(padd(padd(p01, p02), p03), bc(0.25f));
-        float2 v6 = pdot(p01, pcross(p02, p03));
-        acc_add3p(a, Q_CB, pmul(cg, v6), true, validB);
-        acc_add2(a.q[Q_V6], v6, true, validB);
+        const float2 v6 = keep2(true, validB, pdot(p01, pcross(p02, p03)));
+        acc_add3p(a, Q_CB, pmul(cg, v6));
+        acc_add2(a.q[Q_V6], v6);
     }
     P3 fc, fn1;
     float2 A;
-    bool okA, okB;
-    tri_props2(p1, p2, p3, fc, fn1, A, okA, okB);
-    okB = okB && validB;
+    tri_props2(p1, p2, p3, fc, fn1, A, validB);
     if (WAVES && B.buoyancy) {
         float2 dc = f2(depth_at(o, fc.x.x, fc.y.x, fc.z.x), depth_at(o, fc.x.y, fc.y.y, fc.z.y));
         P3 Fbi = pmul(pmul(pk(neg2(fn1.x), neg2(fn1.y), neg2(fn1.z)), A), dc);
-        acc_add3p(a, Q_FB, Fbi, okA, okB);
-        acc_add3p(a, Q_TB, pcross(psub(fc, Bp.p), Fbi), okA, okB);
+        acc_add3p(a, Q_FB, Fbi);
+        acc_add3p(a, Q_TB, pcross(psub(fc, Bp.p), Fbi));
     }
-    if (B.damping) damping2(o, Bp, a, fc, fn1, A, okA, okB);
-    acc_add2(a.q[Q_SWET], A, okA, okB);
+    if (B.damping) damping2(o, Bp, a, fc, fn1, A);
+    acc_add2(a.q[Q_SWET], A);
 }
 
 // Two faces of the submerged loop (:1748-1789).
@@ -234,9 +242,8 @@ __device__ __forceinline__ void face_submerged2(const OceanDev& o, const BodyPai
 {
     P3 fc, fn1;
     float2 A;
-    bool okA, okB;
-    tri_props2(p1, p2, p3, fc, fn1, A, okA, okB);
-    damping2(o, Bp, a, fc, fn1, A, okA, okB && validB);
+    tri_props2(p1, p2, p3, fc, fn1, A, validB);
+    damping2(o, Bp, a, fc, fn1, A);
 }
 
 }  // namespace sfh
