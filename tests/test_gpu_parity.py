@@ -382,3 +382,38 @@ def test_argument_errors(hctx):
     with pytest.raises(abi.HydroError) as ei:
         hctx.upload_mesh(np.zeros((0, 3), np.float32), np.zeros((0, 3), np.uint32))   # empty mesh
     assert ei.value.status == abi.HYDRO_ERR_INVALID_ARG
+
+
+def test_hulls_barely_under_water_match_mirror(oracle, hctx):
+    """A finely tiled hull at random attitudes with only its lowest 1-50 mm
+    under a flat surface: most tiles lie wholly above the water and are
+    skipped by the producer (bounding-sphere test); the bodies must still
+    match MIRROR32, so no tile holding an underwater corner was dropped."""
+    rng = np.random.default_rng(77)
+    xyz, faces = meshes.capped_cylinder_for_faces(0.3, 2.0, 20000)
+    n = 192
+    R = scenarios.quat_to_matrix(scenarios.random_quaternions(rng, n))
+    deepest = np.max(np.einsum("nj,vj->nv", R[:, 2, :], xyz.astype(np.float64)), axis=1)
+    pos = np.zeros((n, 3))
+    pos[:, :2] = rng.uniform(-5.0, 5.0, (n, 2))
+    pos[:, 2] = -deepest + rng.uniform(0.001, 0.05, n)
+    half = np.abs(xyz).max(axis=0).astype(np.float64)     # body-frame box about the origin
+    mid = hctx.upload_mesh(xyz, faces)
+    bodies = scenarios.fill_bodies(n, R, pos, rng.uniform(-1, 1, (n, 3)), rng.uniform(-0.5, 0.5, (n, 3)),
+                                   np.tile(half, (n, 1)), 0.5, 4.0, (0.5, 0.6, 0.7), (0.01, 0.02, 0.03), mid,
+                                   mode=abi.MODE_FLOATING)
+    ocean = scenarios.flat_ocean((0.2, 0.0, 0.0))
+    sc = {"bodies": bodies, "meshes": [(xyz, faces)], "ocean": ocean, "_ids": [mid]}
+    sc["bodies"]["mesh"] = 0
+    gpu = run_batch(hctx, sc)
+    mir = run_oracle(oracle, MIRROR32, sc)
+    assert np.array_equal(gpu["position"], mir["position"])
+    cross = gpu["position"] == abi.CROSSING_SURFACE
+    assert cross.sum() > n // 2
+    assert np.all(gpu["Vsub"][cross] > 0)
+    # The submerged caps are small differences of large signed tetra
+    # volumes, so FP32 summation runs cost more digits than on the mixed
+    # batch; a dropped tile would remove O(1) of a cap.  Bar: 1e-4.
+    e = scaled_errors(gpu, mir, body_lengths(sc))
+    for k, v in e.items():
+        assert np.max(v[cross]) < 1e-4, (k, float(np.max(v[cross])))
