@@ -77,7 +77,7 @@ struct hydro_batch {
     double* partials_d = nullptr;
     BodyParams* bparams_d = nullptr;
     unsigned* err_d = nullptr;
-    uint8_t* chunk_active_d = nullptr;
+    ActiveChunk* active_d = nullptr;     // the launch's list of chunks with a face loop
     hydro_body* bodies_d = nullptr;    // staging for the host-buffer entry point
     hydro_wrench* io_d = nullptr;
     cudaStream_t stream = nullptr;
@@ -284,7 +284,7 @@ void batch_free(hydro_batch* b)
     cudaFree(b->partials_d);
     cudaFree(b->bparams_d);
     cudaFree(b->err_d);
-    cudaFree(b->chunk_active_d);
+    cudaFree(b->active_d);
     cudaFree(b->bodies_d);
     cudaFree(b->io_d);
     cudaFree(b->aparams_d);
@@ -324,17 +324,17 @@ hydro_status build_work(hydro_ctx* ctx, hydro_batch* b, uint32_t tpc)
     cudaFree(b->chunks_d);
     cudaFree(b->binfo_d);
     cudaFree(b->partials_d);
-    cudaFree(b->chunk_active_d);
+    cudaFree(b->active_d);
     b->chunks_d = nullptr;
     b->binfo_d = nullptr;
     b->partials_d = nullptr;
-    b->chunk_active_d = nullptr;
+    b->active_d = nullptr;
     b->n_chunks = (uint32_t)chunks.size();
     b->chunk_tiles = tpc;
     CK(ctx, cudaMalloc(&b->chunks_d, chunks.size() * sizeof(ChunkDesc)));
     CK(ctx, cudaMalloc(&b->binfo_d, n * sizeof(BodyInfo)));
     CK(ctx, cudaMalloc(&b->partials_d, chunks.size() * kPartialStride * sizeof(double)));
-    CK(ctx, cudaMalloc(&b->chunk_active_d, chunks.size()));
+    CK(ctx, cudaMalloc(&b->active_d, chunks.size() * sizeof(ActiveChunk)));
     CK(ctx, cudaMemcpy(b->chunks_d, chunks.data(), chunks.size() * sizeof(ChunkDesc), cudaMemcpyHostToDevice));
     CK(ctx, cudaMemcpy(b->binfo_d, info.data(), n * sizeof(BodyInfo), cudaMemcpyHostToDevice));
     CK(ctx, cudaMemset(b->partials_d, 0, chunks.size() * kPartialStride * sizeof(double)));
@@ -396,11 +396,11 @@ hydro_status batch_launch(hydro_batch* b, const hydro_body* d_bodies, const hydr
     P.bparams = b->bparams_d;
     P.err = b->err_d;
     P.work = b->err_d + 32;
-    P.active_end = b->err_d + 48;
+    P.n_listed = b->err_d + 48;
     P.n_active = d_count;
     P.aero_io = d_aero;
     P.aero_params = d_aero_params;
-    P.chunk_active = b->chunk_active_d;
+    P.active = b->active_d;
     P.n_bodies = b->n_bodies;
     P.n_chunks = b->n_chunks;
     P.ocean = make_ocean(ctx, ocean);
@@ -581,14 +581,14 @@ hydro_status hydro_mesh_upload(hydro_ctx* ctx, const void* vertex_data, size_t v
     std::vector<uint32_t> tv;              // global ids of the open tile's vertices
     std::vector<uint32_t> ti;              // packed local indices of the open tile's faces
     std::vector<char> host;                // all tile blocks of this mesh
-    struct Pending { size_t offset; uint16_t nv, nf; uint32_t first_face; };
+    struct Pending { size_t offset; uint16_t nv, nf; uint32_t first_face; float4 sphere; };
     std::vector<Pending> pend;
     uint32_t tile_first_face = 0;
     auto close_tile = [&](uint32_t next_face) {
         if (ti.empty()) return;
         const uint32_t nv = (uint32_t)tv.size(), nf = (uint32_t)ti.size();
         const uint32_t nvp = (nv + 3) & ~3u;
-        const size_t bytes = tile_block_bytes(nv, nf);
+        const size_t bytes = tile_bytes(nv, nf);
         size_t off = host.size();
         host.resize(off + bytes, 0);
         float* f = reinterpret_cast<float*>(host.data() + off);
@@ -616,9 +616,8 @@ hydro_status hydro_mesh_upload(hydro_ctx* ctx, const void* vertex_data, size_t v
             const double dx = (double)p[0] - c[0], dy = (double)p[1] - c[1], dz = (double)p[2] - c[2];
             r2 = std::max(r2, dx * dx + dy * dy + dz * dz);
         }
-        const float sphere[4] = {c[0], c[1], c[2], std::nextafter((float)(std::sqrt(r2) * (1.0 + 1e-6)), 1e30f)};
-        std::memcpy(host.data() + off + tile_bytes(nv, nf), sphere, 16);
-        pend.push_back(Pending{off, (uint16_t)nv, (uint16_t)nf, tile_first_face});
+        const float4 sphere = make_float4(c[0], c[1], c[2], std::nextafter((float)(std::sqrt(r2) * (1.0 + 1e-6)), 1e30f));
+        pend.push_back(Pending{off, (uint16_t)nv, (uint16_t)nf, tile_first_face, sphere});
         for (uint32_t g : tv) local[g] = -1;
         tv.clear();
         ti.clear();
@@ -656,7 +655,7 @@ hydro_status hydro_mesh_upload(hydro_ctx* ctx, const void* vertex_data, size_t v
     m.first_tile = (uint32_t)ctx->tiles_h.size();
     m.n_tiles = (uint32_t)pend.size();
     for (const Pending& p : pend)
-        ctx->tiles_h.push_back(TileDesc{reinterpret_cast<const float*>(dev + p.offset), p.nv, p.nf, p.first_face});
+        ctx->tiles_h.push_back(TileDesc{reinterpret_cast<const float*>(dev + p.offset), p.nv, p.nf, p.first_face, p.sphere});
     *out_id = (hydro_mesh_id)ctx->meshes.size();
     ctx->meshes.push_back(m);
     return HYDRO_OK;
@@ -1036,7 +1035,7 @@ hydro_status compound_launch(hydro_compound_batch* cb, const hydro_body* d_compo
         P.binfo = b->binfo_d;
         P.partials = b->partials_d;
         P.bparams = b->bparams_d;
-        P.chunk_active = b->chunk_active_d;
+        P.active = b->active_d;
         P.n_bodies = b->n_bodies;
         P.n_chunks = b->n_chunks;
         err = b->err_d;
@@ -1049,7 +1048,7 @@ hydro_status compound_launch(hydro_compound_batch* cb, const hydro_body* d_compo
     P.tiles = ctx->tiles_d;
     P.err = err;
     P.work = err + 32;
-    P.active_end = err + 48;
+    P.n_listed = err + 48;
     P.ocean = make_ocean(ctx, ocean);
     P.st.damping = settings->damping_forces ? 1 : 0;
     P.st.buoyancy = settings->realistic_buoyancy ? 1 : 0;
@@ -1935,7 +1934,7 @@ static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBy
 
 std::mutex g_static_mu;
 void* g_static_ptr[kStaticMaxDevices] = {};
-ChunkDesc g_static_chunks[kStaticScratchBytes / 208];
+ChunkDesc g_static_chunks[kStaticScratchBytes / 224];
 BodyInfo g_static_binfo[HYDRO_STATIC_MAX_BODIES];
 
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
@@ -2020,7 +2019,7 @@ extern "C" hydro_status hydro_compute_wrenches_static(hydro_ctx* ctx, const hydr
     const size_t off_bparams = align256(off_binfo + (size_t)n_bodies * sizeof(BodyInfo));
     const size_t off_chunks = align256(off_bparams + (size_t)n_bodies * sizeof(BodyParams));
     const size_t off_active = align256(off_chunks + nc * sizeof(ChunkDesc));
-    const size_t off_partials = align256(off_active + nc);
+    const size_t off_partials = align256(off_active + nc * sizeof(ActiveChunk));
     const size_t total = off_partials + nc * kPartialStride * sizeof(double);
     if (total > kStaticScratchBytes)
         return fail(ctx, HYDRO_ERR_INVALID_ARG, "static step: needs %zu scratch bytes, the maximum is %zu",
@@ -2043,8 +2042,8 @@ extern "C" hydro_status hydro_compute_wrenches_static(hydro_ctx* ctx, const hydr
     P.partials = reinterpret_cast<double*>(base + off_partials);
     P.err = reinterpret_cast<unsigned*>(base + off_err);
     P.work = reinterpret_cast<unsigned*>(base + off_err) + 32;
-    P.active_end = reinterpret_cast<unsigned*>(base + off_err) + 48;
-    P.chunk_active = reinterpret_cast<uint8_t*>(base + off_active);
+    P.n_listed = reinterpret_cast<unsigned*>(base + off_err) + 48;
+    P.active = reinterpret_cast<ActiveChunk*>(base + off_active);
     P.n_bodies = n_bodies;
     P.n_chunks = (uint32_t)nc;
     P.ocean = make_ocean(ctx, ocean);

@@ -45,11 +45,16 @@ enum : int { OP_BODY = 0, OP_SURFACE = 1, OP_SUBMERGED = 2, OP_AERO = 3, OP_AERO
 // (nvp = nv rounded up to 4) followed by one uint32 per face holding its
 // three local vertex indices (9 bits each: i0 | i1 << 9 | i2 << 18), padded
 // to 16 bytes; `first_face` is the tile's first face in the uploaded order.
-struct TileDesc {
+// `sphere` bounds the tile's vertices in mesh coordinates (centre x, y, z,
+// radius rounded up so that every vertex lies inside); it lives in this
+// table (L2-resident) rather than in the tile block, so that the chunk
+// kernel can test a chunk's tiles against the surface without an HBM read.
+struct __align__(16) TileDesc {
     const float* block;
     uint16_t nv;
     uint16_t nf;
     uint32_t first_face;
+    float4 sphere;
 };
 
 // Bytes of one tile block: x, y, z (nv rounded up to 4 each) and one packed
@@ -60,14 +65,6 @@ __host__ __device__ __forceinline__ uint32_t tile_bytes(uint32_t nv, uint32_t nf
     return (nvp * 12u + nf * 4u + 15u) & ~15u;
 }
 
-// Each tile block is followed in memory (not copied with it) by the tile's
-// bounding sphere in mesh coordinates: float4 (centre x, y, z, radius),
-// radius rounded up so that every vertex of the tile lies inside.
-__host__ __device__ __forceinline__ uint32_t tile_block_bytes(uint32_t nv, uint32_t nf)
-{
-    return tile_bytes(nv, nf) + 16u;
-}
-
 constexpr int kMaxTilesPerChunk = 16;
 
 // One work item: tiles [first_tile, first_tile + n_tiles) of one body.
@@ -76,6 +73,17 @@ struct ChunkDesc {
     uint32_t first_tile;
     uint32_t n_tiles;
     uint32_t chunk_in_body;
+};
+
+// A chunk whose body runs a face loop in this launch: the prep kernels
+// append one per such chunk (in the order their atomics land, which no
+// result depends on: every chunk writes its own partial) and the chunk
+// kernel's producers claim them in list order.
+struct ActiveChunk {
+    uint32_t body;
+    uint32_t first_tile;
+    uint32_t n_tiles;
+    uint32_t chunk;      // index of the chunk's partial
 };
 
 // Per body of a batch.

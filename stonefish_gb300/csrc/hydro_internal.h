@@ -18,11 +18,11 @@ struct KParams {
     double* partials;        // n_chunks * kPartialStride
     unsigned* err;           // per-launch error word (bit 0: a bounded wait timed out)
     unsigned* work;          // chunk counter of the persistent kernel
-    unsigned* active_end;    // 1 + last chunk with a face loop (atomicMax in prep, reset by finalize)
+    unsigned* n_listed;      // length of `active` (atomicAdd in prep, reset by finalize)
     const uint32_t* n_active;  // optional (device): only bodies [0, *n_active) are evaluated
     hydro_aero_wrench* aero_io;            // OP_AERO / OP_AERO_BODY outputs
     const hydro_aero_params* aero_params;  // OP_AERO_BODY correction inputs
-    uint8_t* chunk_active;   // per chunk: 1 when its body runs a face loop
+    ActiveChunk* active;     // chunks with a face loop, n_chunks entries of room
     uint32_t n_bodies;
     uint32_t n_chunks;
     OceanDev ocean;

@@ -7,10 +7,10 @@
 //             SolidEntity.cpp:1239-1261), loop kind and the body's FP32
 //             parameters (the glm casts of ComputeHydrodynamicForcesSurface);
 //   chunk     persistent CTAs.  One producer lane claims chunks (runs of up
-//             to 16 tiles of <= 384 faces with their <= 384 distinct
-//             vertices, contiguous in HBM) and streams their tiles into an
-//             8-stage shared-memory ring with 1-D TMA bulk copies signalled
-//             on mbarriers; 6 consumer warps transform each vertex once
+//             to 16 tiles of <= 448 faces with their <= 448 distinct
+//             vertices, contiguous in HBM) and streams their tiles into a
+//             4-stage shared-memory ring with 1-D TMA bulk copies signalled
+//             on mbarriers; 7 consumer warps transform each vertex once
 //             (with its depth, Ocean::GetDepth) and evaluate the faces
 //             (surface loop :1337-1687, submerged loop :1748-1789, or the
 //             aerodynamic loop :1885-1915) from shared memory.  Per-face
@@ -18,8 +18,8 @@
 //             per thread, then by a butterfly reduce-scatter across the warp
 //             into a two-sum (float-float) accumulator per lane, combined
 //             across warps and stored as one FP64 partial per chunk;
-//   finalise  one warp per body: the body's chunk partials are added in
-//             chunk order in FP64 and the FP64 finalisation is applied:
+//   finalise  four threads per body: the body's chunk partials are added
+//             in chunk order in FP64 and the FP64 finalisation is applied:
 //             buoyancy (:1689-1720, :1828-1836), the stale-output rules and
 //             CorrectHydrodynamicForces (:1263-1287).
 // No result depends on scheduling: every sum has a fixed order.
@@ -502,6 +502,19 @@ __device__ __forceinline__ void prefetch_lines(const void* p, size_t bytes, int 
         asm volatile("prefetch.global.L1 [%0];" ::"l"(a));
 }
 
+// Appends the chunks of a body that runs a face loop to the launch's list
+// of active chunks, so that the producers never claim the chunks of bodies
+// outside the water or switched off.
+__device__ __forceinline__ void list_chunks(const KParams& P, uint32_t body, const BodyInfo& bi)
+{
+    if (bi.n_chunks == 0u) return;
+    const uint32_t base = atomicAdd(P.n_listed, bi.n_chunks);
+    for (uint32_t c = 0; c < bi.n_chunks; ++c) {
+        const ChunkDesc d = P.chunks[bi.first_chunk + c];
+        P.active[base + c] = ActiveChunk{body, d.first_tile, d.n_tiles, bi.first_chunk + c};
+    }
+}
+
 // One thread per body, grid-stride over the bodies to evaluate (the first
 // *n_active of them when a device count is given).
 __global__ void prep_kernel(const KParams P)
@@ -517,11 +530,7 @@ __global__ void prep_kernel(const KParams P)
         const BodyInfo bi = P.binfo[b];
         body_prologue(P.bodies + b, bi.mesh, P.op, P.ocean, P.st, B);
         P.bparams[b] = B;
-        const uint8_t active = (B.loop != LOOP_NONE) ? 1 : 0;
-        for (uint32_t c = 0; c < bi.n_chunks; ++c) P.chunk_active[bi.first_chunk + c] = active;
-        // chunks are numbered body by body, so the producers can stop after the
-        // last active one (bodies switched off at the end of a batch cost nothing)
-        if (active && bi.n_chunks) atomicMax(P.active_end, bi.first_chunk + bi.n_chunks);
+        if (B.loop != LOOP_NONE) list_chunks(P, b, bi);
     }
 }
 
@@ -585,20 +594,18 @@ size_t chunk_kernel_smem() { return sizeof(ChunkSmem); }
 // :1353-1354) is not loaded at all.  The test bounds the consumer's FP32
 // transform of each vertex with a margin far above its rounding error.  A
 // chunk keeps at least one tile, which carries its (zero) partial.
-__device__ __forceinline__ uint32_t tiles_to_issue(const KParams& P, uint32_t body, const TileDesc (&td)[kMaxTilesPerChunk],
-                                                   uint32_t nt)
+__device__ __forceinline__ uint32_t tiles_to_issue(const KParams& P, const ActiveChunk& ch, uint32_t nt)
 {
     uint32_t keep = (1u << nt) - 1u;
     if (P.ocean.waves) return keep;
-    const BodyParams& B = P.bparams[body];
+    const BodyParams& B = P.bparams[ch.body];
     if (B.loop != LOOP_SURFACE) return keep;
     const float4 T = *reinterpret_cast<const float4*>(B.TC + 8);   // row giving z
     const float rsum = fabsf(T.x) + fabsf(T.y) + fabsf(T.z);
 #pragma unroll
     for (int t = 0; t < kMaxTilesPerChunk; ++t) {
         if ((uint32_t)t >= nt) break;
-        const float4 c = *reinterpret_cast<const float4*>(reinterpret_cast<const char*>(td[t].block) +
-                                                          tile_bytes(td[t].nv, td[t].nf));
+        const float4 c = P.tiles[ch.first_tile + t].sphere;
         const float zc = (T.x * c.x + T.y * c.y) + (T.z * c.z + T.w);
         const float reach = rsum * c.w;
         const float margin = 1e-5f * (rsum * (fabsf(c.x) + fabsf(c.y) + fabsf(c.z) + c.w) + fabsf(T.w)) + 1e-6f;
@@ -607,25 +614,32 @@ __device__ __forceinline__ uint32_t tiles_to_issue(const KParams& P, uint32_t bo
     return keep ? keep : 1u;
 }
 
+// A tile as the producer needs it: where its block starts and its sizes.
+struct TileRef {
+    const float* block;
+    uint16_t nv, nf;
+};
+
 __device__ __forceinline__ void producer(const KParams& P, ChunkSmem& S)
 {
     uint32_t item = 0;
     bool ok = true;
-    // claims run one chunk ahead so that the atomic's latency overlaps work
-    const uint32_t end = min(P.n_chunks, *P.active_end);
+    // claims run one chunk ahead so that the atomic's latency overlaps work;
+    // the list holds only chunks whose body runs a face loop
+    const uint32_t end = min(P.n_chunks, *P.n_listed);
     uint32_t next = atomicAdd(P.work, 1u);
     while (ok && next < end) {
-        const uint32_t c = next;
-        const ChunkDesc ch = P.chunks[c];
-        const uint8_t active = P.chunk_active[c];
+        const ActiveChunk ch = P.active[next];
         next = atomicAdd(P.work, 1u);
-        if (!active) continue;
         const uint32_t nt = ch.n_tiles < (uint32_t)kMaxTilesPerChunk ? ch.n_tiles : (uint32_t)kMaxTilesPerChunk;
-        TileDesc td[kMaxTilesPerChunk];
+        TileRef td[kMaxTilesPerChunk];
 #pragma unroll
         for (int t = 0; t < kMaxTilesPerChunk; ++t)
-            if ((uint32_t)t < nt) td[t] = P.tiles[ch.first_tile + t];
-        const uint32_t keep = tiles_to_issue(P, ch.body, td, nt);
+            if ((uint32_t)t < nt) {
+                const TileDesc& d = P.tiles[ch.first_tile + t];
+                td[t] = TileRef{d.block, d.nv, d.nf};
+            }
+        const uint32_t keep = tiles_to_issue(P, ch, nt);
 #pragma unroll 1
         for (uint32_t t = 0; t < nt; ++t) {
             if (!((keep >> t) & 1u)) continue;
@@ -635,13 +649,13 @@ __device__ __forceinline__ void producer(const KParams& P, ChunkSmem& S)
                 ok = false;
                 break;
             }
-            TileDesc d = td[0];
+            TileRef d = td[0];
 #pragma unroll
             for (int k = 1; k < kMaxTilesPerChunk; ++k)
                 if ((uint32_t)k == t) d = td[k];
             const uint32_t bytes = tile_bytes(d.nv, d.nf);
             ItemMeta m;
-            m.chunk = c;
+            m.chunk = ch.chunk;
             m.flags = ((keep & ((1u << t) - 1u)) == 0u ? ITEM_FIRST : 0) | ((keep >> (t + 1)) == 0u ? ITEM_LAST : 0);
             m.nv = d.nv;
             m.nf = d.nf;
@@ -966,7 +980,7 @@ __global__ void __launch_bounds__(kBodyThreads) finalize_kernel(const KParams P)
     __shared__ double sums[kPerCta][kPartialStride];
     const int sub = (int)(threadIdx.x % kFinSub), slot = (int)(threadIdx.x / kFinSub);
     const int lane = (int)(threadIdx.x & 31u);
-    if (blockIdx.x == 0 && threadIdx.x == 0) *P.active_end = 0u;   // the chunk kernel has finished with it
+    if (blockIdx.x == 0 && threadIdx.x == 0) *P.n_listed = 0u;   // the chunk kernel has finished with it
     const uint32_t limit = P.n_active ? min(P.n_bodies, *P.n_active) : P.n_bodies;
     // grid-stride over groups of kPerCta bodies (uniform across the warp)
     for (uint32_t base = blockIdx.x * kPerCta; base < limit; base += gridDim.x * kPerCta) {
@@ -1129,9 +1143,7 @@ __global__ void compound_prep_kernel(const KParams P, const CompoundParams C)
     B.position = pos;
     B.pad[0] = B.pad[1] = B.pad[2] = 0;
     P.bparams[p] = B;
-    const uint8_t active = (B.loop != LOOP_NONE) ? 1 : 0;
-    for (uint32_t c = 0; c < bi.n_chunks; ++c) P.chunk_active[bi.first_chunk + c] = active;
-    if (active && bi.n_chunks) atomicMax(P.active_end, bi.first_chunk + bi.n_chunks);
+    if (B.loop != LOOP_NONE) list_chunks(P, p, bi);
 }
 
 __device__ __forceinline__ void add3(double* a, const double* b)
@@ -1147,7 +1159,7 @@ __device__ __forceinline__ void add3(double* a, const double* b)
 __global__ void __launch_bounds__(kBodyThreads) compound_finalize_kernel(const KParams P, const CompoundParams C)
 {
     const uint32_t c = blockIdx.x * kBodyThreads + threadIdx.x;
-    if (c == 0) *P.active_end = 0u;
+    if (c == 0) *P.n_listed = 0u;
     if (c >= C.n_compounds) return;
     const hydro_body& cb = C.compounds[c];
     const CompoundInfo ci = C.cinfo[c];
