@@ -109,6 +109,8 @@ struct OceanDev {
     uint32_t wave_layers;
     uint32_t wave_channel[HYDRO_MAX_WAVE_LAYERS];
     float wave_grid[HYDRO_MAX_WAVE_LAYERS];
+    float wave_inv_grid[HYDRO_MAX_WAVE_LAYERS];   // RN(1 / wave_grid[l])
+    int wave_idx32;              // N * N * channels < 2^32: texel offsets fit 32 bits
     hydro_current currents[HYDRO_MAX_CURRENTS];
 };
 
@@ -195,6 +197,18 @@ __device__ __forceinline__ v3 xform(const float* M, float x, float y, float z)
 // ------------------------------------------------------------- wave height
 __device__ __forceinline__ float fracf_(float x) { return x - truncf(x); }
 
+// Texel offset j * N + i of the four bilinear taps, wrapped modulo N * N,
+// times the channel count plus the channel; U is 32-bit when every offset
+// fits (the result is the same integer either way).
+template <class U>
+__device__ __forceinline__ U texel_offset(uint32_t N, int j, int i, uint32_t C, uint32_t ch)
+{
+    const U NN = (U)N * N;
+    U l = (U)j * N + (U)i;
+    if (l >= NN) l -= NN;
+    return l * C + ch;
+}
+
 // OpenGLRealOcean::ComputeInterpolatedWaveData (OpenGLRealOcean.cpp:282-319),
 // texel-centred periodic bilinear; the linear texel index wraps modulo N*N
 // where the reference would read texel N of a row.
@@ -217,29 +231,33 @@ __device__ __forceinline__ float wave_interp(const OceanDev& o, float x, float y
     int j1 = (int)truncf(j1f * Nf);
     float alpha = fracf_(i0f * Nf);
     float beta = fracf_(j0f * Nf);
-    const uint64_t NN = (uint64_t)N * N;
-    uint64_t l0 = (uint64_t)j0 * N + (uint64_t)i0; if (l0 >= NN) l0 -= NN;
-    uint64_t l1 = (uint64_t)j0 * N + (uint64_t)i1; if (l1 >= NN) l1 -= NN;
-    uint64_t l2 = (uint64_t)j1 * N + (uint64_t)i0; if (l2 >= NN) l2 -= NN;
-    uint64_t l3 = (uint64_t)j1 * N + (uint64_t)i1; if (l3 >= NN) l3 -= NN;
     const float* d = o.wave_data;
     const uint32_t C = o.wave_channels;
-    float t0 = __ldg(d + l0 * C + ch);
-    float t1 = __ldg(d + l1 * C + ch);
-    float t2 = __ldg(d + l2 * C + ch);
-    float t3 = __ldg(d + l3 * C + ch);
+    float t0, t1, t2, t3;
+    if (o.wave_idx32) {
+        t0 = __ldg(d + texel_offset<uint32_t>(N, j0, i0, C, ch));
+        t1 = __ldg(d + texel_offset<uint32_t>(N, j0, i1, C, ch));
+        t2 = __ldg(d + texel_offset<uint32_t>(N, j1, i0, C, ch));
+        t3 = __ldg(d + texel_offset<uint32_t>(N, j1, i1, C, ch));
+    } else {
+        t0 = __ldg(d + texel_offset<uint64_t>(N, j0, i0, C, ch));
+        t1 = __ldg(d + texel_offset<uint64_t>(N, j0, i1, C, ch));
+        t2 = __ldg(d + texel_offset<uint64_t>(N, j1, i0, C, ch));
+        t3 = __ldg(d + texel_offset<uint64_t>(N, j1, i1, C, ch));
+    }
     return (1.f - alpha) * (1.f - beta) * t0 + alpha * (1.f - beta) * t1
          + (1.f - alpha) * beta * t2 + alpha * beta * t3;
 }
 
-// OpenGLRealOcean::ComputeWaveHeight (:321-331)
+// OpenGLRealOcean::ComputeWaveHeight (:321-331).  x / gs is the IEEE
+// quotient, formed from RN(1 / gs) with one FMA correction (div_by_rcp).
 __device__ __forceinline__ float wave_height(const OceanDev& o, float x, float y)
 {
     float z = 0.f;
     if (o.wave_data == nullptr) return z;
     for (uint32_t l = 0; l < o.wave_layers; ++l) {
-        float gs = o.wave_grid[l];
-        z -= wave_interp(o, x / gs, y / gs, o.wave_channel[l]);
+        const float gs = o.wave_grid[l], r = o.wave_inv_grid[l];
+        z -= wave_interp(o, div_by_rcp(x, gs, r), div_by_rcp(y, gs, r), o.wave_channel[l]);
     }
     return z;
 }
