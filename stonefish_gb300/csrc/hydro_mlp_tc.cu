@@ -11,12 +11,18 @@
 //     (pack_sw128_kernel), so each layer's weights arrive with one 1-D bulk
 //     copy (cp.async.bulk, mbarrier complete_tx) while the previous layer's
 //     epilogue runs;
-//   * one thread issues tcgen05.mma (M = 128, N = 256 or 16, K = 16 per
-//     instruction, FP32 accumulate in 256 TMEM columns) and commits to an
-//     mbarrier; sixteen warps read the accumulator with tcgen05.ld (warp w
-//     reads TMEM lanes 32 (w % 4) .. +31, a quarter of the columns, 32 at
-//     a time), add the bias, apply SiLU, round to BF16 and write the next
-//     layer's A operand;
+//   * one lane of a dedicated warp issues tcgen05.mma (M = 128, N = 256 or
+//     16, K = 16 per instruction, FP32 accumulate) and commits to an
+//     mbarrier; the accumulators of consecutive layers alternate between
+//     the two halves of 512 TMEM columns;
+//   * sixteen epilogue warps read a layer's accumulator with tcgen05.ld
+//     (warp w reads TMEM lanes 32 (w % 4) .. +31), one 64-column K-block
+//     at a time, add the bias, apply SiLU, round to BF16 and write that
+//     K-block of the next layer's A operand, then arrive on the K-block's
+//     mbarrier: the next layer's MMAs on K-block g start while the
+//     epilogue works on K-blocks g + 1 ..;
+//   * the next layer's weights stream in as four K-block copies, each on
+//     its own mbarrier, as soon as the current layer's MMAs have retired;
 //   * the input features are normalised and rounded in the kernel, the
 //     output (bias added) is written as FP32 rows of 16.
 //
@@ -39,16 +45,17 @@ constexpr int kRows = 128;      // states per CTA = UMMA M
 constexpr int kHid = 256;
 constexpr int kIn = 16;         // features = layer-0 K
 constexpr int kOut = 16;        // output columns (6 used)
-constexpr int kThreads = 512;   // 16 warps
-constexpr uint32_t kTmemCols = 256;
+constexpr int kEpiWarps = 16;                   // epilogue warps
+constexpr int kThreads = (kEpiWarps + 1) * 32;  // + one MMA warp
+constexpr uint32_t kTmemCols = 512;             // two 256-column accumulators
 
 // shared-memory image (offsets from a 1024-byte-aligned base)
 constexpr uint32_t kOffA = 0;                        // 128 x 256 bf16, 4 K-blocks of 16 KB
 constexpr uint32_t kOffW = kOffA + 4 * 16384;        // 256 x 256 bf16, 4 K-blocks of 32 KB
 constexpr uint32_t kOffW3 = kOffW + 4 * 32768;       // 16 x 256 bf16, 4 K-blocks of 2 KB
 constexpr uint32_t kOffBias = kOffW3 + 4 * 2048;     // 3 x 256 + 16 floats
-constexpr uint32_t kOffBar = kOffBias + (3 * kHid + kOut) * 4;
-constexpr uint32_t kOffTmem = kOffBar + 4 * 8;
+constexpr uint32_t kOffBar = kOffBias + (3 * kHid + kOut) * 4;   // 10 mbarriers
+constexpr uint32_t kOffTmem = kOffBar + 10 * 8;
 constexpr uint32_t kSmemBytes = kOffTmem + 16 + 1024; // + alignment slack
 
 // global weight image (bytes)
@@ -174,6 +181,28 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32])
     for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// Split form of tmem_ld16 for software pipelining: the load is issued
+// without waiting, and the wait names the destination registers as in-out
+// operands so that no use of them can be scheduled before it.
+__device__ __forceinline__ void tmem_ld16_issue(uint32_t taddr, uint32_t (&r)[16])
+{
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+                 "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                   "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                   "=r"(r[14]), "=r"(r[15])
+                 : "r"(taddr));
+}
+
+__device__ __forceinline__ void tmem_ld_wait(uint32_t (&r)[16])
+{
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]),
+                   "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]),
+                   "+r"(r[14]), "+r"(r[15])
+                 :: "memory");
+}
+
 // SiLU(z) = z sigmoid(z) = h + h tanh(h) with h = z / 2: one hardware tanh
 // (tanh.approx.f32, relative error about 2^-11) per value, so the absolute
 // error is at most |z| 2^-12, below the BF16 rounding of the activation that
@@ -192,28 +221,48 @@ __device__ __forceinline__ uint32_t pack2(float a, float b)
     return *reinterpret_cast<const uint32_t*>(&h);
 }
 
-// Epilogue of a hidden layer: D (TMEM, 128 x 256 FP32) + bias -> SiLU ->
-// BF16 -> A operand (row = TMEM lane).  Warp w: lanes 32 (w % 4).., columns
-// (w / 4) * 64 .., 32 per TMEM load.
-__device__ __forceinline__ void hidden_epilogue(uint32_t tmem, unsigned char* base, const float* bias)
+__device__ __forceinline__ void mbar_arrive(uint32_t bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(bar) : "memory");
+}
+
+// A hidden layer's epilogue, one K-block (64 columns) at a time: D (TMEM)
+// + bias -> SiLU -> BF16 -> columns 64 g .. of the A operand (row = TMEM
+// lane), then an arrival on K-block g's mbarrier so that the next layer's
+// MMAs on it can start.  Warp w: lanes 32 (w % 4).., columns
+// 64 g + 16 (w / 4) ..; the tensor-memory load of K-block g + 1 is in
+// flight while K-block g is converted.
+__device__ __forceinline__ void hidden_epilogue(uint32_t acc, unsigned char* base, const float* bias, uint32_t abar)
 {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t q = (uint32_t)(warp & 3), quarter = (uint32_t)(warp >> 2);
+    const uint32_t q = (uint32_t)(warp & 3), sub = (uint32_t)(warp >> 2);
     const uint32_t row = 32u * q + (uint32_t)lane;
-#pragma unroll 1
-    for (uint32_t g = 0; g < 2; ++g) {
-        const uint32_t col = quarter * 64u + g * 32u;
-        float v[32];
-        tmem_ld32(tmem + ((32u * q) << 16) + col, v);
-        uint32_t w[16];
+    const uint32_t lanes = (32u * q) << 16;
+    uint32_t cur[16], nxt[16];
+    tmem_ld16_issue(acc + lanes + 16u * sub, cur);
+    tmem_ld_wait(cur);
 #pragma unroll
-        for (int i = 0; i < 16; ++i)
-            w[i] = pack2(silu_fast(v[2 * i] + bias[col + 2 * i]), silu_fast(v[2 * i + 1] + bias[col + 2 * i + 1]));
+    for (uint32_t g = 0; g < 4; ++g) {
+        const uint32_t col = 64u * g + 16u * sub;
+        if (g < 3) tmem_ld16_issue(acc + lanes + col + 64u, nxt);
+        uint32_t w[8];
 #pragma unroll
-        for (int c = 0; c < 4; ++c)
+        for (int i = 0; i < 8; ++i)
+            w[i] = pack2(silu_fast(__uint_as_float(cur[2 * i]) + bias[col + 2 * i]),
+                         silu_fast(__uint_as_float(cur[2 * i + 1]) + bias[col + 2 * i + 1]));
+#pragma unroll
+        for (int c = 0; c < 2; ++c)
             *reinterpret_cast<uint4*>(base + kOffA + sw128_offset(kRows, row, col + 8u * c)) =
                 make_uint4(w[4 * c], w[4 * c + 1], w[4 * c + 2], w[4 * c + 3]);
+        fence_async_smem();
+        mbar_arrive(abar + 8u * g);
+        if (g < 3) {
+            tmem_ld_wait(nxt);
+#pragma unroll
+            for (int i = 0; i < 16; ++i) cur[i] = nxt[i];
+        }
     }
+    fence_before();
 }
 
 }  // namespace tc
@@ -229,10 +278,12 @@ mlp_tc_kernel(const float* __restrict__ feats, uint32_t n, const float* __restri
     const uint32_t raw = smem_u32(smem_raw);
     unsigned char* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
     const uint32_t sb = smem_u32(base);
-    const uint32_t barW = sb + kOffBar, barM = sb + kOffBar + 8;
+    // mbarriers: weights of layers 0 and 3; MMA commits; the four K-block
+    // copies of a hidden layer's weights; the four K-blocks of A
+    const uint32_t barW0 = sb + kOffBar, barM = barW0 + 8, wbar = barW0 + 16, abar = barW0 + 48;
     float* bias = reinterpret_cast<float*>(base + kOffBias);
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(base + kOffTmem);
-    const int tid = threadIdx.x, warp = tid >> 5;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint32_t row0 = blockIdx.x * (uint32_t)kRows;
     const uint64_t kLimit = 1000000000ull;   // 1 s per wait
 
@@ -242,8 +293,13 @@ mlp_tc_kernel(const float* __restrict__ feats, uint32_t n, const float* __restri
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(barW) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(barW0) : "memory");
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(barM) : "memory");
+        for (uint32_t g = 0; g < 4; ++g) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(wbar + 8u * g) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(abar + 8u * g), "r"(kEpiWarps * 32)
+                         : "memory");
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     fence_before();
@@ -253,9 +309,9 @@ mlp_tc_kernel(const float* __restrict__ feats, uint32_t n, const float* __restri
 
     // weights of layers 0 and 3 (40 KB)
     if (tid == 0) {
-        expect_tx(barW, 32768u + 8192u);
-        bulk_load(sb + kOffW, wimg + kImgW0, 32768u, barW);
-        bulk_load(sb + kOffW3, wimg + kImgW3, 8192u, barW);
+        expect_tx(barW0, 32768u + 8192u);
+        bulk_load(sb + kOffW, wimg + kImgW0, 32768u, barW0);
+        bulk_load(sb + kOffW3, wimg + kImgW3, 8192u, barW0);
     }
     for (int i = tid; i < kHid; i += kThreads) {
         bias[i] = b0[i];
@@ -280,84 +336,103 @@ mlp_tc_kernel(const float* __restrict__ feats, uint32_t n, const float* __restri
     __syncthreads();
 
     bool ok = true;
-    uint32_t phaseW = 0, phaseM = 0;
-    // ---- layers 0..2: hidden, N = 256
-#pragma unroll 1
-    for (int layer = 0; layer < 3 && ok; ++layer) {
-        if (tid == 0) {
-            ok = mbar_wait(barW, phaseW, kLimit);
+    if (warp == kEpiWarps) {
+        // ---- MMA warp: one lane issues every layer's MMAs and the weight copies
+        if (lane == 0) {
+            const uint32_t id_hid = idesc_bf16(128, 256), id_out = idesc_bf16(128, kOut);
+            uint32_t w_pending = 0;   // K-block copies issued and not yet waited for
+            uint32_t w_phase = 0;
+            uint32_t commits = 0, seen = 0;   // barM phases committed / observed complete
+            ok = mbar_wait(barW0, 0u, kLimit);
             if (ok) {
                 fence_after();
-                const uint32_t idesc = idesc_bf16(128, 256);
-                const int ksteps = layer == 0 ? 1 : kHid / 16;
-                for (int j = 0; j < ksteps; ++j) {
-                    const uint32_t off_a = kOffA + (uint32_t)(j >> 2) * (kRows * 128u) + (uint32_t)(j & 3) * 32u;
-                    const uint32_t off_b = kOffW + (uint32_t)(j >> 2) * (kHid * 128u) + (uint32_t)(j & 3) * 32u;
-                    mma(tmem, sw128_desc(sb + off_a), sw128_desc(sb + off_b), idesc, j > 0 ? 1u : 0u);
-                }
+                mma(tmem, sw128_desc(sb + kOffA), sw128_desc(sb + kOffW), id_hid, 0u);   // layer 0: K = 16
                 mma_commit(barM);
+                ++commits;
             }
-        }
-        phaseW ^= 1u;
-        ok = __syncthreads_and(ok) != 0;
-        if (!ok) break;
-        ok = mbar_wait(barM, phaseM, kLimit);
-        phaseM ^= 1u;
-        ok = __syncthreads_and(ok) != 0;
-        if (!ok) break;
-        fence_after();
-        // the weight buffer is free again: stream the next layer's weights
-        if (tid == 0 && layer < 2) {
-            expect_tx(barW, 131072u);
-            bulk_load(sb + kOffW, wimg + (layer == 0 ? kImgW1 : kImgW2), 131072u, barW);
-        }
-        hidden_epilogue(tmem, base, bias + layer * kHid);
-        fence_before();
-        fence_async_smem();
-        __syncthreads();
-    }
-    // ---- layer 3: N = 16, bias, FP32 rows of 16
-    if (ok) {
-        if (tid == 0) {
-            fence_after();
-            const uint32_t idesc = idesc_bf16(128, kOut);
-            for (int j = 0; j < kHid / 16; ++j) {
-                const uint32_t off_a = kOffA + (uint32_t)(j >> 2) * (kRows * 128u) + (uint32_t)(j & 3) * 32u;
-                const uint32_t off_b = kOffW3 + (uint32_t)(j >> 2) * (kOut * 128u) + (uint32_t)(j & 3) * 32u;
-                mma(tmem, sw128_desc(sb + off_a), sw128_desc(sb + off_b), idesc, j > 0 ? 1u : 0u);
-            }
-            mma_commit(barM);
-        }
-        ok = mbar_wait(barM, phaseM, kLimit);
-        phaseM ^= 1u;
-        ok = __syncthreads_and(ok) != 0;
-        if (ok) {
-            fence_after();
-            if (warp < 4) {
-                const int lane = tid & 31;
-                float v[16];
-                tmem_ld16(tmem + ((32u * (uint32_t)warp) << 16), v);
-                const uint32_t gr = row0 + 32u * (uint32_t)warp + (uint32_t)lane;
-                if (gr < n) {
-                    float4* o = reinterpret_cast<float4*>(out + (size_t)gr * kOut);
-                    const float* bb = bias + 3 * kHid;
-#pragma unroll
-                    for (int i = 0; i < 4; ++i)
-                        o[i] = make_float4(v[4 * i] + bb[4 * i], v[4 * i + 1] + bb[4 * i + 1],
-                                           v[4 * i + 2] + bb[4 * i + 2], v[4 * i + 3] + bb[4 * i + 3]);
+#pragma unroll 1
+            for (uint32_t l = 1; l <= 3 && ok; ++l) {
+                const uint32_t prev = (l - 1u) & 1u;   // parity of layer l - 1's completions
+                if (l < 3) {
+                    // layer l - 1's MMAs have retired: the weight buffer takes layer l's
+                    ok = mbar_wait(barM, prev, kLimit);
+                    if (!ok) break;
+                    ++seen;
+                    for (uint32_t g = 0; g < 4; ++g) {
+                        expect_tx(wbar + 8u * g, 32768u);
+                        bulk_load(sb + kOffW + 32768u * g, wimg + (l == 1 ? kImgW1 : kImgW2) + 32768u * g, 32768u,
+                                  wbar + 8u * g);
+                    }
+                    w_pending = 0xFu;
                 }
+                const uint32_t acc = tmem + 256u * (l & 1u);
+#pragma unroll 1
+                for (uint32_t g = 0; g < 4 && ok; ++g) {
+                    if (l < 3) {
+                        ok = mbar_wait(wbar + 8u * g, w_phase, kLimit);
+                        if (!ok) break;
+                        w_pending &= ~(1u << g);
+                    }
+                    ok = mbar_wait(abar + 8u * g, prev, kLimit);   // K-block g of layer l's input
+                    if (!ok) break;
+                    fence_after();
+#pragma unroll
+                    for (uint32_t j = 0; j < 4; ++j) {
+                        const uint32_t off_a = kOffA + g * (kRows * 128u) + j * 32u;
+                        if (l < 3) {
+                            const uint32_t off_b = kOffW + g * (kHid * 128u) + j * 32u;
+                            mma(acc, sw128_desc(sb + off_a), sw128_desc(sb + off_b), id_hid, (g | j) ? 1u : 0u);
+                        } else {
+                            const uint32_t off_b = kOffW3 + g * (kOut * 128u) + j * 32u;
+                            mma(acc, sw128_desc(sb + off_a), sw128_desc(sb + off_b), id_out, (g | j) ? 1u : 0u);
+                        }
+                    }
+                }
+                if (!ok) break;
+                mma_commit(barM);
+                ++commits;
+                if (l < 3) w_phase ^= 1u;
+            }
+            if (!ok) {
+                // let issued tensor-core work and weight copies retire before
+                // the tensor memory is freed and the CTA exits (bounded): one
+                // more commit, then the barrier's phases in order
+                atomicOr(err, 1u);
+                mma_commit(barM);
+                ++commits;
+                for (uint32_t k = seen; k < commits; ++k) mbar_wait(barM, k & 1u, kLimit);
+                for (uint32_t g = 0; g < 4; ++g)
+                    if ((w_pending >> g) & 1u) mbar_wait(wbar + 8u * g, w_phase, kLimit);
             }
         }
-    }
-    if (!ok) {
-        // let issued tensor-core work and weight copies retire before the
-        // tensor memory is freed and the CTA exits (bounded)
-        if (tid == 0) {
-            atomicOr(err, 1u);
-            mma_commit(barM);
-            mbar_wait(barM, phaseM, kLimit);
-            mbar_wait(barW, phaseW, kLimit);
+        __syncwarp();
+        ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+    } else {
+        // ---- epilogue warps: layers 0..2 feed the next layer K-block by K-block
+#pragma unroll 1
+        for (uint32_t l = 0; l < 3 && ok; ++l) {
+            ok = mbar_wait(barM, l & 1u, kLimit);
+            if (!ok) break;
+            fence_after();
+            hidden_epilogue(tmem + 256u * (l & 1u), base, bias + l * kHid, abar);
         }
+        // ---- output layer: N = 16, bias, FP32 rows of 16
+        if (ok) ok = mbar_wait(barM, 1u, kLimit);
+        if (ok && warp < 4) {
+            fence_after();
+            float v[16];
+            tmem_ld16(tmem + 256u + ((32u * (uint32_t)warp) << 16), v);
+            const uint32_t gr = row0 + 32u * (uint32_t)warp + (uint32_t)lane;
+            if (gr < n) {
+                float4* o = reinterpret_cast<float4*>(out + (size_t)gr * kOut);
+                const float* bb = bias + 3 * kHid;
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+                    o[i] = make_float4(v[4 * i] + bb[4 * i], v[4 * i + 1] + bb[4 * i + 1],
+                                       v[4 * i + 2] + bb[4 * i + 2], v[4 * i + 3] + bb[4 * i + 3]);
+            }
+        }
+        if (!ok && lane == 0) atomicOr(err, 1u);
     }
     fence_before();
     __syncthreads();
