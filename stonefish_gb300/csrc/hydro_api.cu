@@ -583,7 +583,7 @@ hydro_status hydro_mesh_upload(hydro_ctx* ctx, const void* vertex_data, size_t v
     std::vector<uint32_t> tv;              // global ids of the open tile's vertices
     std::vector<uint32_t> ti;              // packed local indices of the open tile's faces
     std::vector<char> host;                // all tile blocks of this mesh
-    struct Pending { size_t offset; uint16_t nv, nf; uint32_t first_face; float4 sphere; };
+    struct Pending { size_t offset; uint16_t nv, nf; uint32_t first_face; float4 sphere, half; };
     std::vector<Pending> pend;
     uint32_t tile_first_face = 0;
     auto close_tile = [&](uint32_t next_face) {
@@ -611,15 +611,20 @@ hydro_status hydro_mesh_upload(hydro_ctx* ctx, const void* vertex_data, size_t v
         // from the stored (float) centre, rounded up
         float c[3];
         for (int a = 0; a < 3; ++a) c[a] = (float)(0.5 * (lo[a] + hi[a]));
-        double r2 = 0.0;
+        double r2 = 0.0, hx = 0.0, hy = 0.0, hz = 0.0;
         for (uint32_t k = 0; k < nv; ++k) {
             float p[3];
             pos(tv[k], p);
             const double dx = (double)p[0] - c[0], dy = (double)p[1] - c[1], dz = (double)p[2] - c[2];
             r2 = std::max(r2, dx * dx + dy * dy + dz * dz);
+            hx = std::max(hx, std::fabs(dx));
+            hy = std::max(hy, std::fabs(dy));
+            hz = std::max(hz, std::fabs(dz));
         }
-        const float4 sphere = make_float4(c[0], c[1], c[2], std::nextafter((float)(std::sqrt(r2) * (1.0 + 1e-6)), 1e30f));
-        pend.push_back(Pending{off, (uint16_t)nv, (uint16_t)nf, tile_first_face, sphere});
+        auto up = [](double x) { return std::nextafter((float)(x * (1.0 + 1e-6)), 1e30f); };
+        const float4 sphere = make_float4(c[0], c[1], c[2], up(std::sqrt(r2)));
+        const float4 half = make_float4(up(hx), up(hy), up(hz), 0.f);
+        pend.push_back(Pending{off, (uint16_t)nv, (uint16_t)nf, tile_first_face, sphere, half});
         for (uint32_t g : tv) local[g] = -1;
         tv.clear();
         ti.clear();
@@ -657,7 +662,8 @@ hydro_status hydro_mesh_upload(hydro_ctx* ctx, const void* vertex_data, size_t v
     m.first_tile = (uint32_t)ctx->tiles_h.size();
     m.n_tiles = (uint32_t)pend.size();
     for (const Pending& p : pend)
-        ctx->tiles_h.push_back(TileDesc{reinterpret_cast<const float*>(dev + p.offset), p.nv, p.nf, p.first_face, p.sphere});
+        ctx->tiles_h.push_back(TileDesc{reinterpret_cast<const float*>(dev + p.offset), p.nv, p.nf, p.first_face, p.sphere,
+                                        p.half});
     *out_id = (hydro_mesh_id)ctx->meshes.size();
     ctx->meshes.push_back(m);
     return HYDRO_OK;

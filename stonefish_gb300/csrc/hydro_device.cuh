@@ -45,16 +45,19 @@ enum : int { OP_BODY = 0, OP_SURFACE = 1, OP_SUBMERGED = 2, OP_AERO = 3, OP_AERO
 // (nvp = nv rounded up to 4) followed by one uint32 per face holding its
 // three local vertex indices (9 bits each: i0 | i1 << 9 | i2 << 18), padded
 // to 16 bytes; `first_face` is the tile's first face in the uploaded order.
-// `sphere` bounds the tile's vertices in mesh coordinates (centre x, y, z,
-// radius rounded up so that every vertex lies inside); it lives in this
-// table (L2-resident) rather than in the tile block, so that the chunk
-// kernel can test a chunk's tiles against the surface without an HBM read.
+// `sphere` and `half` bound the tile's vertices in mesh coordinates: the
+// centre of their box (x, y, z) with the radius of a sphere about it, and
+// the box's half extents, each rounded up so that every vertex lies inside.
+// They live in this table (L2-resident) rather than in the tile block, so
+// that the chunk kernel can test a chunk's tiles against the surface
+// without an HBM read.
 struct __align__(16) TileDesc {
     const float* block;
     uint16_t nv;
     uint16_t nf;
     uint32_t first_face;
-    float4 sphere;
+    float4 sphere;      // centre x, y, z; radius
+    float4 half;        // half extents x, y, z of the box about the centre; w unused
 };
 
 // Bytes of one tile block: x, y, z (nv rounded up to 4 each) and one packed

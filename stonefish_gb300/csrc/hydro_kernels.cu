@@ -589,11 +589,15 @@ struct __align__(128) ChunkSmem {
 size_t chunk_kernel_smem() { return sizeof(ChunkSmem); }
 
 // Tiles of a chunk to stream (bit t for tile t).  On a flat surface a tile
-// of a surface-loop body whose bounding sphere lies wholly above the water
-// (every vertex at depth < 0, so every face is skipped, SolidEntity.cpp
-// :1353-1354) is not loaded at all.  The test bounds the consumer's FP32
-// transform of each vertex with a margin far above its rounding error.  A
-// chunk keeps at least one tile, which carries its (zero) partial.
+// of a surface-loop body that lies wholly above the water (every vertex at
+// depth < 0, so every face is skipped, SolidEntity.cpp:1353-1354) is not
+// loaded at all.  The highest vertex of the tile is bounded by its centre's
+// height plus the smaller of two reaches along the row of T_C that gives z:
+// the bounding sphere's radius times the row's norm (2^-20 covers its FP32
+// evaluation) and the box's half extents weighted by the row's magnitudes.
+// The margin bounds the consumer's FP32 transform of each vertex far above
+// its rounding error.  A chunk keeps at least one tile, which carries its
+// (zero) partial.
 __device__ __forceinline__ uint32_t tiles_to_issue(const KParams& P, const ActiveChunk& ch, uint32_t nt)
 {
     uint32_t keep = (1u << nt) - 1u;
@@ -601,14 +605,17 @@ __device__ __forceinline__ uint32_t tiles_to_issue(const KParams& P, const Activ
     const BodyParams& B = P.bparams[ch.body];
     if (B.loop != LOOP_SURFACE) return keep;
     const float4 T = *reinterpret_cast<const float4*>(B.TC + 8);   // row giving z
-    const float rsum = fabsf(T.x) + fabsf(T.y) + fabsf(T.z);
+    const float ax = fabsf(T.x), ay = fabsf(T.y), az = fabsf(T.z);
+    const float rn = sqrtf((T.x * T.x + T.y * T.y) + T.z * T.z) * (1.f + 0x1p-20f);
 #pragma unroll
     for (int t = 0; t < kMaxTilesPerChunk; ++t) {
         if ((uint32_t)t >= nt) break;
-        const float4 c = P.tiles[ch.first_tile + t].sphere;
+        const TileDesc& d = P.tiles[ch.first_tile + t];
+        const float4 c = d.sphere, h = d.half;
         const float zc = (T.x * c.x + T.y * c.y) + (T.z * c.z + T.w);
-        const float reach = rsum * c.w;
-        const float margin = 1e-5f * (rsum * (fabsf(c.x) + fabsf(c.y) + fabsf(c.z) + c.w) + fabsf(T.w)) + 1e-6f;
+        const float reach = fminf(c.w * rn, (ax * h.x + ay * h.y) + az * h.z);
+        const float margin = 1e-5f * ((ax * (fabsf(c.x) + h.x) + ay * (fabsf(c.y) + h.y)) +
+                                      (az * (fabsf(c.z) + h.z) + fabsf(T.w))) + 1e-6f;
         if (zc + reach + margin < 0.f) keep &= ~(1u << t);
     }
     return keep ? keep : 1u;
