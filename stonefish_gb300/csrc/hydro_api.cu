@@ -558,6 +558,103 @@ void hydro_destroy(hydro_ctx* ctx)
     delete ctx;
 }
 
+// Tile membership: faces grouped into compact patches of the surface, so
+// that a tile lies wholly above or wholly under the water more often and
+// shares more vertices between its faces.  A tile grows from a seed face by
+// repeatedly taking, among the unused faces that share a vertex with it,
+// one that adds the fewest new vertices (ties: the one reached first, so
+// that the tile grows ring by ring).  When no such face is left
+// the next unused face in upload order seeds the same tile (disconnected
+// parts, such as the separately indexed sides of a box, then share tiles).
+// A tile closes at kTileFaces faces or when no reachable face fits under
+// kTileVerts vertices.  `order` lists the faces tile by tile, `starts` the
+// tiles' first positions in it (plus the end).
+static void build_tiles(uint32_t n_vertices, const uint32_t* fi, uint32_t n_faces, std::vector<uint32_t>& order,
+                        std::vector<uint32_t>& starts)
+{
+    std::vector<uint32_t> first(n_vertices + 1, 0);          // faces around each vertex (CSR)
+    for (size_t i = 0; i < 3 * (size_t)n_faces; ++i) ++first[fi[i] + 1];
+    for (uint32_t v = 0; v < n_vertices; ++v) first[v + 1] += first[v];
+    std::vector<uint32_t> around(3 * (size_t)n_faces);
+    {
+        std::vector<uint32_t> fill(first.begin(), first.end() - 1);
+        for (uint32_t f = 0; f < n_faces; ++f)
+            for (int k = 0; k < 3; ++k) around[fill[fi[3 * (size_t)f + k]]++] = f;
+    }
+    std::vector<uint8_t> used(n_faces, 0), best(n_faces, 4);
+    std::vector<uint8_t> in_tile(n_vertices, 0);
+    std::vector<uint32_t> tverts, touched;
+    std::vector<uint32_t> queue[4];        // candidates by count of new vertices, in the order reached
+    size_t head[4];
+    order.clear();
+    order.reserve(n_faces);
+    starts.assign(1, 0u);
+    auto fresh = [&](uint32_t f) {
+        const uint32_t* t = fi + 3 * (size_t)f;
+        uint32_t n = 0;
+        for (int k = 0; k < 3; ++k) {
+            bool dup = false;
+            for (int j = 0; j < k; ++j) dup |= (t[j] == t[k]);
+            if (!dup && !in_tile[t[k]]) ++n;
+        }
+        return n;
+    };
+    uint32_t seed = 0;
+    while (order.size() < n_faces) {
+        uint32_t tf = 0;
+        for (int b = 0; b < 4; ++b) {
+            queue[b].clear();
+            head[b] = 0;
+        }
+        touched.clear();
+        auto push = [&](uint32_t g) {
+            if (used[g]) return;
+            const uint32_t nw = fresh(g);
+            if (nw >= best[g]) return;
+            if (best[g] == 4) touched.push_back(g);
+            best[g] = (uint8_t)nw;
+            queue[nw].push_back(g);
+        };
+        // only the faces around a vertex that joins the tile change their
+        // count of new vertices, so only those are (re)considered
+        auto take = [&](uint32_t f) {
+            used[f] = 1;
+            order.push_back(f);
+            ++tf;
+            uint32_t joined[3];
+            int nj = 0;
+            for (int k = 0; k < 3; ++k) {
+                const uint32_t v = fi[3 * (size_t)f + k];
+                if (!in_tile[v]) {
+                    in_tile[v] = 1;
+                    tverts.push_back(v);
+                    joined[nj++] = v;
+                }
+            }
+            for (int k = 0; k < nj; ++k)
+                for (uint32_t i = first[joined[k]]; i < first[joined[k] + 1]; ++i) push(around[i]);
+        };
+        while (tf < (uint32_t)kTileFaces) {
+            int b = 0;
+            while (b < 4 && head[b] == queue[b].size()) ++b;
+            if (b == 4) {
+                while (seed < n_faces && used[seed]) ++seed;
+                if (seed >= n_faces || tverts.size() + fresh(seed) > (size_t)kTileVerts) break;
+                take(seed);
+                continue;
+            }
+            const uint32_t g = queue[b][head[b]++];
+            if (used[g] || best[g] != (uint8_t)b) continue;       // taken, or queued again with fewer
+            if (tverts.size() + (size_t)b > (size_t)kTileVerts) continue;
+            take(g);
+        }
+        starts.push_back((uint32_t)order.size());
+        for (uint32_t v : tverts) in_tile[v] = 0;
+        tverts.clear();
+        for (uint32_t g : touched) best[g] = 4;
+    }
+}
+
 hydro_status hydro_mesh_upload(hydro_ctx* ctx, const void* vertex_data, size_t vertex_stride,
                                uint32_t n_vertices, const uint32_t* face_indices,
                                uint32_t n_faces, hydro_mesh_id* out_id)
@@ -577,20 +674,22 @@ hydro_status hydro_mesh_upload(hydro_ctx* ctx, const void* vertex_data, size_t v
     const char* vbytes = static_cast<const char*>(vertex_data);
     auto pos = [&](uint32_t v, float* p) { std::memcpy(p, vbytes + (size_t)v * vertex_stride, 12); };
 
-    // Greedy tiling in face order: a tile closes when it would exceed
-    // kTileFaces faces or kTileVerts distinct vertices.
+    // Tiles are compact patches of the surface (build_tiles); within a tile
+    // faces keep the order in which they joined it.
+    std::vector<uint32_t> order, starts;
+    build_tiles(n_vertices, face_indices, n_faces, order, starts);
     std::vector<int32_t> local(n_vertices, -1);
     std::vector<uint32_t> tv;              // global ids of the open tile's vertices
     std::vector<uint32_t> ti;              // packed local indices of the open tile's faces
+    std::vector<uint32_t> tid;             // upload indices of the open tile's faces
     std::vector<char> host;                // all tile blocks of this mesh
     struct Pending { size_t offset; uint16_t nv, nf; uint32_t first_face; float4 sphere, half; };
     std::vector<Pending> pend;
-    uint32_t tile_first_face = 0;
-    auto close_tile = [&](uint32_t next_face) {
+    auto close_tile = [&](uint32_t tile_first) {
         if (ti.empty()) return;
         const uint32_t nv = (uint32_t)tv.size(), nf = (uint32_t)ti.size();
         const uint32_t nvp = (nv + 3) & ~3u;
-        const size_t bytes = tile_bytes(nv, nf);
+        const size_t bytes = tile_block_bytes(nv, nf);
         size_t off = host.size();
         host.resize(off + bytes, 0);
         float* f = reinterpret_cast<float*>(host.data() + off);
@@ -607,8 +706,9 @@ hydro_status hydro_mesh_upload(hydro_ctx* ctx, const void* vertex_data, size_t v
             }
         }
         std::memcpy(host.data() + off + (size_t)nvp * 12, ti.data(), ti.size() * 4);
-        // bounding sphere: centre of the box, radius to the farthest vertex
-        // from the stored (float) centre, rounded up
+        std::memcpy(host.data() + off + tile_bytes(nv, nf), tid.data(), tid.size() * 4);
+        // bounds: centre of the box, radius to the farthest vertex from the
+        // stored (float) centre and half extents about it, rounded up
         float c[3];
         for (int a = 0; a < 3; ++a) c[a] = (float)(0.5 * (lo[a] + hi[a]));
         double r2 = 0.0, hx = 0.0, hy = 0.0, hz = 0.0;
@@ -624,33 +724,29 @@ hydro_status hydro_mesh_upload(hydro_ctx* ctx, const void* vertex_data, size_t v
         auto up = [](double x) { return std::nextafter((float)(x * (1.0 + 1e-6)), 1e30f); };
         const float4 sphere = make_float4(c[0], c[1], c[2], up(std::sqrt(r2)));
         const float4 half = make_float4(up(hx), up(hy), up(hz), 0.f);
-        pend.push_back(Pending{off, (uint16_t)nv, (uint16_t)nf, tile_first_face, sphere, half});
+        pend.push_back(Pending{off, (uint16_t)nv, (uint16_t)nf, tile_first, sphere, half});
         for (uint32_t g : tv) local[g] = -1;
         tv.clear();
         ti.clear();
-        tile_first_face = next_face;
+        tid.clear();
     };
-    for (uint32_t f = 0; f < n_faces; ++f) {
-        const uint32_t* fi = face_indices + 3 * (size_t)f;
-        uint32_t fresh = 0;
-        for (int k = 0; k < 3; ++k) {
-            bool dup = false;
-            for (int j = 0; j < k; ++j) dup |= (fi[j] == fi[k]);
-            if (local[fi[k]] < 0 && !dup) ++fresh;
-        }
-        if (ti.size() + 1 > (size_t)kTileFaces || tv.size() + fresh > (size_t)kTileVerts)
-            close_tile(f);
-        uint32_t word = 0;
-        for (int k = 0; k < 3; ++k) {
-            if (local[fi[k]] < 0) {
-                local[fi[k]] = (int32_t)tv.size();
-                tv.push_back(fi[k]);
+    for (size_t t = 0; t + 1 < starts.size(); ++t) {
+        for (uint32_t k = starts[t]; k < starts[t + 1]; ++k) {
+            const uint32_t f = order[k];
+            const uint32_t* fv = face_indices + 3 * (size_t)f;
+            uint32_t word = 0;
+            for (int j = 0; j < 3; ++j) {
+                if (local[fv[j]] < 0) {
+                    local[fv[j]] = (int32_t)tv.size();
+                    tv.push_back(fv[j]);
+                }
+                word |= (uint32_t)local[fv[j]] << (9 * j);
             }
-            word |= (uint32_t)local[fi[k]] << (9 * k);
+            ti.push_back(word);
+            tid.push_back(f);
         }
-        ti.push_back(word);
+        close_tile(starts[t]);
     }
-    close_tile(n_faces);
 
     char* dev = nullptr;
     hydro_status st = slab_alloc(ctx, host.size(), &dev);

@@ -44,7 +44,10 @@ enum : int { OP_BODY = 0, OP_SURFACE = 1, OP_SUBMERGED = 2, OP_AERO = 3, OP_AERO
 // One tile of a mesh: nv vertices stored as x[nvp], y[nvp], z[nvp] floats
 // (nvp = nv rounded up to 4) followed by one uint32 per face holding its
 // three local vertex indices (9 bits each: i0 | i1 << 9 | i2 << 18), padded
-// to 16 bytes; `first_face` is the tile's first face in the uploaded order.
+// to 16 bytes; that much is copied to shared memory.  Behind it, not
+// copied, each face's index in the uploaded mesh (for per-face debug
+// output).  `first_face` is the position of the tile's first face in the
+// mesh's tile order.
 // `sphere` and `half` bound the tile's vertices in mesh coordinates: the
 // centre of their box (x, y, z) with the radius of a sphere about it, and
 // the box's half extents, each rounded up so that every vertex lies inside.
@@ -66,6 +69,12 @@ __host__ __device__ __forceinline__ uint32_t tile_bytes(uint32_t nv, uint32_t nf
 {
     const uint32_t nvp = (nv + 3u) & ~3u;
     return (nvp * 12u + nf * 4u + 15u) & ~15u;
+}
+
+// Bytes of a tile block with the faces' upload indices behind it.
+__host__ __device__ __forceinline__ uint32_t tile_block_bytes(uint32_t nv, uint32_t nf)
+{
+    return tile_bytes(nv, nf) + ((nf * 4u + 15u) & ~15u);
 }
 
 constexpr int kMaxTilesPerChunk = 16;

@@ -1312,6 +1312,8 @@ __global__ void __launch_bounds__(kBlock) face_terms_kernel(const TileDesc* tile
     }
     __syncthreads();
     const uint32_t* idx = reinterpret_cast<const uint32_t*>(td.block + 3 * nvp);
+    const uint32_t* face_id = reinterpret_cast<const uint32_t*>(reinterpret_cast<const char*>(td.block) +
+                                                                tile_bytes(td.nv, td.nf));
     // Thread t takes faces 2t and 2t+1: a pair of fully submerged faces goes
     // through the packed path (as in the batched kernel), any other face
     // through the scalar path, so that both are checked.
@@ -1321,8 +1323,8 @@ __global__ void __launch_bounds__(kBlock) face_terms_kernel(const TileDesc* tile
         const float4 a1 = verts[wa & 511u], a2 = verts[(wa >> 9) & 511u], a3 = verts[wa >> 18];
         const float4 b1 = verts[wb & 511u], b2 = verts[(wb >> 9) & 511u], b3 = verts[wb >> 18];
         const int ca = face_class(a1.w, a2.w, a3.w), cb = face_class(b1.w, b2.w, b3.w);
-        float* oa = out + (size_t)(td.first_face + f) * kQ;
-        float* ob = oa + kQ;
+        float* oa = out + (size_t)face_id[f] * kQ;
+        float* ob = out + (size_t)face_id[hasB ? f + 1 : f] * kQ;
         if (packed && ca == 1 && cb == 1 && hasB) {
             // the packed path adds face A then face B into one set of sums:
             // evaluate (A, B) with B's half switched off, then (B, A)

@@ -9,14 +9,16 @@ FORCES = ("Fb", "Fdq", "Fdf")
 TORQUES = ("Tb", "Tdq", "Tdf")
 
 
-def scaled_errors(a: np.ndarray, c: np.ndarray, length) -> dict:
+def scaled_errors(a: np.ndarray, c: np.ndarray, length, volume=None, surface=None) -> dict:
     """Per-body error of wrench array ``a`` against reference ``c``.
 
     Forces are measured against the body's force scale S = max(|Fb|, |Fdq|,
     |Fdf|) of the reference, torques against S * length (the torque a force
-    of that size makes at the body's size); Swet and Vsub relatively.  This
-    is the pair-scaled relative error: components that cancel to ~0 are not
-    divided by their own tiny size."""
+    of that size makes at the body's size); Swet and Vsub relatively, or,
+    when the body's ``surface`` and ``volume`` are given, against those (a
+    body barely in the water has a tiny Vsub summed from tetrahedra that
+    cancel).  This is the pair-scaled relative error: components that cancel
+    to ~0 are not divided by their own tiny size."""
     L = np.broadcast_to(np.asarray(length, dtype=np.float64), (len(c),))
     S = np.max(np.stack([np.linalg.norm(c[k], axis=1) for k in FORCES]), axis=0)
     S = np.maximum(S, 1e-300)
@@ -25,8 +27,9 @@ def scaled_errors(a: np.ndarray, c: np.ndarray, length) -> dict:
         out[k] = np.linalg.norm(a[k] - c[k], axis=1) / S
     for k in TORQUES:
         out[k] = np.linalg.norm(a[k] - c[k], axis=1) / (S * L)
-    for k in ("Swet", "Vsub"):
-        out[k] = np.abs(a[k] - c[k]) / np.maximum(np.abs(c[k]), 1e-300)
+    for k, ref in (("Swet", surface), ("Vsub", volume)):
+        scale = np.abs(c[k]) if ref is None else np.maximum(np.abs(c[k]), np.asarray(ref, dtype=np.float64))
+        out[k] = np.abs(a[k] - c[k]) / np.maximum(scale, 1e-300)
     return out
 
 

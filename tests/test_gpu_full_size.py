@@ -4,8 +4,9 @@ The mixed batch of 4096 bodies (37.8M faces, flat surface) and the 1024
 torpedo hulls of 20000 faces on the 1024 x 1024 wave grid are evaluated in
 one batched step each and compared, body by body, with the CPU oracle's
 MIRROR32 variant (the reference's FP32 face arithmetic with exact sums)
-over every body: same fluid positions, pair-scaled wrench errors within the
-same 2e-6 bar as the small parity tests, and against the all-FP64 REF64 the
+over every body: same fluid positions, pair-scaled wrench errors (Swet and
+Vsub against the body's surface and volume) within the same 2e-6 bar as the
+small parity tests, and against the all-FP64 REF64 the
 errors of the reference's own FP32 arithmetic.  Size-independent properties
 are checked on the same runs: a repeated step gives the same bits and
 bodies outside the water get zeros.  (With CG depths up to 0.3 m no body of
@@ -63,11 +64,12 @@ def _check_against_oracle(oracle, sc, gpu, min_active):
     act = (gpu["position"] == abi.CROSSING_SURFACE) | (gpu["position"] == abi.INSIDE)
     assert act.sum() >= min_active
     L = _lengths(sc["bodies"])
-    e = scaled_errors(gpu, mir, L)
+    b = sc["bodies"]
+    e = scaled_errors(gpu, mir, L, volume=b["volume"], surface=b["surface"])
     for k, v in e.items():
         assert np.max(v[act]) < TOL_MIRROR, (k, float(np.max(v[act])), int(np.argmax(np.where(act, v, 0))))
     r64 = _oracle(oracle, REF64, sc)
-    e64 = scaled_errors(gpu, r64, L)
+    e64 = scaled_errors(gpu, r64, L, volume=b["volume"], surface=b["surface"])
     worst = np.max(np.stack([v for v in e64.values()]), axis=0)[act]
     assert np.median(worst) < 1e-5 and np.percentile(worst, 99) < 1e-3, (np.median(worst), np.percentile(worst, 99))
     assert np.all(gpu["status"] == 0)
