@@ -11,6 +11,7 @@
 // order; the boundary and finalisation are FP64 as in the reference.
 #pragma once
 
+#include <cstddef>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -196,6 +197,10 @@ struct __align__(16) BodyParams {
     int pad[3];
 };
 static_assert(sizeof(BodyParams) == 128, "BodyParams is staged as a 128-byte block");
+static_assert(offsetof(BodyParams, p) == 48 && offsetof(BodyParams, p0) == 60 && offsetof(BodyParams, v) == 72 &&
+                  offsetof(BodyParams, omega) == 84 && offsetof(BodyParams, loop) == 96 &&
+                  offsetof(BodyParams, buoyancy) == 100 && offsetof(BodyParams, damping) == 104,
+              "the chunk kernel reads BodyParams bytes 48..111 as four 16-byte words");
 
 __device__ __forceinline__ v3 xform(const float* M, float x, float y, float z)
 {

@@ -602,22 +602,28 @@ __device__ __forceinline__ uint32_t tiles_to_issue(const KParams& P, const Activ
 {
     uint32_t keep = (1u << nt) - 1u;
     if (P.ocean.waves) return keep;
-    const BodyParams& B = P.bparams[ch.body];
-    if (B.loop != LOOP_SURFACE) return keep;
-    const float4 T = *reinterpret_cast<const float4*>(B.TC + 8);   // row giving z
+    // the body's loop kind, its z row and the tiles' bounds are requested
+    // together (one round trip), the loop kind decides afterwards
+    const BodyParams* B = P.bparams + ch.body;
+    const int loop = B->loop;
+    const float4 T = *reinterpret_cast<const float4*>(B->TC + 8);   // row giving z
     const float ax = fabsf(T.x), ay = fabsf(T.y), az = fabsf(T.z);
     const float rn = sqrtf((T.x * T.x + T.y * T.y) + T.z * T.z) * (1.f + 0x1p-20f);
-#pragma unroll
+    uint32_t drop = 0;
+#pragma unroll 4
     for (int t = 0; t < kMaxTilesPerChunk; ++t) {
-        if ((uint32_t)t >= nt) break;
-        const TileDesc& d = P.tiles[ch.first_tile + t];
-        const float4 c = d.sphere, h = d.half;
-        const float zc = (T.x * c.x + T.y * c.y) + (T.z * c.z + T.w);
-        const float reach = fminf(c.w * rn, (ax * h.x + ay * h.y) + az * h.z);
-        const float margin = 1e-5f * ((ax * (fabsf(c.x) + h.x) + ay * (fabsf(c.y) + h.y)) +
-                                      (az * (fabsf(c.z) + h.z) + fabsf(T.w))) + 1e-6f;
-        if (zc + reach + margin < 0.f) keep &= ~(1u << t);
+        if ((uint32_t)t < nt) {
+            const TileDesc* d = P.tiles + ch.first_tile + t;
+            const float4 c = __ldg(&d->sphere), h = __ldg(&d->half);
+            const float zc = (T.x * c.x + T.y * c.y) + (T.z * c.z + T.w);
+            const float reach = fminf(c.w * rn, (ax * h.x + ay * h.y) + az * h.z);
+            const float margin = 1e-5f * ((ax * (fabsf(c.x) + h.x) + ay * (fabsf(c.y) + h.y)) +
+                                          (az * (fabsf(c.z) + h.z) + fabsf(T.w))) + 1e-6f;
+            if (zc + reach + margin < 0.f) drop |= 1u << t;
+        }
     }
+    if (loop != LOOP_SURFACE) return keep;
+    keep &= ~drop;
     return keep ? keep : 1u;
 }
 
@@ -740,10 +746,16 @@ __device__ __forceinline__ int tile_faces(const KParams& P, const StageBuf& st, 
 {
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    const BodyParams& B = st.bp;
+    // the body's vectors and flags as four 16-byte loads (BodyParams bytes 48..111)
+    const float4* bq = reinterpret_cast<const float4*>(&st.bp) + 3;
+    const float4 q0 = bq[0], q1 = bq[1], q2 = bq[2];
+    const int4 fl = *reinterpret_cast<const int4*>(bq + 3);
     BodyParams Bl;
-    Bl.p = B.p; Bl.p0 = B.p0; Bl.v = B.v; Bl.omega = B.omega;
-    Bl.loop = B.loop; Bl.buoyancy = B.buoyancy; Bl.damping = B.damping;
+    Bl.p = mk(q0.x, q0.y, q0.z);
+    Bl.p0 = mk(q0.w, q1.x, q1.y);
+    Bl.v = mk(q1.z, q1.w, q2.x);
+    Bl.omega = mk(q2.y, q2.z, q2.w);
+    Bl.loop = fl.x; Bl.buoyancy = fl.y; Bl.damping = fl.z;
     const int nf = m.nf, nvp = (m.nv + 3) & ~3;
     const uint32_t* idx = reinterpret_cast<const uint32_t*>(reinterpret_cast<const float*>(st.raw) + 3 * nvp);
     if (Bl.loop == LOOP_AERO) {
