@@ -502,14 +502,26 @@ __device__ __forceinline__ void prefetch_lines(const void* p, size_t bytes, int 
         asm volatile("prefetch.global.L1 [%0];" ::"l"(a));
 }
 
-// Appends the chunks of a body that runs a face loop to the launch's list
-// of active chunks, so that the producers never claim the chunks of bodies
-// outside the water or switched off.
-__device__ __forceinline__ void list_chunks(const KParams& P, uint32_t body, const BodyInfo& bi)
+// Appends the chunks of a body that runs a face loop (`n` of them, 0 for a
+// body without one or a lane without a body) to the launch's list of active
+// chunks, so that the producers never claim the chunks of bodies outside
+// the water or switched off.  Called by all 32 lanes of a warp: one atomic
+// per warp reserves the run of its lanes' chunks, whose counts are
+// prefix-summed with shuffles.
+__device__ __forceinline__ void list_chunks(const KParams& P, uint32_t body, const BodyInfo& bi, uint32_t n)
 {
-    if (bi.n_chunks == 0u) return;
-    const uint32_t base = atomicAdd(P.n_listed, bi.n_chunks);
-    for (uint32_t c = 0; c < bi.n_chunks; ++c) {
+    const int lane = (int)(threadIdx.x & 31u);
+    uint32_t incl = n;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += y;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    uint32_t base = 0;
+    if (lane == 0 && total) base = atomicAdd(P.n_listed, total);
+    base = __shfl_sync(0xffffffffu, base, 0) + incl - n;
+    for (uint32_t c = 0; c < n; ++c) {
         const ChunkDesc d = P.chunks[bi.first_chunk + c];
         P.active[base + c] = ActiveChunk{body, d.first_tile, d.n_tiles, bi.first_chunk + c};
     }
@@ -524,13 +536,21 @@ __global__ void prep_kernel(const KParams P)
         *P.work = 0u;
     }
     const uint32_t limit = P.n_active ? min(P.n_bodies, *P.n_active) : P.n_bodies;
-    for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < limit; b += gridDim.x * blockDim.x) {
-        prefetch_lines(P.bodies + b, sizeof(hydro_body), 0, 1);
-        BodyParams B;
-        const BodyInfo bi = P.binfo[b];
-        body_prologue(P.bodies + b, bi.mesh, P.op, P.ocean, P.st, B);
-        P.bparams[b] = B;
-        if (B.loop != LOOP_NONE) list_chunks(P, b, bi);
+    // warp-uniform grid stride: every lane reaches list_chunks
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t w0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); w0 < limit; w0 += stride) {
+        const uint32_t b = w0 + (threadIdx.x & 31u);
+        BodyInfo bi{};
+        uint32_t n = 0;
+        if (b < limit) {
+            prefetch_lines(P.bodies + b, sizeof(hydro_body), 0, 1);
+            BodyParams B;
+            bi = P.binfo[b];
+            body_prologue(P.bodies + b, bi.mesh, P.op, P.ocean, P.st, B);
+            P.bparams[b] = B;
+            n = B.loop != LOOP_NONE ? bi.n_chunks : 0u;
+        }
+        list_chunks(P, b, bi, n);
     }
 }
 
@@ -1131,6 +1151,7 @@ __device__ void compound_part_loop(int pos, const hydro_compound_part& pt, Setti
     }
 }
 
+// One thread per part (warp-sized CTAs; every lane reaches list_chunks).
 __global__ void compound_prep_kernel(const KParams P, const CompoundParams C)
 {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1138,31 +1159,36 @@ __global__ void compound_prep_kernel(const KParams P, const CompoundParams C)
         *P.err = 0u;
         *P.work = 0u;
     }
-    if (p >= P.n_bodies) return;
-    const hydro_compound_part& pt = C.parts[p];
-    const hydro_body& cb = C.compounds[C.part_compound[p]];
-    int pos = HYDRO_SKIPPED;
-    if (fluid_mode(cb.mode)) pos = classify(P.ocean, cb.aabb_min, cb.aabb_max);   // :293, :299
-    int loop, buoy, damp;
-    compound_part_loop(pos, pt, P.st, loop, buoy, damp);
-    const BodyInfo bi = P.binfo[p];
-    BodyParams B;
-    for (int r = 0; r < 3; ++r) {
-        for (int c = 0; c < 3; ++c) B.TC[4 * r + c] = (float)pt.T_C.basis[3 * r + c];
-        B.TC[4 * r + 3] = (float)pt.T_C.origin[r];
+    BodyInfo part_info{};
+    uint32_t n = 0;
+    if (p < P.n_bodies) {
+        const hydro_compound_part& pt = C.parts[p];
+        const hydro_body& cb = C.compounds[C.part_compound[p]];
+        int pos = HYDRO_SKIPPED;
+        if (fluid_mode(cb.mode)) pos = classify(P.ocean, cb.aabb_min, cb.aabb_max);   // :293, :299
+        int loop, buoy, damp;
+        compound_part_loop(pos, pt, P.st, loop, buoy, damp);
+        const BodyInfo bi = P.binfo[p];
+        BodyParams B;
+        for (int r = 0; r < 3; ++r) {
+            for (int c = 0; c < 3; ++c) B.TC[4 * r + c] = (float)pt.T_C.basis[3 * r + c];
+            B.TC[4 * r + 3] = (float)pt.T_C.origin[r];
+        }
+        B.p = mk((float)cb.T_CG.origin[0], (float)cb.T_CG.origin[1], (float)cb.T_CG.origin[2]);
+        B.p0 = mk(B.p.x, B.p.y, 0.f);
+        B.v = mk((float)cb.v[0], (float)cb.v[1], (float)cb.v[2]);
+        B.omega = mk((float)cb.omega[0], (float)cb.omega[1], (float)cb.omega[2]);
+        B.mismatch = (pt.mesh != bi.mesh);
+        B.loop = (B.mismatch || bi.mesh == HYDRO_NO_MESH) ? LOOP_NONE : loop;
+        B.buoyancy = buoy;
+        B.damping = damp;
+        B.position = pos;
+        B.pad[0] = B.pad[1] = B.pad[2] = 0;
+        P.bparams[p] = B;
+        part_info = bi;
+        n = B.loop != LOOP_NONE ? bi.n_chunks : 0u;
     }
-    B.p = mk((float)cb.T_CG.origin[0], (float)cb.T_CG.origin[1], (float)cb.T_CG.origin[2]);
-    B.p0 = mk(B.p.x, B.p.y, 0.f);
-    B.v = mk((float)cb.v[0], (float)cb.v[1], (float)cb.v[2]);
-    B.omega = mk((float)cb.omega[0], (float)cb.omega[1], (float)cb.omega[2]);
-    B.mismatch = (pt.mesh != bi.mesh);
-    B.loop = (B.mismatch || bi.mesh == HYDRO_NO_MESH) ? LOOP_NONE : loop;
-    B.buoyancy = buoy;
-    B.damping = damp;
-    B.position = pos;
-    B.pad[0] = B.pad[1] = B.pad[2] = 0;
-    P.bparams[p] = B;
-    if (B.loop != LOOP_NONE) list_chunks(P, p, bi);
+    list_chunks(P, p, part_info, n);
 }
 
 __device__ __forceinline__ void add3(double* a, const double* b)
