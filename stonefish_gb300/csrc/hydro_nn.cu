@@ -337,7 +337,7 @@ __global__ void features_kernel(const hydro_body* __restrict__ bodies, uint32_t 
     const double* R = b.T_CG.basis;
     const double x = b.T_CG.origin[0], y = b.T_CG.origin[1], z = b.T_CG.origin[2];
     // heading (unit horizontal projection of the body x axis), FP32
-    float ux = (float)R[0], uy = (float)R[3];
+    float ux = (float)R[0], uy = (float)R[3];   // (same values as Rf[0], Rf[3] below)
     const float hn = sqrtf(ux * ux + uy * uy);
     if (hn > 1e-6f) {
         ux /= hn;
@@ -359,16 +359,21 @@ __global__ void features_kernel(const hydro_body* __restrict__ bodies, uint32_t 
         s_ac = (el - er) / (2.f * a);
         k_al = (ef + eb - 2.f * h) / (a * a);
     }
-    // R^T u for the body-frame vectors
+    // R^T u for the body-frame vectors, in FP32 (GB300's FP64 pipe would
+    // set this kernel's pace; the features are rounded to BF16 downstream)
+    float Rf[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) Rf[k] = (float)R[k];
     auto tb = [&](const double* u, float* out) {
-        out[0] = (float)(R[0] * u[0] + R[3] * u[1] + R[6] * u[2]);
-        out[1] = (float)(R[1] * u[0] + R[4] * u[1] + R[7] * u[2]);
-        out[2] = (float)(R[2] * u[0] + R[5] * u[1] + R[8] * u[2]);
+        const float u0 = (float)u[0], u1 = (float)u[1], u2 = (float)u[2];
+        out[0] = (Rf[0] * u0 + Rf[3] * u1) + Rf[6] * u2;
+        out[1] = (Rf[1] * u0 + Rf[4] * u1) + Rf[7] * u2;
+        out[2] = (Rf[2] * u0 + Rf[5] * u1) + Rf[8] * u2;
     };
     float* o16 = f + (size_t)i * 16;
     o16[0] = (float)z + h;                          // depth below the local surface (NED: surface at -h)
-    o16[1] = atan2f((float)R[7], (float)R[8]);      // roll
-    o16[2] = asinf(fmaxf(-1.f, fminf(1.f, (float)-R[6])));   // pitch
+    o16[1] = atan2f(Rf[7], Rf[8]);                  // roll
+    o16[2] = asinf(fmaxf(-1.f, fminf(1.f, -Rf[6])));  // pitch
     tb(b.v, o16 + 3);
     tb(b.omega, o16 + 6);
     double u[3] = {o.U[0], o.U[1], o.U[2]};
