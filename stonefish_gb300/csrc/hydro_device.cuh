@@ -28,7 +28,7 @@ static_assert(kTileFaces == 64 * kWarps, "a tile gives each compute warp 64 face
 static_assert(kTileVerts < 512, "vertex indices are packed in 9 bits");
 constexpr int kQ = 23;               // accumulated quantities per body
 constexpr int kPartialStride = 24;   // doubles per chunk partial (23 + status)
-constexpr int kFlushFaces = 16;      // faces a thread sums in FP32 before a flush
+constexpr int kFlushFaces = 32;      // faces a thread sums in FP32 before a flush
 
 // indices of the accumulated quantities
 enum : int {
