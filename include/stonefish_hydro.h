@@ -614,6 +614,18 @@ hydro_status hydro_debug_face_terms(hydro_ctx* ctx, const hydro_body* body,
                                     const hydro_settings* settings, int32_t packed,
                                     float* out);
 
+/* The tiling hydro_mesh_upload applies to a mesh (no device work, no
+ * context): the faces in tile order (order[n_faces]) and each tile's first
+ * position in it, followed by n_faces (tile_starts[n_tiles + 1]).  Tiles are
+ * compact patches of at most HYDRO_TILE_FACES faces and 448 distinct
+ * vertices, grown over shared vertices whatever the mesh's face order.
+ * With starts_capacity < n_tiles + 1 nothing is written but *n_tiles and
+ * HYDRO_ERR_INVALID_ARG is returned.  For checking and inspecting the mesh
+ * layout; it has no counterpart in the reference. */
+hydro_status hydro_debug_tile_order(const uint32_t* face_indices, uint32_t n_vertices, uint32_t n_faces,
+                                    uint32_t* order, uint32_t* tile_starts, uint32_t starts_capacity,
+                                    uint32_t* n_tiles);
+
 /* Checks on the GPU that the division the kernels use for x/|n| and x/3
  * (a correctly rounded reciprocal plus one FMA correction) returns the bits
  * of IEEE round-to-nearest division: x/3 over every float, x/b over n_pairs

@@ -235,6 +235,7 @@ def _declare(lib: C.CDLL) -> None:
         "hydro_correct_forces": (i32, [vp, C.POINTER(Ocean), d, d, d, d, d, d, d]),
         "hydro_fluid_position": (i32, [vp, C.POINTER(Ocean), d, d, C.POINTER(i32)]),
         "hydro_debug_division_check": (i32, [vp, C.c_uint64, C.c_uint64, vp]),
+        "hydro_debug_tile_order": (i32, [vp, u32, u32, vp, vp, u32, C.POINTER(u32)]),
         "hydro_debug_arith_check": (i32, [vp, C.c_uint64, C.c_uint64, vp, vp, vp]),
         "hydro_debug_wait_timeout": (i32, [vp, u32, C.POINTER(i32)]),
         "hydro_compute_wrenches_static": (i32, [vp, vp, u32, vp, C.POINTER(Ocean), C.POINTER(Settings),
@@ -290,6 +291,23 @@ def exported_symbols_from_header(header: str | None = None) -> list[str]:
     text = open(path).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     return sorted(set(re.findall(r"\b(hydro_[a-z0-9_]+)\s*\(", text)))
+
+
+def tile_order(faces: np.ndarray, n_vertices: int, lib_path: str | None = None):
+    """hydro_debug_tile_order: the faces in the upload's tile order and each
+    tile's first position in it (plus the end); host code only, no GPU."""
+    lib = load_library(lib_path)
+    fc = np.ascontiguousarray(faces, dtype=np.uint32)
+    nf = len(fc)
+    order = np.zeros(nf, dtype=np.uint32)
+    nt = C.c_uint32(0)
+    cap = nf + 1
+    starts = np.zeros(cap, dtype=np.uint32)
+    st = lib.hydro_debug_tile_order(fc.ctypes.data, int(n_vertices), nf, order.ctypes.data, starts.ctypes.data,
+                                    cap, C.byref(nt))
+    if st != HYDRO_OK:
+        raise HydroError(st, "tile order")
+    return order, starts[: nt.value + 1].copy()
 
 
 def obj_parse(text: str, scale: float = 1.0, refine_threshold: float = 0.0, lib_path: str | None = None):

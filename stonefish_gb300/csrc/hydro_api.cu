@@ -563,10 +563,13 @@ void hydro_destroy(hydro_ctx* ctx)
 // shares more vertices between its faces.  A tile grows from a seed face by
 // repeatedly taking, among the unused faces that share a vertex with it,
 // one that adds the fewest new vertices (ties: the one reached first, so
-// that the tile grows ring by ring).  When no such face is left
-// the next unused face in upload order seeds the same tile (disconnected
-// parts, such as the separately indexed sides of a box, then share tiles).
-// A tile closes at kTileFaces faces or when no reachable face fits under
+// that the tile grows ring by ring).  The next tile starts from the face on
+// the closed tile's border that comes first in upload order, so tiles
+// follow one another across the surface whatever the upload order.  When a tile has used up its connected part of
+// the mesh (the separately indexed sides of a box are separate parts), it
+// closes if at least half full and otherwise takes the next unused face in
+// upload order as a further seed, so that small parts share tiles.  A tile
+// closes at kTileFaces faces or when no reachable face fits under
 // kTileVerts vertices.  `order` lists the faces tile by tile, `starts` the
 // tiles' first positions in it (plus the end).
 static void build_tiles(uint32_t n_vertices, const uint32_t* fi, uint32_t n_faces, std::vector<uint32_t>& order,
@@ -600,6 +603,7 @@ static void build_tiles(uint32_t n_vertices, const uint32_t* fi, uint32_t n_face
         return n;
     };
     uint32_t seed = 0;
+    uint32_t border = UINT32_MAX;          // a face on the last tile's border, if any
     while (order.size() < n_faces) {
         uint32_t tf = 0;
         for (int b = 0; b < 4; ++b) {
@@ -634,10 +638,13 @@ static void build_tiles(uint32_t n_vertices, const uint32_t* fi, uint32_t n_face
             for (int k = 0; k < nj; ++k)
                 for (uint32_t i = first[joined[k]]; i < first[joined[k] + 1]; ++i) push(around[i]);
         };
+        if (border != UINT32_MAX && !used[border]) take(border);
+        border = UINT32_MAX;
         while (tf < (uint32_t)kTileFaces) {
             int b = 0;
             while (b < 4 && head[b] == queue[b].size()) ++b;
             if (b == 4) {
+                if (2 * tf >= (uint32_t)kTileFaces) break;
                 while (seed < n_faces && used[seed]) ++seed;
                 if (seed >= n_faces || tverts.size() + fresh(seed) > (size_t)kTileVerts) break;
                 take(seed);
@@ -648,6 +655,11 @@ static void build_tiles(uint32_t n_vertices, const uint32_t* fi, uint32_t n_face
             if (tverts.size() + (size_t)b > (size_t)kTileVerts) continue;
             take(g);
         }
+        // the next tile's seed: of the unused faces this tile reached, the
+        // first in upload order (meshes generated in a sweep keep sweeping)
+        for (int b = 0; b < 4; ++b)
+            for (size_t i = head[b]; i < queue[b].size(); ++i)
+                if (!used[queue[b][i]] && (border == UINT32_MAX || queue[b][i] < border)) border = queue[b][i];
         starts.push_back((uint32_t)order.size());
         for (uint32_t v : tverts) in_tile[v] = 0;
         tverts.clear();
@@ -1649,6 +1661,23 @@ hydro_status hydro_debug_face_terms(hydro_ctx* ctx, const hydro_body* body, cons
     if (e != cudaSuccess) return cuda_fail(ctx, e, "face terms kernel");
     CK(ctx, cudaMemcpyAsync(out, dout, terms, cudaMemcpyDeviceToHost, ctx->stream));
     CK(ctx, cudaStreamSynchronize(ctx->stream));
+    return HYDRO_OK;
+}
+
+hydro_status hydro_debug_tile_order(const uint32_t* face_indices, uint32_t n_vertices, uint32_t n_faces,
+                                    uint32_t* order, uint32_t* tile_starts, uint32_t starts_capacity,
+                                    uint32_t* n_tiles)
+{
+    if (!face_indices || !order || !tile_starts || !n_tiles || n_vertices == 0 || n_faces == 0)
+        return HYDRO_ERR_INVALID_ARG;
+    for (size_t i = 0; i < (size_t)n_faces * 3; ++i)
+        if (face_indices[i] >= n_vertices) return HYDRO_ERR_INDEX_RANGE;
+    std::vector<uint32_t> ord, starts;
+    build_tiles(n_vertices, face_indices, n_faces, ord, starts);
+    *n_tiles = (uint32_t)starts.size() - 1u;
+    if (starts.size() > (size_t)starts_capacity) return HYDRO_ERR_INVALID_ARG;
+    std::memcpy(order, ord.data(), ord.size() * sizeof(uint32_t));
+    std::memcpy(tile_starts, starts.data(), starts.size() * sizeof(uint32_t));
     return HYDRO_OK;
 }
 
