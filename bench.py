@@ -612,7 +612,10 @@ def run_gpu(args, rank: int, world: int, local_rank: int, dist):
         "faces_per_s": faces_per_s,
         "e2e": {"value": e2e_value, "unit": UNIT,
                 "h2d_bytes_per_step": int(nb * (abi.BODY_DTYPE.itemsize + abi.WRENCH_DTYPE.itemsize)),
-                "d2h_bytes_per_step": int(nb * abi.WRENCH_DTYPE.itemsize), "steps": e2e_steps},
+                "d2h_bytes_per_step": int(nb * abi.WRENCH_DTYPE.itemsize), "steps": e2e_steps,
+                "transfer": "hydro_batch_compute on page-locked host buffers: every step the per-body "
+                            "kernels read the bodies and in-out wrenches from host memory and write the "
+                            "wrenches back over the host link (no staging copies)"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
                      "traffic": profile_traffic(args.workload),

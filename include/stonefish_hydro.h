@@ -298,9 +298,11 @@ hydro_status hydro_batch_compute_device_prefix(hydro_batch* batch, const hydro_b
                                                const hydro_settings* settings,
                                                hydro_wrench* d_inout, void* stream);
 
-/* Host-buffer step: copies bodies and in-out wrenches host->device, runs the
- * step, copies the wrenches back and synchronises.  With pinned host memory
- * the copies are asynchronous on the batch's own stream. */
+/* Host-buffer step, synchronous.  Page-locked mapped buffers (cudaHostAlloc,
+ * cudaHostRegister with mapping, or a pinned torch tensor) are read and
+ * written in place by the step's per-body kernels over the host link; other
+ * host memory is staged: bodies and in-out wrenches copied host->device on
+ * the batch's own stream, the wrenches copied back. */
 hydro_status hydro_batch_compute(hydro_batch* batch, const hydro_body* bodies,
                                  const hydro_ocean* ocean,
                                  const hydro_settings* settings,

@@ -902,6 +902,19 @@ hydro_status hydro_batch_compute_device_prefix(hydro_batch* b, const hydro_body*
                         d_count);
 }
 
+// Device address of host memory that kernels can read and write in place
+// (page-locked and mapped, e.g. from cudaHostAlloc), or null for memory
+// that has to be staged through copies.
+static void* mapped_host_ptr(const void* p)
+{
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 hydro_status hydro_batch_compute(hydro_batch* b, const hydro_body* bodies, const hydro_ocean* ocean,
                                  const hydro_settings* settings, hydro_wrench* inout)
 {
@@ -912,13 +925,25 @@ hydro_status hydro_batch_compute(hydro_batch* b, const hydro_body* bodies, const
         return fail(ctx, HYDRO_ERR_INVALID_ARG, "batch compute: bad arguments");
     if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, HYDRO_ERR_DEVICE, "cudaSetDevice");
     const size_t nb = (size_t)b->n_bodies;
-    if (!b->bodies_d) CK(ctx, cudaMalloc(&b->bodies_d, nb * sizeof(hydro_body)));
-    if (!b->io_d) CK(ctx, cudaMalloc(&b->io_d, nb * sizeof(hydro_wrench)));
-    CK(ctx, cudaMemcpyAsync(b->bodies_d, bodies, nb * sizeof(hydro_body), cudaMemcpyHostToDevice, b->stream));
-    CK(ctx, cudaMemcpyAsync(b->io_d, inout, nb * sizeof(hydro_wrench), cudaMemcpyHostToDevice, b->stream));
-    hydro_status st = batch_launch(b, b->bodies_d, ocean, settings, b->io_d, b->stream, OP_BODY);
+    // page-locked mapped buffers are read and written in place by the step's
+    // per-body kernels (the face kernel never touches them); others are staged
+    const hydro_body* db = static_cast<const hydro_body*>(mapped_host_ptr(bodies));
+    hydro_wrench* dio = static_cast<hydro_wrench*>(mapped_host_ptr(inout));
+    if (!db) {
+        if (!b->bodies_d) CK(ctx, cudaMalloc(&b->bodies_d, nb * sizeof(hydro_body)));
+        CK(ctx, cudaMemcpyAsync(b->bodies_d, bodies, nb * sizeof(hydro_body), cudaMemcpyHostToDevice, b->stream));
+        db = b->bodies_d;
+    }
+    const bool staged_io = (dio == nullptr);
+    if (staged_io) {
+        if (!b->io_d) CK(ctx, cudaMalloc(&b->io_d, nb * sizeof(hydro_wrench)));
+        CK(ctx, cudaMemcpyAsync(b->io_d, inout, nb * sizeof(hydro_wrench), cudaMemcpyHostToDevice, b->stream));
+        dio = b->io_d;
+    }
+    hydro_status st = batch_launch(b, db, ocean, settings, dio, b->stream, OP_BODY);
     if (st != HYDRO_OK) return st;
-    CK(ctx, cudaMemcpyAsync(inout, b->io_d, nb * sizeof(hydro_wrench), cudaMemcpyDeviceToHost, b->stream));
+    if (staged_io)
+        CK(ctx, cudaMemcpyAsync(inout, b->io_d, nb * sizeof(hydro_wrench), cudaMemcpyDeviceToHost, b->stream));
     CK(ctx, cudaStreamSynchronize(b->stream));
     return HYDRO_OK;
 }

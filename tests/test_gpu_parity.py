@@ -294,6 +294,14 @@ def test_host_and_device_entry_points_agree(hctx):
     dev = d_w.cpu().numpy().view(abi.WRENCH_DTYPE)
     assert dev.tobytes() == host.tobytes()
     assert bt.last_launches() == 3          # prep, chunk, finalise
+    # page-locked buffers: read and written in place by the kernels
+    h_b = torch.from_numpy(bodies.view(np.uint8).copy()).pin_memory()
+    h_w = torch.zeros(len(bodies) * abi.WRENCH_DTYPE.itemsize, dtype=torch.uint8).pin_memory()
+    for _ in range(2):                      # the second call starts from the first one's outputs
+        bt.compute_ptr(h_b.data_ptr(), sc["ocean"], scenarios.settings(), h_w.data_ptr())
+    bt.compute_device(d_b.data_ptr(), sc["ocean"], scenarios.settings(), d_w.data_ptr(), s.cuda_stream)
+    torch.cuda.synchronize()
+    assert h_w.numpy().tobytes() == d_w.cpu().numpy().tobytes()
     bt.close()
 
 
