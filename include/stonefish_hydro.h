@@ -308,6 +308,13 @@ hydro_status hydro_batch_compute(hydro_batch* batch, const hydro_body* bodies,
                                  const hydro_settings* settings,
                                  hydro_wrench* inout);
 
+/* Device address under which kernels can read and write the page-locked
+ * mapped host memory at `host` (cudaHostAlloc, cudaHostRegister with
+ * mapping, a pinned torch tensor); HYDRO_ERR_INVALID_ARG for other memory.
+ * Lets device entry points take host buffers without staging copies (no
+ * counterpart in the reference). */
+hydro_status hydro_mapped_host_ptr(const void* host, void** device);
+
 /* Autotuner (no counterpart in the reference).  Times the step on this
  * batch's own bodies for every work-chunk size in {768, 1536, 3072, 4224,
  * 6144} faces and 1 or 2 resident CTAs per SM (reps timed steps each, after

@@ -236,6 +236,7 @@ def _declare(lib: C.CDLL) -> None:
         "hydro_fluid_position": (i32, [vp, C.POINTER(Ocean), d, d, C.POINTER(i32)]),
         "hydro_debug_division_check": (i32, [vp, C.c_uint64, C.c_uint64, vp]),
         "hydro_debug_tile_order": (i32, [vp, u32, u32, vp, vp, u32, C.POINTER(u32)]),
+        "hydro_mapped_host_ptr": (i32, [vp, C.POINTER(vp)]),
         "hydro_debug_arith_check": (i32, [vp, C.c_uint64, C.c_uint64, vp, vp, vp]),
         "hydro_debug_wait_timeout": (i32, [vp, u32, C.POINTER(i32)]),
         "hydro_compute_wrenches_static": (i32, [vp, vp, u32, vp, C.POINTER(Ocean), C.POINTER(Settings),
@@ -291,6 +292,16 @@ def exported_symbols_from_header(header: str | None = None) -> list[str]:
     text = open(path).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     return sorted(set(re.findall(r"\b(hydro_[a-z0-9_]+)\s*\(", text)))
+
+
+def mapped_host_ptr(host_ptr: int, lib_path: str | None = None) -> int:
+    """hydro_mapped_host_ptr: the device address of page-locked mapped host memory."""
+    lib = load_library(lib_path)
+    d = C.c_void_p()
+    st = lib.hydro_mapped_host_ptr(C.c_void_p(host_ptr), C.byref(d))
+    if st != HYDRO_OK:
+        raise HydroError(st, "host memory is not page-locked and mapped")
+    return int(d.value)
 
 
 def tile_order(faces: np.ndarray, n_vertices: int, lib_path: str | None = None):

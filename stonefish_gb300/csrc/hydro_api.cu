@@ -915,6 +915,15 @@ static void* mapped_host_ptr(const void* p)
     return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
 }
 
+hydro_status hydro_mapped_host_ptr(const void* host, void** device)
+{
+    if (!host || !device) return HYDRO_ERR_INVALID_ARG;
+    void* d = mapped_host_ptr(host);
+    if (!d) return HYDRO_ERR_INVALID_ARG;
+    *device = d;
+    return HYDRO_OK;
+}
+
 hydro_status hydro_batch_compute(hydro_batch* b, const hydro_body* bodies, const hydro_ocean* ocean,
                                  const hydro_settings* settings, hydro_wrench* inout)
 {

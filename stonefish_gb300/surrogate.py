@@ -475,14 +475,20 @@ class GatedPredictor:
         _check(self.lib, self.h.ctx, st)
 
     def predict(self, d_bodies: torch.Tensor) -> torch.Tensor:
-        """d_bodies: device bytes of n hydro_body (mesh ids are ignored: the
-        exact slots use this predictor's mesh).  Returns out [n,6] (device)."""
+        """d_bodies: bytes of n hydro_body on the device, or in page-locked
+        host memory, which the kernels then read in place (mesh ids are
+        ignored: the exact slots use this predictor's mesh).  Returns out
+        [n,6] (device)."""
         s = self.s
         st = s._s()
         n, b = self.n, self.bufs
         g = s.gate
         ctx = self.h.ctx
-        self._ck(self.lib.hydro_nn_features(ctx, _ptr(d_bodies), n, C.byref(self.ocean), _ptr(b["feats"]), st))
+        if d_bodies.is_cuda:
+            bodies = _ptr(d_bodies)
+        else:
+            bodies = C.c_void_p(abi.mapped_host_ptr(d_bodies.data_ptr()))
+        self._ck(self.lib.hydro_nn_features(ctx, bodies, n, C.byref(self.ocean), _ptr(b["feats"]), st))
         self._ck(self.lib.hydro_nn_gate(ctx, _ptr(b["feats"]), n, _ptr(g["lo"]), _ptr(g["hi"]), _ptr(g["mean"]),
                                         _ptr(g["P"]), g["thr"], _ptr(b["mask"]), st))
         if self.mode == "tcgen05":
@@ -492,12 +498,12 @@ class GatedPredictor:
             s.to_bf16(b["feats"], self.n_pad, N_FEAT, IN_PAD, b["X0"], s.f_mean, s.f_istd)
             s._mlp(b, self.n_pad)
             z, ldz, mlp_launches = b["z"], OUT_PAD, 5
-        self._ck(self.lib.hydro_nn_route(ctx, _ptr(d_bodies), _ptr(b["mask"]), n, _ptr(self.counts),
+        self._ck(self.lib.hydro_nn_route(ctx, bodies, _ptr(b["mask"]), n, _ptr(self.counts),
                                          _ptr(self.packed), _ptr(self.pos), _ptr(self.n_packed), st))
         self.exact_io.zero_()
         self.batch.compute_device_prefix(self.packed.data_ptr(), self.n_packed.data_ptr(), self.ocean,
                                          self.settings, self.exact_io.data_ptr(), st)
-        self._ck(self.lib.hydro_nn_merge(ctx, _ptr(d_bodies), _ptr(z), ldz, _ptr(self.pos),
+        self._ck(self.lib.hydro_nn_merge(ctx, bodies, _ptr(z), ldz, _ptr(self.pos),
                                          _ptr(self.exact_io), n, _ptr(self.out), st))
         # features, gate, network, 2 route, exact step, merge
         self.launches = 1 + 1 + mlp_launches + 2 + self.batch.last_launches() + 1

@@ -250,6 +250,9 @@ def test_surrogate_learns_and_beats_exact_step(built_library):
     test_bodies["mesh"] = m32
     d_b = torch.from_numpy(np.frombuffer(test_bodies.tobytes(), dtype=np.uint8).copy()).cuda()
     out = gp.predict(d_b).cpu().numpy()
+    # the same states from page-locked host memory, read in place
+    h_b = torch.from_numpy(np.frombuffer(test_bodies.tobytes(), dtype=np.uint8).copy()).pin_memory()
+    assert np.array_equal(gp.predict(h_b).cpu().numpy(), out)
     err = S.wrench_errors(out, tt, ocean)
     const = S.wrench_errors(np.tile(tt.mean(0), (n_test, 1)), tt, ocean)
     assert err["wrench_median"] < 0.15 * const["wrench_median"], (err, const)
