@@ -272,8 +272,8 @@ hydro_status hydro_batch_create(hydro_ctx* ctx, const hydro_mesh_id* mesh_of_bod
                                 uint32_t n_bodies, hydro_batch** out);
 
 /* As hydro_batch_create, with the work-chunk size of this batch in faces
- * (rounded up to whole 384-face tiles, at most 16 tiles; 0 = the context's
- * setting).  Small chunks suit batches of which only a few bodies are
+ * (rounded up to whole tiles of HYDRO_TILE_FACES faces, at most 16 tiles;
+ * 0 = the context's setting).  Small chunks suit batches of which only a few bodies are
  * active at a time (no counterpart in the reference). */
 hydro_status hydro_batch_create_ex(hydro_ctx* ctx, const hydro_mesh_id* mesh_of_body,
                                    uint32_t n_bodies, uint32_t chunk_faces, hydro_batch** out);
@@ -288,6 +288,16 @@ hydro_status hydro_batch_compute_device(hydro_batch* batch, const hydro_body* d_
                                         const hydro_ocean* ocean,
                                         const hydro_settings* settings,
                                         hydro_wrench* d_inout, void* stream);
+
+/* The per-body hydrodynamics loop of a simulation tick in one call
+ * (SimulationManager.cpp:1620-1655 -> Ocean::ApplyFluidForces, Ocean.cpp:
+ * 219-268 -> SolidEntity::ComputeHydrodynamicForces for every body):
+ * hydro_batch_compute_device on a batch that the context builds for this
+ * list of meshes on the first call and keeps until the list changes.
+ * d_bodies and d_inout are device pointers, enqueued on `stream`. */
+hydro_status hydro_compute_wrenches(hydro_ctx* ctx, const hydro_mesh_id* mesh_of_body, uint32_t n_bodies,
+                                    const hydro_body* d_bodies, const hydro_ocean* ocean,
+                                    const hydro_settings* settings, hydro_wrench* d_inout, void* stream);
 
 /* As hydro_batch_compute_device for the first *d_count bodies only, the
  * count read on the device when the step runs (e.g. written by an earlier

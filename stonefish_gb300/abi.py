@@ -237,6 +237,7 @@ def _declare(lib: C.CDLL) -> None:
         "hydro_debug_division_check": (i32, [vp, C.c_uint64, C.c_uint64, vp]),
         "hydro_debug_tile_order": (i32, [vp, u32, u32, vp, vp, u32, C.POINTER(u32)]),
         "hydro_mapped_host_ptr": (i32, [vp, C.POINTER(vp)]),
+        "hydro_compute_wrenches": (i32, [vp, vp, u32, vp, vp, vp, vp, vp]),
         "hydro_debug_arith_check": (i32, [vp, C.c_uint64, C.c_uint64, vp, vp, vp]),
         "hydro_debug_wait_timeout": (i32, [vp, u32, C.POINTER(i32)]),
         "hydro_compute_wrenches_static": (i32, [vp, vp, u32, vp, C.POINTER(Ocean), C.POINTER(Settings),

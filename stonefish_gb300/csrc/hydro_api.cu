@@ -57,6 +57,9 @@ struct hydro_ctx {
     float wave_grid[HYDRO_MAX_WAVE_LAYERS] = {1.f, 1.f, 1.f, 1.f};
     // single-body calls
     std::unordered_map<uint32_t, hydro_batch*> single;
+    // hydro_compute_wrenches: the batch of the last list of meshes
+    hydro_batch* oneshot = nullptr;
+    std::vector<hydro_mesh_id> oneshot_meshes;
     void* small_d = nullptr;   // scratch for the small entry points
     size_t small_cap = 0;
     std::string tune_path;     // autotuner cache file ("" = none)
@@ -548,6 +551,7 @@ void hydro_destroy(hydro_ctx* ctx)
     cudaSetDevice(ctx->device);
     cudaDeviceSynchronize();
     for (auto& kv : ctx->single) batch_free(kv.second);
+    if (ctx->oneshot) batch_free(ctx->oneshot);
     for (auto& s : ctx->slabs) cudaFree(s.base);
     cudaFree(ctx->tiles_d);
     cudaFree(ctx->wave_d);
@@ -565,8 +569,9 @@ void hydro_destroy(hydro_ctx* ctx)
 // one that adds the fewest new vertices (ties: the one reached first, so
 // that the tile grows ring by ring).  The next tile starts from the face on
 // the closed tile's border that comes first in upload order, so tiles
-// follow one another across the surface whatever the upload order.  When a tile has used up its connected part of
-// the mesh (the separately indexed sides of a box are separate parts), it
+// follow one another across the surface whatever the upload order.  When a
+// tile has used up its connected part of the mesh (the separately indexed
+// sides of a box are separate parts), it
 // closes if at least half full and otherwise takes the next unused face in
 // upload order as a further seed, so that small parts share tiles.  A tile
 // closes at kTileFaces faces or when no reachable face fits under
@@ -900,6 +905,27 @@ hydro_status hydro_batch_compute_device_prefix(hydro_batch* b, const hydro_body*
         return fail(ctx, HYDRO_ERR_INVALID_ARG, "batch compute prefix: bad arguments");
     return batch_launch(b, d_bodies, ocean, settings, d_inout, static_cast<cudaStream_t>(stream), OP_BODY,
                         d_count);
+}
+
+hydro_status hydro_compute_wrenches(hydro_ctx* ctx, const hydro_mesh_id* mesh_of_body, uint32_t n_bodies,
+                                    const hydro_body* d_bodies, const hydro_ocean* ocean,
+                                    const hydro_settings* settings, hydro_wrench* d_inout, void* stream)
+{
+    if (!ctx) return HYDRO_ERR_INVALID_ARG;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (!mesh_of_body || n_bodies == 0)
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "compute wrenches: no bodies");
+    const bool same = ctx->oneshot && ctx->oneshot_meshes.size() == n_bodies &&
+                      std::equal(mesh_of_body, mesh_of_body + n_bodies, ctx->oneshot_meshes.begin());
+    if (!same) {
+        hydro_batch* nb = nullptr;
+        const hydro_status st = hydro_batch_create(ctx, mesh_of_body, n_bodies, &nb);
+        if (st != HYDRO_OK) return st;
+        if (ctx->oneshot) hydro_batch_destroy(ctx->oneshot);
+        ctx->oneshot = nb;
+        ctx->oneshot_meshes.assign(mesh_of_body, mesh_of_body + n_bodies);
+    }
+    return hydro_batch_compute_device(ctx->oneshot, d_bodies, ocean, settings, d_inout, stream);
 }
 
 // Device address of host memory that kernels can read and write in place

@@ -259,6 +259,13 @@ class HydroContext:
                                                         C.byref(ocean), C.byref(settings), d_io,
                                                         stream or None))
 
+    def compute_wrenches(self, mesh_of_body, d_bodies: int, ocean, settings, d_io: int, stream: int = 0) -> None:
+        """hydro_compute_wrenches: one call per tick, device pointers in/out; the
+        context keeps the batch for this list of meshes between calls."""
+        ids = np.ascontiguousarray(mesh_of_body, dtype=np.uint32)
+        self._ck(self.lib.hydro_compute_wrenches(self.ctx, ids.ctypes.data, ids.size, d_bodies, C.byref(ocean),
+                                                 C.byref(settings), d_io, stream or None))
+
     def batch(self, mesh_of_body, chunk_faces: int = 0) -> "Batch":
         return Batch(self, mesh_of_body, chunk_faces)
 

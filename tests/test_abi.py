@@ -87,6 +87,9 @@ def test_null_context_is_rejected_without_device(built_library):
     assert lib.hydro_batch_compute(None, None, C.byref(oc), C.byref(st), None) == abi.HYDRO_ERR_INVALID_ARG
     assert lib.hydro_batch_compute_device(None, None, C.byref(oc), C.byref(st), None, None) == abi.HYDRO_ERR_INVALID_ARG
     assert lib.hydro_body_forces(None, None, C.byref(oc), C.byref(st), None) == abi.HYDRO_ERR_INVALID_ARG
+    assert lib.hydro_compute_wrenches(None, None, 0, None, C.byref(oc), C.byref(st), None, None) == abi.HYDRO_ERR_INVALID_ARG
+    d = C.c_void_p()
+    assert lib.hydro_mapped_host_ptr(None, C.byref(d)) == abi.HYDRO_ERR_INVALID_ARG
     assert lib.hydro_create(None, None) == abi.HYDRO_ERR_INVALID_ARG
     assert lib.hydro_status_string(abi.HYDRO_ERR_INDEX_RANGE) == b"face index out of range"
     assert lib.hydro_last_error(None) == b"null context"

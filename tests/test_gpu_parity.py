@@ -305,6 +305,28 @@ def test_host_and_device_entry_points_agree(hctx):
     bt.close()
 
 
+def test_one_call_step_matches_batch(hctx):
+    """hydro_compute_wrenches (the context keeps a batch per list of meshes)
+    gives the batch's bits, keeps its batch while the list is unchanged and
+    rebuilds it when the list changes."""
+    torch = pytest.importorskip("torch")
+    sc = upload(hctx, scenarios.mixed_batch(n_bodies=48, seed=14, scale_faces=0.05))
+    ids = np.asarray(sc["_ids"], dtype=np.uint32)[sc["bodies"]["mesh"]]
+    bodies = sc["bodies"].copy()
+    bodies["mesh"] = ids
+    ref = scenarios.new_wrenches(len(bodies))
+    bt = hctx.batch(ids)
+    bt.compute(bodies, sc["ocean"], scenarios.settings(), ref)
+    bt.close()
+    s = torch.cuda.current_stream().cuda_stream
+    for n in (len(bodies), len(bodies), len(bodies) // 2):
+        d_b = torch.from_numpy(bodies[:n].view(np.uint8).copy()).cuda()
+        d_w = torch.zeros(n * abi.WRENCH_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+        hctx.compute_wrenches(ids[:n], d_b.data_ptr(), sc["ocean"], scenarios.settings(), d_w.data_ptr(), s)
+        torch.cuda.synchronize()
+        assert d_w.cpu().numpy().tobytes() == ref[:n].tobytes(), n
+
+
 @pytest.mark.parametrize("chunk_faces", [abi.TILE_FACES, 4 * abi.TILE_FACES])
 def test_prefix_entry_and_chunk_size(hctx, chunk_faces):
     """hydro_batch_compute_device_prefix evaluates exactly the first *count
