@@ -647,10 +647,13 @@ def run_gpu(args, rank: int, world: int, local_rank: int, dist):
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         cpu_s, n = cpu_baseline(sc, threads)
+        cpu1_s, n1 = cpu_baseline(sc, 1, budget_s=5.0, max_steps=3)
         result["cpu_baseline"] = {"value": nb / cpu_s, "unit": UNIT, "cores": threads, "kind": "port",
                                   "sample": f"median of {n} full steps of the same workload "
                                             f"(REF32 oracle, one task per body)",
-                                  "faces_per_s": int(per_body_faces.sum()) / cpu_s}
+                                  "faces_per_s": int(per_body_faces.sum()) / cpu_s,
+                                  "value_1_thread": nb / cpu1_s,
+                                  "sample_1_thread": f"median of {n1} full steps on one host thread"}
     batch.close()
     h.close()
     return result
