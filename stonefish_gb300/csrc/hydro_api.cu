@@ -266,6 +266,7 @@ OceanDev make_ocean(const hydro_ctx* ctx, const hydro_ocean* o)
     d.wave_channels = ctx->wave_channels;
     d.wave_layers = ctx->wave_layers;
     d.wave_idx32 = (uint64_t)ctx->wave_n * ctx->wave_n * ctx->wave_channels < (uint64_t(1) << 32) ? 1 : 0;
+    d.wave_half = ctx->wave_n ? 0.5f / (float)ctx->wave_n : 0.f;
     for (int l = 0; l < HYDRO_MAX_WAVE_LAYERS; ++l) {
         d.wave_channel[l] = ctx->wave_channel[l];
         d.wave_grid[l] = ctx->wave_grid[l];

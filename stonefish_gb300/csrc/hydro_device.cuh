@@ -123,6 +123,7 @@ struct OceanDev {
     uint32_t wave_channel[HYDRO_MAX_WAVE_LAYERS];
     float wave_grid[HYDRO_MAX_WAVE_LAYERS];
     float wave_inv_grid[HYDRO_MAX_WAVE_LAYERS];   // RN(1 / wave_grid[l])
+    float wave_half;             // 0.5f / (float)wave_n, the texel-centre offset
     int wave_idx32;              // N * N * channels < 2^32: texel offsets fit 32 bits
     hydro_current currents[HYDRO_MAX_CURRENTS];
 };
@@ -233,7 +234,7 @@ __device__ __forceinline__ float wave_interp(const OceanDev& o, float x, float y
 {
     const uint32_t N = o.wave_n;
     const float Nf = (float)N;
-    const float half = 0.5f / Nf;
+    const float half = o.wave_half;   // 0.5f / Nf, formed once on the host (IEEE division there too)
     float i0f = fracf_(x - half);
     float j0f = fracf_(y - half);
     if (i0f < 0.f) i0f = 1.f - fabsf(i0f);
