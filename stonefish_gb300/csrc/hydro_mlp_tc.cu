@@ -1,8 +1,11 @@
 // hydro_mlp_tc.cu -- fused inference of the wrench surrogate on the 5th-
-// generation tensor cores: one CTA takes 128 states through all four layers
-// (16 -> 256 -> 256 -> 256 -> 16) with the activations kept in shared memory
-// and the accumulators in tensor memory.
+// generation tensor cores: a CTA takes blocks of 128 states through all four
+// layers (16 -> 256 -> 256 -> 256 -> 16) with the activations kept in shared
+// memory and the accumulators in tensor memory.
 //
+//   * persistent: one CTA per SM loops over the blocks; the next block's
+//     features are loaded into registers while the current block runs, and
+//     its first-layer weights are copied while the last layer runs;
 //   * operands are K-major BF16 in the 128-byte-swizzled canonical layout
 //     (8-row x 128-byte atoms, 16-byte chunk c of row r stored at chunk
 //     c ^ (r % 8)); each [rows x 64] K-block is contiguous, blocks follow
@@ -54,8 +57,8 @@ constexpr uint32_t kOffA = 0;                        // 128 x 256 bf16, 4 K-bloc
 constexpr uint32_t kOffW = kOffA + 4 * 16384;        // 256 x 256 bf16, 4 K-blocks of 32 KB
 constexpr uint32_t kOffW3 = kOffW + 4 * 32768;       // 16 x 256 bf16, 4 K-blocks of 2 KB
 constexpr uint32_t kOffBias = kOffW3 + 4 * 2048;     // 3 x 256 + 16 floats
-constexpr uint32_t kOffBar = kOffBias + (3 * kHid + kOut) * 4;   // 10 mbarriers
-constexpr uint32_t kOffTmem = kOffBar + 10 * 8;
+constexpr uint32_t kOffBar = kOffBias + (3 * kHid + kOut) * 4;   // 11 mbarriers
+constexpr uint32_t kOffTmem = kOffBar + 12 * 8;
 constexpr uint32_t kSmemBytes = kOffTmem + 16 + 1024; // + alignment slack
 
 // global weight image (bytes)
@@ -267,6 +270,36 @@ __device__ __forceinline__ void hidden_epilogue(uint32_t acc, unsigned char* bas
 
 }  // namespace tc
 
+// Normalised BF16 inputs of one 128-state block: thread t < 256 holds row
+// t % 128, features 8 (t / 128) .. + 7.
+__device__ __forceinline__ void load_features(const float* __restrict__ feats, uint32_t n, uint32_t row0,
+                                              const float* __restrict__ fmean, const float* __restrict__ fistd,
+                                              float (&x)[8])
+{
+    using namespace tc;
+    const uint32_t r = threadIdx.x & (kRows - 1), h = threadIdx.x >> 7;
+    const uint32_t gr = row0 + r;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const int k = (int)h * 8 + j;
+        x[j] = gr < n ? (feats[(size_t)gr * kIn + k] - fmean[k]) * fistd[k] : 0.f;
+    }
+}
+
+__device__ __forceinline__ void store_features(unsigned char* base, const float (&x)[8])
+{
+    using namespace tc;
+    const uint32_t r = threadIdx.x & (kRows - 1), h = threadIdx.x >> 7;
+    *reinterpret_cast<uint4*>(base + kOffA + sw128_offset(kRows, r, h * 8)) =
+        make_uint4(pack2(x[0], x[1]), pack2(x[2], x[3]), pack2(x[4], x[5]), pack2(x[6], x[7]));
+}
+
+// Persistent: CTA c takes the 128-state blocks c, c + gridDim.x, ...; the
+// tensor memory, the mbarriers, the biases and the last layer's weights are
+// set up once.  While a block runs, the epilogue threads hold the next
+// block's features in registers and write them once the block's last MMAs
+// have retired; the next block's first-layer weights are copied as soon as
+// the weight buffer is free.
 __global__ void __launch_bounds__(tc::kThreads, 1)
 mlp_tc_kernel(const float* __restrict__ feats, uint32_t n, const float* __restrict__ fmean,
               const float* __restrict__ fistd, const unsigned char* __restrict__ wimg,
@@ -278,13 +311,14 @@ mlp_tc_kernel(const float* __restrict__ feats, uint32_t n, const float* __restri
     const uint32_t raw = smem_u32(smem_raw);
     unsigned char* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
     const uint32_t sb = smem_u32(base);
-    // mbarriers: weights of layers 0 and 3; MMA commits; the four K-block
-    // copies of a hidden layer's weights; the four K-blocks of A
-    const uint32_t barW0 = sb + kOffBar, barM = barW0 + 8, wbar = barW0 + 16, abar = barW0 + 48;
+    // mbarriers: first-layer weights; MMA commits; the four K-block copies of
+    // a hidden layer's weights; the four K-blocks of A; a block's features
+    const uint32_t barW0 = sb + kOffBar, barM = barW0 + 8, wbar = barW0 + 16, abar = barW0 + 48,
+                   barF = barW0 + 80;
     float* bias = reinterpret_cast<float*>(base + kOffBias);
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(base + kOffTmem);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const uint32_t row0 = blockIdx.x * (uint32_t)kRows;
+    const uint32_t n_blocks = (n + kRows - 1) / kRows;
     const uint64_t kLimit = 1000000000ull;   // 1 s per wait
 
     if (warp == 0) {
@@ -300,6 +334,7 @@ mlp_tc_kernel(const float* __restrict__ feats, uint32_t n, const float* __restri
             asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(abar + 8u * g), "r"(kEpiWarps * 32)
                          : "memory");
         }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(barF), "r"(kEpiWarps * 32) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     fence_before();
@@ -307,7 +342,7 @@ mlp_tc_kernel(const float* __restrict__ feats, uint32_t n, const float* __restri
     fence_after();
     const uint32_t tmem = *tmem_slot;
 
-    // weights of layers 0 and 3 (40 KB)
+    // the first block's first-layer weights and the last layer's (which stay)
     if (tid == 0) {
         expect_tx(barW0, 32768u + 8192u);
         bulk_load(sb + kOffW, wimg + kImgW0, 32768u, barW0);
@@ -319,18 +354,10 @@ mlp_tc_kernel(const float* __restrict__ feats, uint32_t n, const float* __restri
         bias[2 * kHid + i] = b2[i];
     }
     if (tid < kOut) bias[3 * kHid + tid] = b3[tid];
-    // normalised BF16 inputs: thread -> (row, 8 features)
+    float x[8];
     if (tid < kRows * (kIn / 8)) {
-        const uint32_t r = (uint32_t)(tid & (kRows - 1)), h = (uint32_t)(tid >> 7);
-        const uint32_t gr = row0 + r;
-        float x[8];
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            const int k = (int)h * 8 + j;
-            x[j] = gr < n ? (feats[(size_t)gr * kIn + k] - fmean[k]) * fistd[k] : 0.f;
-        }
-        *reinterpret_cast<uint4*>(base + kOffA + sw128_offset(kRows, r, h * 8)) =
-            make_uint4(pack2(x[0], x[1]), pack2(x[2], x[3]), pack2(x[4], x[5]), pack2(x[6], x[7]));
+        load_features(feats, n, blockIdx.x * (uint32_t)kRows, fmean, fistd, x);
+        store_features(base, x);
     }
     fence_async_smem();
     __syncthreads();
@@ -340,96 +367,133 @@ mlp_tc_kernel(const float* __restrict__ feats, uint32_t n, const float* __restri
         // ---- MMA warp: one lane issues every layer's MMAs and the weight copies
         if (lane == 0) {
             const uint32_t id_hid = idesc_bf16(128, 256), id_out = idesc_bf16(128, kOut);
-            uint32_t w_pending = 0;   // K-block copies issued and not yet waited for
-            uint32_t w_phase = 0;
+            uint32_t w_pending = 0, w_par = 0;    // K-block copies issued and not yet waited for; their parity
+            uint32_t w0_pending = 1, w0_par = 0;  // first-layer copy issued and not yet waited for; its parity
             uint32_t commits = 0, seen = 0;   // barM phases committed / observed complete
-            ok = mbar_wait(barW0, 0u, kLimit);
-            if (ok) {
+            uint32_t a_done = 0;              // completions of the A K-block barriers waited for
+            uint32_t k = 0;
+#pragma unroll 1
+            for (uint32_t blk = blockIdx.x; blk < n_blocks && ok; blk += gridDim.x, ++k) {
+                ok = mbar_wait(barW0, k & 1u, kLimit);
+                if (ok) w0_pending = 0;
+                // this block's features: written once the epilogue has seen
+                // the previous block's last commit
+                if (ok && k > 0) {
+                    ok = mbar_wait(barF, (k - 1u) & 1u, kLimit);
+                    if (ok) ++seen;
+                }
+                if (!ok) break;
                 fence_after();
                 mma(tmem, sw128_desc(sb + kOffA), sw128_desc(sb + kOffW), id_hid, 0u);   // layer 0: K = 16
                 mma_commit(barM);
                 ++commits;
-            }
 #pragma unroll 1
-            for (uint32_t l = 1; l <= 3 && ok; ++l) {
-                const uint32_t prev = (l - 1u) & 1u;   // parity of layer l - 1's completions
-                if (l < 3) {
-                    // layer l - 1's MMAs have retired: the weight buffer takes layer l's
-                    ok = mbar_wait(barM, prev, kLimit);
+                for (uint32_t l = 1; l <= 3 && ok; ++l) {
+                    // layer l - 1's MMAs have retired: the weight buffer takes
+                    // layer l's weights (or, before the last layer, the next
+                    // block's first-layer weights)
+                    ok = mbar_wait(barM, (l - 1u) & 1u, kLimit);
                     if (!ok) break;
                     ++seen;
-                    for (uint32_t g = 0; g < 4; ++g) {
-                        expect_tx(wbar + 8u * g, 32768u);
-                        bulk_load(sb + kOffW + 32768u * g, wimg + (l == 1 ? kImgW1 : kImgW2) + 32768u * g, 32768u,
-                                  wbar + 8u * g);
-                    }
-                    w_pending = 0xFu;
-                }
-                const uint32_t acc = tmem + 256u * (l & 1u);
-#pragma unroll 1
-                for (uint32_t g = 0; g < 4 && ok; ++g) {
                     if (l < 3) {
-                        ok = mbar_wait(wbar + 8u * g, w_phase, kLimit);
-                        if (!ok) break;
-                        w_pending &= ~(1u << g);
+                        for (uint32_t g = 0; g < 4; ++g) {
+                            expect_tx(wbar + 8u * g, 32768u);
+                            bulk_load(sb + kOffW + 32768u * g, wimg + (l == 1 ? kImgW1 : kImgW2) + 32768u * g,
+                                      32768u, wbar + 8u * g);
+                        }
+                        w_pending = 0xFu;
+                        w_par = (l - 1u) & 1u;
+                    } else if (blk + gridDim.x < n_blocks) {
+                        expect_tx(barW0, 32768u);
+                        bulk_load(sb + kOffW, wimg + kImgW0, 32768u, barW0);
+                        w0_pending = 1;
+                        w0_par = (k + 1u) & 1u;
                     }
-                    ok = mbar_wait(abar + 8u * g, prev, kLimit);   // K-block g of layer l's input
-                    if (!ok) break;
-                    fence_after();
-#pragma unroll
-                    for (uint32_t j = 0; j < 4; ++j) {
-                        const uint32_t off_a = kOffA + g * (kRows * 128u) + j * 32u;
+                    const uint32_t acc = tmem + 256u * (l & 1u);
+#pragma unroll 1
+                    for (uint32_t g = 0; g < 4 && ok; ++g) {
                         if (l < 3) {
-                            const uint32_t off_b = kOffW + g * (kHid * 128u) + j * 32u;
-                            mma(acc, sw128_desc(sb + off_a), sw128_desc(sb + off_b), id_hid, (g | j) ? 1u : 0u);
-                        } else {
-                            const uint32_t off_b = kOffW3 + g * (kOut * 128u) + j * 32u;
-                            mma(acc, sw128_desc(sb + off_a), sw128_desc(sb + off_b), id_out, (g | j) ? 1u : 0u);
+                            ok = mbar_wait(wbar + 8u * g, (l - 1u) & 1u, kLimit);
+                            if (!ok) break;
+                            w_pending &= ~(1u << g);
+                        }
+                        ok = mbar_wait(abar + 8u * g, a_done & 1u, kLimit);   // K-block g of layer l's input
+                        if (!ok) break;
+                        fence_after();
+#pragma unroll
+                        for (uint32_t j = 0; j < 4; ++j) {
+                            const uint32_t off_a = kOffA + g * (kRows * 128u) + j * 32u;
+                            if (l < 3) {
+                                const uint32_t off_b = kOffW + g * (kHid * 128u) + j * 32u;
+                                mma(acc, sw128_desc(sb + off_a), sw128_desc(sb + off_b), id_hid, (g | j) ? 1u : 0u);
+                            } else {
+                                const uint32_t off_b = kOffW3 + g * (kOut * 128u) + j * 32u;
+                                mma(acc, sw128_desc(sb + off_a), sw128_desc(sb + off_b), id_out, (g | j) ? 1u : 0u);
+                            }
                         }
                     }
+                    if (!ok) break;
+                    ++a_done;
+                    mma_commit(barM);
+                    ++commits;
                 }
-                if (!ok) break;
-                mma_commit(barM);
-                ++commits;
-                if (l < 3) w_phase ^= 1u;
+                // the epilogue waits for the last layer's commit; this warp
+                // counts it as seen once the next block's features arrive
             }
             if (!ok) {
-                // let issued tensor-core work and weight copies retire before
-                // the tensor memory is freed and the CTA exits (bounded): one
-                // more commit, then the barrier's phases in order
+                // let issued tensor-core work and copies retire before the
+                // tensor memory is freed and the CTA exits (bounded): one more
+                // commit, then the barrier's phases in order
                 atomicOr(err, 1u);
                 mma_commit(barM);
                 ++commits;
-                for (uint32_t k = seen; k < commits; ++k) mbar_wait(barM, k & 1u, kLimit);
+                for (uint32_t c = seen; c < commits; ++c) mbar_wait(barM, c & 1u, kLimit);
                 for (uint32_t g = 0; g < 4; ++g)
-                    if ((w_pending >> g) & 1u) mbar_wait(wbar + 8u * g, w_phase, kLimit);
+                    if ((w_pending >> g) & 1u) mbar_wait(wbar + 8u * g, w_par, kLimit);
+                if (w0_pending) mbar_wait(barW0, w0_par, kLimit);
             }
         }
         __syncwarp();
         ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
     } else {
-        // ---- epilogue warps: layers 0..2 feed the next layer K-block by K-block
+        // ---- epilogue warps
 #pragma unroll 1
-        for (uint32_t l = 0; l < 3 && ok; ++l) {
-            ok = mbar_wait(barM, l & 1u, kLimit);
+        for (uint32_t blk = blockIdx.x; blk < n_blocks && ok; blk += gridDim.x) {
+            const uint32_t next = blk + gridDim.x;
+            if (tid < kRows * (kIn / 8)) {
+                if (next < n_blocks) load_features(feats, n, next * (uint32_t)kRows, fmean, fistd, x);
+            }
+            // layers 0..2 feed the next layer K-block by K-block
+#pragma unroll 1
+            for (uint32_t l = 0; l < 3 && ok; ++l) {
+                ok = mbar_wait(barM, l & 1u, kLimit);
+                if (!ok) break;
+                fence_after();
+                hidden_epilogue(tmem + 256u * (l & 1u), base, bias + l * kHid, abar);
+            }
+            // output layer: N = 16, bias, FP32 rows of 16
+            if (ok) ok = mbar_wait(barM, 1u, kLimit);
             if (!ok) break;
             fence_after();
-            hidden_epilogue(tmem + 256u * (l & 1u), base, bias + l * kHid, abar);
-        }
-        // ---- output layer: N = 16, bias, FP32 rows of 16
-        if (ok) ok = mbar_wait(barM, 1u, kLimit);
-        if (ok && warp < 4) {
-            fence_after();
-            float v[16];
-            tmem_ld16(tmem + 256u + ((32u * (uint32_t)warp) << 16), v);
-            const uint32_t gr = row0 + 32u * (uint32_t)warp + (uint32_t)lane;
-            if (gr < n) {
-                float4* o = reinterpret_cast<float4*>(out + (size_t)gr * kOut);
-                const float* bb = bias + 3 * kHid;
+            if (warp < 4) {
+                float v[16];
+                tmem_ld16(tmem + 256u + ((32u * (uint32_t)warp) << 16), v);
+                const uint32_t gr = blk * (uint32_t)kRows + 32u * (uint32_t)warp + (uint32_t)lane;
+                if (gr < n) {
+                    float4* o = reinterpret_cast<float4*>(out + (size_t)gr * kOut);
+                    const float* bb = bias + 3 * kHid;
 #pragma unroll
-                for (int i = 0; i < 4; ++i)
-                    o[i] = make_float4(v[4 * i] + bb[4 * i], v[4 * i + 1] + bb[4 * i + 1],
-                                       v[4 * i + 2] + bb[4 * i + 2], v[4 * i + 3] + bb[4 * i + 3]);
+                    for (int i = 0; i < 4; ++i)
+                        o[i] = make_float4(v[4 * i] + bb[4 * i], v[4 * i + 1] + bb[4 * i + 1],
+                                           v[4 * i + 2] + bb[4 * i + 2], v[4 * i + 3] + bb[4 * i + 3]);
+                }
+            }
+            // the next block's features into A (its last MMAs have retired)
+            if (next < n_blocks) {
+                if (tid < kRows * (kIn / 8)) store_features(base, x);
+                fence_before();
+                fence_async_smem();
+                mbar_arrive(barF);
             }
         }
         if (!ok && lane == 0) atomicOr(err, 1u);
@@ -482,7 +546,11 @@ cudaError_t launch_mlp_tc(const float* feats, uint32_t n, const float* fmean, co
     cudaError_t e = cudaFuncSetAttribute(mlp_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)tc::kSmemBytes);
     if (e != cudaSuccess) return e;
-    const uint32_t grid = (n + tc::kRows - 1) / tc::kRows;
+    int dev = 0, sms = 1;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    const uint32_t blocks = (n + tc::kRows - 1) / tc::kRows;
+    const uint32_t grid = blocks < (uint32_t)sms ? blocks : (uint32_t)sms;   // one CTA per SM
     mlp_tc_kernel<<<grid, tc::kThreads, tc::kSmemBytes, s>>>(feats, n, fmean, fistd,
                                                             static_cast<const unsigned char*>(wimg), b0, b1, b2,
                                                             b3, out, err);
