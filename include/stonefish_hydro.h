@@ -769,10 +769,12 @@ hydro_status hydro_nn_pack_sw128(hydro_ctx* ctx, const void* src, int32_t rows, 
  * d_packed (n entries) and switches the rest of d_packed off (mode
  * HYDRO_MODE_DISABLED), so an exact step over d_packed integrates only the
  * rejected states; d_pos[i] = packed slot or -1, *d_n_packed = count.
- * d_counts holds ceil(n / 256) words of scratch. */
+ * d_counts holds ceil(n / 256) words of scratch.  d_exact (n records, may
+ * be null): slots 0 .. count - 1 are zeroed, the fresh in-out records of
+ * the exact step over d_packed. */
 hydro_status hydro_nn_route(hydro_ctx* ctx, const hydro_body* d_bodies, const uint8_t* d_mask,
                             uint32_t n, uint32_t* d_counts, hydro_body* d_packed, int32_t* d_pos,
-                            uint32_t* d_n_packed, void* stream);
+                            uint32_t* d_n_packed, hydro_wrench* d_exact, void* stream);
 
 /* d_out[i][6] = body-frame wrench: columns 0..5 of d_z[i] (row stride ld)
  * when d_pos[i] < 0, else R^T (Fb+Fdq+Fdf, Tb+Tdq+Tdf) of d_exact[d_pos[i]]. */

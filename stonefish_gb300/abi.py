@@ -251,7 +251,7 @@ def _declare(lib: C.CDLL) -> None:
         "hydro_nn_to_bf16": (i32, [vp, vp, i32, i32, i32, vp, vp, vp, vp]),
         "hydro_nn_features": (i32, [vp, vp, u32, C.POINTER(Ocean), vp, vp]),
         "hydro_nn_gate": (i32, [vp, vp, u32, vp, vp, vp, vp, C.c_float, vp, vp]),
-        "hydro_nn_route": (i32, [vp, vp, vp, u32, vp, vp, vp, vp, vp]),
+        "hydro_nn_route": (i32, [vp, vp, vp, u32, vp, vp, vp, vp, vp, vp]),
         "hydro_nn_merge": (i32, [vp, vp, vp, i32, vp, vp, u32, vp, vp]),
         "hydro_nn_wrench_body": (i32, [vp, vp, vp, u32, vp, vp]),
         "hydro_nn_pack_sw128": (i32, [vp, vp, i32, i32, i32, i32, vp, vp]),

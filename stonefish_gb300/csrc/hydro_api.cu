@@ -2068,12 +2068,12 @@ extern "C" hydro_status hydro_nn_mlp_tc(hydro_ctx* ctx, const float* d_features,
 
 extern "C" hydro_status hydro_nn_route(hydro_ctx* ctx, const hydro_body* d_bodies, const uint8_t* d_mask,
                                        uint32_t n, uint32_t* d_counts, hydro_body* d_packed, int32_t* d_pos,
-                                       uint32_t* d_n_packed, void* stream)
+                                       uint32_t* d_n_packed, hydro_wrench* d_exact, void* stream)
 {
     NN_CTX_CHECK();
     if (!d_bodies || !d_mask || !d_counts || !d_packed || !d_pos || !d_n_packed)
         return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn route");
-    NN_RET(launch_route(d_bodies, d_mask, n, d_counts, d_packed, d_pos, d_n_packed,
+    NN_RET(launch_route(d_bodies, d_mask, n, d_counts, d_packed, d_pos, d_n_packed, d_exact,
                         static_cast<cudaStream_t>(stream)), "nn route");
 }
 

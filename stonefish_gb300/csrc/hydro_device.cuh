@@ -81,7 +81,7 @@ __host__ __device__ __forceinline__ uint32_t tile_block_bytes(uint32_t nv, uint3
 constexpr int kMaxTilesPerChunk = 16;
 
 // One work item: tiles [first_tile, first_tile + n_tiles) of one body.
-struct ChunkDesc {
+struct __align__(16) ChunkDesc {
     uint32_t body;
     uint32_t first_tile;
     uint32_t n_tiles;
@@ -92,12 +92,13 @@ struct ChunkDesc {
 // append one per such chunk (in the order their atomics land, which no
 // result depends on: every chunk writes its own partial) and the chunk
 // kernel's producers claim them in list order.
-struct ActiveChunk {
+struct __align__(16) ActiveChunk {
     uint32_t body;
     uint32_t first_tile;
     uint32_t n_tiles;
     uint32_t chunk;      // index of the chunk's partial
 };
+static_assert(sizeof(ChunkDesc) == 16 && sizeof(ActiveChunk) == 16, "chunk records are read and written as uint4");
 
 // Per body of a batch.
 struct BodyInfo {

@@ -116,7 +116,8 @@ cudaError_t launch_features(const hydro_body* bodies, uint32_t n, OceanDev o, fl
 cudaError_t launch_gate(const float* f, uint32_t n, const float* lo, const float* hi, const float* mean,
                         const float* P, float thresh, uint8_t* mask, cudaStream_t s);
 cudaError_t launch_route(const hydro_body* bodies, const uint8_t* mask, uint32_t n, uint32_t* counts,
-                         hydro_body* packed, int32_t* pos, uint32_t* n_packed, cudaStream_t s);
+                         hydro_body* packed, int32_t* pos, uint32_t* n_packed, hydro_wrench* exact,
+                         cudaStream_t s);
 cudaError_t launch_merge(const hydro_body* bodies, const float* z, int ld, const int32_t* pos,
                          const hydro_wrench* exact, uint32_t n, float* out, cudaStream_t s);
 cudaError_t launch_wrench_body(const hydro_body* bodies, const hydro_wrench* w, uint32_t n, float* out,

@@ -521,9 +521,18 @@ __device__ __forceinline__ void list_chunks(const KParams& P, uint32_t body, con
     uint32_t base = 0;
     if (lane == 0 && total) base = atomicAdd(P.n_listed, total);
     base = __shfl_sync(0xffffffffu, base, 0) + incl - n;
-    for (uint32_t c = 0; c < n; ++c) {
-        const ChunkDesc d = P.chunks[bi.first_chunk + c];
-        P.active[base + c] = ActiveChunk{body, d.first_tile, d.n_tiles, bi.first_chunk + c};
+    // four descriptors are requested before any entry is written (the
+    // stores would otherwise order each load behind the previous store)
+    const uint4* src = reinterpret_cast<const uint4*>(P.chunks + bi.first_chunk);
+    uint4* dst = reinterpret_cast<uint4*>(P.active + base);
+    for (uint32_t c0 = 0; c0 < n; c0 += 4) {
+        uint4 d[4];
+#pragma unroll
+        for (uint32_t j = 0; j < 4; ++j)
+            if (c0 + j < n) d[j] = __ldg(src + c0 + j);
+#pragma unroll
+        for (uint32_t j = 0; j < 4; ++j)   // ActiveChunk{body, first_tile, n_tiles, chunk}
+            if (c0 + j < n) dst[c0 + j] = make_uint4(body, d[j].y, d[j].z, bi.first_chunk + c0 + j);
     }
 }
 
@@ -1033,14 +1042,24 @@ __global__ void __launch_bounds__(kBodyThreads) finalize_kernel(const KParams P)
         if (live) {
             B = P.bparams[body];
             const BodyInfo bi = P.binfo[body];
-            for (int q = sub; q < kQ; q += kFinSub) {
-                double s = 0.0;
-                if (B.loop != LOOP_NONE) {
-                    const double* p = P.partials + (size_t)bi.first_chunk * kPartialStride + q;
-                    for (uint32_t c = 0; c < bi.n_chunks; ++c, p += kPartialStride) s += *p;
+            // quantities sub, sub + 4, ...: each summed in chunk order from
+            // +0, all of a chunk's loads in flight together
+            constexpr int kPer = (kQ + kFinSub - 1) / kFinSub;
+            double s[kPer];
+#pragma unroll
+            for (int i = 0; i < kPer; ++i) s[i] = 0.0;
+            if (B.loop != LOOP_NONE) {
+                const double* p = P.partials + (size_t)bi.first_chunk * kPartialStride + sub;
+#pragma unroll 2
+                for (uint32_t c = 0; c < bi.n_chunks; ++c, p += kPartialStride) {
+#pragma unroll
+                    for (int i = 0; i < kPer; ++i)
+                        if (sub + kFinSub * i < kQ) s[i] += p[kFinSub * i];
                 }
-                sums[slot][q] = s;
             }
+#pragma unroll
+            for (int i = 0; i < kPer; ++i)
+                if (sub + kFinSub * i < kQ) sums[slot][sub + kFinSub * i] = s[i];
         }
         __syncwarp();
         bool correct = false;

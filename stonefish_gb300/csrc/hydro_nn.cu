@@ -488,7 +488,7 @@ __global__ void route_count_kernel(const uint8_t* __restrict__ mask, uint32_t n,
 __global__ void route_pack_kernel(const hydro_body* __restrict__ bodies, const uint8_t* __restrict__ mask,
                                   uint32_t n, const uint32_t* __restrict__ counts, uint32_t n_blocks,
                                   hydro_body* __restrict__ packed, int32_t* __restrict__ pos,
-                                  uint32_t* __restrict__ n_packed)
+                                  uint32_t* __restrict__ n_packed, hydro_wrench* __restrict__ exact)
 {
     __shared__ uint32_t warp_base[kRouteBlock / 32];
     __shared__ uint32_t sums[2];
@@ -523,6 +523,12 @@ __global__ void route_pack_kernel(const hydro_body* __restrict__ bodies, const u
             const uint32_t j = base + __popc(bal & ((1u << lane) - 1u));
             packed[j] = bodies[i];
             pos[i] = (int32_t)j;
+            if (exact) {   // fresh in-out record for the exact step
+                static_assert(sizeof(hydro_wrench) % 8 == 0, "zeroed as 8-byte words");
+                uint64_t* w = reinterpret_cast<uint64_t*>(exact + j);
+#pragma unroll
+                for (uint32_t k = 0; k < sizeof(hydro_wrench) / 8; ++k) w[k] = 0ull;
+            }
         } else {
             pos[i] = -1;
         }
@@ -532,12 +538,13 @@ __global__ void route_pack_kernel(const hydro_body* __restrict__ bodies, const u
 }
 
 cudaError_t launch_route(const hydro_body* bodies, const uint8_t* mask, uint32_t n, uint32_t* counts,
-                         hydro_body* packed, int32_t* pos, uint32_t* n_packed, cudaStream_t s)
+                         hydro_body* packed, int32_t* pos, uint32_t* n_packed, hydro_wrench* exact,
+                         cudaStream_t s)
 {
     if (n == 0) return cudaSuccess;
     const uint32_t nb = (n + kRouteBlock - 1) / kRouteBlock;
     route_count_kernel<<<nb, kRouteBlock, 0, s>>>(mask, n, counts);
-    route_pack_kernel<<<nb, kRouteBlock, 0, s>>>(bodies, mask, n, counts, nb, packed, pos, n_packed);
+    route_pack_kernel<<<nb, kRouteBlock, 0, s>>>(bodies, mask, n, counts, nb, packed, pos, n_packed, exact);
     return cudaGetLastError();
 }
 

@@ -499,8 +499,8 @@ class GatedPredictor:
             s._mlp(b, self.n_pad)
             z, ldz, mlp_launches = b["z"], OUT_PAD, 5
         self._ck(self.lib.hydro_nn_route(ctx, bodies, _ptr(b["mask"]), n, _ptr(self.counts),
-                                         _ptr(self.packed), _ptr(self.pos), _ptr(self.n_packed), st))
-        self.exact_io.zero_()
+                                         _ptr(self.packed), _ptr(self.pos), _ptr(self.n_packed),
+                                         _ptr(self.exact_io), st))
         self.batch.compute_device_prefix(self.packed.data_ptr(), self.n_packed.data_ptr(), self.ocean,
                                          self.settings, self.exact_io.data_ptr(), st)
         self._ck(self.lib.hydro_nn_merge(ctx, bodies, _ptr(z), ldz, _ptr(self.pos),

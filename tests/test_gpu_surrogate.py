@@ -187,7 +187,7 @@ def test_gate_and_routing(hctx):
     packed = torch.zeros(n * abi.BODY_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
     pos = torch.zeros(n, dtype=torch.int32, device="cuda")
     npk = torch.zeros(1, dtype=torch.int32, device="cuda")
-    _ck(hctx, hctx.lib.hydro_nn_route(hctx.ctx, P(d_b), P(mask), n, P(counts), P(packed), P(pos), P(npk), None))
+    _ck(hctx, hctx.lib.hydro_nn_route(hctx.ctx, P(d_b), P(mask), n, P(counts), P(packed), P(pos), P(npk), None, None))
     torch.cuda.synchronize()
     rej = np.nonzero(~got)[0]
     k = int(npk.item())
@@ -198,6 +198,14 @@ def test_gate_and_routing(hctx):
     p = pos.cpu().numpy()
     assert np.array_equal(p[rej], np.arange(k))
     assert np.all(p[got] == -1)
+    # with an exact in-out array: its first k records zeroed, the rest untouched
+    stale = torch.full((n * abi.WRENCH_DTYPE.itemsize,), 0xAB, dtype=torch.uint8, device="cuda")
+    _ck(hctx, hctx.lib.hydro_nn_route(hctx.ctx, P(d_b), P(mask), n, P(counts), P(packed), P(pos), P(npk),
+                                      P(stale), None))
+    torch.cuda.synchronize()
+    st = stale.cpu().numpy().reshape(n, abi.WRENCH_DTYPE.itemsize)
+    assert int(npk.item()) == k and np.array_equal(pos.cpu().numpy(), p)
+    assert np.all(st[:k] == 0) and np.all(st[k:] == 0xAB)
 
     # merge: surrogate rows for accepted bodies, rotated exact wrench for the rest
     z = rng.normal(size=(n, 64)).astype(np.float32)
