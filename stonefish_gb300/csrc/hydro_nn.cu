@@ -8,6 +8,7 @@
 // mma.sync m16n8k16 tiles fed by ldmatrix from shared memory; 64x64 CTA
 // tiles, four warps of 32x32.  M, N multiples of 64 and K a multiple of 32
 // (the host pads), so no tile is partial.
+#include <cstddef>
 #include <cstdint>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -329,13 +330,42 @@ cudaError_t launch_to_bf16(const float* x, int rows, int n_in, int ld, const flo
 // projection of the body x axis, so the wave features do not depend on yaw.
 constexpr float kWaveReach = 1.0f;
 
-__global__ void features_kernel(const hydro_body* __restrict__ bodies, uint32_t n, OceanDev o, float* __restrict__ f)
+// The fields a state's features read, as 8-byte words of its hydro_body:
+// T_CG (words 0..11: basis, origin) and v, omega (words 33..38).
+constexpr int kFeatWords = 18;
+constexpr int kFeatStride = kFeatWords + 1;   // odd: 8-byte reads of a warp free of bank conflicts
+constexpr int kFeatBlock = 128;
+static_assert(offsetof(hydro_body, T_CG) == 0 && offsetof(hydro_body, v) == 33 * 8 &&
+                  offsetof(hydro_body, omega) == 36 * 8 && sizeof(hydro_body) % 8 == 0,
+              "feature words of hydro_body");
+
+__global__ void __launch_bounds__(kFeatBlock) features_kernel(const hydro_body* __restrict__ bodies, uint32_t n,
+                                                              OceanDev o, float* __restrict__ f)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    // Each warp first copies the feature words of its 32 records into shared
+    // memory, consecutive lanes reading consecutive words, so that a load
+    // instruction touches two records instead of 32 (the records may be
+    // page-locked host memory read in place).
+    __shared__ double stage[kFeatBlock / 32][32 * kFeatStride];
+    const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
+    const uint32_t first = blockIdx.x * kFeatBlock + 32u * wib;
+    const double* words = reinterpret_cast<const double*>(bodies);
+    constexpr uint32_t kRecWords = sizeof(hydro_body) / 8;
+#pragma unroll
+    for (uint32_t j = 0; j < (uint32_t)kFeatWords; ++j) {
+        const uint32_t t = lane + 32u * j, r = t / kFeatWords, p = t % kFeatWords;
+        const uint32_t w = p < 12u ? p : 33u + (p - 12u);
+        if (first + r < n) stage[wib][r * kFeatStride + p] = words[(size_t)(first + r) * kRecWords + w];
+    }
+    __syncwarp();
+    const uint32_t i = first + lane;
     if (i >= n) return;
-    const hydro_body& b = bodies[i];
-    const double* R = b.T_CG.basis;
-    const double x = b.T_CG.origin[0], y = b.T_CG.origin[1], z = b.T_CG.origin[2];
+    const double* sw = &stage[wib][lane * kFeatStride];
+    double R[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) R[k] = sw[k];
+    const double x = sw[9], y = sw[10], z = sw[11];
+    const double bv[3] = {sw[12], sw[13], sw[14]}, bw[3] = {sw[15], sw[16], sw[17]};
     // heading (unit horizontal projection of the body x axis), FP32
     float ux = (float)R[0], uy = (float)R[3];   // (same values as Rf[0], Rf[3] below)
     const float hn = sqrtf(ux * ux + uy * uy);
@@ -374,8 +404,8 @@ __global__ void features_kernel(const hydro_body* __restrict__ bodies, uint32_t 
     o16[0] = (float)z + h;                          // depth below the local surface (NED: surface at -h)
     o16[1] = atan2f(Rf[7], Rf[8]);                  // roll
     o16[2] = asinf(fmaxf(-1.f, fminf(1.f, -Rf[6])));  // pitch
-    tb(b.v, o16 + 3);
-    tb(b.omega, o16 + 6);
+    tb(bv, o16 + 3);
+    tb(bw, o16 + 6);
     double u[3] = {o.U[0], o.U[1], o.U[2]};
     tb(u, o16 + 9);
     o16[12] = h;
@@ -387,7 +417,7 @@ __global__ void features_kernel(const hydro_body* __restrict__ bodies, uint32_t 
 cudaError_t launch_features(const hydro_body* bodies, uint32_t n, OceanDev o, float* f, cudaStream_t s)
 {
     if (n == 0) return cudaSuccess;
-    features_kernel<<<(n + 127) / 128, 128, 0, s>>>(bodies, n, o, f);
+    features_kernel<<<(n + kFeatBlock - 1) / kFeatBlock, kFeatBlock, 0, s>>>(bodies, n, o, f);
     return cudaGetLastError();
 }
 
