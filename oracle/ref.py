@@ -1,0 +1,151 @@
+"""ctypes front end of oracle/_ref/libstonefish_ref.so -- test infrastructure.
+
+The library is the reference's own hydrodynamics code (SolidEntity.cpp,
+Ocean.cpp, OpenGLRealOcean.cpp, Uniform/Jet/Pipe.cpp, OpenGLDataStructs)
+compiled on the CPU by oracle/build_ref.py.  It exists only where the
+reference's source tree is present; ``Reference.available()`` says whether
+it is.  Argument conventions follow oracle.Oracle so tests can run both on
+the same inputs.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from stonefish_gb300 import abi
+
+from .build_ref import LIB, ROOT_NOTE, build_ref
+from .oracle import Oracle, OracleMesh
+
+
+def source_root() -> str | None:
+    """The reference tree the library was built from (None if not built)."""
+    if not os.path.exists(ROOT_NOTE):
+        return None
+    with open(ROOT_NOTE) as f:
+        root = f.read().strip()
+    return root if os.path.isdir(root) else None
+
+
+class Reference:
+    """The reference's functions, loaded from oracle/_ref."""
+
+    @staticmethod
+    def available() -> bool:
+        try:
+            return build_ref() is not None and os.path.exists(LIB)
+        except RuntimeError:
+            return False
+
+    def __init__(self):
+        path = build_ref()
+        if path is None:
+            raise RuntimeError("the reference's source tree is not present: oracle/_ref cannot be built")
+        self.lib = L = C.CDLL(path)
+        vp, i32, u32, d = C.c_void_p, C.c_int32, C.c_uint32, C.POINTER(C.c_double)
+        P = C.POINTER
+        L.ref_depth.restype = C.c_float
+        L.ref_depth.argtypes = [P(abi.Ocean), vp, C.c_float, C.c_float, C.c_float]
+        L.ref_fluid_position.restype = i32
+        L.ref_fluid_position.argtypes = [P(abi.Ocean), vp, d, d]
+        L.ref_body_forces.restype = i32
+        L.ref_body_forces.argtypes = [vp, vp, P(abi.Ocean), vp, P(abi.Settings), vp]
+        L.ref_surface_forces.restype = i32
+        L.ref_surface_forces.argtypes = [P(abi.Settings), vp, P(abi.Ocean), vp, P(abi.Transform),
+                                         P(abi.Transform), d, d, d, d, d, d, d, d, d, d]
+        L.ref_submerged_forces.restype = i32
+        L.ref_submerged_forces.argtypes = [vp, P(abi.Ocean), P(abi.Transform), P(abi.Transform), d, d,
+                                           d, d, d, d]
+        L.ref_correct_forces.restype = None
+        L.ref_correct_forces.argtypes = [P(abi.Ocean), d, d, d, d, d, d, d]
+        L.ref_aero_forces.restype = None
+        L.ref_aero_forces.argtypes = [vp, P(abi.Atmosphere), P(abi.Transform), P(abi.Transform), d, d, d, d]
+        L.ref_aero_correct.restype = None
+        L.ref_aero_correct.argtypes = [P(abi.AeroParams), d, d]
+        L.ref_batch.restype = C.c_double
+        L.ref_batch.argtypes = [i32, vp, u32, vp, u32, P(abi.Ocean), vp, P(abi.Settings), vp]
+
+    _p = staticmethod(Oracle._p)
+    _vec = staticmethod(Oracle._vec)
+    make_mesh = staticmethod(Oracle.make_mesh)
+    make_waves = staticmethod(Oracle.make_waves)
+
+    def depth(self, ocean, waves, x, y, z) -> float:
+        w = self.make_waves(waves)
+        return float(self.lib.ref_depth(C.byref(ocean), self._p(w), x, y, z))
+
+    def fluid_position(self, ocean, aabb_min, aabb_max, waves=None) -> int:
+        w = self.make_waves(waves)
+        a, pa = self._vec(aabb_min)
+        b, pb = self._vec(aabb_max)
+        return int(self.lib.ref_fluid_position(C.byref(ocean), self._p(w), pa, pb))
+
+    def body_forces(self, body, mesh, ocean, settings, io, waves=None):
+        m = None if mesh is None else self.make_mesh(*mesh)
+        w = self.make_waves(waves)
+        rc = self.lib.ref_body_forces(body.ctypes.data, self._p(m), C.byref(ocean), self._p(w),
+                                      C.byref(settings), io.ctypes.data)
+        if rc != 0:
+            raise ValueError("wave data not expressible as the reference's two-layer texture")
+        return io
+
+    def batch(self, threads, bodies, meshes, ocean, settings, io, waves=None) -> float:
+        oms = (OracleMesh * max(1, len(meshes)))()
+        keep = []
+        for i, (xyz, faces) in enumerate(meshes):
+            m = self.make_mesh(xyz, faces)
+            keep.append(m)
+            oms[i] = m
+        w = self.make_waves(waves)
+        t = float(self.lib.ref_batch(threads, bodies.ctypes.data, len(bodies), C.cast(oms, C.c_void_p),
+                                     len(meshes), C.byref(ocean), self._p(w), C.byref(settings),
+                                     io.ctypes.data))
+        if t < 0:
+            raise ValueError("wave data not expressible as the reference's two-layer texture")
+        return t
+
+    def surface_forces(self, settings, mesh, ocean, T_CG, T_C, v, omega, io, waves=None):
+        m = None if mesh is None else self.make_mesh(*mesh)
+        w = self.make_waves(waves)
+        vv, pv = self._vec(v)
+        ww, pw = self._vec(omega)
+        ptrs = [io[k].ctypes.data_as(C.POINTER(C.c_double)) for k in
+                ("Fb", "Tb", "Fdq", "Tdq", "Fdf", "Tdf", "Swet", "Vsub")]
+        self.lib.ref_surface_forces(C.byref(settings), self._p(m), C.byref(ocean), self._p(w), C.byref(T_CG),
+                                    C.byref(T_C), pv, pw, *ptrs)
+        return io
+
+    def submerged_forces(self, mesh, ocean, T_CG, T_C, v, omega, io):
+        m = None if mesh is None else self.make_mesh(*mesh)
+        vv, pv = self._vec(v)
+        ww, pw = self._vec(omega)
+        ptrs = [io[k].ctypes.data_as(C.POINTER(C.c_double)) for k in ("Fdq", "Tdq", "Fdf", "Tdf")]
+        self.lib.ref_submerged_forces(self._p(m), C.byref(ocean), C.byref(T_CG), C.byref(T_C), pv, pw, *ptrs)
+        return io
+
+    def correct_forces(self, ocean, io, Cd, Cf, R_O):
+        cd, pcd = self._vec(Cd)
+        cf, pcf = self._vec(Cf)
+        ro, pro = self._vec(R_O)
+        ptrs = [io[k].ctypes.data_as(C.POINTER(C.c_double)) for k in ("Fdq", "Tdq", "Fdf", "Tdf")]
+        self.lib.ref_correct_forces(C.byref(ocean), *ptrs, pcd, pcf, pro)
+        return io
+
+    def aero_forces(self, mesh, atm, T_CG, T_C, v, omega):
+        m = None if mesh is None else self.make_mesh(*mesh)
+        vv, pv = self._vec(v)
+        ww, pw = self._vec(omega)
+        F = np.zeros(3)
+        T = np.zeros(3)
+        self.lib.ref_aero_forces(self._p(m), C.byref(atm), C.byref(T_CG), C.byref(T_C), pv, pw,
+                                 F.ctypes.data_as(C.POINTER(C.c_double)), T.ctypes.data_as(C.POINTER(C.c_double)))
+        return F, T
+
+    def aero_correct(self, params, Fda, Tda):
+        F = np.array(Fda, dtype=np.float64)
+        T = np.array(Tda, dtype=np.float64)
+        self.lib.ref_aero_correct(C.byref(params), F.ctypes.data_as(C.POINTER(C.c_double)),
+                                  T.ctypes.data_as(C.POINTER(C.c_double)))
+        return F, T

@@ -1,10 +1,15 @@
-"""Generates the golden fixtures in this directory from the CPU oracle.
+"""Generates the golden fixtures in this directory.
 
-The reference's own tests hold no active known-answer vectors for the
-hydrodynamics path, so these fixtures pin the oracle (its FP32 reference
-arithmetic REF32, the all-FP64 REF64 and the GPU-mirror MIRROR32 variants)
-on small seeded cases: inputs (meshes, body tables, ocean, wave grid) and
-outputs are stored together.  Run from the repository root:
+Each fixture holds a small seeded case -- inputs (meshes, body tables, ocean,
+wave grid) and outputs together.  The outputs are those of the reference's
+own hydrodynamics code (``reference``: SolidEntity.cpp and the functions it
+calls, compiled from the reference's source tree by oracle/build_ref.py)
+and of the oracle's variants (REF32, the reference's arithmetic restated;
+REF64, all FP64; MIRROR32, the GPU kernel's arithmetic).
+``ref_face_patterns.npz`` holds single triangles, one per case of the
+waterline clip plus random ones on a flat and a wavy surface, with the
+reference's per-face outputs.  Needs the reference's source tree; run from
+the repository root:
 
     python tests/golden/make_golden.py
 """
@@ -17,7 +22,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
 from oracle import MIRROR32, REF32, REF64, Oracle  # noqa: E402
-from stonefish_gb300 import abi, meshes, scenarios  # noqa: E402
+from oracle.ref import Reference  # noqa: E402
+from stonefish_gb300 import abi, scenarios  # noqa: E402
 
 
 def ocean_array(o: abi.Ocean) -> np.ndarray:
@@ -34,6 +40,11 @@ def save(name, sc, settings=None):
         io["Vsub"] = 0.25
         o.batch(var, 1, sc["bodies"], sc["meshes"], sc["ocean"], st, io, waves=sc.get("waves"))
         out[tag] = io
+    io = scenarios.new_wrenches(len(sc["bodies"]))
+    io["Fb"] = 0.5
+    io["Vsub"] = 0.25
+    Reference().batch(1, sc["bodies"], sc["meshes"], sc["ocean"], st, io, waves=sc.get("waves"))
+    out["reference"] = io
     arrays = {"bodies": sc["bodies"], "ocean": ocean_array(sc["ocean"]),
               "settings": np.array([st.damping_forces, st.realistic_buoyancy], np.int32)}
     for i, (x, f) in enumerate(sc["meshes"]):
@@ -71,6 +82,59 @@ def main():
     p.dir[:] = (0.0, 1.0, 0.0)
     p.radius, p.radius2, p.length, p.speed, p.gamma = 0.5, 1.0, 5.0, 1.5, 0.7
     save("currents_jet_pipe", sc)
+    save_face_patterns()
+
+
+def save_face_patterns():
+    """Single-face bodies through the reference's ComputeHydrodynamicForcesSurface:
+    the 27 depth-sign patterns of one triangle on a flat surface, then random
+    triangles (every 7th a sliver) on a flat surface and on a wave grid."""
+    from tests.helpers import body_transform, io_dict
+    ref = Reference()
+    rng = np.random.default_rng(107)
+    waves = scenarios.wave_grid(n=64, n_waves=8, seed=108)
+    base = np.array([[0.0, 0.0, 0.0], [1.0, 0.1, 0.0], [0.2, 1.0, 0.0]], dtype=np.float32)
+    levels = (-0.3, 0.0, 0.25)
+    xyz, bodies, oceans, wavy = [], [], [], []
+    for za in levels:
+        for zb in levels:
+            for zc in levels:
+                p = base.copy()
+                p[:, 2] = (za, zb, zc)
+                xyz.append(p)
+                bodies.append(scenarios.fill_bodies(1, np.eye(3)[None], np.zeros((1, 3)), np.array([[0.3, -0.2, 0.1]]),
+                                                    np.array([[0.1, 0.2, -0.3]]), np.ones((1, 3)), 1.0, 1.0, (1, 1, 1),
+                                                    (.1, .1, .1), 0))
+                oceans.append((0.2, 0.1, -0.3))
+                wavy.append(0)
+    for t in range(200):
+        p = rng.uniform(-1.0, 1.0, (3, 3)).astype(np.float32)
+        p[:, 2] = rng.uniform(-0.6, 0.6, 3).astype(np.float32)
+        if t % 7 == 0:
+            p[2] = p[0] + np.float32(1e-4) * (p[1] - p[0])
+        xyz.append(p)
+        R = scenarios.quat_to_matrix(scenarios.random_quaternions(rng, 1))
+        pos = np.array([[rng.uniform(0, 6.4), rng.uniform(0, 6.4), rng.uniform(-0.3, 0.3)]])
+        bodies.append(scenarios.fill_bodies(1, R, pos, rng.uniform(-1, 1, (1, 3)), rng.uniform(-0.5, 0.5, (1, 3)),
+                                            np.ones((1, 3)), 1.0, 1.0, (1, 1, 1), (.1, .1, .1), 0))
+        oceans.append(tuple(rng.uniform(-0.5, 0.5, 3)))
+        wavy.append(t % 2)
+    faces = np.array([[0, 1, 2]], dtype=np.uint32)
+    keys = ("Fb", "Tb", "Fdq", "Tdq", "Fdf", "Tdf", "Swet", "Vsub")
+    out = np.zeros((len(xyz), 20))
+    for i, (p, b) in enumerate(zip(xyz, bodies)):
+        oc = scenarios.flat_ocean(oceans[i])
+        oc.waves = wavy[i]
+        io = io_dict()
+        T = body_transform(b)
+        ref.surface_forces(scenarios.settings(), (p, faces), oc, T, T, b["v"][0], b["omega"][0], io,
+                           waves=waves if wavy[i] else None)
+        out[i] = np.concatenate([io[k] for k in keys])
+    np.savez_compressed(os.path.join(HERE, "ref_face_patterns.npz"), xyz=np.stack(xyz),
+                        bodies=np.concatenate(bodies), current=np.array(oceans), waves=np.array(wavy, np.int32),
+                        wave_data=waves["data"], wave_layers=np.array(waves["layers"], dtype=np.float64),
+                        reference=out)
+    print("ref_face_patterns", len(xyz))
 
 
 if __name__ == "__main__":

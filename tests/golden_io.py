@@ -10,7 +10,8 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 def names():
-    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
+                  if not os.path.basename(p).startswith("ref_"))
 
 
 def load(name):
@@ -25,7 +26,7 @@ def load(name):
     waves = None
     if "wave_data" in z:
         waves = {"data": z["wave_data"], "layers": [(int(c), float(g)) for c, g in z["wave_layers"]]}
-    out = {k: z[k] for k in ("ref32", "ref64", "mirror32")}
+    out = {k: z[k] for k in ("ref32", "ref64", "mirror32", "reference")}
     return {"meshes": meshes, "bodies": z["bodies"], "ocean": ocean, "settings": st, "waves": waves,
             "out": out}
 
@@ -35,3 +36,12 @@ def initial_io(n):
     io["Fb"] = 0.5
     io["Vsub"] = 0.25
     return io
+
+
+def load_face_patterns():
+    """Single-face cases with the reference's outputs: columns Fb Tb Fdq Tdq
+    Fdf Tdf (3 each), Swet, Vsub."""
+    z = np.load(os.path.join(GOLDEN, "ref_face_patterns.npz"))
+    waves = {"data": z["wave_data"], "layers": [(int(c), float(g)) for c, g in z["wave_layers"]]}
+    return {"xyz": z["xyz"], "bodies": z["bodies"], "current": z["current"], "waves_on": z["waves"],
+            "waves": waves, "reference": z["reference"]}

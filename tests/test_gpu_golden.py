@@ -1,9 +1,12 @@
-"""The CUDA path against the committed golden fixtures (through the C ABI)."""
+"""The CUDA path against the committed golden fixtures (through the C ABI).
+
+The fixtures hold the reference's own outputs (its SolidEntity code compiled
+from source on the CPU) next to the oracle's."""
 import numpy as np
 import pytest
 
-from stonefish_gb300 import abi
-from tests.golden_io import initial_io, load, names
+from stonefish_gb300 import abi, scenarios
+from tests.golden_io import initial_io, load, load_face_patterns, names
 from tests.helpers import scaled_errors
 
 pytestmark = pytest.mark.gpu
@@ -32,3 +35,44 @@ def test_gpu_matches_golden(hctx, name):
     e_ref = scaled_errors(g["out"]["ref32"], g["out"]["ref64"], L)
     for k in e_gpu:
         assert np.max(e_gpu[k][act], initial=0.0) <= np.max(e_ref[k][act], initial=0.0) + 2e-6, (name, k)
+    # against the reference's own outputs: same fluid positions, and per body
+    # no further from them than the reference's FP32 sums are from FP64
+    ref = g["out"]["reference"]
+    assert np.array_equal(io["position"], ref["position"])
+    e_vs_ref = scaled_errors(io, ref, L)
+    e_ref64 = scaled_errors(ref, g["out"]["ref64"], L)
+    for k in e_vs_ref:
+        assert np.all(e_vs_ref[k][act] <= e_ref64[k][act] + 2e-6), (name, k)
+
+
+@pytest.mark.parametrize("packed", [False, True])
+def test_gpu_face_terms_equal_reference_single_faces(hctx, packed):
+    """Single triangles -- the 27 depth-sign patterns of the waterline clip
+    and 200 random ones on flat and wavy surfaces -- through the GPU's face
+    code against the reference's ComputeHydrodynamicForcesSurface on the
+    same face: with one face the reference's FP32 sums are the face's terms,
+    so drag, friction and wetted area must match bit for bit, and so must
+    the buoyancy and volume the reference derives from them."""
+    fp = load_face_patterns()
+    hctx.set_wave_grid(fp["waves"])
+    faces = np.array([[0, 1, 2]], dtype=np.uint32)
+    st = scenarios.settings()
+    for i in range(len(fp["xyz"])):
+        oc = scenarios.flat_ocean(tuple(fp["current"][i]))
+        oc.waves = int(fp["waves_on"][i])
+        body = fp["bodies"][i:i + 1].copy()
+        body["mesh"] = hctx.upload_mesh(fp["xyz"][i], faces)
+        t = hctx.face_terms(body, oc, st, packed=packed)[0]
+        r = fp["reference"][i]
+        for name, lo in (("Fdq", 6), ("Tdq", 9), ("Fdf", 12), ("Tdf", 15)):
+            assert np.array_equal(t[lo:lo + 3].astype(np.float64), r[lo:lo + 3]), (i, name, t[lo:lo + 3], r[lo:lo + 3])
+        assert np.float64(t[18]) == r[18], (i, "Swet")
+        v6 = t[19]
+        if v6 > np.float32(1e-9):      # SolidEntity.cpp:1689: buoyancy only when Vsub > 1e-9f
+            assert np.float64(np.float32(v6 / np.float32(6.0))) == r[19], (i, "Vsub")
+            if oc.waves:
+                k = np.float32(oc.density * oc.gravity)
+                assert np.array_equal((t[0:3] * k).astype(np.float64), r[0:3]), (i, "Fb")
+                assert np.array_equal((t[3:6] * k).astype(np.float64), r[3:6]), (i, "Tb")
+        else:
+            assert r[19] == 0.0 and np.all(r[0:6] == 0.0), (i, "stale outputs")
