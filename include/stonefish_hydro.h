@@ -496,8 +496,40 @@ typedef struct hydro_mesh_properties {
 hydro_status hydro_mesh_compute_properties(hydro_ctx* ctx, hydro_mesh_id mesh, double thickness, double density,
                                            hydro_mesh_properties* out);
 
+/* --------------------------------------------------- coefficient setup */
+/* Result of SolidEntity::ComputeFluidDynamicsApprox (SolidEntity.cpp:698-1040):
+ * the proxy shape fitted to the physics mesh and what it gives the body. */
+typedef struct hydro_fluid_approx_result {
+    int32_t approx_type;         /* fdApproxType: SPHERE, CYLINDER or ELLIPSOID (AUTO fits an ellipsoid) */
+    int32_t n_params;            /* fdApproxParams.size(): 1, 2 or 3 */
+    double params[3];            /* sphere: radius; cylinder: radius, length; ellipsoid: semi-axes */
+    hydro_transform T_CG2H;      /* proxy frame in the CG frame (hydro_aero_params.R_CG2H) */
+    double added_mass[3];        /* aMass */
+    double added_inertia[3];     /* aI */
+    double Cd[3];                /* fdCd, origin frame (hydro_body.Cd) */
+    double Cf[3];                /* fdCf = 0.1 Cd (hydro_body.Cf) */
+} hydro_fluid_approx_result;
+
+/* The coefficient setup the reference runs once per body when it is built
+ * (ComputeSphericalApprox :720-758, ComputeCylindricalApprox :760-847,
+ * ComputeEllipsoidalApprox :849-1025).  vertex_data / vertex_stride /
+ * n_vertices are the physics mesh's vertex array as getMeshVertices reads it
+ * (Mesh::getVertexDataPointer(), getVertexSize(), getNumOfVertices(); the
+ * position is the first three floats of each vertex); T_CG2C and T_CG2O are
+ * the body's CG-to-mesh and CG-to-origin transforms, P_CB its centre of
+ * buoyancy in the CG frame, density the ocean's liquid density (the
+ * reference takes 1000 when the simulation has no ocean).  Host only, FP64,
+ * the reference's bits.  HYDRO_ERR_INVALID_ARG for fewer than two vertices
+ * (where the reference leaves the body's coefficients unchanged). */
+hydro_status hydro_fluid_approx(const void* vertex_data, size_t vertex_stride, uint32_t n_vertices,
+                                int32_t approx_type, const hydro_transform* T_CG2C,
+                                const hydro_transform* T_CG2O, const double P_CB[3], double density,
+                                hydro_fluid_approx_result* out);
+
 /* OBJ text to the physics mesh the reference builds from it: positions
- * times scale, every face of every shape, polygons triangulated as
+ * times scale (LoadOBJ scales only files that have normals; a file without
+ * "vn" lines keeps its size, GeometryFileUtil.cpp:253-254), every face of
+ * every shape, polygons triangulated as
  * rapidobj::Triangulate does (quads along the shorter diagonal, larger
  * polygons by ear slicing; LoadOBJ, GeometryFileUtil.cpp:52-230, physics
  * part), then, when

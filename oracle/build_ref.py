@@ -3,9 +3,9 @@ functions, compiled on the CPU from the reference's source tree.
 
 TEST INFRASTRUCTURE ONLY.  The reference as a whole does not build without
 SDL2, GL, FreeType and glm, but the functions of its hydrodynamics path use
-only glm vector arithmetic, Bullet's LinearMath (vendored in the reference,
-3rdparty/LinearMath) and a few members of Ocean, SolidEntity and
-OpenGLRealOcean.  This recipe reads those functions and type definitions out
+only glm vector arithmetic, Bullet's LinearMath and rapidobj (both vendored
+in the reference, 3rdparty/) and a few members of Ocean, SolidEntity,
+OpenGLRealOcean and OpenGLContent.  This recipe reads those functions and type definitions out
 of the reference's files where they lie, finds each by its signature and
 brace matching, and pipes them with ``#line`` markers into g++ between the
 two halves of ``oracle/ref_harness.hpp`` (stand-ins for the reference's
@@ -50,6 +50,11 @@ TYPES = [
     ("Library/include/graphics/OpenGLDataStructs.h", "struct Mesh"),
     ("Library/include/graphics/OpenGLDataStructs.h", "struct PlainMesh"),
     ("Library/include/graphics/OpenGLDataStructs.h", "struct TexturableMesh"),
+    ("Library/include/utils/GeometryFileUtil.h", "inline void hashCombine("),
+    ("Library/include/utils/GeometryFileUtil.h", "struct IndexedVertex"),
+    ("Library/include/utils/GeometryFileUtil.h", "struct IndexedVertexHash"),
+    ("Library/include/utils/GeometryFileUtil.h", "struct IndexedTexturableVertex"),
+    ("Library/include/utils/GeometryFileUtil.h", "struct IndexedTexturableVertexHash"),
 ]
 FUNCTIONS = [
     ("Library/src/graphics/OpenGLDataStructs.cpp", "glm::mat4 glMatrixFromTransform("),
@@ -75,6 +80,20 @@ FUNCTIONS = [
     ("Library/src/entities/SolidEntity.cpp", "void SolidEntity::ComputeAerodynamicForces(Atmosphere*"),
     ("Library/src/entities/SolidEntity.cpp", "void SolidEntity::ComputeAerodynamicForces(const Mesh*"),
     ("Library/src/entities/SolidEntity.cpp", "void SolidEntity::CorrectAerodynamicForces("),
+    ("Library/src/entities/SolidEntity.cpp", "void SolidEntity::SetHydrodynamicCoefficients("),
+    ("Library/src/entities/SolidEntity.cpp", "std::vector<Vector3>* SolidEntity::getMeshVertices()"),
+    ("Library/src/entities/SolidEntity.cpp", "void SolidEntity::ComputeFluidDynamicsApprox("),
+    ("Library/src/entities/SolidEntity.cpp", "void SolidEntity::ComputeSphericalApprox()"),
+    ("Library/src/entities/SolidEntity.cpp", "void SolidEntity::ComputeCylindricalApprox()"),
+    ("Library/src/entities/SolidEntity.cpp", "void SolidEntity::ComputeEllipsoidalApprox()"),
+    ("Library/src/entities/SolidEntity.cpp", "Scalar SolidEntity::LambKFactor("),
+    ("Library/src/graphics/OpenGLContent.cpp", "GLuint vertex4Edge(std::map"),
+    ("Library/src/graphics/OpenGLContent.cpp", "GLfloat OpenGLContent::ComputeAverageFaceArea("),
+    ("Library/src/graphics/OpenGLContent.cpp", "void OpenGLContent::Refine("),
+    ("Library/src/utils/GeometryFileUtil.cpp", "Mesh* LoadOBJ("),
+    ("Library/src/utils/GeometryFileUtil.cpp", "void ComputePhysicalProperties(const Mesh* mesh, Scalar thickness, Scalar density, Scalar& mass"),
+    ("Library/src/utils/GeometryFileUtil.cpp", "Vector3 FindInertialAxis("),
+    ("Library/src/utils/GeometryFileUtil.cpp", "bool IsDiagonal("),
 ]
 
 CXXFLAGS = ["-O3", "-DNDEBUG", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-pthread",

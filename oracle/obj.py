@@ -1,12 +1,31 @@
 """CPU restatement of the physics-mesh ingest (test infrastructure only):
-the physics part of LoadOBJ (Library/src/utils/GeometryFileUtil.cpp:52-230:
-positions times scale, all shapes fused), the triangulation LoadOBJ asks of
+the physics part of LoadOBJ (Library/src/utils/GeometryFileUtil.cpp:52-283:
+positions times scale -- only when the file has normals, :253-254 copies the
+unscaled positions back otherwise -- all shapes fused), the triangulation LoadOBJ asks of
 rapidobj (rapidobj::Triangulate, 3rdparty/rapidobj.hpp:7338-7503: quads cut
 along the shorter diagonal, larger polygons ear-sliced by mapbox earcut
 v2.2.4, rapidobj.hpp:358-1160, in the axis plane of largest projected area,
 each triangle's first two corners swapped), and OpenGLContent::Refine
 (Library/src/graphics/OpenGLContent.cpp:2833-2895) with the FP32 face areas
-of PlainMesh::ComputeFaceArea (Library/include/graphics/OpenGLDataStructs.h:219-224)."""
+of PlainMesh::ComputeFaceArea (Library/include/graphics/OpenGLDataStructs.h:219-224).
+
+The ear slicer follows mapbox earcut.hpp v2.2.4 step for step; its licence:
+
+    ISC License
+
+    Copyright (c) 2015, Mapbox
+
+    Permission to use, copy, modify, and/or distribute this software for any
+    purpose with or without fee is hereby granted, provided that the above
+    copyright notice and this permission notice appear in all copies.
+
+    THE SOFTWARE IS PROVIDED "AS IS" AND THE AUTHOR DISCLAIMS ALL WARRANTIES
+    WITH REGARD TO THIS SOFTWARE INCLUDING ALL IMPLIED WARRANTIES OF
+    MERCHANTABILITY AND FITNESS. IN NO EVENT SHALL THE AUTHOR BE LIABLE FOR ANY
+    SPECIAL, DIRECT, INDIRECT, OR CONSEQUENTIAL DAMAGES OR ANY DAMAGES
+    WHATSOEVER RESULTING FROM LOSS OF USE, DATA OR PROFITS, WHETHER IN AN ACTION
+    OF CONTRACT, NEGLIGENCE OR OTHER TORTIOUS ACTION, ARISING OUT OF OR IN
+    CONNECTION WITH THE USE OR PERFORMANCE OF THIS SOFTWARE."""
 from __future__ import annotations
 
 import numpy as np
@@ -247,10 +266,13 @@ def triangulate(raw: np.ndarray, poly: list[int]) -> list[tuple[int, int, int]]:
 
 def parse_obj(text: str, scale: float = 1.0):
     raw, polys = [], []
+    has_normals = False
     for line in text.splitlines():
         tok = line.split()
         if not tok:
             continue
+        if tok[0] == "vn":
+            has_normals = True
         if tok[0] == "v":
             raw.append([f32(float(t)) for t in tok[1:4]])
         elif tok[0] == "f":
@@ -261,6 +283,8 @@ def parse_obj(text: str, scale: float = 1.0):
             polys.append(idx)
     raw = np.array(raw, dtype=np.float32).reshape(-1, 3)
     faces = [f for p in polys for f in triangulate(raw, p)]
+    if not has_normals:
+        scale = 1.0
     return (f32(scale) * raw).astype(np.float32), np.array(faces, dtype=np.uint32).reshape(-1, 3)
 
 

@@ -66,6 +66,14 @@ class Reference:
         L.ref_aero_correct.argtypes = [P(abi.AeroParams), d, d]
         L.ref_batch.restype = C.c_double
         L.ref_batch.argtypes = [i32, vp, u32, vp, u32, P(abi.Ocean), vp, P(abi.Settings), vp]
+        L.ref_load_obj.restype = i32
+        L.ref_load_obj.argtypes = [C.c_char_p, C.c_float, C.c_float, vp, u32, vp, u32, P(u32), P(u32), P(i32)]
+        L.ref_mesh_properties.restype = None
+        L.ref_mesh_properties.argtypes = [vp, C.c_double, C.c_double, vp]
+        L.ref_last_error.restype = C.c_char_p
+        L.ref_last_error.argtypes = []
+        L.ref_fluid_approx.restype = None
+        L.ref_fluid_approx.argtypes = [vp, i32, P(abi.Transform), P(abi.Transform), d, C.c_double, vp]
 
     _p = staticmethod(Oracle._p)
     _vec = staticmethod(Oracle._vec)
@@ -149,3 +157,36 @@ class Reference:
         self.lib.ref_aero_correct(C.byref(params), F.ctypes.data_as(C.POINTER(C.c_double)),
                                   T.ctypes.data_as(C.POINTER(C.c_double)))
         return F, T
+
+    def load_obj(self, path: str, scale: float = 1.0, refine: float = 0.0):
+        """LoadOBJ (+ Refine when refine > 0): (xyz float32 [V,3], faces uint32 [F,3], texturable)."""
+        nv, nf, tex = C.c_uint32(0), C.c_uint32(0), C.c_int32(0)
+        b = path.encode()
+        if self.lib.ref_load_obj(b, scale, refine, None, 0, None, 0, C.byref(nv), C.byref(nf), C.byref(tex)):
+            raise OSError(f"the reference's LoadOBJ failed on {path}: {self.lib.ref_last_error().decode()}")
+        xyz = np.zeros((nv.value, 3), dtype=np.float32)
+        faces = np.zeros((nf.value, 3), dtype=np.uint32)
+        self.lib.ref_load_obj(b, scale, refine, xyz.ctypes.data, nv.value, faces.ctypes.data, nf.value,
+                              C.byref(nv), C.byref(nf), C.byref(tex))
+        return xyz, faces, bool(tex.value)
+
+    def mesh_properties(self, mesh, thickness: float, density: float) -> dict:
+        """ComputePhysicalProperties: mass, volume, surface, CG, Ipri, Irot."""
+        m = self.make_mesh(*mesh)
+        out = np.zeros(18)
+        self.lib.ref_mesh_properties(self._p(m), thickness, density, out.ctypes.data)
+        return {"mass": out[0], "volume": out[1], "surface": out[2], "CG": out[3:6].copy(),
+                "Ipri": out[6:9].copy(), "Irot": out[9:18].reshape(3, 3).copy()}
+
+    def fluid_approx(self, mesh, approx: int, T_CG2C, T_CG2O, P_CB, density: float = -1.0) -> dict:
+        """ComputeFluidDynamicsApprox for a body with this physics mesh;
+        density < 0 = no ocean (the reference then takes 1000)."""
+        m = self.make_mesh(*mesh)
+        pc, ppc = self._vec(P_CB)
+        out = np.zeros(31)
+        self.lib.ref_fluid_approx(self._p(m), approx, C.byref(T_CG2C), C.byref(T_CG2O), ppc, density,
+                                  out.ctypes.data)
+        n = int(out[1])
+        return {"type": int(out[0]), "params": out[2:2 + n].copy(), "R_CG2H": out[5:14].reshape(3, 3).copy(),
+                "origin_CG2H": out[14:17].copy(), "added_mass": out[17:20].copy(),
+                "added_inertia": out[20:23].copy(), "Cd": out[23:26].copy(), "Cf": out[26:29].copy()}

@@ -3,11 +3,13 @@
  * reference's own hydrodynamics functions compile on the CPU.
  *
  * TEST INFRASTRUCTURE ONLY.  oracle/build_ref.py reads the reference's
- * functions (SolidEntity.cpp:205-208, :1239-1956; Ocean.cpp:77-80,
+ * functions (SolidEntity.cpp:170-208, :671-1040, :1239-1956; Ocean.cpp:77-80,
  * :149-201; Atmosphere.cpp:146-157; Uniform/Jet/Pipe GetVelocityAtPoint;
- * OpenGLRealOcean.cpp:282-331; OpenGLDataStructs.cpp:148-171) and its type
- * definitions (Entity.h:57-69, Ocean.h:36-40, SolidEntity.h:39-41,
- * OpenGLDataStructs.h:120-310) out of the reference tree at build time and
+ * OpenGLRealOcean.cpp:282-331; OpenGLDataStructs.cpp:148-171;
+ * GeometryFileUtil.cpp:52-283, :335-620; OpenGLContent.cpp:2733-2897) and its
+ * type definitions (Entity.h:57-69, Ocean.h:36-40, SolidEntity.h:39-41,
+ * OpenGLDataStructs.h:120-310, GeometryFileUtil.h:34-123) out of the
+ * reference tree at build time and
  * compiles them between this header's two halves into oracle/_ref/.  Nothing
  * of the reference's text is stored in this repository; this header declares
  * only what those functions use, in place of the reference's headers, which
@@ -23,6 +25,33 @@
 /* ------------------------------------------------------------------ part 2:
  * classes whose declarations need the extracted mesh and settings types. */
 namespace sf {
+
+/* Console output and timing used by LoadOBJ (SimulationApp.h:34-37,
+ * SystemUtil.hpp).  cInfo is silent; cCritical, which aborts the reference's
+ * process, records its message instead (ref_last_error). */
+extern thread_local char ref_error_message[512];
+inline void cInfo(const char*, ...) {}
+inline void cCritical(const char* format, ...)
+{
+    va_list ap;
+    va_start(ap, format);
+    vsnprintf(ref_error_message, sizeof(ref_error_message), format, ap);
+    va_end(ap);
+}
+inline int64_t GetTimeInMicroseconds() { return 0; }
+
+Mesh* LoadOBJ(const std::string& path, GLfloat scale);
+void ComputePhysicalProperties(const Mesh* mesh, Scalar thickness, Scalar density, Scalar& mass, Vector3& CG,
+                               Scalar& volume, Scalar& surface, Vector3& Ipri, Matrix3& Irot);
+Vector3 FindInertialAxis(const Matrix3& I, Scalar value);
+bool IsDiagonal(const Matrix3& A);
+GLuint vertex4Edge(std::map<std::pair<GLuint, GLuint>, GLuint>& lookup, Mesh* mesh, GLuint firstID, GLuint secondID);
+
+class OpenGLContent {
+public:
+    static GLfloat ComputeAverageFaceArea(Mesh* mesh);
+    static void Refine(Mesh* mesh, GLfloat sizeThreshold);
+};
 
 struct Renderable {
     std::shared_ptr<std::vector<glm::vec3>> points;
@@ -102,7 +131,9 @@ public:
 class SimulationManager {
 public:
     Vector3 gravity = Vector3(0, 0, 9.81);
+    Ocean* ocean = nullptr;
     Vector3 getGravity() const { return gravity; }
+    Ocean* getOcean() { return ocean; }
 };
 
 class SimulationApp {
@@ -134,6 +165,13 @@ public:
     void ComputeHydrodynamicForces(HydrodynamicsSettings settings, Ocean* ocn);
     void ComputeAerodynamicForces(Atmosphere* atm);
     void CorrectAerodynamicForces(Atmosphere* atm, Vector3& _Fda, Vector3& _Tda);
+    void ComputeFluidDynamicsApprox(GeometryApproxType t);
+    void ComputeSphericalApprox();
+    void ComputeCylindricalApprox();
+    void ComputeEllipsoidalApprox();
+    Scalar LambKFactor(Scalar r1, Scalar r2);
+    void SetHydrodynamicCoefficients(const Vector3& Cd, const Vector3& Cf);
+    std::vector<Vector3>* getMeshVertices() const;
 
     /* stand-ins for the Bullet-backed accessors */
     void getAABB(Vector3& min, Vector3& max) { min = aabbMin; max = aabbMax; }
@@ -157,6 +195,9 @@ public:
     std::vector<Scalar> fdApproxParams;
     Vector3 fdCd, fdCf;
     Transform T_CG2H;
+    Transform T_CG2C, T_CG2O;
+    Vector3 aMass, aI;
+    Mesh* phyMesh = nullptr;
     Vector3 Fb, Tb, Fdq, Tdq, Fdf, Tdf, Fda, Tda;
     Scalar Swet = Scalar(0);
     Scalar Vsub = Scalar(0);
@@ -168,10 +209,21 @@ public:
 #elif !defined(REF_HARNESS_PART1_DONE)
 #define REF_HARNESS_PART1_DONE
 /* ------------------------------------------------------------------ part 1 */
+#include <algorithm>
 #include <cmath>
+#include <cstdarg>
+#include <cstdio>
 #include <cstdint>
+#include <cstring>
+#include <functional>
+#include <map>
 #include <memory>
+#include <string>
+#include <unordered_set>
+#include <utility>
 #include <vector>
+
+#include "rapidobj.hpp"
 
 #include "LinearMath/btMatrix3x3.h"
 #include "LinearMath/btQuaternion.h"
@@ -188,6 +240,9 @@ typedef btQuaternion Quaternion;
 typedef btVector3 Vector3;
 typedef btMatrix3x3 Matrix3;
 typedef btTransform Transform;
+inline Transform I4() { return Transform::getIdentity(); }
+inline Matrix3 I3() { return Matrix3::getIdentity(); }
+inline Quaternion IQ() { return Quaternion::getIdentity(); }
 inline Vector3 V0() { return Vector3(0, 0, 0); }
 }  // namespace sf
 

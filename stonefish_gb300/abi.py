@@ -77,6 +77,11 @@ class MeshProperties(C.Structure):
                 ("Ipri", _d3), ("Irot", C.c_double * 9)]
 
 
+class FluidApprox(C.Structure):
+    _fields_ = [("approx_type", C.c_int32), ("n_params", C.c_int32), ("params", _d3), ("T_CG2H", Transform),
+                ("added_mass", _d3), ("added_inertia", _d3), ("Cd", _d3), ("Cf", _d3)]
+
+
 class FftOceanParams(C.Structure):
     _fields_ = [("wind", C.c_float), ("omega", C.c_float), ("amplitude", C.c_float), ("km", C.c_float),
                 ("cm", C.c_float), ("grid_sizes", C.c_float * 4), ("passes", C.c_uint32), ("propagate", C.c_int32)]
@@ -261,6 +266,8 @@ def _declare(lib: C.CDLL) -> None:
         "hydro_compound_compute_device": (i32, [vp, vp, vp, C.POINTER(Ocean), C.POINTER(Settings), vp, vp]),
         "hydro_compound_compute": (i32, [vp, vp, vp, C.POINTER(Ocean), C.POINTER(Settings), vp]),
         "hydro_mesh_compute_properties": (i32, [vp, u32, C.c_double, C.c_double, C.POINTER(MeshProperties)]),
+        "hydro_fluid_approx": (i32, [vp, C.c_size_t, u32, i32, C.POINTER(Transform), C.POINTER(Transform), d,
+                                     C.c_double, C.POINTER(FluidApprox)]),
         "hydro_obj_parse": (i32, [C.c_char_p, C.c_size_t, C.c_float, C.c_float, vp, u32, vp, u32, C.POINTER(u32),
                                   C.POINTER(u32)]),
         "hydro_mesh_upload_obj": (i32, [vp, C.c_char_p, C.c_size_t, C.c_float, C.c_float, C.POINTER(u32)]),
@@ -337,3 +344,25 @@ def obj_parse(text: str, scale: float = 1.0, refine_threshold: float = 0.0, lib_
     if st != HYDRO_OK:
         raise HydroError(st, "hydro_obj_parse")
     return xyz, faces
+
+
+def fluid_approx(vertices: np.ndarray, approx: int, T_CG2C, T_CG2O, P_CB, density: float = 1000.0,
+                 vertex_stride: int | None = None, lib_path: str | None = None) -> dict:
+    """hydro_fluid_approx (host only): the proxy shape, Cd/Cf and added mass of
+    a body from its physics-mesh vertices.  ``vertices`` is float32 [V, 3] or
+    the reference's interleaved vertex array (give ``vertex_stride`` in bytes)."""
+    lib = load_library(lib_path)
+    v = np.ascontiguousarray(vertices)
+    stride = vertex_stride if vertex_stride is not None else 12
+    n = v.nbytes // stride
+    pcb = np.ascontiguousarray(P_CB, dtype=np.float64)
+    out = FluidApprox()
+    st = lib.hydro_fluid_approx(v.ctypes.data, stride, n, approx, C.byref(T_CG2C), C.byref(T_CG2O),
+                                pcb.ctypes.data_as(C.POINTER(C.c_double)), density, C.byref(out))
+    if st != HYDRO_OK:
+        raise HydroError(st, "hydro_fluid_approx")
+    k = out.n_params
+    return {"type": out.approx_type, "params": np.array(out.params[:k]),
+            "R_CG2H": np.array(out.T_CG2H.basis[:]).reshape(3, 3), "origin_CG2H": np.array(out.T_CG2H.origin[:]),
+            "added_mass": np.array(out.added_mass[:]), "added_inertia": np.array(out.added_inertia[:]),
+            "Cd": np.array(out.Cd[:]), "Cf": np.array(out.Cf[:])}

@@ -20,7 +20,7 @@ OBJ_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(LIB_DIR, "libstonefish_hydro.so")
 
 SOURCES = ["hydro_kernels.cu", "hydro_api.cu", "hydro_nn.cu", "hydro_rollout.cu", "hydro_mlp_tc.cu", "hydro_cable.cu", "hydro_fft_ocean.cu",
-           "hydro_ingest.cu"]
+           "hydro_ingest.cu", "hydro_approx.cu"]
 HEADERS = ["hydro_device.cuh", "hydro_internal.h", "hydro_pair.cuh"]
 
 NVCC_FLAGS = [

@@ -33,7 +33,10 @@ namespace sfh {
 // earcut ear slicer (mapbox earcut.hpp v2.2.4, rapidobj.hpp:358-1160) in the
 // axis plane where the polygon's projected area is largest.  Both rules work
 // on the positions as written in the file; the scale is applied afterwards
-// (GeometryFileUtil.cpp:161-166).  LoadOBJ splits vertices that carry
+// (GeometryFileUtil.cpp:161-166), and only to a file that has normals: for a
+// file without "vn" statements LoadOBJ copies the unscaled positions over the
+// scaled ones (GeometryFileUtil.cpp:253-254), so such a mesh keeps the
+// file's size whatever the scale.  LoadOBJ splits vertices that carry
 // several normals or texture coordinates (GeometryFileUtil.cpp:100-228);
 // those copies share the position, so the physics mesh here indexes the
 // position list directly.
@@ -46,6 +49,24 @@ constexpr size_t kMaxPolygon = 255;
 // repeated points, cure local self-intersections, split along a valid
 // diagonal.  The z-order hash the original uses above 80 points only
 // narrows the point-in-ear search and does not change which ears are cut.
+// The steps follow mapbox earcut.hpp v2.2.4 function for function (the
+// triangles must be the ones rapidobj produces), under its licence:
+//
+//   ISC License
+//
+//   Copyright (c) 2015, Mapbox
+//
+//   Permission to use, copy, modify, and/or distribute this software for any
+//   purpose with or without fee is hereby granted, provided that the above
+//   copyright notice and this permission notice appear in all copies.
+//
+//   THE SOFTWARE IS PROVIDED "AS IS" AND THE AUTHOR DISCLAIMS ALL WARRANTIES
+//   WITH REGARD TO THIS SOFTWARE INCLUDING ALL IMPLIED WARRANTIES OF
+//   MERCHANTABILITY AND FITNESS. IN NO EVENT SHALL THE AUTHOR BE LIABLE FOR
+//   ANY SPECIAL, DIRECT, INDIRECT, OR CONSEQUENTIAL DAMAGES OR ANY DAMAGES
+//   WHATSOEVER RESULTING FROM LOSS OF USE, DATA OR PROFITS, WHETHER IN AN
+//   ACTION OF CONTRACT, NEGLIGENCE OR OTHER TORTIOUS ACTION, ARISING OUT OF OR
+//   IN CONNECTION WITH THE USE OR PERFORMANCE OF THIS SOFTWARE.
 class EarSlicer {
 public:
     std::vector<uint32_t> tri;   // polygon-local indices, three per triangle
@@ -329,8 +350,11 @@ bool triangulate(const std::vector<float>& raw, const long* poly, size_t n, std:
 }  // namespace
 
 // "v x y z ..." and "f i[/t][/n] ..." lines; 1-based or negative (relative
-// to the vertices read so far) indices.  Other statements (vt, vn, o, g, s,
-// usemtl, mtllib, l, p, comments) carry nothing the physics uses.  Returns
+// to the vertices read so far) indices; whether any "vn" line is present.
+// Other statements (vt, o, g, s, usemtl, mtllib, l, p, comments) carry
+// nothing the physics uses (material libraries are not read: the reference's
+// loader rejects a file whose material library is missing, this one reads
+// its geometry).  Returns
 // false, with a message, on malformed input or a polygon the triangulation
 // rejects.
 bool parse_obj(const char* text, size_t len, float scale, std::vector<float>& xyz, std::vector<uint32_t>& faces,
@@ -341,6 +365,7 @@ bool parse_obj(const char* text, size_t len, float scale, std::vector<float>& xy
     std::vector<long> corners;                 // every face's resolved indices
     std::vector<std::pair<size_t, size_t>> polys;  // (first corner, line)
     size_t pos = 0, line_no = 0;
+    bool has_normals = false;
     while (pos < len) {
         size_t end = pos;
         while (end < len && text[end] != '\n' && text[end] != '\r') ++end;
@@ -350,6 +375,8 @@ bool parse_obj(const char* text, size_t len, float scale, std::vector<float>& xy
         size_t i = 0;
         while (i < line.size() && (line[i] == ' ' || line[i] == '\t')) ++i;
         if (i + 1 >= line.size()) continue;
+        if (line[i] == 'v' && line[i + 1] == 'n' && i + 2 < line.size() && (line[i + 2] == ' ' || line[i + 2] == '\t'))
+            has_normals = true;
         if (line[i] == 'v' && (line[i + 1] == ' ' || line[i + 1] == '\t')) {
             const char* s = line.c_str() + i + 1;
             char* e = nullptr;
@@ -404,7 +431,8 @@ bool parse_obj(const char* text, size_t len, float scale, std::vector<float>& xy
         err = "no faces";
         return false;
     }
-    for (float& v : xyz) v = scale * v;
+    if (has_normals)
+        for (float& v : xyz) v = scale * v;
     return true;
 }
 

@@ -83,6 +83,62 @@ def main():
     p.radius, p.radius2, p.length, p.speed, p.gamma = 0.5, 1.0, 5.0, 1.5, 0.7
     save("currents_jet_pipe", sc)
     save_face_patterns()
+    save_ingest()
+
+
+def ingest_meshes():
+    """Synthetic physics meshes for the mass-property and coefficient-setup
+    fixtures: sphere, box, capped cylinders along x and y, and a sphere with
+    seeded radial noise (distinct principal moments)."""
+    from stonefish_gb300 import meshes
+    rng = np.random.default_rng(109)
+    ico = meshes.build_icosphere(0.7, 3)
+    bumpy = (ico[0] * (1.0 + 0.08 * rng.standard_normal((len(ico[0]), 1))).astype(np.float32)
+             * np.array([1.0, 0.8, 0.6], np.float32), ico[1])
+    cyl = meshes.capped_cylinder_for_faces(0.2, 1.6, 3000)
+    ycyl = (np.ascontiguousarray(cyl[0][:, [1, 0, 2]] * np.array([-1.0, 1.0, 1.0], np.float32)), cyl[1])
+    return {"sphere": ico, "box": meshes.build_box((0.3, 0.2, 0.5), 2), "cylinder_x": cyl,
+            "cylinder_y": ycyl, "bumpy": bumpy}
+
+
+def save_ingest():
+    """The reference's ComputePhysicalProperties (solid and shell) and
+    ComputeFluidDynamicsApprox (every approximation, rotated frames) on
+    ingest_meshes()."""
+    ref = Reference()
+    rng = np.random.default_rng(110)
+    arrays = {}
+    for name, (xyz, faces) in ingest_meshes().items():
+        arrays[f"{name}_xyz"] = xyz
+        arrays[f"{name}_faces"] = faces
+        props = []
+        for th in (-1.0, 0.01):
+            p = ref.mesh_properties((xyz, faces), th, 900.0)
+            props.append(np.concatenate([[p["mass"], p["volume"], p["surface"]], p["CG"], p["Ipri"],
+                                         p["Irot"].reshape(-1)]))
+        arrays[f"{name}_props"] = np.array(props)
+        frames, approx = [], []
+        for trial in range(3):
+            R1 = scenarios.quat_to_matrix(scenarios.random_quaternions(rng, 1))[0] if trial else np.eye(3)
+            R2 = scenarios.quat_to_matrix(scenarios.random_quaternions(rng, 1))[0] if trial == 2 else np.eye(3)
+            o1, o2, pcb = rng.uniform(-0.1, 0.1, 3), rng.uniform(-0.1, 0.1, 3), rng.uniform(-0.05, 0.05, 3)
+            frames.append(np.concatenate([R1.reshape(-1), o1, R2.reshape(-1), o2, pcb]))
+            t1, t2 = abi.Transform(), abi.Transform()
+            for i in range(9):
+                t1.basis[i], t2.basis[i] = float(R1.reshape(-1)[i]), float(R2.reshape(-1)[i])
+            for i in range(3):
+                t1.origin[i], t2.origin[i] = float(o1[i]), float(o2[i])
+            for ap in (abi.APPROX_AUTO, abi.APPROX_SPHERE, abi.APPROX_CYLINDER, abi.APPROX_ELLIPSOID):
+                a = ref.fluid_approx((xyz, faces), ap, t1, t2, pcb, 1025.0)
+                par = np.zeros(3)
+                par[:len(a["params"])] = a["params"]
+                approx.append(np.concatenate([[ap, a["type"], len(a["params"])], par, a["R_CG2H"].reshape(-1),
+                                              a["origin_CG2H"], a["added_mass"], a["added_inertia"], a["Cd"],
+                                              a["Cf"]]))
+        arrays[f"{name}_frames"] = np.array(frames)
+        arrays[f"{name}_approx"] = np.array(approx)
+    np.savez_compressed(os.path.join(HERE, "ref_ingest.npz"), **arrays)
+    print("ref_ingest", sorted(arrays))
 
 
 def save_face_patterns():

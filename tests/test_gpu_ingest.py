@@ -5,6 +5,7 @@ the principal axes against an eigen-decomposition of the inertia tensor
 restated here in numpy, and hydro_mesh_upload_obj against hydro_obj_parse +
 hydro_mesh_upload."""
 import math
+import os
 
 import numpy as np
 import pytest
@@ -115,3 +116,29 @@ def test_properties_unknown_mesh(hctx):
     with pytest.raises(abi.HydroError) as e:
         hctx.mesh_properties(10 ** 6)
     assert e.value.status == abi.HYDRO_ERR_NOT_FOUND
+
+
+@pytest.mark.parametrize("name", ["sphere", "box", "cylinder_x", "cylinder_y", "bumpy"])
+def test_properties_match_reference_fixture(hctx, name):
+    """hydro_mesh_compute_properties against the reference's own
+    ComputePhysicalProperties (tests/golden/ref_ingest.npz, made by the
+    reference's code compiled from its source): the GPU's FP64 face sums
+    differ from the reference's serial sums only in order."""
+    z = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_ingest.npz"))
+    xyz, faces = z[f"{name}_xyz"], z[f"{name}_faces"]
+    mid = hctx.upload_mesh(xyz, faces)
+    ext = float(np.abs(xyz).max())
+    for row, th in zip(z[f"{name}_props"], (-1.0, 0.01)):
+        g = hctx.mesh_properties(mid, th, 900.0)
+        for k, v in (("mass", row[0]), ("volume", row[1]), ("surface", row[2])):
+            assert math.isclose(g[k], v, rel_tol=1e-12), (name, th, k, g[k], v)
+        np.testing.assert_allclose(g["CG"], row[3:6], rtol=0, atol=1e-12 * ext)
+        ipri = row[6:9]
+        np.testing.assert_allclose(np.sort(g["Ipri"]), np.sort(ipri), rtol=1e-9, atol=1e-12 * ipri.max())
+        lam = np.sort(ipri)
+        if np.min(np.diff(lam)) > 1e-3 * lam.max():     # distinct moments: the axes are defined
+            R_ref = row[9:18].reshape(3, 3)
+            for j in range(3):
+                col = g["Irot"][:, j]
+                jr = int(np.argmin(np.abs(ipri - g["Ipri"][j])))
+                assert abs(abs(float(col @ R_ref[:, jr])) - 1.0) < 1e-6, (name, th, j)
