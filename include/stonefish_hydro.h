@@ -702,6 +702,18 @@ hydro_status hydro_debug_arith_check(hydro_ctx* ctx, uint64_t n_pairs, uint64_t 
                                      uint64_t division[3], uint64_t packed[4],
                                      float examples[16]);
 
+/* The host tables of the FFT ocean (no device work, no context): the wave
+ * spectrum as hydro_fft_ocean_create builds it (OpenGLOcean::
+ * GenerateWavesSpectrum, OpenGLOcean.cpp:1025-1048, seed 1234 of the
+ * reference's generator; each value rounded to binary16 as the reference's
+ * RGBA16F textures hold it), N x N x 4 floats each for s12 and s34, and the
+ * butterfly table (ComputeButterflyLookupTable, :878-926) decoded per pass p
+ * and output i at [p * N + i]: the two input indices (butterfly_index, 2
+ * int32 each) and the binary16 weight (butterfly_weight, re and im).  Any
+ * output may be NULL.  For checking the tables against the reference. */
+hydro_status hydro_debug_fft_ocean_tables(const hydro_fft_ocean_params* params, float* s12, float* s34,
+                                          int32_t* butterfly_index, float* butterfly_weight);
+
 /* ------------------------------------------------------------------------
  * Learned wrench surrogate (no counterpart in the reference).
  *

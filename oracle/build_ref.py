@@ -5,7 +5,8 @@ TEST INFRASTRUCTURE ONLY.  The reference as a whole does not build without
 SDL2, GL, FreeType and glm, but the functions of its hydrodynamics path use
 only glm vector arithmetic, Bullet's LinearMath and rapidobj (both vendored
 in the reference, 3rdparty/) and a few members of Ocean, SolidEntity,
-OpenGLRealOcean and OpenGLContent.  This recipe reads those functions and type definitions out
+OpenGLRealOcean, OpenGLOcean (its host-side spectrum and butterfly table),
+OpenGLContent, Compound and CableEntity.  This recipe reads those functions and type definitions out
 of the reference's files where they lie, finds each by its signature and
 brace matching, and pipes them with ``#line`` markers into g++ between the
 two halves of ``oracle/ref_harness.hpp`` (stand-ins for the reference's
@@ -55,6 +56,10 @@ TYPES = [
     ("Library/include/utils/GeometryFileUtil.h", "struct IndexedVertexHash"),
     ("Library/include/utils/GeometryFileUtil.h", "struct IndexedTexturableVertex"),
     ("Library/include/utils/GeometryFileUtil.h", "struct IndexedTexturableVertexHash"),
+    ("Library/include/entities/CableEntity.h", "struct CableNodalForces"),
+    ("Library/include/graphics/OpenGLOcean.h", "struct OceanParams"),
+    ("Library/include/utils/SystemUtil.hpp", "inline long lrandom("),
+    ("Library/include/utils/SystemUtil.hpp", "inline float frandom("),
 ]
 FUNCTIONS = [
     ("Library/src/graphics/OpenGLDataStructs.cpp", "glm::mat4 glMatrixFromTransform("),
@@ -94,6 +99,20 @@ FUNCTIONS = [
     ("Library/src/utils/GeometryFileUtil.cpp", "void ComputePhysicalProperties(const Mesh* mesh, Scalar thickness, Scalar density, Scalar& mass"),
     ("Library/src/utils/GeometryFileUtil.cpp", "Vector3 FindInertialAxis("),
     ("Library/src/utils/GeometryFileUtil.cpp", "bool IsDiagonal("),
+    ("Library/src/entities/SolidEntity.cpp", "PhysicsMode SolidEntity::getPhysicsMode()"),
+    ("Library/src/entities/SolidEntity.cpp", "Transform SolidEntity::getO2CTransform()"),
+    ("Library/src/entities/SolidEntity.cpp", "void SolidEntity::getHydrodynamicCoefficients("),
+    ("Library/src/entities/solids/Compound.cpp", "void Compound::ComputeHydrodynamicForces("),
+    ("Library/src/entities/CableEntity.cpp", "Scalar CableEntity::circularSegmentArea("),
+    ("Library/src/entities/CableEntity.cpp", "void CableEntity::ComputeHydrodynamicForces("),
+    ("Library/src/graphics/OpenGLOcean.cpp", "int OpenGLOcean::bitReverse("),
+    ("Library/src/graphics/OpenGLOcean.cpp", "void OpenGLOcean::computeWeight("),
+    ("Library/src/graphics/OpenGLOcean.cpp", "GLfloat* OpenGLOcean::ComputeButterflyLookupTable("),
+    ("Library/src/graphics/OpenGLOcean.cpp", "float OpenGLOcean::sqr("),
+    ("Library/src/graphics/OpenGLOcean.cpp", "float OpenGLOcean::omega("),
+    ("Library/src/graphics/OpenGLOcean.cpp", "float OpenGLOcean::spectrum("),
+    ("Library/src/graphics/OpenGLOcean.cpp", "void OpenGLOcean::GetSpectrumSample("),
+    ("Library/src/graphics/OpenGLOcean.cpp", "void OpenGLOcean::GenerateWavesSpectrum()"),
 ]
 
 CXXFLAGS = ["-O3", "-DNDEBUG", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-pthread",

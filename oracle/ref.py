@@ -29,6 +29,15 @@ def source_root() -> str | None:
     return root if os.path.isdir(root) else None
 
 
+class RefCompoundPart(C.Structure):
+    """One part of a compound as the reference holds it (ref_api.inc)."""
+    _fields_ = [("origin", abi.Transform), ("O2C", abi.Transform), ("Cd", C.c_double * 3), ("Cf", C.c_double * 3),
+                ("mesh", C.c_uint32), ("mode", C.c_int32), ("buoyancy", C.c_int32), ("external", C.c_int32)]
+
+
+REF_PART_DTYPE = abi._dtype_of(RefCompoundPart)
+
+
 class Reference:
     """The reference's functions, loaded from oracle/_ref."""
 
@@ -72,6 +81,14 @@ class Reference:
         L.ref_mesh_properties.argtypes = [vp, C.c_double, C.c_double, vp]
         L.ref_last_error.restype = C.c_char_p
         L.ref_last_error.argtypes = []
+        L.ref_compound_part_frames.restype = None
+        L.ref_compound_part_frames.argtypes = [P(abi.Transform), P(abi.Transform), P(abi.Transform),
+                                               P(abi.Transform), d]
+        L.ref_compound_forces.restype = i32
+        L.ref_compound_forces.argtypes = [vp, P(abi.Transform), vp, u32, vp, u32, P(abi.Ocean), vp,
+                                          P(abi.Settings), vp]
+        L.ref_cable_forces.restype = i32
+        L.ref_cable_forces.argtypes = [vp, u32, vp, vp, u32, P(abi.Ocean), vp, P(abi.Settings), vp]
         L.ref_fluid_approx.restype = None
         L.ref_fluid_approx.argtypes = [vp, i32, P(abi.Transform), P(abi.Transform), d, C.c_double, vp]
 
@@ -190,3 +207,64 @@ class Reference:
         return {"type": int(out[0]), "params": out[2:2 + n].copy(), "R_CG2H": out[5:14].reshape(3, 3).copy(),
                 "origin_CG2H": out[14:17].copy(), "added_mass": out[17:20].copy(),
                 "added_inertia": out[20:23].copy(), "Cd": out[23:26].copy(), "Cf": out[26:29].copy()}
+
+    def compound_part_frames(self, T_O, origin, O2C):
+        """(T_C of the part, basis of T_O * origin) as Compound.cpp:343-344 forms them."""
+        tc = abi.Transform()
+        ro = np.zeros(9)
+        self.lib.ref_compound_part_frames(C.byref(T_O), C.byref(origin), C.byref(O2C), C.byref(tc),
+                                          ro.ctypes.data_as(C.POINTER(C.c_double)))
+        return tc, ro
+
+    def compound_forces(self, compound, T_O, parts, meshes, ocean, settings, io, waves=None):
+        """Compound::ComputeHydrodynamicForces: compound = hydro_body[1],
+        parts = REF_PART_DTYPE[n] (mesh = index into meshes or NO_MESH),
+        io = hydro_wrench[1] updated in place."""
+        oms = (OracleMesh * max(1, len(meshes)))()
+        keep = []
+        for i, (xyz, faces) in enumerate(meshes):
+            m = self.make_mesh(xyz, faces)
+            keep.append(m)
+            oms[i] = m
+        w = self.make_waves(waves)
+        parts = np.ascontiguousarray(parts)
+        rc = self.lib.ref_compound_forces(compound.ctypes.data, C.byref(T_O), parts.ctypes.data, len(parts),
+                                          C.cast(oms, C.c_void_p), len(meshes), C.byref(ocean), self._p(w),
+                                          C.byref(settings), io.ctypes.data)
+        if rc != 0:
+            raise ValueError("wave data not expressible as the reference's two-layer texture")
+        return io
+
+    def cable_forces(self, cables, x, v, ocean, settings, out, waves=None):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        w = self.make_waves(waves)
+        self.lib.ref_cable_forces(cables.ctypes.data, len(cables), x.ctypes.data, v.ctypes.data, len(x),
+                                  C.byref(ocean), self._p(w), C.byref(settings), out.ctypes.data)
+        return out
+
+    def fft_spectrum(self, params):
+        """GenerateWavesSpectrum: (spectrum12, spectrum34), each [N, N, 4]
+        float32.  The reference's generator seed is a function-local static,
+        so each call loads a fresh copy of the library."""
+        import shutil
+        import tempfile
+        n = 1 << params.passes
+        s12 = np.zeros((n, n, 4), np.float32)
+        s34 = np.zeros((n, n, 4), np.float32)
+        with tempfile.TemporaryDirectory() as d:
+            path = os.path.join(d, "libstonefish_ref_copy.so")
+            shutil.copyfile(LIB, path)
+            lib = C.CDLL(path)
+            lib.ref_fft_spectrum.restype = None
+            lib.ref_fft_spectrum.argtypes = [C.POINTER(abi.FftOceanParams), C.c_void_p, C.c_void_p]
+            lib.ref_fft_spectrum(C.byref(params), s12.ctypes.data, s34.ctypes.data)
+        return s12, s34
+
+    def fft_butterfly(self, size: int, passes: int) -> np.ndarray:
+        """ComputeButterflyLookupTable: [passes, size, 4] float32."""
+        out = np.zeros((passes, size, 4), np.float32)
+        self.lib.ref_fft_butterfly.restype = None
+        self.lib.ref_fft_butterfly.argtypes = [C.c_uint, C.c_uint, C.c_void_p]
+        self.lib.ref_fft_butterfly(size, passes, out.ctypes.data)
+        return out

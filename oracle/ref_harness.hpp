@@ -6,9 +6,12 @@
  * functions (SolidEntity.cpp:170-208, :671-1040, :1239-1956; Ocean.cpp:77-80,
  * :149-201; Atmosphere.cpp:146-157; Uniform/Jet/Pipe GetVelocityAtPoint;
  * OpenGLRealOcean.cpp:282-331; OpenGLDataStructs.cpp:148-171;
- * GeometryFileUtil.cpp:52-283, :335-620; OpenGLContent.cpp:2733-2897) and its
- * type definitions (Entity.h:57-69, Ocean.h:36-40, SolidEntity.h:39-41,
- * OpenGLDataStructs.h:120-310, GeometryFileUtil.h:34-123) out of the
+ * GeometryFileUtil.cpp:52-283, :335-620; OpenGLContent.cpp:2733-2897;
+ * Compound.cpp:291-436; CableEntity.cpp:218-376; OpenGLOcean.cpp:856-1048)
+ * and its type definitions (Entity.h:57-69, Ocean.h:36-40, SolidEntity.h:39-41,
+ * OpenGLDataStructs.h:120-310, GeometryFileUtil.h:34-123, CableEntity.h:42-54,
+ * OpenGLOcean.h:36-51, SystemUtil.hpp:208-218)
+ * out of the
  * reference tree at build time and
  * compiles them between this header's two halves into oracle/_ref/.  Nothing
  * of the reference's text is stored in this repository; this header declares
@@ -58,17 +61,26 @@ struct Renderable {
     std::shared_ptr<std::vector<glm::vec3>> getDataAsPoints() const { return points; }
 };
 
-struct OceanParams {
-    int fftSize;
-    glm::vec4 gridSizes;
-};
-
 class OpenGLRealOcean {
 public:
     OceanParams params;
     GLfloat* fftData;
     GLfloat ComputeInterpolatedWaveData(GLfloat x, GLfloat y, GLuint channel);
     GLfloat ComputeWaveHeight(GLfloat x, GLfloat y);
+};
+
+/* The host half of the FFT ocean (OpenGLOcean.h): spectrum and butterfly table. */
+class OpenGLOcean {
+public:
+    OceanParams params;
+    int bitReverse(int i, int N);
+    void computeWeight(int N, int k, float& Wr, float& Wi);
+    GLfloat* ComputeButterflyLookupTable(unsigned int size, unsigned int passes);
+    float sqr(float x);
+    float omega(float k);
+    float spectrum(float kx, float ky, bool omnispectrum = false);
+    void GetSpectrumSample(int i, int j, float lengthScale, float kMin, float* result);
+    void GenerateWavesSpectrum();
 };
 
 class VelocityField {
@@ -172,6 +184,9 @@ public:
     Scalar LambKFactor(Scalar r1, Scalar r2);
     void SetHydrodynamicCoefficients(const Vector3& Cd, const Vector3& Cf);
     std::vector<Vector3>* getMeshVertices() const;
+    PhysicsMode getPhysicsMode() const;
+    Transform getO2CTransform() const;
+    void getHydrodynamicCoefficients(Vector3& Cd, Vector3& Cf) const;
 
     /* stand-ins for the Bullet-backed accessors */
     void getAABB(Vector3& min, Vector3& max) { min = aabbMin; max = aabbMax; }
@@ -195,13 +210,45 @@ public:
     std::vector<Scalar> fdApproxParams;
     Vector3 fdCd, fdCf;
     Transform T_CG2H;
-    Transform T_CG2C, T_CG2O;
+    Transform T_CG2C, T_CG2O, T_O2C;
     Vector3 aMass, aI;
     Mesh* phyMesh = nullptr;
     Vector3 Fb, Tb, Fdq, Tdq, Fdf, Tdf, Fda, Tda;
     Scalar Swet = Scalar(0);
     Scalar Vsub = Scalar(0);
     Renderable submerged;
+};
+
+/* Compound.h:33-39. */
+typedef struct {
+    SolidEntity* solid;
+    Transform origin;
+    bool isExternal;
+    bool alwaysVisible;
+} CompoundPart;
+
+class Compound : public SolidEntity {
+public:
+    std::vector<CompoundPart> parts;
+    void ComputeHydrodynamicForces(HydrodynamicsSettings settings, Ocean* ocn);
+};
+
+/* The node array of the cable's btSoftBody: positions m_x, velocities m_v. */
+struct SoftBodyNode {
+    Vector3 m_x, m_v;
+};
+struct SoftBodyNodes {
+    std::vector<SoftBodyNode> m_nodes;
+};
+
+class CableEntity {
+public:
+    SoftBodyNodes* cableBody_ = nullptr;
+    Scalar radius_ = Scalar(0);
+    std::vector<CableNodalForces> nodalForces_;
+    PhysicsSettings phy_;
+    Scalar circularSegmentArea(Scalar h) const;
+    void ComputeHydrodynamicForces(HydrodynamicsSettings settings, Ocean* ocn);
 };
 
 }  // namespace sf

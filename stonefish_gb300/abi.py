@@ -266,6 +266,7 @@ def _declare(lib: C.CDLL) -> None:
         "hydro_compound_compute_device": (i32, [vp, vp, vp, C.POINTER(Ocean), C.POINTER(Settings), vp, vp]),
         "hydro_compound_compute": (i32, [vp, vp, vp, C.POINTER(Ocean), C.POINTER(Settings), vp]),
         "hydro_mesh_compute_properties": (i32, [vp, u32, C.c_double, C.c_double, C.POINTER(MeshProperties)]),
+        "hydro_debug_fft_ocean_tables": (i32, [C.POINTER(FftOceanParams), vp, vp, vp, vp]),
         "hydro_fluid_approx": (i32, [vp, C.c_size_t, u32, i32, C.POINTER(Transform), C.POINTER(Transform), d,
                                      C.c_double, C.POINTER(FluidApprox)]),
         "hydro_obj_parse": (i32, [C.c_char_p, C.c_size_t, C.c_float, C.c_float, vp, u32, vp, u32, C.POINTER(u32),
@@ -366,3 +367,19 @@ def fluid_approx(vertices: np.ndarray, approx: int, T_CG2C, T_CG2O, P_CB, densit
             "R_CG2H": np.array(out.T_CG2H.basis[:]).reshape(3, 3), "origin_CG2H": np.array(out.T_CG2H.origin[:]),
             "added_mass": np.array(out.added_mass[:]), "added_inertia": np.array(out.added_inertia[:]),
             "Cd": np.array(out.Cd[:]), "Cf": np.array(out.Cf[:])}
+
+
+def fft_ocean_tables(params, lib_path: str | None = None):
+    """hydro_debug_fft_ocean_tables (host only): (s12 [N,N,4], s34 [N,N,4],
+    butterfly indices [passes, N, 2], butterfly weights [passes, N, 2])."""
+    lib = load_library(lib_path)
+    n = 1 << params.passes
+    s12 = np.zeros((n, n, 4), np.float32)
+    s34 = np.zeros((n, n, 4), np.float32)
+    idx = np.zeros((params.passes, n, 2), np.int32)
+    w = np.zeros((params.passes, n, 2), np.float32)
+    st = lib.hydro_debug_fft_ocean_tables(C.byref(params), s12.ctypes.data, s34.ctypes.data, idx.ctypes.data,
+                                          w.ctypes.data)
+    if st != HYDRO_OK:
+        raise HydroError(st, "hydro_debug_fft_ocean_tables")
+    return s12, s34, idx, w

@@ -21,6 +21,7 @@
 // 0 and 1 at the first two grid sizes (OpenGLRealOcean.cpp:321-331).
 #include <cmath>
 #include <cstdint>
+#include <cstring>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <vector>
@@ -239,3 +240,20 @@ cudaError_t launch_fft_ocean(const float4* s12, const float4* s34, const int2* i
 }
 
 }  // namespace sfh
+
+extern "C" hydro_status hydro_debug_fft_ocean_tables(const hydro_fft_ocean_params* params, float* s12, float* s34,
+                                                     int32_t* butterfly_index, float* butterfly_weight)
+{
+    if (params == nullptr || params->passes < 1 || params->passes > 12) return HYDRO_ERR_INVALID_ARG;
+    const size_t N = (size_t)1 << params->passes;
+    std::vector<float4> a, b;
+    sfh::fft_ocean_spectrum(*params, a, b);
+    if (s12 != nullptr) std::memcpy(s12, a.data(), N * N * sizeof(float4));
+    if (s34 != nullptr) std::memcpy(s34, b.data(), N * N * sizeof(float4));
+    std::vector<int2> idx;
+    std::vector<float2> w;
+    sfh::fft_ocean_butterfly((int)params->passes, idx, w);
+    if (butterfly_index != nullptr) std::memcpy(butterfly_index, idx.data(), idx.size() * sizeof(int2));
+    if (butterfly_weight != nullptr) std::memcpy(butterfly_weight, w.data(), w.size() * sizeof(float2));
+    return HYDRO_OK;
+}

@@ -7,6 +7,7 @@ oracle's REF32 variant -- the restatement every GPU bar is measured against
 -- must give the same bits as that code: per body on whole batches, and per
 face on single triangles in every depth-sign pattern.  The module is skipped
 where the reference's source tree is absent."""
+import ctypes as C
 import math
 
 import numpy as np
@@ -247,3 +248,112 @@ def test_reference_buoyancy_of_a_submerged_sphere_mesh(ref):
     assert a["Vsub"][0] == pytest.approx(V, rel=5e-5)
     assert a["Fb"][2] == pytest.approx(-V * oc.density * oc.gravity, rel=5e-5)
     assert V == pytest.approx(4 / 3 * math.pi * 0.125, rel=1e-6)
+
+
+# ------------------------------------------------------ compound, cable
+def _transform(R, o):
+    t = abi.Transform()
+    for i in range(9):
+        t.basis[i] = float(np.asarray(R).reshape(-1)[i])
+    for i in range(3):
+        t.origin[i] = float(o[i])
+    return t
+
+
+def test_compound_equals_reference(oracle, ref):
+    """Compound::ComputeHydrodynamicForces (Compound.cpp:291-436) from the
+    reference's code against the oracle: compounds whose origin, part origins
+    and part mesh frames are general transforms (the part frames formed by
+    the reference's own products), external and internal parts, parts out of
+    the fluid computation, a part without a mesh; INSIDE, OUTSIDE, CROSSING."""
+    from oracle.ref import REF_PART_DTYPE
+    rng = np.random.default_rng(41)
+    mesh_list = [meshes.capped_cylinder_for_faces(0.2, 1.2, 600), meshes.build_box((0.5, 0.08, 0.06), 2),
+                 meshes.build_box((0.3, 0.1, 0.05), 1), meshes.build_icosphere(0.15, 2)]
+    positions = set()
+    for c in range(60):
+        n_parts = int(rng.integers(1, 6))
+        R = scenarios.quat_to_matrix(scenarios.random_quaternions(rng, 1))[0]
+        cg = np.array([rng.uniform(-3, 3), rng.uniform(-3, 3), rng.uniform(-1.2, 1.2)])
+        Ro = scenarios.quat_to_matrix(scenarios.random_quaternions(rng, 1))[0]
+        T_O = _transform(Ro @ R, cg + rng.uniform(-0.05, 0.05, 3))
+        comp = np.zeros(1, dtype=abi.BODY_DTYPE)
+        comp["T_CG"]["basis"] = R.reshape(9)
+        comp["T_CG"]["origin"] = cg
+        comp["v"] = rng.uniform(-1, 1, 3)
+        comp["omega"] = rng.uniform(-0.5, 0.5, 3)
+        comp["volume"], comp["surface"] = 0.12, 1.7
+        comp["P_CB"] = rng.uniform(-0.05, 0.05, 3)
+        comp["aabb_min"] = cg - 0.9
+        comp["aabb_max"] = cg + 0.9
+        comp["mode"] = abi.MODE_SUBMERGED if c % 9 else abi.MODE_FLOATING
+        comp["buoyancy"] = int(c % 7 != 3)
+        rp = np.zeros(n_parts, dtype=REF_PART_DTYPE)
+        op = np.zeros(n_parts, dtype=abi.COMPOUND_PART_DTYPE)
+        for i in range(n_parts):
+            o = _transform(scenarios.quat_to_matrix(scenarios.random_quaternions(rng, 1))[0], rng.uniform(-0.4, 0.4, 3))
+            o2c = _transform(scenarios.quat_to_matrix(scenarios.random_quaternions(rng, 1))[0],
+                             rng.uniform(-0.05, 0.05, 3))
+            for name, t in (("origin", o), ("O2C", o2c)):
+                rp[i][name]["basis"] = t.basis[:]
+                rp[i][name]["origin"] = t.origin[:]
+            mesh = int(rng.integers(0, 4)) if (c + i) % 11 else abi.NO_MESH
+            mode = [abi.MODE_SUBMERGED, abi.MODE_FLOATING, abi.MODE_SUBMERGED, abi.MODE_DISABLED][int(rng.integers(0, 4))]
+            cd, cf = rng.uniform(0.2, 1.0, 3), rng.uniform(0.01, 0.1, 3)
+            external = int(i == 0 or rng.uniform() < 0.7)
+            for arr in (rp, op):
+                arr[i]["Cd"], arr[i]["Cf"], arr[i]["mesh"], arr[i]["mode"] = cd, cf, mesh, mode
+                arr[i]["external"] = external
+            rp[i]["buoyancy"] = op[i]["buoyant"] = int(rng.uniform() < 0.85)
+            tc, ro = ref.compound_part_frames(T_O, o, o2c)
+            op[i]["T_C"]["basis"] = tc.basis[:]
+            op[i]["T_C"]["origin"] = tc.origin[:]
+            op[i]["R_O"] = ro
+        io_r = scenarios.new_wrenches(1)
+        io_o = scenarios.new_wrenches(1)
+        for io in (io_r, io_o):
+            io["Fb"], io["Vsub"] = 0.5, 0.25
+        ref.compound_forces(comp, T_O, rp, mesh_list, scenarios.flat_ocean(), scenarios.settings(), io_r)
+        part_meshes = [None if p["mesh"] == abi.NO_MESH else mesh_list[int(p["mesh"])] for p in op]
+        oracle.compound_forces(REF32, comp, op, part_meshes, scenarios.flat_ocean(), scenarios.settings(), io_o)
+        assert_same(io_r, io_o, f"compound {c}")
+        positions.add(int(io_r["position"][0]))
+    assert {abi.INSIDE, abi.OUTSIDE, abi.CROSSING_SURFACE} <= positions
+
+
+@pytest.mark.parametrize("seed", [6, 7])
+def test_cables_equal_reference(oracle, ref, seed):
+    """CableEntity::ComputeHydrodynamicForces (CableEntity.cpp:240-376) from
+    the reference's code against the oracle, every submersion case."""
+    cs = scenarios.cable_set(48, seed=seed)
+    for st in (scenarios.settings(), scenarios.settings(damping=False), scenarios.settings(buoyancy=False)):
+        a = np.zeros(len(cs["x"]), dtype=abi.CABLE_FORCES_DTYPE)
+        b = np.zeros(len(cs["x"]), dtype=abi.CABLE_FORCES_DTYPE)
+        a["Fb"] = b["Fb"] = 0.75           # untouched where the mode gate skips a cable
+        ref.cable_forces(cs["cables"], cs["x"], cs["v"], cs["ocean"], st, a)
+        oracle.cable_forces(cs["cables"], cs["x"], cs["v"], cs["ocean"], st, b)
+        for k in ("Fb", "Fdq", "Fdf"):
+            assert np.array_equal(a[k], b[k]), k
+
+
+@pytest.mark.parametrize("state,passes", [(3.0, 8), (1.0, 7), (6.0, 8)])
+def test_fft_ocean_tables_equal_reference(built_library, ref, state, passes):
+    """The FFT ocean's host tables against the reference's OpenGLOcean code:
+    the wave spectrum (GenerateWavesSpectrum with its seeded generator) and
+    the butterfly table, each value as the reference's RGBA16F textures hold
+    it (binary16, round to nearest even)."""
+    p = abi.FftOceanParams()
+    built = abi.load_library()
+    built.hydro_fft_ocean_params_for_state(C.c_float(state), C.byref(p))
+    p.passes = passes
+    s12, s34, idx, w = abi.fft_ocean_tables(p)
+    r12, r34 = ref.fft_spectrum(p)
+    assert np.array_equal(s12, r12.astype(np.float16).astype(np.float32))
+    assert np.array_equal(s34, r34.astype(np.float16).astype(np.float32))
+    assert np.count_nonzero(r12) > 0.4 * r12.size
+    n = 1 << passes
+    bt = ref.fft_butterfly(n, passes)
+    j = np.rint(bt[:, :, 0:2].astype(np.float64) * n - 0.5).astype(np.int32)
+    assert np.array_equal(bt[:, :, 0:2], ((j + 0.5) / n).astype(np.float32))
+    assert np.array_equal(idx, j)
+    assert np.array_equal(w, bt[:, :, 2:4].astype(np.float16).astype(np.float32))
