@@ -2221,6 +2221,13 @@ extern "C" hydro_status hydro_compute_wrenches_static(hydro_ctx* ctx, const hydr
 
     char* base = static_cast<char*>(base_ptr);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // The control block (error word, claim counters, the count of listed
+    // chunks) must start at zero.  A previous call that failed between its
+    // launches can leave a count behind in the shared array, so every call
+    // clears the block on its own stream first (a memset allocates nothing).
+    CK(ctx, cudaMemsetAsync(base + off_err, 0, 256, s));
+    // The work list goes up from pageable host arrays: cudaMemcpyAsync stages
+    // pageable memory and may make the host wait for that.
     CK(ctx, cudaMemcpyAsync(base + off_binfo, g_static_binfo, (size_t)n_bodies * sizeof(BodyInfo),
                             cudaMemcpyHostToDevice, s));
     CK(ctx, cudaMemcpyAsync(base + off_chunks, g_static_chunks, nc * sizeof(ChunkDesc),

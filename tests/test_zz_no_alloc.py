@@ -60,3 +60,79 @@ def test_static_step_rejects_too_many_bodies(hctx):
     with pytest.raises(abi.HydroError) as ei:
         hctx.compute_static(ids, d.data_ptr(), scenarios.flat_ocean(), scenarios.settings(), d.data_ptr())
     assert ei.value.status == abi.HYDRO_ERR_INVALID_ARG
+
+
+def _static_counts(hctx, mesh_xyz_faces):
+    """Tiles of the mesh and chunks per body at the context's chunk size."""
+    xyz, faces = mesh_xyz_faces
+    n_tiles = abi.tile_order(faces, len(xyz))[1].size - 1
+    tpc = -(-4096 // abi.TILE_FACES)            # default chunk of 4096 faces in whole tiles
+    return n_tiles, -(-n_tiles // tpc)
+
+
+def test_static_step_rejects_oversized_work_lists(hctx):
+    """More chunks than the static work list holds, and a work list whose
+    scratch exceeds the array, are rejected before anything is launched."""
+    torch = pytest.importorskip("torch")
+    from stonefish_gb300 import meshes
+    big = meshes.build_icosphere(1.0, 5)                 # 20480 faces
+    mid = hctx.upload_mesh(*big)
+    hctx.batch(np.array([mid], dtype=np.uint32)).close()  # grows the device tile table
+    n_tiles, cpb = _static_counts(hctx, big)
+    assert cpb >= 5, (n_tiles, cpb)
+    d = torch.zeros(8, dtype=torch.uint8, device="cuda")
+    per_chunk = 16 + 16 + 24 * 8                          # ChunkDesc, ActiveChunk, partial sums
+    max_chunks = abi.STATIC_SCRATCH_BYTES // per_chunk
+    # chunk count above the work-list limit
+    n = abi.STATIC_MAX_BODIES
+    assert n * cpb > max_chunks
+    with pytest.raises(abi.HydroError) as ei:
+        hctx.compute_static(np.full(n, mid, np.uint32), d.data_ptr(), scenarios.flat_ocean(), scenarios.settings(),
+                            d.data_ptr())
+    assert ei.value.status == abi.HYDRO_ERR_INVALID_ARG and "chunks" in str(ei.value)
+    # within the chunk limit, over the scratch bytes (per body 16 + 128 B)
+    n = max_chunks // cpb
+    assert n * cpb <= max_chunks and n * 144 + n * cpb * per_chunk > abi.STATIC_SCRATCH_BYTES
+    with pytest.raises(abi.HydroError) as ei:
+        hctx.compute_static(np.full(n, mid, np.uint32), d.data_ptr(), scenarios.flat_ocean(), scenarios.settings(),
+                            d.data_ptr())
+    assert ei.value.status == abi.HYDRO_ERR_INVALID_ARG and "scratch" in str(ei.value)
+
+
+def test_static_step_after_a_rejected_call_and_a_different_batch(hctx):
+    """A large batch, a rejected oversized request, then a smaller batch of
+    other meshes: the last call matches hydro_batch_compute_device, so no
+    state of the earlier calls in the shared array leaks into it."""
+    torch = pytest.importorskip("torch")
+    st = scenarios.settings()
+    stream = torch.cuda.current_stream().cuda_stream
+    large = scenarios.mixed_batch(n_bodies=1024, seed=31, scale_faces=0.2)
+    ids = np.array([hctx.upload_mesh(x, f) for x, f in large["meshes"]], dtype=np.uint32)
+    lb = large["bodies"].copy()
+    lb["mesh"] = ids[large["bodies"]["mesh"]]
+    small = scenarios.mixed_batch(n_bodies=96, seed=32, scale_faces=0.05)
+    ids2 = np.array([hctx.upload_mesh(x, f) for x, f in small["meshes"]], dtype=np.uint32)
+    sb = small["bodies"].copy()
+    sb["mesh"] = ids2[small["bodies"]["mesh"]]
+    bt = hctx.batch(sb["mesh"])                            # reference result; also grows the tile table
+    d_sb, d_ref = _device_arrays(torch, sb, len(sb))
+    bt.compute_device(d_sb.data_ptr(), small["ocean"], st, d_ref.data_ptr(), stream)
+    torch.cuda.synchronize()
+    ref = d_ref.cpu().numpy().view(abi.WRENCH_DTYPE).copy()
+    bt.close()
+    hctx.batch(lb["mesh"]).close()
+    d_lb, d_lw = _device_arrays(torch, lb, len(lb))
+    hctx.compute_static(lb["mesh"], d_lb.data_ptr(), large["ocean"], st, d_lw.data_ptr(), stream)
+    with pytest.raises(abi.HydroError):
+        hctx.compute_static(np.full(abi.STATIC_MAX_BODIES + 1, abi.NO_MESH, np.uint32), d_lb.data_ptr(),
+                            large["ocean"], st, d_lw.data_ptr(), stream)
+    _, d_sw = _device_arrays(torch, sb, len(sb))
+    hctx.compute_static(sb["mesh"], d_sb.data_ptr(), small["ocean"], st, d_sw.data_ptr(), stream)
+    torch.cuda.synchronize()
+    out = d_sw.cpu().numpy().view(abi.WRENCH_DTYPE).copy()
+    assert np.array_equal(out["position"], ref["position"])
+    assert np.all(out["status"] == 0)
+    L = 0.5 * np.linalg.norm(sb["aabb_max"] - sb["aabb_min"], axis=1)
+    act = ref["position"] != abi.OUTSIDE
+    for k, v in scaled_errors(out, ref, L).items():
+        assert np.max(v[act]) < 2e-6, (k, float(np.max(v[act])))
