@@ -36,6 +36,7 @@ INSIDE, OUTSIDE, CROSSING_SURFACE, SKIPPED = 0, 1, 2, -1
 # VelocityFieldType
 CURRENT_UNIFORM, CURRENT_JET, CURRENT_PIPE = 0, 1, 2
 CUT_FP64, CUT_FP32 = 0, 1
+ABI_VERSION = 1     # HYDRO_ABI_VERSION
 MAX_CURRENTS = 8
 MAX_WAVE_LAYERS = 4
 NO_MESH = 0xFFFFFFFF
