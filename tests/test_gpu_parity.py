@@ -447,3 +447,34 @@ def test_hulls_barely_under_water_match_mirror(oracle, hctx):
     e = scaled_errors(gpu, mir, body_lengths(sc))
     for k, v in e.items():
         assert np.max(v[cross]) < 1e-4, (k, float(np.max(v[cross])))
+
+
+@pytest.mark.parametrize("floats_per_vertex", [6, 11])
+def test_reference_vertex_layouts_upload_bit_identical(oracle, hctx, floats_per_vertex):
+    """A mesh uploaded as the reference stores it -- interleaved Vertex (24 B:
+    position, normal) or TexturableVertex (44 B: position, normal, uv,
+    tangent), OpenGLDataStructs.h:120-155, what Mesh::getVertexDataPointer()
+    and getVertexSize() give -- yields bit-identical face terms and wrenches
+    to the packed 12-byte upload of the same positions."""
+    rng = np.random.default_rng(floats_per_vertex)
+    xyz, faces = meshes.build_icosphere(0.5, 3)
+    aos = rng.standard_normal((len(xyz), floats_per_vertex)).astype(np.float32)
+    aos[:, :3] = xyz
+    m_packed = hctx.upload_mesh(xyz, faces)
+    m_aos = hctx.upload_mesh(aos, faces, stride=4 * floats_per_vertex)
+    sc = scenarios.single_sphere(steps=64, seed=51)
+    st = scenarios.settings()
+    out = []
+    for mid in (m_packed, m_aos):
+        b = sc["bodies"].copy()
+        b["mesh"] = mid
+        terms = [hctx.face_terms(b[i:i + 1], sc["ocean"], st, packed=p) for i in (0, 7) for p in (False, True)]
+        bt = hctx.batch(b["mesh"])
+        io = scenarios.new_wrenches(len(b))
+        bt.compute(b, sc["ocean"], st, io)
+        bt.close()
+        out.append((terms, io))
+    for ta, tb in zip(out[0][0], out[1][0]):
+        assert np.array_equal(ta, tb)
+    for k in list(abi.WRENCH_VECTORS) + ["Swet", "Vsub", "position"]:
+        assert np.array_equal(out[0][1][k], out[1][1][k]), k

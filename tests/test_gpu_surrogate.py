@@ -314,3 +314,110 @@ def test_fused_tensor_core_inference_matches_gemm_path(hctx, n):
     med = np.median(np.abs(got - ref), axis=0) / scale
     assert np.all(med < 1e-3), med
     assert np.all(out[n:].cpu().numpy() == 0.0)      # rows past n are not written
+
+
+def _oracle_tc_forward(x_norm_bf16, Ws_bf16, bs, silu_rounding=True):
+    """oracle/mlp.py's forward with the fused kernel's rounding points: BF16
+    inputs and weights, FP32 pre-activations, BF16 hidden activations, FP32
+    output.  Returns (a1, a2, a3, out), a_l the BF16 output of hidden layer l."""
+    zs, acts = mlp.forward(x_norm_bf16, Ws_bf16, bs, bf16=True)
+    return acts[1], acts[2], acts[3], zs[3]
+
+
+def _pack_image(hctx, Wt_bf16):
+    """The kernel's operand image from four transposed BF16 weight matrices
+    (W0^T 256 x 16 padded to K 64, W1^T, W2^T 256 x 256, W3^T 16 x 256)."""
+    img = torch.zeros(S.TC_IMAGE_BYTES, dtype=torch.uint8, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    for Wt, off, kpad in zip(Wt_bf16, (0, 32768, 163840, 294912), (64, 256, 256, 256)):
+        t = _dev(Wt, torch.bfloat16).contiguous()
+        rows, K = t.shape
+        _ck(hctx, hctx.lib.hydro_nn_pack_sw128(hctx.ctx, C.c_void_p(t.data_ptr()), rows, K, K, kpad,
+                                               C.c_void_p(img.data_ptr() + off), s))
+    torch.cuda.synchronize()
+    return img
+
+
+def _run_tc(hctx, feats, fmean, fistd, img, biases):
+    n = feats.shape[0]
+    out = torch.zeros(((n + 127) // 128 * 128, 16), dtype=torch.float32, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    b = [_dev(x) for x in biases]
+    _ck(hctx, hctx.lib.hydro_nn_mlp_tc(hctx.ctx, C.c_void_p(feats.data_ptr()), n, C.c_void_p(fmean.data_ptr()),
+                                       C.c_void_p(fistd.data_ptr()), C.c_void_p(img.data_ptr()),
+                                       *[C.c_void_p(x.data_ptr()) for x in b], C.c_void_p(out.data_ptr()),
+                                       C.c_void_p(err.data_ptr()), torch.cuda.current_stream().cuda_stream))
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    return out[:n].cpu().numpy()
+
+
+def _random_net(rng, H=256):
+    Ws = [rng.uniform(-1, 1, (16, H)) * np.sqrt(3.0 / 16), rng.uniform(-1, 1, (H, H)) * np.sqrt(3.0 / H),
+          rng.uniform(-1, 1, (H, H)) * np.sqrt(3.0 / H)]
+    bs = [rng.normal(size=H) * 0.3 for _ in range(3)]
+    return [mlp.bf16_round(w.astype(np.float32)) for w in Ws], [b.astype(np.float32) for b in bs]
+
+
+@pytest.mark.parametrize("n", [1000, 65536])
+def test_fused_tensor_core_kernel_against_oracle_layers(hctx, n):
+    """The shipped inference kernel (hydro_nn_mlp_tc) against oracle/mlp.py
+    with the same BF16 rounding points.  The last layer is set to select 16
+    of the 256 third-layer activations (weights 1, bias 0: one exact product
+    each), so the kernel's output is those activations themselves; two runs
+    observe columns 0-15 and 240-255.  Each activation may differ from the
+    oracle's by the BF16 roundings that the FP32 summation order and the
+    kernel's tanh-based SiLU move across a rounding boundary: per layer at
+    most one BF16 step (2^-8 of the value), and over three layers the bar is
+    2^-6 of max(|a|, the row's RMS), with the median under 2^-10.  n = 1000
+    is not a multiple of the kernel's 128-row block; 65536 is the benchmark
+    batch (checked on 4096 of its rows)."""
+    rng = np.random.default_rng(41)
+    Ws, bs = _random_net(rng)
+    f = (rng.normal(size=(n, 16)) * 1.5 + 0.5).astype(np.float32)
+    fmean = rng.normal(size=16).astype(np.float32) * 0.2
+    fistd = rng.uniform(0.5, 1.5, 16).astype(np.float32)
+    x = mlp.bf16_round((f - fmean) * fistd)
+    rows = np.arange(n) if n <= 4096 else np.sort(rng.choice(n, 4096, replace=False))
+    a1, a2, a3, _ = _oracle_tc_forward(x[rows], Ws + [np.zeros((256, 16), np.float32)], bs + [np.zeros(16)])
+    feats, dm, di = _dev(f), _dev(fmean), _dev(fistd)
+    for first in (0, 240):
+        W3 = np.zeros((256, 16), np.float32)
+        W3[first + np.arange(16), np.arange(16)] = 1.0
+        img = _pack_image(hctx, [np.ascontiguousarray(W.T) for W in Ws + [W3]])
+        got = _run_tc(hctx, feats, dm, di, img, bs + [np.zeros(16, np.float32)])[rows]
+        ref = a3[:, first:first + 16]
+        scale = np.maximum(np.abs(ref), np.sqrt(np.mean(a3 * a3, axis=1, keepdims=True)))
+        rel = np.abs(got - ref) / scale
+        assert float(rel.max()) <= 2.0 ** -6, (first, float(rel.max()))
+        assert float(np.median(rel)) <= 2.0 ** -10, (first, float(np.median(rel)))
+
+
+def test_fused_tensor_core_kernel_against_oracle_output(hctx):
+    """The whole network as the gated predictor runs it (trained weights, the
+    target de-normalisation folded into the last layer) against
+    oracle/mlp.py: per output column, max error within 2^-7 and median within
+    2^-10 of the column's scale."""
+    rng = np.random.default_rng(43)
+    n = 3000
+    sur = S.Surrogate(hctx, hidden=256, seed=9, batch=256)
+    feats = _dev(rng.normal(size=(n, S.N_FEAT)) * 1.5 + 0.5)
+    targ = _dev(rng.normal(size=(n, S.N_OUT)) * 40.0 + 5.0)
+    sur.fit_normalisation(feats, targ)
+    sur.fit(feats[: 4 * 256].contiguous(), targ[: 4 * 256].contiguous(), epochs=2, lr=3e-3, warmup=1)
+    tcw = sur.tc_weights()
+    out = torch.zeros(((n + 127) // 128 * 128, 16), dtype=torch.float32, device="cuda")
+    got = sur.infer_tc(feats, out, tcw)[:n, :6].cpu().numpy()
+    # the same weights on the host, rounded where the kernel's image holds them
+    Ws = [_bf16(sur.layers[l]["w16"])[:16 if l == 0 else 256, :256] for l in range(3)]
+    w3 = sur.layers[3]["w"].cpu().numpy().astype(np.float64)
+    w3[:, :S.N_OUT] *= sur.stats["t_std"]
+    Ws.append(mlp.bf16_round(w3[:, :16].astype(np.float32)))
+    bs = [sur.layers[l]["b"].cpu().numpy() for l in range(3)] + [tcw["b"][3].cpu().numpy()]
+    f = feats.cpu().numpy()
+    x = mlp.bf16_round((f - sur.f_mean.cpu().numpy()) * sur.f_istd.cpu().numpy())
+    ref = _oracle_tc_forward(x, Ws, bs)[3][:, :6]
+    scale = np.max(np.abs(ref), axis=0)
+    err = np.abs(got - ref) / scale
+    assert np.all(err.max(axis=0) <= 2.0 ** -7), err.max(axis=0)
+    assert np.all(np.median(err, axis=0) <= 2.0 ** -10), np.median(err, axis=0)
