@@ -184,33 +184,54 @@ def cpu_baseline(sc, threads: int, budget_s: float = 12.0, max_steps: int = 20):
     return float(np.median(times)), len(times)
 
 
-def fp64_error_sample(sc, gpu_io, n: int = 128) -> dict:
-    """Pair-scaled error of the GPU result against the all-FP64 oracle on a
-    seeded sample of active bodies."""
-    from oracle import REF64, Oracle
-    from stonefish_gb300 import abi, scenarios
-    act = np.flatnonzero((gpu_io["position"] == abi.CROSSING_SURFACE) | (gpu_io["position"] == abi.INSIDE))
-    if act.size == 0:
-        return {}
-    rng = np.random.default_rng(0)
-    pick = np.sort(rng.choice(act, size=min(n, act.size), replace=False))
-    bodies = sc["bodies"][pick].copy()
-    ref = scenarios.new_wrenches(len(pick))
-    Oracle().batch(REF64, os.cpu_count() or 1, bodies, sc["meshes"], sc["ocean"],
-                   scenarios.settings(), ref, waves=sc.get("waves"))
-    g = gpu_io[pick]
-    S = np.maximum(np.max(np.stack([np.linalg.norm(ref[k], axis=1) for k in ("Fb", "Fdq", "Fdf")]), axis=0), 1e-300)
+def _pair_scaled(a, c, bodies) -> np.ndarray:
+    """Per-body worst pair-scaled error of wrenches a against c: forces over
+    the body's force scale S = max(|Fb|, |Fdq|, |Fdf|) of c, torques over S
+    times the body's half AABB diagonal."""
+    S = np.maximum(np.max(np.stack([np.linalg.norm(c[k], axis=1) for k in ("Fb", "Fdq", "Fdf")]), axis=0), 1e-300)
     L = 0.5 * np.linalg.norm(bodies["aabb_max"] - bodies["aabb_min"], axis=1)
-    errs = []
-    for k in ("Fb", "Fdq", "Fdf"):
-        errs.append(np.linalg.norm(g[k] - ref[k], axis=1) / S)
-    for k in ("Tb", "Tdq", "Tdf"):
-        errs.append(np.linalg.norm(g[k] - ref[k], axis=1) / (S * L))
-    e = np.max(np.stack(errs), axis=0)
-    return {"metric": "pair-scaled |x-x64| / force scale (torques / force scale x size)",
-            "median": float(np.median(e)), "p99": float(np.percentile(e, 99)),
-            "max": float(e.max()), "frac_le_1e-5": float(np.mean(e <= 1e-5)),
-            "sample_bodies": int(len(pick))}
+    errs = [np.linalg.norm(a[k] - c[k], axis=1) / S for k in ("Fb", "Fdq", "Fdf")]
+    errs += [np.linalg.norm(a[k] - c[k], axis=1) / (S * L) for k in ("Tb", "Tdq", "Tdf")]
+    return np.max(np.stack(errs), axis=0)
+
+
+def fp64_error(sc, gpu_io, frame: str) -> dict:
+    """The GPU result against the all-FP64 evaluation on every body with a
+    face loop, next to the reference's own FP32 arithmetic (REF32) on the
+    same bodies; and the GPU against the oracle variant with its own
+    arithmetic (MIRROR32: the reference's FP32 faces with FP64 sums, on the
+    bodies moved to the origin for the centred frame)."""
+    from oracle import MIRROR32, REF32, REF64, Oracle
+    from oracle.oracle import centred_scene
+    from stonefish_gb300 import abi, scenarios
+    act = (gpu_io["position"] == abi.CROSSING_SURFACE) | (gpu_io["position"] == abi.INSIDE)
+    if not act.any():
+        return {}
+    o = Oracle()
+    threads = os.cpu_count() or 1
+    st = scenarios.settings()
+    b = sc["bodies"]
+    out = {}
+    for tag, var, bodies in (("ref64", REF64, b), ("ref32", REF32, b),
+                             ("mirror", MIRROR32, centred_scene(b) if frame == "centred" else b)):
+        io = scenarios.new_wrenches(len(b))
+        o.batch(var, threads, bodies, sc["meshes"], sc["ocean"], st, io, waves=sc.get("waves"))
+        out[tag] = io
+
+    def stats(e):
+        e = e[act]
+        return {"median": float(np.median(e)), "p99": float(np.percentile(e, 99)), "max": float(e.max()),
+                "frac_le_1e-5": float(np.mean(e <= 1e-5))}
+    res = {"metric": "pair-scaled |x-x64| / force scale (torques / force scale x size), every active body",
+           "frame": frame, "bodies": int(act.sum())}
+    res.update(stats(_pair_scaled(gpu_io, out["ref64"], b)))
+    res["reference_fp32_vs_fp64"] = stats(_pair_scaled(out["ref32"], out["ref64"], b))
+    if sc.get("waves") is None or frame == "world":
+        m = _pair_scaled(gpu_io, out["mirror"], b)[act]
+        res["parity_vs_own_arithmetic"] = {"oracle": "MIRROR32" + (" on centred bodies" if frame == "centred" else ""),
+                                          "max": float(m.max()), "positions_equal":
+                                          bool(np.array_equal(gpu_io["position"], out["mirror"]["position"]))}
+    return res
 
 
 # ------------------------------------------------------------- surrogate
@@ -495,7 +516,8 @@ def run_gpu(args, rank: int, world: int, local_rank: int, dist):
     cfg, per_body_faces = workload_config(args.workload, sc)
     log(f"[rank {rank}] workload built in {time.perf_counter() - t0:.1f}s: {cfg}")
     h = HydroContext(device=local_rank, cut_precision=abi.CUT_FP32 if args.cut == "fp32" else abi.CUT_FP64,
-                     tile_faces=args.chunk_faces, ctas_per_sm=args.ctas_per_sm)
+                     tile_faces=args.chunk_faces, ctas_per_sm=args.ctas_per_sm,
+                     frame=abi.FRAME_CENTRED if args.frame == "centred" else abi.FRAME_WORLD)
     t0 = time.perf_counter()
     if sc.get("waves") is not None:
         h.set_wave_grid(sc["waves"])
@@ -631,14 +653,14 @@ def run_gpu(args, rank: int, world: int, local_rank: int, dist):
                              "(profiles/chunk_kernel_batch.txt)"},
         "kernel_ms": kernel_ms,
         "gpu_launches": args.steps * batch.last_launches(),
-        "kernel_config": {"cut": args.cut,
+        "kernel_config": {"cut": args.cut, "frame": args.frame,
                           "chunk_faces": tune["chunk_faces"] if tune else (args.chunk_faces or 4096),
                           "ctas_per_sm": tune["ctas_per_sm"] if tune else (args.ctas_per_sm or 2),
                           "autotune": tune, "cuda_graph": graph is not None},
         "clocks": clocks,
     }
     if not args.no_error:
-        result["error_vs_fp64"] = fp64_error_sample(sc, gpu_io)
+        result["error_vs_fp64"] = fp64_error(sc, gpu_io, args.frame)
     if not args.no_surrogate and world == 1:
         batch.close()
         result["surrogate"] = surrogate_bench(args, local_rank)
@@ -706,6 +728,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-error", action="store_true")
     ap.add_argument("--cut", default="fp32", choices=["fp64", "fp32"])
+    ap.add_argument("--frame", default="centred", choices=["centred", "world"],
+                    help="frame of the FP32 face arithmetic: centred on each body (default) or the "
+                         "reference's world frame")
     ap.add_argument("--chunk-faces", type=int, default=0)
     ap.add_argument("--ctas-per-sm", type=int, default=0)
     ap.add_argument("--no-autotune", action="store_true")

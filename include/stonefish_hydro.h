@@ -88,6 +88,27 @@ enum {
     HYDRO_CUT_FP32 = 1
 };
 
+/* Frame of the FP32 face arithmetic (hydro_set_frame).
+ * HYDRO_FRAME_WORLD (default) is the reference's: the body's transforms are
+ * cast to FP32 as they are (glMatrixFromTransform, OpenGLDataStructs.cpp:
+ * 148-165) and every face is evaluated in world coordinates, so each face's
+ * terms are the reference's bits.  HYDRO_FRAME_CENTRED subtracts the body's
+ * CG x and y (rounded to FP32) in FP64 before the cast and evaluates the
+ * faces in that horizontally centred frame; wave lookups and
+ * position-dependent currents add the offset back.  The physics is the same
+ * (the ocean is level and uniform in x and y), but the FP32 rounding no
+ * longer grows with the body's distance from the world origin: on the
+ * 4096-body mixed batch, whose bodies lie up to 50 m from it, the pair-scaled
+ * error against an all-FP64 evaluation drops from a median of 1.0e-6 and a
+ * 99th percentile of 3.5e-5 to 6e-8 and 2.6e-6.  The fluid position, the
+ * submerged loop's branches and the outputs' meaning are unchanged.  Applies
+ * to the body entry points (batches, single bodies, the allocation-free
+ * step, aerodynamics); compounds and cables keep the world frame. */
+enum {
+    HYDRO_FRAME_WORLD = 0,
+    HYDRO_FRAME_CENTRED = 1
+};
+
 #define HYDRO_MAX_CURRENTS 8
 #define HYDRO_MAX_WAVE_LAYERS 4
 #define HYDRO_NO_MESH 0xFFFFFFFFu   /* stands for the reference's mesh == nullptr */
@@ -222,6 +243,11 @@ void hydro_config_default(hydro_config* cfg);
 
 hydro_status hydro_create(hydro_ctx** ctx, const hydro_config* cfg);
 void hydro_destroy(hydro_ctx* ctx);
+
+/* Selects the frame of the FP32 face arithmetic for later calls on this
+ * context (HYDRO_FRAME_WORLD or HYDRO_FRAME_CENTRED, see above).  No
+ * counterpart in the reference, whose arithmetic is HYDRO_FRAME_WORLD. */
+hydro_status hydro_set_frame(hydro_ctx* ctx, int32_t frame);
 
 /* Message of the last failing call on this context (never NULL). */
 const char* hydro_last_error(const hydro_ctx* ctx);

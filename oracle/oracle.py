@@ -36,6 +36,24 @@ def build_oracle(force: bool = False) -> str:
     return path
 
 
+def centred_scene(bodies: np.ndarray) -> np.ndarray:
+    """The bodies shifted so that each one's CG x and y, rounded to FP32, sit
+    at the origin: the scene that the library's HYDRO_FRAME_CENTRED evaluates,
+    written as a world-frame scene (equivalent for a level ocean with
+    position-independent currents, whose forces do not depend on x and y)."""
+    b = bodies.copy()
+    ox = b["T_CG"]["origin"][:, 0].astype(np.float32).astype(np.float64)
+    oy = b["T_CG"]["origin"][:, 1].astype(np.float32).astype(np.float64)
+    for key in ("T_CG", "T_C"):
+        b[key]["origin"][:, 0] -= ox
+        b[key]["origin"][:, 1] -= oy
+    b["aabb_min"][:, 0] -= ox
+    b["aabb_max"][:, 0] -= ox
+    b["aabb_min"][:, 1] -= oy
+    b["aabb_max"][:, 1] -= oy
+    return b
+
+
 class OracleMesh(C.Structure):
     _fields_ = [("xyz", C.c_void_p), ("stride", C.c_uint32), ("n_vertices", C.c_uint32),
                 ("idx", C.c_void_p), ("n_faces", C.c_uint32)]

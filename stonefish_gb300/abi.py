@@ -36,6 +36,7 @@ INSIDE, OUTSIDE, CROSSING_SURFACE, SKIPPED = 0, 1, 2, -1
 # VelocityFieldType
 CURRENT_UNIFORM, CURRENT_JET, CURRENT_PIPE = 0, 1, 2
 CUT_FP64, CUT_FP32 = 0, 1
+FRAME_WORLD, FRAME_CENTRED = 0, 1
 ABI_VERSION = 1     # HYDRO_ABI_VERSION
 MAX_CURRENTS = 8
 MAX_WAVE_LAYERS = 4
@@ -216,6 +217,7 @@ def _declare(lib: C.CDLL) -> None:
         "hydro_last_error": (C.c_char_p, [vp]),
         "hydro_status_string": (C.c_char_p, [i32]),
         "hydro_abi_version": (i32, []),
+        "hydro_set_frame": (i32, [vp, i32]),
         "hydro_mesh_upload": (i32, [vp, vp, C.c_size_t, u32, vp, u32, C.POINTER(u32)]),
         "hydro_mesh_info": (i32, [vp, u32, C.POINTER(u32), C.POINTER(u32), C.POINTER(u32)]),
         "hydro_wave_grid_set": (i32, [vp, vp, u32, u32, u32, vp, vp]),

@@ -63,6 +63,7 @@ struct hydro_ctx {
     void* small_d = nullptr;   // scratch for the small entry points
     size_t small_cap = 0;
     std::string tune_path;     // autotuner cache file ("" = none)
+    int frame = HYDRO_FRAME_WORLD;   // body-op frame (hydro_set_frame)
     double* cable_seg = nullptr;   // cable segment scratch (9 doubles per node)
     size_t cable_cap = 0;
     void* cable_stage = nullptr;   // host-buffer cable call staging
@@ -86,6 +87,7 @@ struct hydro_batch {
     cudaStream_t stream = nullptr;
     uint32_t last_launches = 0;
     uint32_t chunk_tiles = 0;    // tiles per work chunk of this batch
+    uint32_t class_start[kClaimClasses + 1] = {};   // claim-class regions of the active list
     uint32_t ctas_per_sm = 0;    // 0 = the context's setting
     hydro_aero_params* aparams_d = nullptr;   // staging for the host-buffer aerodynamic call
     hydro_aero_wrench* aio_d = nullptr;
@@ -337,6 +339,7 @@ hydro_status build_work(hydro_ctx* ctx, hydro_batch* b, uint32_t tpc)
     b->active_d = nullptr;
     b->n_chunks = (uint32_t)chunks.size();
     b->chunk_tiles = tpc;
+    claim_class_starts(chunks.data(), chunks.size(), b->class_start);
     CK(ctx, cudaMalloc(&b->chunks_d, chunks.size() * sizeof(ChunkDesc)));
     CK(ctx, cudaMalloc(&b->binfo_d, n * sizeof(BodyInfo)));
     CK(ctx, cudaMalloc(&b->partials_d, chunks.size() * kPartialStride * sizeof(double)));
@@ -413,6 +416,8 @@ hydro_status batch_launch(hydro_batch* b, const hydro_body* d_bodies, const hydr
     P.st.damping = settings->damping_forces ? 1 : 0;
     P.st.buoyancy = settings->realistic_buoyancy ? 1 : 0;
     P.op = op;
+    P.frame = ctx->frame;
+    std::memcpy(P.class_start, b->class_start, sizeof(P.class_start));
     if (P.ocean.waves && ctx->wave_d == nullptr)
         return fail(ctx, HYDRO_ERR_INVALID_ARG, "ocean.waves set but no wave grid was given");
     const int cut64 = ctx->cfg.cut_precision == HYDRO_CUT_FP64;
@@ -490,6 +495,16 @@ void hydro_config_default(hydro_config* cfg)
 }
 
 int hydro_abi_version(void) { return HYDRO_ABI_VERSION; }
+
+hydro_status hydro_set_frame(hydro_ctx* ctx, int32_t frame)
+{
+    if (!ctx) return HYDRO_ERR_INVALID_ARG;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (frame != HYDRO_FRAME_WORLD && frame != HYDRO_FRAME_CENTRED)
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "frame %d: not HYDRO_FRAME_WORLD or HYDRO_FRAME_CENTRED", frame);
+    ctx->frame = frame;
+    return HYDRO_OK;
+}
 
 const char* hydro_status_string(hydro_status s)
 {
@@ -1215,6 +1230,7 @@ hydro_status compound_launch(hydro_compound_batch* cb, const hydro_body* d_compo
         P.active = b->active_d;
         P.n_bodies = b->n_bodies;
         P.n_chunks = b->n_chunks;
+        std::memcpy(P.class_start, b->class_start, sizeof(P.class_start));
         err = b->err_d;
     } else {
         // no parts at all: a scratch error word from the context
@@ -1717,8 +1733,8 @@ hydro_status hydro_debug_face_terms(hydro_ctx* ctx, const hydro_body* body, cons
     CK(ctx, cudaMemcpyAsync(db, body, sizeof(hydro_body), cudaMemcpyHostToDevice, ctx->stream));
     SettingsDev sd{settings->damping_forces ? 1 : 0, settings->realistic_buoyancy ? 1 : 0};
     cudaError_t e = launch_face_terms(ctx->tiles_d, m.first_tile, m.n_tiles, db, make_ocean(ctx, ocean), sd,
-                                      ctx->cfg.cut_precision == HYDRO_CUT_FP64, packed ? 1 : 0, dout,
-                                      ctx->stream);
+                                      ctx->frame, ctx->cfg.cut_precision == HYDRO_CUT_FP64, packed ? 1 : 0,
+                                      dout, ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "face terms kernel");
     CK(ctx, cudaMemcpyAsync(out, dout, terms, cudaMemcpyDeviceToHost, ctx->stream));
     CK(ctx, cudaStreamSynchronize(ctx->stream));
@@ -2251,6 +2267,8 @@ extern "C" hydro_status hydro_compute_wrenches_static(hydro_ctx* ctx, const hydr
     P.st.damping = settings->damping_forces ? 1 : 0;
     P.st.buoyancy = settings->realistic_buoyancy ? 1 : 0;
     P.op = OP_BODY;
+    P.frame = ctx->frame;
+    claim_class_starts(g_static_chunks, nc, P.class_start);
     const int cut64 = ctx->cfg.cut_precision == HYDRO_CUT_FP64;
     LaunchShape shape{};
     const int want = ctx->cfg.ctas_per_sm ? (int)ctx->cfg.ctas_per_sm : 2;

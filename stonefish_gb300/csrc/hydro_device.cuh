@@ -79,6 +79,10 @@ __host__ __device__ __forceinline__ uint32_t tile_block_bytes(uint32_t nv, uint3
 }
 
 constexpr int kMaxTilesPerChunk = 16;
+// The active-chunk list is claimed largest chunks first, in one class per
+// tile count: the last chunks a persistent CTA takes are the short ones, so
+// the SMs run out of work at nearly the same time.
+constexpr int kClaimClasses = kMaxTilesPerChunk;
 
 // One work item: tiles [first_tile, first_tile + n_tiles) of one body.
 struct __align__(16) ChunkDesc {
@@ -89,9 +93,9 @@ struct __align__(16) ChunkDesc {
 };
 
 // A chunk whose body runs a face loop in this launch: the prep kernels
-// append one per such chunk (in the order their atomics land, which no
-// result depends on: every chunk writes its own partial) and the chunk
-// kernel's producers claim them in list order.
+// append one per such chunk to the region of its claim class (in the order
+// their atomics land, which no result depends on: every chunk writes its own
+// partial) and the chunk kernel's producers claim them class by class.
 struct __align__(16) ActiveChunk {
     uint32_t body;
     uint32_t first_tile;
@@ -196,13 +200,20 @@ struct __align__(16) BodyParams {
     int damping;
     int position;     // BodyFluidPosition or HYDRO_SKIPPED
     int mismatch;     // body.mesh differs from the batch's mesh
-    int pad[3];
+    // HYDRO_FRAME_CENTRED: TC, p and p0 are relative to (off[0], off[1], 0),
+    // the body's CG x and y rounded to FP32; a point's world x and y are the
+    // local ones plus off (wave lookups, position-dependent currents).
+    float off[2];
+    int centred;
 };
 static_assert(sizeof(BodyParams) == 128, "BodyParams is staged as a 128-byte block");
 static_assert(offsetof(BodyParams, p) == 48 && offsetof(BodyParams, p0) == 60 && offsetof(BodyParams, v) == 72 &&
                   offsetof(BodyParams, omega) == 84 && offsetof(BodyParams, loop) == 96 &&
                   offsetof(BodyParams, buoyancy) == 100 && offsetof(BodyParams, damping) == 104,
               "the chunk kernel reads BodyParams bytes 48..111 as four 16-byte words");
+static_assert(offsetof(BodyParams, mismatch) == 112 && offsetof(BodyParams, off) == 116 &&
+                  offsetof(BodyParams, centred) == 124,
+              "the chunk kernel reads the frame offset as BodyParams bytes 112..127");
 
 __device__ __forceinline__ v3 xform(const float* M, float x, float y, float z)
 {
@@ -352,6 +363,34 @@ __device__ __forceinline__ v3 fluid_velocity(const OceanDev& o, v3 pt)
     return mk((float)fv[0], (float)fv[1], (float)fv[2]);
 }
 
+// The same queries for a point given in a body's frame: the world frame, or
+// the centred one of HYDRO_FRAME_CENTRED (local x, y plus the body's offset;
+// the offset enters the currents in FP64).
+__device__ __forceinline__ float depth_at_b(const OceanDev& o, const BodyParams& B, float x, float y, float z)
+{
+    if (!o.waves) return z;
+    if (B.centred) return z - wave_height(o, x + B.off[0], y + B.off[1]);
+    return z - wave_height(o, x, y);
+}
+
+__device__ __forceinline__ v3 fluid_velocity_b(const OceanDev& o, const BodyParams& B, v3 pt)
+{
+    if (!o.field_currents) return mk(o.U[0], o.U[1], o.U[2]);
+    if (!B.centred) return fluid_velocity(o, pt);
+    double p[3] = {(double)pt.x + (double)B.off[0], (double)pt.y + (double)B.off[1], (double)pt.z};
+    double fv[3] = {0.0, 0.0, 0.0};
+    for (int i = 0; i < o.n_currents; ++i) {
+        const hydro_current& c = o.currents[i];
+        if (!c.enabled) continue;
+        double u[3] = {0.0, 0.0, 0.0};
+        if (c.type == HYDRO_CURRENT_UNIFORM) { u[0] = c.vel[0]; u[1] = c.vel[1]; u[2] = c.vel[2]; }
+        else if (c.type == HYDRO_CURRENT_JET) jet_velocity(c, p, u);
+        else if (c.type == HYDRO_CURRENT_PIPE) pipe_velocity(c, p, u);
+        fv[0] += u[0]; fv[1] += u[1]; fv[2] += u[2];
+    }
+    return mk((float)fv[0], (float)fv[1], (float)fv[2]);
+}
+
 // ------------------------------------------------------- per-face terms
 // Running FP32 sums of one thread (or the terms of one face).
 struct Acc {
@@ -393,7 +432,7 @@ __device__ __forceinline__ void damping(const OceanDev& o, const BodyParams& B, 
                                         v3 fc, v3 fn1, float A)
 {
     v3 r = sub(fc, B.p);
-    v3 vc = sub(fluid_velocity(o, fc), add(B.v, cross(B.omega, r)));
+    v3 vc = sub(fluid_velocity_b(o, B, fc), add(B.v, cross(B.omega, r)));
     float vc_n = dot(vc, fn1);
     v3 vn = mk(vc_n * fn1.x, vc_n * fn1.y, vc_n * fn1.z);
     v3 vt = sub(vc, vn);
@@ -437,7 +476,7 @@ __device__ __forceinline__ void face_aero(const OceanDev& o, const BodyParams& B
     float A;
     if (!tri_props(p1, p2, p3, fc, fn1, A)) return;
     const v3 r = sub(fc, B.p);
-    const v3 vc = sub(fluid_velocity(o, fc), add(B.v, cross(B.omega, r)));
+    const v3 vc = sub(fluid_velocity_b(o, B, fc), add(B.v, cross(B.omega, r)));
     const float s = dot(vc, fn1);
     const v3 vn = mk(s * fn1.x, s * fn1.y, s * fn1.z);
     if (dot(fn1, vn) < -1e-12f) {
@@ -455,7 +494,7 @@ __device__ __forceinline__ void face_forces(const OceanDev& o, const BodyParams&
                                             v3 fc, v3 fn1, float A)
 {
     if (WAVES && B.buoyancy) {
-        float depthc = depth_at(o, fc.x, fc.y, fc.z);
+        float depthc = depth_at_b(o, B, fc.x, fc.y, fc.z);
         v3 Fbi = mul(mul(neg(fn1), A), depthc);
         acc_add3(a, Q_FB, Fbi);
         acc_add3(a, Q_TB, cross(sub(fc, B.p), Fbi));

@@ -17,8 +17,8 @@ struct KParams {
     BodyParams* bparams;     // per body, written by the prep kernel
     double* partials;        // n_chunks * kPartialStride
     unsigned* err;           // per-launch error word (bit 0: a bounded wait timed out)
-    unsigned* work;          // chunk counter of the persistent kernel
-    unsigned* n_listed;      // length of `active` (atomicAdd in prep, reset by finalize)
+    unsigned* work;          // kClaimClasses claim counters of the persistent kernel (reset by prep)
+    unsigned* n_listed;      // kClaimClasses counts of listed chunks (atomicAdd in prep, reset by finalize)
     const uint32_t* n_active;  // optional (device): only bodies [0, *n_active) are evaluated
     hydro_aero_wrench* aero_io;            // OP_AERO / OP_AERO_BODY outputs
     const hydro_aero_params* aero_params;  // OP_AERO_BODY correction inputs
@@ -28,7 +28,28 @@ struct KParams {
     OceanDev ocean;
     SettingsDev st;
     int op;                  // OP_BODY / OP_SURFACE / OP_SUBMERGED
+    int frame;               // HYDRO_FRAME_WORLD / HYDRO_FRAME_CENTRED (body ops)
+    // The list of active chunks is kept in claim classes by tile count,
+    // largest first: class c (chunks of kMaxTilesPerChunk - c tiles) owns
+    // active[class_start[c], class_start[c + 1]).
+    uint32_t class_start[kClaimClasses + 1];
 };
+
+// Claim class of a chunk of n_tiles tiles (largest chunks first), and the
+// class regions of a work list (exclusive prefix sums of the class sizes).
+__host__ __device__ inline uint32_t claim_class(uint32_t n_tiles)
+{
+    const uint32_t t = n_tiles < 1u ? 1u : (n_tiles > (uint32_t)kMaxTilesPerChunk ? (uint32_t)kMaxTilesPerChunk : n_tiles);
+    return (uint32_t)kMaxTilesPerChunk - t;
+}
+
+inline void claim_class_starts(const ChunkDesc* chunks, size_t n, uint32_t* starts)
+{
+    uint32_t count[kClaimClasses] = {};
+    for (size_t i = 0; i < n; ++i) ++count[claim_class(chunks[i].n_tiles)];
+    starts[0] = 0;
+    for (int c = 0; c < kClaimClasses; ++c) starts[c + 1] = starts[c] + count[c];
+}
 
 // Compounds: the KParams bodies are the parts; these describe the grouping.
 struct CompoundInfo {
@@ -71,7 +92,7 @@ cudaError_t launch_step(const KParams& P, LaunchShape shape, int cut64, cudaStre
 // fully submerged faces through the packed FP32 path, 0 uses the scalar
 // path for every face.
 cudaError_t launch_face_terms(const TileDesc* tiles, uint32_t first_tile, uint32_t n_tiles,
-                             const hydro_body* body, OceanDev ocean, SettingsDev st,
+                             const hydro_body* body, OceanDev ocean, SettingsDev st, int frame,
                              int cut64, int packed, float* out, cudaStream_t s);
 
 // CorrectHydrodynamicForces on 4 vectors (io: Fdq, Tdq, Fdf, Tdf), one thread.

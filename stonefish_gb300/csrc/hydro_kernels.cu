@@ -145,7 +145,7 @@ __device__ void finalize_surface(const OceanDev& o, int buoyancy, int damping,
 // --------------------------------------------------------------- prologue
 // Per-body FP32 parameters and loop kind (SolidEntity.cpp:1799-1846).
 __device__ void body_prologue(const hydro_body* b, uint32_t batch_mesh, int op, const OceanDev& o,
-                              SettingsDev st, BodyParams& B)
+                              SettingsDev st, int frame, BodyParams& B)
 {
     int loop = LOOP_NONE, pos = HYDRO_SKIPPED, buoy = st.buoyancy, damp = st.damping;
     const int mismatch = (b->mesh != batch_mesh);
@@ -176,12 +176,28 @@ __device__ void body_prologue(const hydro_body* b, uint32_t batch_mesh, int op, 
         if (op == OP_SUBMERGED) damp = 1;
     }
     if (batch_mesh == HYDRO_NO_MESH) loop = LOOP_NONE;
+    // HYDRO_FRAME_CENTRED: translations relative to the CG's x and y rounded
+    // to FP32, subtracted in FP64 before the cast, so that the face
+    // arithmetic works on coordinates of the body's size instead of its
+    // distance from the world origin.  HYDRO_FRAME_WORLD (default): the
+    // reference's casts (glMatrixFromTransform, OpenGLDataStructs.cpp:148-165).
+    const bool centred = frame == HYDRO_FRAME_CENTRED;
+    const float ox = centred ? (float)b->T_CG.origin[0] : 0.f;
+    const float oy = centred ? (float)b->T_CG.origin[1] : 0.f;
+    const double shift[3] = {(double)ox, (double)oy, 0.0};
     for (int r = 0; r < 3; ++r) {
         for (int c = 0; c < 3; ++c) B.TC[4 * r + c] = (float)b->T_C.basis[3 * r + c];
-        B.TC[4 * r + 3] = (float)b->T_C.origin[r];
+        B.TC[4 * r + 3] = centred ? (float)(b->T_C.origin[r] - shift[r]) : (float)b->T_C.origin[r];
     }
-    B.p = mk((float)b->T_CG.origin[0], (float)b->T_CG.origin[1], (float)b->T_CG.origin[2]);
+    if (centred)
+        B.p = mk((float)(b->T_CG.origin[0] - shift[0]), (float)(b->T_CG.origin[1] - shift[1]),
+                 (float)b->T_CG.origin[2]);
+    else
+        B.p = mk((float)b->T_CG.origin[0], (float)b->T_CG.origin[1], (float)b->T_CG.origin[2]);
     B.p0 = mk(B.p.x, B.p.y, 0.f);
+    B.off[0] = ox;
+    B.off[1] = oy;
+    B.centred = centred ? 1 : 0;
     B.v = mk((float)b->v[0], (float)b->v[1], (float)b->v[2]);
     B.omega = mk((float)b->omega[0], (float)b->omega[1], (float)b->omega[2]);
     B.loop = loop;
@@ -189,7 +205,14 @@ __device__ void body_prologue(const hydro_body* b, uint32_t batch_mesh, int op, 
     B.damping = damp;
     B.position = pos;
     B.mismatch = mismatch;
-    B.pad[0] = B.pad[1] = B.pad[2] = 0;
+}
+
+// The CG origin in the frame of the body's FP32 parameters (FP64).
+__device__ __forceinline__ void frame_origin(const hydro_body* b, const BodyParams& B, double* og)
+{
+    og[0] = B.centred ? b->T_CG.origin[0] - (double)B.off[0] : b->T_CG.origin[0];
+    og[1] = B.centred ? b->T_CG.origin[1] - (double)B.off[1] : b->T_CG.origin[1];
+    og[2] = b->T_CG.origin[2];
 }
 
 // CorrectAerodynamicForces (SolidEntity.cpp:1925-1956): both vectors scaled
@@ -280,8 +303,9 @@ __device__ void body_finalize(const KParams& P, uint32_t body, const BodyParams&
             w.Swet = 0.0;
             w.Vsub = 0.0;
         } else {
-            finalize_surface(P.ocean, B.buoyancy, B.damping, b->T_CG.origin,
-                             (double)B.p0.x, (double)B.p0.y, S, w);
+            double og[3];
+            frame_origin(b, B, og);
+            finalize_surface(P.ocean, B.buoyancy, B.damping, og, (double)B.p0.x, (double)B.p0.y, S, w);
         }
     } else if (P.op == OP_SUBMERGED) {
         copy3(w.Fdq, S + Q_FDQ);
@@ -324,8 +348,9 @@ __device__ void body_finalize(const KParams& P, uint32_t body, const BodyParams&
                 w.Swet = 0.0;
                 w.Vsub = 0.0;
             } else {
-                finalize_surface(P.ocean, B.buoyancy, B.damping, b->T_CG.origin,
-                                 (double)B.p0.x, (double)B.p0.y, S, w);
+                double og[3];
+                frame_origin(b, B, og);
+                finalize_surface(P.ocean, B.buoyancy, B.damping, og, (double)B.p0.x, (double)B.p0.y, S, w);
             }
             if (B.damping) {
                 if (defer) *correct = true;
@@ -504,35 +529,32 @@ __device__ __forceinline__ void prefetch_lines(const void* p, size_t bytes, int 
 
 // Appends the chunks of a body that runs a face loop (`n` of them, 0 for a
 // body without one or a lane without a body) to the launch's list of active
-// chunks, so that the producers never claim the chunks of bodies outside
-// the water or switched off.  Called by all 32 lanes of a warp: one atomic
-// per warp reserves the run of its lanes' chunks, whose counts are
-// prefix-summed with shuffles.
+// chunks, each into the region of its claim class (its tile count), so that
+// the producers never claim the chunks of bodies outside the water or
+// switched off, and claim the largest chunks first.  Called by all 32 lanes
+// of a warp: round j places every lane's j-th chunk, the lanes whose chunks
+// share a class taking consecutive slots with one atomic.
 __device__ __forceinline__ void list_chunks(const KParams& P, uint32_t body, const BodyInfo& bi, uint32_t n)
 {
-    const int lane = (int)(threadIdx.x & 31u);
-    uint32_t incl = n;
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned lt = (1u << lane) - 1u;
+    uint32_t rounds = n;
 #pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
-        if (lane >= d) incl += y;
-    }
-    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-    uint32_t base = 0;
-    if (lane == 0 && total) base = atomicAdd(P.n_listed, total);
-    base = __shfl_sync(0xffffffffu, base, 0) + incl - n;
-    // four descriptors are requested before any entry is written (the
-    // stores would otherwise order each load behind the previous store)
+    for (int d = 16; d > 0; d >>= 1) rounds = max(rounds, __shfl_xor_sync(0xffffffffu, rounds, d));
     const uint4* src = reinterpret_cast<const uint4*>(P.chunks + bi.first_chunk);
-    uint4* dst = reinterpret_cast<uint4*>(P.active + base);
-    for (uint32_t c0 = 0; c0 < n; c0 += 4) {
-        uint4 d[4];
-#pragma unroll
-        for (uint32_t j = 0; j < 4; ++j)
-            if (c0 + j < n) d[j] = __ldg(src + c0 + j);
-#pragma unroll
-        for (uint32_t j = 0; j < 4; ++j)   // ActiveChunk{body, first_tile, n_tiles, chunk}
-            if (c0 + j < n) dst[c0 + j] = make_uint4(body, d[j].y, d[j].z, bi.first_chunk + c0 + j);
+    for (uint32_t j = 0; j < rounds; ++j) {
+        const bool has = j < n;
+        uint4 d = make_uint4(0u, 0u, 0u, 0u);
+        if (has) d = __ldg(src + j);
+        const uint32_t cls = has ? claim_class(d.z) : 0xFFFFFFFFu;
+        const unsigned same = __match_any_sync(0xffffffffu, cls);
+        const int leader = __ffs(same) - 1;
+        uint32_t base = 0;
+        if (has && (int)lane == leader) base = atomicAdd(P.n_listed + cls, (uint32_t)__popc(same));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (has)   // ActiveChunk{body, first_tile, n_tiles, chunk}
+            reinterpret_cast<uint4*>(P.active)[P.class_start[cls] + base + __popc(same & lt)] =
+                make_uint4(body, d.y, d.z, bi.first_chunk + j);
     }
 }
 
@@ -540,9 +562,9 @@ __device__ __forceinline__ void list_chunks(const KParams& P, uint32_t body, con
 // *n_active of them when a device count is given).
 __global__ void prep_kernel(const KParams P)
 {
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        *P.err = 0u;
-        *P.work = 0u;
+    if (blockIdx.x == 0) {
+        if (threadIdx.x == 0) *P.err = 0u;
+        if (threadIdx.x < (unsigned)kClaimClasses) P.work[threadIdx.x] = 0u;
     }
     const uint32_t limit = P.n_active ? min(P.n_bodies, *P.n_active) : P.n_bodies;
     // warp-uniform grid stride: every lane reaches list_chunks
@@ -555,7 +577,7 @@ __global__ void prep_kernel(const KParams P)
             prefetch_lines(P.bodies + b, sizeof(hydro_body), 0, 1);
             BodyParams B;
             bi = P.binfo[b];
-            body_prologue(P.bodies + b, bi.mesh, P.op, P.ocean, P.st, B);
+            body_prologue(P.bodies + b, bi.mesh, P.op, P.ocean, P.st, P.frame, B);
             P.bparams[b] = B;
             n = B.loop != LOOP_NONE ? bi.n_chunks : 0u;
         }
@@ -666,13 +688,27 @@ __device__ __forceinline__ void producer(const KParams& P, ChunkSmem& S)
 {
     uint32_t item = 0;
     bool ok = true;
-    // claims run one chunk ahead so that the atomic's latency overlaps work;
-    // the list holds only chunks whose body runs a face loop
-    const uint32_t end = min(P.n_chunks, *P.n_listed);
-    uint32_t next = atomicAdd(P.work, 1u);
-    while (ok && next < end) {
+    // Claims go class by class, largest chunks first: a producer moves to the
+    // next class once its claim in the current one comes back past the
+    // class's listed count.  They run one chunk ahead so that the atomic's
+    // latency overlaps work; the list holds only chunks whose body runs a
+    // face loop.
+    uint32_t cls = 0;
+    auto claim = [&]() -> uint32_t {
+        while (cls < (uint32_t)kClaimClasses) {
+            const uint32_t listed = min(P.n_listed[cls], P.class_start[cls + 1] - P.class_start[cls]);
+            if (listed != 0u) {
+                const uint32_t i = atomicAdd(P.work + cls, 1u);
+                if (i < listed) return P.class_start[cls] + i;
+            }
+            ++cls;
+        }
+        return 0xFFFFFFFFu;
+    };
+    uint32_t next = claim();
+    while (ok && next != 0xFFFFFFFFu) {
         const ActiveChunk ch = P.active[next];
-        next = atomicAdd(P.work, 1u);
+        next = claim();
         const uint32_t nt = ch.n_tiles < (uint32_t)kMaxTilesPerChunk ? ch.n_tiles : (uint32_t)kMaxTilesPerChunk;
         TileRef td[kMaxTilesPerChunk];
 #pragma unroll
@@ -741,7 +777,7 @@ __device__ __forceinline__ void transform_tile(const KParams& P, const StageBuf&
     bool above = false, under = false;
     for (int v = threadIdx.x; v < nv; v += kBlock) {
         v3 p = xform(TC, raw[v], raw[nvp + v], raw[2 * nvp + v]);
-        float d = WAVES ? depth_at(P.ocean, p.x, p.y, p.z) : p.z;
+        float d = WAVES ? depth_at_b(P.ocean, st.bp, p.x, p.y, p.z) : p.z;
         out[v] = make_float4(p.x, p.y, p.z, d);
         above |= d < 0.f;
         under |= !(d < 0.f);
@@ -785,6 +821,13 @@ __device__ __forceinline__ int tile_faces(const KParams& P, const StageBuf& st, 
     Bl.v = mk(q1.z, q1.w, q2.x);
     Bl.omega = mk(q2.y, q2.z, q2.w);
     Bl.loop = fl.x; Bl.buoyancy = fl.y; Bl.damping = fl.z;
+    Bl.centred = 0;
+    if (WAVES || P.ocean.field_currents) {      // the frame offset, bytes 112..127
+        const float4 q3 = bq[4];
+        Bl.off[0] = q3.y;
+        Bl.off[1] = q3.z;
+        Bl.centred = __float_as_int(q3.w);
+    }
     const int nf = m.nf, nvp = (m.nv + 3) & ~3;
     const uint32_t* idx = reinterpret_cast<const uint32_t*>(reinterpret_cast<const float*>(st.raw) + 3 * nvp);
     if (Bl.loop == LOOP_AERO) {
@@ -887,7 +930,7 @@ __device__ __forceinline__ int tile_faces(const KParams& P, const StageBuf& st, 
             }
             const BodyPair Bp = body_pair(Bl, P.ocean);
             if (Bl.loop == LOOP_SURFACE) face_full2<WAVES>(P.ocean, Bl, Bp, acc, p1, p2, p3, hasB);
-            else face_submerged2(P.ocean, Bp, acc, p1, p2, p3, hasB);
+            else face_submerged2(P.ocean, Bl, Bp, acc, p1, p2, p3, hasB);
         }
         if (from_queue) {
             pq.head = wrap_pair_queue(pq.head + n);
@@ -1028,7 +1071,8 @@ __global__ void __launch_bounds__(kBodyThreads) finalize_kernel(const KParams P)
     __shared__ double sums[kPerCta][kPartialStride];
     const int sub = (int)(threadIdx.x % kFinSub), slot = (int)(threadIdx.x / kFinSub);
     const int lane = (int)(threadIdx.x & 31u);
-    if (blockIdx.x == 0 && threadIdx.x == 0) *P.n_listed = 0u;   // the chunk kernel has finished with it
+    if (blockIdx.x == 0 && threadIdx.x < (unsigned)kClaimClasses)
+        P.n_listed[threadIdx.x] = 0u;   // the chunk kernel has finished with them
     const uint32_t limit = P.n_active ? min(P.n_bodies, *P.n_active) : P.n_bodies;
     // grid-stride over groups of kPerCta bodies (uniform across the warp)
     for (uint32_t base = blockIdx.x * kPerCta; base < limit; base += gridDim.x * kPerCta) {
@@ -1174,10 +1218,8 @@ __device__ void compound_part_loop(int pos, const hydro_compound_part& pt, Setti
 __global__ void compound_prep_kernel(const KParams P, const CompoundParams C)
 {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p == 0) {
-        *P.err = 0u;
-        *P.work = 0u;
-    }
+    if (p == 0) *P.err = 0u;
+    if (p < (uint32_t)kClaimClasses) P.work[p] = 0u;
     BodyInfo part_info{};
     uint32_t n = 0;
     if (p < P.n_bodies) {
@@ -1202,7 +1244,8 @@ __global__ void compound_prep_kernel(const KParams P, const CompoundParams C)
         B.buoyancy = buoy;
         B.damping = damp;
         B.position = pos;
-        B.pad[0] = B.pad[1] = B.pad[2] = 0;
+        B.off[0] = B.off[1] = 0.f;   // compounds stay in the world frame
+        B.centred = 0;
         P.bparams[p] = B;
         part_info = bi;
         n = B.loop != LOOP_NONE ? bi.n_chunks : 0u;
@@ -1223,7 +1266,7 @@ __device__ __forceinline__ void add3(double* a, const double* b)
 __global__ void __launch_bounds__(kBodyThreads) compound_finalize_kernel(const KParams P, const CompoundParams C)
 {
     const uint32_t c = blockIdx.x * kBodyThreads + threadIdx.x;
-    if (c == 0) *P.n_listed = 0u;
+    if (c < (uint32_t)kClaimClasses) P.n_listed[c] = 0u;
     if (c >= C.n_compounds) return;
     const hydro_body& cb = C.compounds[c];
     const CompoundInfo ci = C.cinfo[c];
@@ -1353,19 +1396,19 @@ cudaError_t launch_compound_step(const KParams& P, const CompoundParams& C, Laun
 template <bool CUT64>
 __global__ void __launch_bounds__(kBlock) face_terms_kernel(const TileDesc* tiles, uint32_t first_tile,
                                                             const hydro_body* body, OceanDev ocean,
-                                                            SettingsDev st, float* out, int packed)
+                                                            SettingsDev st, int frame, float* out, int packed)
 {
     __shared__ float4 verts[kTileVerts];
     __shared__ BodyParams Bs;
     const int tid = threadIdx.x;
     const TileDesc td = tiles[first_tile + blockIdx.x];
-    if (tid == 0) body_prologue(body, body->mesh, OP_SURFACE, ocean, st, Bs);
+    if (tid == 0) body_prologue(body, body->mesh, OP_SURFACE, ocean, st, frame, Bs);
     __syncthreads();
     const BodyParams B = Bs;
     const int nv = td.nv, nvp = (nv + 3) & ~3;
     for (int v = tid; v < nv; v += kBlock) {
         v3 p = xform(B.TC, td.block[v], td.block[nvp + v], td.block[2 * nvp + v]);
-        verts[v] = make_float4(p.x, p.y, p.z, depth_at(ocean, p.x, p.y, p.z));
+        verts[v] = make_float4(p.x, p.y, p.z, depth_at_b(ocean, B, p.x, p.y, p.z));
     }
     __syncthreads();
     const uint32_t* idx = reinterpret_cast<const uint32_t*>(td.block + 3 * nvp);
@@ -1414,12 +1457,14 @@ __global__ void __launch_bounds__(kBlock) face_terms_kernel(const TileDesc* tile
 }
 
 cudaError_t launch_face_terms(const TileDesc* tiles, uint32_t first_tile, uint32_t n_tiles,
-                              const hydro_body* body, OceanDev ocean, SettingsDev st,
+                              const hydro_body* body, OceanDev ocean, SettingsDev st, int frame,
                               int cut64, int packed, float* out, cudaStream_t s)
 {
     if (n_tiles == 0) return cudaSuccess;
-    if (cut64) face_terms_kernel<true><<<n_tiles, kBlock, 0, s>>>(tiles, first_tile, body, ocean, st, out, packed);
-    else face_terms_kernel<false><<<n_tiles, kBlock, 0, s>>>(tiles, first_tile, body, ocean, st, out, packed);
+    if (cut64)
+        face_terms_kernel<true><<<n_tiles, kBlock, 0, s>>>(tiles, first_tile, body, ocean, st, frame, out, packed);
+    else
+        face_terms_kernel<false><<<n_tiles, kBlock, 0, s>>>(tiles, first_tile, body, ocean, st, frame, out, packed);
     return cudaGetLastError();
 }
 

@@ -49,7 +49,7 @@ class HydroContext:
 
     def __init__(self, device: int = 0, cut_precision: int = abi.CUT_FP32,
                  tile_faces: int = 0, ctas_per_sm: int = 0, lib_path: str | None = None,
-                 tune_cache_path: str | None = None):
+                 tune_cache_path: str | None = None, frame: int = abi.FRAME_WORLD):
         self.lib = abi.load_library(lib_path)
         lib = self.lib
         if not hasattr(lib, "_debug_declared"):
@@ -72,6 +72,9 @@ class HydroContext:
         self.ctx = h
         self.device = device
         self.cut_precision = cut_precision
+        self.frame = frame
+        if frame != abi.FRAME_WORLD:
+            self._ck(lib.hydro_set_frame(self.ctx, frame))
         self.mesh_faces: dict[int, int] = {}
 
     def close(self) -> None:

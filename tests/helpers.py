@@ -53,3 +53,6 @@ def body_transform(body, which="T_CG") -> abi.Transform:
     for i in range(3):
         t.origin[i] = float(body[which]["origin"][0][i])
     return t
+
+
+from oracle.oracle import centred_scene  # noqa: E402,F401  (re-exported for the tests)

@@ -303,3 +303,25 @@ def test_variants_share_branches(oracle):
         pos.append(io["position"].copy())
     for p in pos[1:]:
         assert np.array_equal(p, pos[0])
+
+
+def test_centred_scene_is_closer_to_fp64(oracle):
+    """The reference's FP32 arithmetic on bodies moved to the origin (what
+    HYDRO_FRAME_CENTRED evaluates) against the all-FP64 evaluation: the
+    rounding no longer grows with the distance from the world origin."""
+    from tests.helpers import centred_scene
+    sc = scenarios.mixed_batch(n_bodies=400, seed=64, scale_faces=0.1)
+    st = scenarios.settings()
+    r64 = scenarios.new_wrenches(len(sc["bodies"]))
+    oracle.batch(REF64, 8, sc["bodies"], sc["meshes"], sc["ocean"], st, r64)
+    out = {}
+    for tag, bodies in (("world", sc["bodies"]), ("centred", centred_scene(sc["bodies"]))):
+        io = scenarios.new_wrenches(len(bodies))
+        oracle.batch(MIRROR32, 8, bodies, sc["meshes"], sc["ocean"], st, io)
+        assert np.array_equal(io["position"], r64["position"])
+        L = 0.5 * np.linalg.norm(bodies["aabb_max"] - bodies["aabb_min"], axis=1)
+        act = r64["position"] == abi.CROSSING_SURFACE
+        e = scaled_errors(io, r64, L)
+        out[tag] = np.max(np.stack(list(e.values())), axis=0)[act]
+    assert np.median(out["centred"]) < 0.25 * np.median(out["world"])
+    assert np.percentile(out["centred"], 99) < np.percentile(out["world"], 99)
