@@ -127,6 +127,43 @@ def profile_traffic(workload: str):
     return None
 
 
+def profile_instructions(workload: str):
+    """Warp instructions the chunk kernel executes per processed face, from
+    the committed ncu summary (smsp__inst_executed.sum of one launch over its
+    processed faces), or None."""
+    p = os.path.join(HERE, "profiles", f"chunk_kernel_{workload}.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("warp_instructions_per_processed_face:"):
+            return float(line.split(":")[1].split()[0])
+    return None
+
+
+ISSUE_PER_SM_CLOCK = 4     # four SM sub-partitions, each issuing one warp instruction per clock
+
+
+def issue_roofline(workload: str, processed_faces: int, kernel_s: float, sm_mhz) -> dict | None:
+    """The chunk kernel against the SMs' instruction-issue rate: its warp
+    instructions per launch (ncu count per processed face x processed faces)
+    over its CUDA-event time, against SMs x 4 issue slots x the SM clock
+    sampled during the run.  For the shared-mesh workloads (one hull, mesh
+    and wave grid in L2) this, not HBM, is the bound; for the distinct-mesh
+    batch it is the bound the kernel is nearer to."""
+    import torch
+    ipf = profile_instructions(workload)
+    if ipf is None or not sm_mhz or kernel_s <= 0:
+        return None
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    achieved = ipf * processed_faces / kernel_s
+    peak = sms * ISSUE_PER_SM_CLOCK * sm_mhz * 1e6
+    return {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "warp instructions/s",
+            "frac": achieved / peak, "instructions_per_face": ipf, "sm_mhz": sm_mhz, "sms": sms,
+            "rule": "ncu smsp__inst_executed.sum per processed face (profiles/chunk_kernel_<workload>.txt) x "
+                    "processed faces / chunk-kernel time; peak = SMs x 4 warp instructions per clock x "
+                    "median SM clock under load"}
+
+
 def hull_states_workload(faces: int, n_bodies: int, seed: int = 505):
     """The surrogate's torpedo hull (``faces`` faces) at n seeded states over
     the wave field, as an exact-step workload (the CPU reference arm of the
@@ -651,6 +688,8 @@ def run_gpu(args, rank: int, world: int, local_rank: int, dist):
                                    "FP32 vertex: a closed mesh has about half as many vertices as faces)",
                      "note": "the chunk kernel is issue-bound, not HBM-bound "
                              "(profiles/chunk_kernel_batch.txt)"},
+        "issue_roofline": issue_roofline(args.workload, processed_faces, kernel_ms["chunk"] / 1e3,
+                                         clocks.get("sm_mhz")),
         "kernel_ms": kernel_ms,
         "gpu_launches": args.steps * batch.last_launches(),
         "kernel_config": {"cut": args.cut, "frame": args.frame,

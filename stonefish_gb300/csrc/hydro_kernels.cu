@@ -532,30 +532,64 @@ __device__ __forceinline__ void prefetch_lines(const void* p, size_t bytes, int 
 // chunks, each into the region of its claim class (its tile count), so that
 // the producers never claim the chunks of bodies outside the water or
 // switched off, and claim the largest chunks first.  Called by all 32 lanes
-// of a warp: round j places every lane's j-th chunk, the lanes whose chunks
-// share a class taking consecutive slots with one atomic.
+// of a warp.  A body's chunks are full (the work list's tiles per chunk)
+// except its last: the warp's full chunks take one run of their class (one
+// atomic, runs prefix-summed with shuffles, descriptors formed from the
+// body's first chunk), the last chunks one atomic per class present.
 __device__ __forceinline__ void list_chunks(const KParams& P, uint32_t body, const BodyInfo& bi, uint32_t n)
 {
     const unsigned lane = threadIdx.x & 31u;
     const unsigned lt = (1u << lane) - 1u;
-    uint32_t rounds = n;
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) rounds = max(rounds, __shfl_xor_sync(0xffffffffu, rounds, d));
     const uint4* src = reinterpret_cast<const uint4*>(P.chunks + bi.first_chunk);
-    for (uint32_t j = 0; j < rounds; ++j) {
-        const bool has = j < n;
-        uint4 d = make_uint4(0u, 0u, 0u, 0u);
-        if (has) d = __ldg(src + j);
-        const uint32_t cls = has ? claim_class(d.z) : 0xFFFFFFFFu;
-        const unsigned same = __match_any_sync(0xffffffffu, cls);
-        const int leader = __ffs(same) - 1;
-        uint32_t base = 0;
-        if (has && (int)lane == leader) base = atomicAdd(P.n_listed + cls, (uint32_t)__popc(same));
-        base = __shfl_sync(0xffffffffu, base, leader);
-        if (has)   // ActiveChunk{body, first_tile, n_tiles, chunk}
-            reinterpret_cast<uint4*>(P.active)[P.class_start[cls] + base + __popc(same & lt)] =
-                make_uint4(body, d.y, d.z, bi.first_chunk + j);
+    uint4 d0 = make_uint4(0u, 0u, 0u, 0u), dl = d0;
+    if (n > 0u) {
+        d0 = __ldg(src);
+        dl = n > 1u ? __ldg(src + (n - 1u)) : d0;
     }
+    uint4* act = reinterpret_cast<uint4*>(P.active);
+    // full chunks 0 .. n-2: the work lists give every full chunk of a batch
+    // the same tile count, so the warp's full chunks form one run of one
+    // class; a lane whose full chunks were of another class would place
+    // them one atomic each
+    const uint32_t nf = n > 1u ? n - 1u : 0u;
+    const unsigned with_full = __ballot_sync(0xffffffffu, nf > 0u);
+    if (with_full) {
+        const uint32_t cf = claim_class(d0.z);
+        const int leader = __ffs(with_full) - 1;
+        const uint32_t cls = __shfl_sync(0xffffffffu, cf, leader);
+        const bool in_run = nf > 0u && cf == cls;
+        const uint32_t cnt = in_run ? nf : 0u;
+        uint32_t incl = cnt;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+            if ((int)lane >= d) incl += y;
+        }
+        const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+        uint32_t base = 0;
+        if ((int)lane == leader) base = atomicAdd(P.n_listed + cls, total);
+        base = __shfl_sync(0xffffffffu, base, leader) + incl - cnt;
+        if (in_run) {
+            for (uint32_t j = 0; j < nf; ++j)   // ActiveChunk{body, first_tile, n_tiles, chunk}
+                act[P.class_start[cls] + base + j] = make_uint4(body, d0.y + j * d0.z, d0.z, bi.first_chunk + j);
+        } else if (nf > 0u) {
+            for (uint32_t j = 0; j < nf; ++j) {
+                const uint4 dj = __ldg(src + j);
+                const uint32_t c = claim_class(dj.z);
+                act[P.class_start[c] + atomicAdd(P.n_listed + c, 1u)] =
+                    make_uint4(body, dj.y, dj.z, bi.first_chunk + j);
+            }
+        }
+    }
+    // each body's last chunk
+    const uint32_t cl = n > 0u ? claim_class(dl.z) : 0xFFFFFFFFu;
+    const unsigned same = __match_any_sync(0xffffffffu, cl);
+    const int leader = __ffs(same) - 1;
+    uint32_t base = 0;
+    if (n > 0u && (int)lane == leader) base = atomicAdd(P.n_listed + cl, (uint32_t)__popc(same));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (n > 0u)
+        act[P.class_start[cl] + base + __popc(same & lt)] = make_uint4(body, dl.y, dl.z, bi.first_chunk + n - 1u);
 }
 
 // One thread per body, grid-stride over the bodies to evaluate (the first
@@ -869,25 +903,29 @@ __device__ __forceinline__ int tile_faces(const KParams& P, const StageBuf& st, 
         for (int k = 0; k < 2; ++k) {
             const int f = (k * 32 + lane) * kWarps + warp;
             int cls = 0;
-            uint32_t w = 0;
+            // the three corners are read once, whole: their depths classify
+            // the face and their positions fill the queue entry
+            float4 c1 = make_float4(0.f, 0.f, 0.f, 0.f), c2 = c1, c3 = c1;
             if (f < nf) {
-                w = idx[f];
-                cls = face_class(verts[w & 511u].w, verts[(w >> 9) & 511u].w, verts[w >> 18].w);
+                const uint32_t w = idx[f];
+                c1 = verts[w & 511u];
+                c2 = verts[(w >> 9) & 511u];
+                c3 = verts[w >> 18];
+                cls = face_class(c1.w, c2.w, c3.w);
             }
             const unsigned mf = __ballot_sync(0xffffffffu, cls == 1);
             const unsigned mc = __ballot_sync(0xffffffffu, cls == 2);
             if (cls == 1) {
                 float* e = pq.q + 9 * wrap_pair_queue(pq.head + pq.len + nq + __popc(mf & lt));
-                const float4 c1 = verts[w & 511u], c2 = verts[(w >> 9) & 511u], c3 = verts[w >> 18];
                 e[0] = c1.x; e[1] = c1.y; e[2] = c1.z;
                 e[3] = c2.x; e[4] = c2.y; e[5] = c2.z;
                 e[6] = c3.x; e[7] = c3.y; e[8] = c3.z;
             }
             if (cls == 2) {
                 float4* e = cq.q[wrap_queue(cq.head + cq.len + nc + __popc(mc & lt))];
-                e[0] = verts[w & 511u];
-                e[1] = verts[(w >> 9) & 511u];
-                e[2] = verts[w >> 18];
+                e[0] = c1;
+                e[1] = c2;
+                e[2] = c3;
             }
             nq += __popc(mf);
             nc += __popc(mc);
