@@ -849,6 +849,36 @@ hydro_status hydro_nn_route(hydro_ctx* ctx, const hydro_body* d_bodies, const ui
                             uint32_t n, uint32_t* d_counts, hydro_body* d_packed, int32_t* d_pos,
                             uint32_t* d_n_packed, hydro_wrench* d_exact, void* stream);
 
+/* Clears d_mask[i] for the bodies whose fluid position is INSIDE (the AABB
+ * rule of CheckBodyFluidPosition, SolidEntity.cpp:1239-1261): there the
+ * reference uses its analytic buoyancy instead of the face integral
+ * (:1827-1843), a regime the surrogate sees rarely and fits worst, so those
+ * states take the exact step. */
+hydro_status hydro_nn_gate_inside(hydro_ctx* ctx, const hydro_body* d_bodies, uint32_t n,
+                                  const hydro_ocean* ocean, uint8_t* d_mask, void* stream);
+
+/* Two-network ensemble: row i of d_za (row stride ld, columns 0..5 the
+ * body-frame wrench) becomes the mean of the rows of d_za and d_zb, and
+ * d_mask[i] is cleared when the two rows differ by more than tau in the
+ * wrench metric max(|dF| / force_scale, |dT| / torque_scale). */
+hydro_status hydro_nn_ensemble(hydro_ctx* ctx, float* d_za, const float* d_zb, int32_t ld, uint32_t n,
+                               double force_scale, double torque_scale, float tau, uint8_t* d_mask,
+                               void* stream);
+
+/* Audit sample of the gated predictor: for j < k, row i = phase + j * stride
+ * (i < n) that the gate admitted (d_mask[i] != 0) is also sent to the exact
+ * step (its mask cleared) and d_idx[j] = i; otherwise d_idx[j] = -1.  After
+ * the exact step and merge, hydro_nn_audit_error gives each sampled row's
+ * error: d_err[j] = max(|dF| / force_scale, |dT| / torque_scale) of d_z's
+ * row (the network's output) against the exact body-frame wrench
+ * d_exact[d_pos[i]], or -1 for an empty slot. */
+hydro_status hydro_nn_audit_pick(hydro_ctx* ctx, uint8_t* d_mask, uint32_t n, uint32_t stride, uint32_t phase,
+                                 uint32_t k, int32_t* d_idx, void* stream);
+hydro_status hydro_nn_audit_error(hydro_ctx* ctx, const hydro_body* d_bodies, const float* d_z, int32_t ld,
+                                  const int32_t* d_pos, const hydro_wrench* d_exact, const int32_t* d_idx,
+                                  uint32_t k, double force_scale, double torque_scale, float* d_err,
+                                  void* stream);
+
 /* d_out[i][6] = body-frame wrench: columns 0..5 of d_z[i] (row stride ld)
  * when d_pos[i] < 0, else R^T (Fb+Fdq+Fdf, Tb+Tdq+Tdf) of d_exact[d_pos[i]]. */
 hydro_status hydro_nn_merge(hydro_ctx* ctx, const hydro_body* d_bodies, const float* d_z, int32_t ld,

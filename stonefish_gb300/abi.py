@@ -269,6 +269,10 @@ def _declare(lib: C.CDLL) -> None:
         "hydro_compound_compute_device": (i32, [vp, vp, vp, C.POINTER(Ocean), C.POINTER(Settings), vp, vp]),
         "hydro_compound_compute": (i32, [vp, vp, vp, C.POINTER(Ocean), C.POINTER(Settings), vp]),
         "hydro_mesh_compute_properties": (i32, [vp, u32, C.c_double, C.c_double, C.POINTER(MeshProperties)]),
+        "hydro_nn_gate_inside": (i32, [vp, vp, u32, C.POINTER(Ocean), vp, vp]),
+        "hydro_nn_ensemble": (i32, [vp, vp, vp, i32, u32, C.c_double, C.c_double, C.c_float, vp, vp]),
+        "hydro_nn_audit_pick": (i32, [vp, vp, u32, u32, u32, u32, vp, vp]),
+        "hydro_nn_audit_error": (i32, [vp, vp, vp, i32, vp, vp, vp, u32, C.c_double, C.c_double, vp, vp]),
         "hydro_debug_fft_ocean_tables": (i32, [C.POINTER(FftOceanParams), vp, vp, vp, vp]),
         "hydro_fluid_approx": (i32, [vp, C.c_size_t, u32, i32, C.POINTER(Transform), C.POINTER(Transform), d,
                                      C.c_double, C.POINTER(FluidApprox)]),

@@ -2104,6 +2104,49 @@ extern "C" hydro_status hydro_nn_merge(hydro_ctx* ctx, const hydro_body* d_bodie
            "nn merge");
 }
 
+extern "C" hydro_status hydro_nn_gate_inside(hydro_ctx* ctx, const hydro_body* d_bodies, uint32_t n,
+                                             const hydro_ocean* ocean, uint8_t* d_mask, void* stream)
+{
+    NN_CTX_CHECK();
+    if (!d_bodies || !d_mask || !valid_ocean(ocean)) return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn gate inside");
+    if (ocean->waves && !ctx->wave_d) return fail(ctx, HYDRO_ERR_INVALID_ARG, "ocean.waves set but no wave grid");
+    NN_RET(launch_gate_inside(d_bodies, n, make_ocean(ctx, ocean), d_mask, static_cast<cudaStream_t>(stream)),
+           "nn gate inside");
+}
+
+extern "C" hydro_status hydro_nn_ensemble(hydro_ctx* ctx, float* d_za, const float* d_zb, int32_t ld, uint32_t n,
+                                          double force_scale, double torque_scale, float tau, uint8_t* d_mask,
+                                          void* stream)
+{
+    NN_CTX_CHECK();
+    if (!d_za || !d_zb || ld < 6 || !d_mask || !(force_scale > 0.0) || !(torque_scale > 0.0))
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn ensemble");
+    NN_RET(launch_ensemble(d_za, d_zb, ld, n, (float)(1.0 / force_scale), (float)(1.0 / torque_scale), tau, d_mask,
+                           static_cast<cudaStream_t>(stream)), "nn ensemble");
+}
+
+extern "C" hydro_status hydro_nn_audit_pick(hydro_ctx* ctx, uint8_t* d_mask, uint32_t n, uint32_t stride,
+                                            uint32_t phase, uint32_t k, int32_t* d_idx, void* stream)
+{
+    NN_CTX_CHECK();
+    if (!d_mask || !d_idx || stride == 0) return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn audit pick");
+    NN_RET(launch_audit_pick(d_mask, n, stride, phase, k, d_idx, static_cast<cudaStream_t>(stream)), "nn audit pick");
+}
+
+extern "C" hydro_status hydro_nn_audit_error(hydro_ctx* ctx, const hydro_body* d_bodies, const float* d_z,
+                                             int32_t ld, const int32_t* d_pos, const hydro_wrench* d_exact,
+                                             const int32_t* d_idx, uint32_t k, double force_scale,
+                                             double torque_scale, float* d_err, void* stream)
+{
+    NN_CTX_CHECK();
+    if (!d_bodies || !d_z || ld < 6 || !d_pos || !d_exact || !d_idx || !d_err || !(force_scale > 0.0) ||
+        !(torque_scale > 0.0))
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn audit error");
+    NN_RET(launch_audit_error(d_bodies, d_z, ld, d_pos, d_exact, d_idx, k, (float)(1.0 / force_scale),
+                              (float)(1.0 / torque_scale), d_err, static_cast<cudaStream_t>(stream)),
+           "nn audit error");
+}
+
 // ====================================================== rigid-body rollout
 extern "C" hydro_status hydro_rigid_step(hydro_ctx* ctx, hydro_rigid_state* d_states, hydro_body* d_bodies,
                                          const hydro_wrench* d_exact, const float* d_body_wrench, uint32_t n,

@@ -143,6 +143,14 @@ cudaError_t launch_merge(const hydro_body* bodies, const float* z, int ld, const
                          const hydro_wrench* exact, uint32_t n, float* out, cudaStream_t s);
 cudaError_t launch_wrench_body(const hydro_body* bodies, const hydro_wrench* w, uint32_t n, float* out,
                                cudaStream_t s);
+cudaError_t launch_gate_inside(const hydro_body* bodies, uint32_t n, OceanDev o, uint8_t* mask, cudaStream_t s);
+cudaError_t launch_ensemble(float* za, const float* zb, int ld, uint32_t n, float inv_fs, float inv_ts, float tau,
+                            uint8_t* mask, cudaStream_t s);
+cudaError_t launch_audit_pick(uint8_t* mask, uint32_t n, uint32_t stride, uint32_t phase, uint32_t k, int32_t* idx,
+                              cudaStream_t s);
+cudaError_t launch_audit_error(const hydro_body* bodies, const float* z, int ld, const int32_t* pos,
+                               const hydro_wrench* exact, const int32_t* idx, uint32_t k, float inv_fs,
+                               float inv_ts, float* err, cudaStream_t s);
 
 cudaError_t launch_rigid_step(hydro_rigid_state* states, hydro_body* bodies, const hydro_wrench* exact,
                               const float* body_wrench, uint32_t n, double dt, double gravity, cudaStream_t s);

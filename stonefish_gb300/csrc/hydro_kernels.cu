@@ -1506,6 +1506,27 @@ cudaError_t launch_face_terms(const TileDesc* tiles, uint32_t first_tile, uint32
     return cudaGetLastError();
 }
 
+// --------------------------------------------------- surrogate: fluid gate
+// Clears the gate mask of the bodies whose fluid position is INSIDE
+// (CheckBodyFluidPosition, SolidEntity.cpp:1239-1261): the reference
+// switches to its analytic buoyancy there (:1827-1843), a regime the learned
+// surrogate sees rarely and fits worst, so those states go to the exact step.
+__global__ void gate_inside_kernel(const hydro_body* __restrict__ bodies, uint32_t n, OceanDev o,
+                                   uint8_t* __restrict__ mask)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || mask[i] == 0) return;
+    const hydro_body& b = bodies[i];
+    if (classify(o, b.aabb_min, b.aabb_max) == HYDRO_INSIDE) mask[i] = 0;
+}
+
+cudaError_t launch_gate_inside(const hydro_body* bodies, uint32_t n, OceanDev o, uint8_t* mask, cudaStream_t s)
+{
+    if (n == 0) return cudaSuccess;
+    gate_inside_kernel<<<(n + 127) / 128, 128, 0, s>>>(bodies, n, o, mask);
+    return cudaGetLastError();
+}
+
 // ------------------------------------------------------------ small kernels
 __global__ void correct_kernel(double density, double* io, const double* Cd, const double* Cf,
                                const double* R_O)

@@ -612,4 +612,104 @@ cudaError_t launch_merge(const hydro_body* bodies, const float* z, int ld, const
     return cudaGetLastError();
 }
 
+// ------------------------------------------------------ ensemble and audit
+// Two networks' outputs: za (ld floats per row, columns 0..5 the wrench)
+// becomes their mean, and the gate mask of a row is cleared when the two
+// disagree by more than tau in the wrench metric (force difference over the
+// force scale, torque difference over the torque scale, the larger of two).
+__global__ void ensemble_kernel(float* __restrict__ za, const float* __restrict__ zb, int ld, uint32_t n,
+                                float inv_fs, float inv_ts, float tau, uint8_t* __restrict__ mask)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float* a = za + (size_t)i * ld;
+    const float* b = zb + (size_t)i * ld;
+    float df = 0.f, dt = 0.f;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float x = a[k] - b[k], y = a[3 + k] - b[3 + k];
+        df += x * x;
+        dt += y * y;
+    }
+    const float d = fmaxf(sqrtf(df) * inv_fs, sqrtf(dt) * inv_ts);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) a[k] = 0.5f * (a[k] + b[k]);
+    if (d > tau) mask[i] = 0;
+}
+
+cudaError_t launch_ensemble(float* za, const float* zb, int ld, uint32_t n, float inv_fs, float inv_ts, float tau,
+                            uint8_t* mask, cudaStream_t s)
+{
+    if (n == 0) return cudaSuccess;
+    ensemble_kernel<<<(n + 127) / 128, 128, 0, s>>>(za, zb, ld, n, inv_fs, inv_ts, tau, mask);
+    return cudaGetLastError();
+}
+
+// Audit sample: rows phase, phase + stride, ... that the gate admitted are
+// sent to the exact step as well (mask cleared, so their output is the exact
+// wrench) and recorded in idx; other sample slots get -1.
+__global__ void audit_pick_kernel(uint8_t* __restrict__ mask, uint32_t n, uint32_t stride, uint32_t phase,
+                                  uint32_t k, int32_t* __restrict__ idx)
+{
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= k) return;
+    const uint32_t i = phase + j * stride;
+    int32_t r = -1;
+    if (i < n && mask[i] != 0) {
+        mask[i] = 0;
+        r = (int32_t)i;
+    }
+    idx[j] = r;
+}
+
+cudaError_t launch_audit_pick(uint8_t* mask, uint32_t n, uint32_t stride, uint32_t phase, uint32_t k, int32_t* idx,
+                              cudaStream_t s)
+{
+    if (k == 0) return cudaSuccess;
+    audit_pick_kernel<<<(k + 127) / 128, 128, 0, s>>>(mask, n, stride, phase, k, idx);
+    return cudaGetLastError();
+}
+
+// Error of the surrogate's row z[i] against the exact body-frame wrench of
+// each audited row i = idx[j] (exact[pos[i]]): err[j] = max(|dF| / fs,
+// |dT| / ts), or -1 for an empty sample slot.
+__global__ void audit_error_kernel(const hydro_body* __restrict__ bodies, const float* __restrict__ z, int ld,
+                                   const int32_t* __restrict__ pos, const hydro_wrench* __restrict__ exact,
+                                   const int32_t* __restrict__ idx, uint32_t k, float inv_fs, float inv_ts,
+                                   float* __restrict__ err)
+{
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= k) return;
+    const int32_t i = idx[j];
+    if (i < 0 || pos[i] < 0) {
+        err[j] = -1.f;
+        return;
+    }
+    const double* R = bodies[i].T_CG.basis;
+    const hydro_wrench& x = exact[pos[i]];
+    double F[3], T[3];
+    for (int c = 0; c < 3; ++c) {
+        F[c] = x.Fb[c] + x.Fdq[c] + x.Fdf[c];
+        T[c] = x.Tb[c] + x.Tdq[c] + x.Tdf[c];
+    }
+    double df = 0.0, dt = 0.0;
+    for (int c = 0; c < 3; ++c) {
+        const double fb = R[c] * F[0] + R[3 + c] * F[1] + R[6 + c] * F[2];
+        const double tb = R[c] * T[0] + R[3 + c] * T[1] + R[6 + c] * T[2];
+        const double a = (double)z[(size_t)i * ld + c] - fb, b = (double)z[(size_t)i * ld + 3 + c] - tb;
+        df += a * a;
+        dt += b * b;
+    }
+    err[j] = (float)fmax(sqrt(df) * (double)inv_fs, sqrt(dt) * (double)inv_ts);
+}
+
+cudaError_t launch_audit_error(const hydro_body* bodies, const float* z, int ld, const int32_t* pos,
+                               const hydro_wrench* exact, const int32_t* idx, uint32_t k, float inv_fs,
+                               float inv_ts, float* err, cudaStream_t s)
+{
+    if (k == 0) return cudaSuccess;
+    audit_error_kernel<<<(k + 127) / 128, 128, 0, s>>>(bodies, z, ld, pos, exact, idx, k, inv_fs, inv_ts, err);
+    return cudaGetLastError();
+}
+
 }  // namespace sfh

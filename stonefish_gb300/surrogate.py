@@ -448,8 +448,26 @@ class GatedPredictor:
 
     def __init__(self, sur: Surrogate, hctx_exact: HydroContext, mesh_id: int, n: int,
                  ocean: abi.Ocean, settings: abi.Settings, tensor_cores: str = "tcgen05",
-                 fallback_chunk_faces: int | None = None):
+                 fallback_chunk_faces: int | None = None, second: Surrogate | None = None,
+                 tau: float = float("inf"), gate_inside: bool = False, audit_stride: int = 0,
+                 audit_ring: int = 256):
+        """``second``: another network of the same hull; the output is then the
+        mean of the two and states where they disagree by more than ``tau``
+        (wrench metric) take the exact step.  ``gate_inside``: states whose
+        fluid position is INSIDE take the exact step.  ``audit_stride`` > 0:
+        every call also sends rows phase, phase + stride, ... that the gate
+        admitted to the exact step (their output becomes exact) and records
+        the network's error on them (``audit_errors``); the phase advances by
+        one per call."""
         self.s = sur
+        self.second = second
+        self.tau = float(tau)
+        self.gate_inside = gate_inside
+        self.fs, self.ts = hull_scales(ocean)
+        self.audit_stride = int(audit_stride)
+        self.audit_k = (n + audit_stride - 1) // audit_stride if audit_stride else 0
+        self.audit_ring = audit_ring
+        self.audit_calls = 0
         self.h = hctx_exact
         self.lib = hctx_exact.lib
         self.n = n
@@ -476,6 +494,13 @@ class GatedPredictor:
         if tensor_cores == "tcgen05":
             self.tcw = sur.tc_weights()
             self.z16 = torch.zeros((self.n_pad, 16), dtype=torch.float32, device=dev)
+        if second is not None:
+            assert tensor_cores == "tcgen05", "the ensemble runs on the fused tensor-core kernel"
+            self.tcw2 = second.tc_weights()
+            self.z16b = torch.zeros((self.n_pad, 16), dtype=torch.float32, device=dev)
+        if self.audit_k:
+            self.audit_idx = torch.zeros(self.audit_k, dtype=torch.int32, device=dev)
+            self.audit_err = torch.full((audit_ring, self.audit_k), -1.0, dtype=torch.float32, device=dev)
 
     def _ck(self, st):
         _check(self.lib, self.h.ctx, st)
@@ -497,13 +522,27 @@ class GatedPredictor:
         self._ck(self.lib.hydro_nn_features(ctx, bodies, n, C.byref(self.ocean), _ptr(b["feats"]), st))
         self._ck(self.lib.hydro_nn_gate(ctx, _ptr(b["feats"]), n, _ptr(g["lo"]), _ptr(g["hi"]), _ptr(g["mean"]),
                                         _ptr(g["P"]), g["thr"], _ptr(b["mask"]), st))
+        extra = 0
+        if self.gate_inside:
+            self._ck(self.lib.hydro_nn_gate_inside(ctx, bodies, n, C.byref(self.ocean), _ptr(b["mask"]), st))
+            extra += 1
         if self.mode == "tcgen05":
             s.infer_tc(b["feats"], self.z16, self.tcw)
             z, ldz, mlp_launches = self.z16, 16, 1
+            if self.second is not None:
+                self.second.infer_tc(b["feats"], self.z16b, self.tcw2)
+                self._ck(self.lib.hydro_nn_ensemble(ctx, _ptr(self.z16), _ptr(self.z16b), 16, n, self.fs, self.ts,
+                                                    self.tau, _ptr(b["mask"]), st))
+                extra += 2
         else:
             s.to_bf16(b["feats"], self.n_pad, N_FEAT, IN_PAD, b["X0"], s.f_mean, s.f_istd)
             s._mlp(b, self.n_pad)
             z, ldz, mlp_launches = b["z"], OUT_PAD, 5
+        if self.audit_k:
+            phase = self.audit_calls % self.audit_stride
+            self._ck(self.lib.hydro_nn_audit_pick(ctx, _ptr(b["mask"]), n, self.audit_stride, phase, self.audit_k,
+                                                  _ptr(self.audit_idx), st))
+            extra += 1
         self._ck(self.lib.hydro_nn_route(ctx, bodies, _ptr(b["mask"]), n, _ptr(self.counts),
                                          _ptr(self.packed), _ptr(self.pos), _ptr(self.n_packed),
                                          _ptr(self.exact_io), st))
@@ -511,15 +550,63 @@ class GatedPredictor:
                                          self.settings, self.exact_io.data_ptr(), st)
         self._ck(self.lib.hydro_nn_merge(ctx, bodies, _ptr(z), ldz, _ptr(self.pos),
                                          _ptr(self.exact_io), n, _ptr(self.out), st))
-        # features, gate, network, 2 route, exact step, merge
-        self.launches = 1 + 1 + mlp_launches + 2 + self.batch.last_launches() + 1
+        if self.audit_k:
+            row = self.audit_err[self.audit_calls % self.audit_ring]
+            self._ck(self.lib.hydro_nn_audit_error(ctx, bodies, _ptr(z), ldz, _ptr(self.pos), _ptr(self.exact_io),
+                                                   _ptr(self.audit_idx), self.audit_k, self.fs, self.ts, _ptr(row),
+                                                   st))
+            self.audit_calls += 1
+            extra += 1
+        # features, gate (+ inside gate, second network, ensemble, audit), network, 2 route, exact step, merge
+        self.launches = 1 + 1 + mlp_launches + 2 + self.batch.last_launches() + 1 + extra
         return self.out
+
+    def admitted(self) -> np.ndarray:
+        """Rows of the last call whose output is the network's (host bool array)."""
+        return self.pos.cpu().numpy() < 0
+
+    def audit_errors(self) -> np.ndarray:
+        """Errors the exact step measured on the audited rows of the last
+        ``audit_ring`` calls (wrench metric), one value per audited row."""
+        if not self.audit_k:
+            return np.zeros(0)
+        e = self.audit_err.cpu().numpy().reshape(-1)
+        return e[e >= 0.0]
 
     def rejected(self) -> int:
         return int(self.n_packed.item())
 
     def close(self):
         self.batch.close()
+
+
+def calibrate_disagreement(pred_a: np.ndarray, pred_b: np.ndarray, exact: np.ndarray, admitted: np.ndarray,
+                           ocean: abi.Ocean, target_p99: float = 0.01, max_reject: float = 0.04) -> dict:
+    """Threshold on two networks' disagreement for the ensemble gate, from
+    held-out states with exact labels: the smallest rejected fraction (in
+    steps of 0.1%, at most ``max_reject``) whose admitted states have a 99th
+    percentile error (of the mean prediction) at or below ``target_p99``;
+    ``admitted`` marks the states the other gates let through."""
+    fs, ts = hull_scales(ocean)
+    d = np.maximum(np.linalg.norm(pred_a[:, :3] - pred_b[:, :3], axis=1) / fs,
+                   np.linalg.norm(pred_a[:, 3:] - pred_b[:, 3:], axis=1) / ts)
+    mean = 0.5 * (pred_a + pred_b)
+    e = np.maximum(np.linalg.norm(mean[:, :3] - exact[:, :3], axis=1) / fs,
+                   np.linalg.norm(mean[:, 3:] - exact[:, 3:], axis=1) / ts)
+    da, ea = d[admitted], e[admitted]
+    order = np.sort(da)[::-1]
+    best = None
+    for k in range(0, int(max_reject * 1000) + 1):
+        r = k / 1000.0
+        m = int(round(r * len(da)))
+        tau = float(order[m - 1]) if m > 0 else float("inf")
+        keep = da < tau if m > 0 else np.ones(len(da), bool)
+        p99 = float(np.percentile(ea[keep], 99))
+        best = {"tau": tau, "reject_frac": r, "admitted_p99": p99}
+        if p99 <= target_p99:
+            break
+    best["target_p99"] = target_p99
+    return best
 
 
 def wrench_errors(pred: np.ndarray, exact: np.ndarray, ocean: abi.Ocean) -> dict:
