@@ -206,19 +206,43 @@ def workload_config(name: str, sc) -> dict:
     return cfg, per_body_faces
 
 
-def cpu_baseline(sc, threads: int, budget_s: float = 12.0, max_steps: int = 20):
-    """REF32 (the reference's arithmetic, one task per body) on host threads."""
-    from oracle import REF32, Oracle
+def cpu_implementation():
+    """The CPU implementation the CPU legs time.  Where the reference's own
+    hydrodynamics functions were compiled from its sources on this machine
+    (oracle/_ref), those; else the oracle's REF32 restatement (the
+    reference's arithmetic).  Both run one task per body on a thread pool, as
+    SimulationManager.cpp:1620-1655 does.  Returns (run, kind, what) where
+    run(threads, workload, io) runs one step and returns its seconds."""
     from stonefish_gb300 import scenarios
-    o = Oracle()
-    io = scenarios.new_wrenches(len(sc["bodies"]))
     st = scenarios.settings()
+    try:
+        from oracle.ref import Reference
+        if Reference.available():
+            r = Reference()
+            return ((lambda threads, sc, io: r.batch(threads, sc["bodies"], sc["meshes"], sc["ocean"], st, io,
+                                                     waves=sc.get("waves"))),
+                    "reference", "the reference's SolidEntity hydrodynamics compiled from its sources, "
+                                 "one task per body")
+    except (OSError, RuntimeError):
+        pass
+    from oracle import REF32, Oracle
+    o = Oracle()
+    return ((lambda threads, sc, io: o.batch(REF32, threads, sc["bodies"], sc["meshes"], sc["ocean"], st, io,
+                                             waves=sc.get("waves"))),
+            "port", "REF32 oracle restatement of the reference's arithmetic, one task per body "
+                    "(the reference's sources are not on this machine)")
+
+
+def cpu_baseline(sc, threads: int, budget_s: float = 12.0, max_steps: int = 20):
+    """Median seconds of full steps of the workload on host threads."""
+    from stonefish_gb300 import scenarios
+    run, kind, what = cpu_implementation()
+    io = scenarios.new_wrenches(len(sc["bodies"]))
     times = []
     t_start = time.perf_counter()
     while len(times) < max_steps and (time.perf_counter() - t_start) < budget_s:
-        times.append(o.batch(REF32, threads, sc["bodies"], sc["meshes"], sc["ocean"], st, io,
-                             waves=sc.get("waves")))
-    return float(np.median(times)), len(times)
+        times.append(run(threads, sc, io))
+    return float(np.median(times)), len(times), kind, what
 
 
 def _pair_scaled(a, c, bodies) -> np.ndarray:
@@ -312,10 +336,30 @@ def surrogate_bench(args, device: int) -> dict:
     F, T = S.generate(lab, args.sur_train, seed=101)
     torch.cuda.synchronize()
     t_gen = time.perf_counter() - t0
-    sur = S.Surrogate(h32, batch=args.sur_batch)
+    fs_, ts_ = S.hull_scales(ocean)
+    # two networks of the same hull (different seeds), targets scaled as the
+    # wrench metric weighs them
+    sur = S.Surrogate(h32, batch=args.sur_batch, seed=0)
+    sur.fit_normalisation(F, T, target_scales=(fs_, ts_))
     info = sur.fit(F, T, epochs=args.sur_epochs, lr=args.sur_lr)
+    sur2 = S.Surrogate(h32, batch=args.sur_batch, seed=1)
+    sur2.fit_normalisation(F, T, target_scales=(fs_, ts_))
+    info2 = sur2.fit(F, T, epochs=args.sur_epochs, lr=args.sur_lr)
     del F, T
     nB, n_sets = 65536, 8
+    # the ensemble gate's threshold, from held-out labelled states (not the
+    # evaluation states below)
+    cal = S.sample_states(np.random.default_rng(303), nB)
+    Fc = torch.empty((nB, 16), dtype=torch.float32, device="cuda")
+    Tc = torch.empty((nB, 6), dtype=torch.float32, device="cuda")
+    Wc = torch.zeros(nB * abi.WRENCH_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    lab.label(cal, Fc, Tc, wrenches=Wc)
+    zc = torch.zeros((nB, 16), dtype=torch.float32, device="cuda")
+    pa = sur.infer_tc(Fc, zc, sur.tc_weights())[:, :6].cpu().numpy()
+    pb = sur2.infer_tc(Fc, zc, sur2.tc_weights())[:, :6].cpu().numpy()
+    cal_in = Wc.cpu().numpy().view(abi.WRENCH_DTYPE)["position"] != abi.INSIDE
+    calib = S.calibrate_disagreement(pa, pb, Tc.cpu().numpy(), cal_in, ocean, target_p99=0.01, max_reject=0.04)
+    del Fc, Tc, Wc, zc
     rng = np.random.default_rng(202)
     sets, d_sets = [], []
     for _ in range(n_sets):
@@ -326,9 +370,16 @@ def surrogate_bench(args, device: int) -> dict:
     Ft = torch.empty((nB, 16), dtype=torch.float32, device="cuda")
     Tt = torch.empty((nB, 6), dtype=torch.float32, device="cuda")
     lab.label(sets[0], Ft, Tt)
-    gp = S.GatedPredictor(sur, h32, m32, nB, ocean, st)
+    # the network alone, for comparison
+    z1 = torch.zeros((nB, 16), dtype=torch.float32, device="cuda")
+    single = S.wrench_errors(sur.infer_tc(Ft, z1, sur.tc_weights())[:, :6].cpu().numpy(), Tt.cpu().numpy(), ocean)
+    del z1
+    gp = S.GatedPredictor(sur, h32, m32, nB, ocean, st, second=sur2, tau=calib["tau"], gate_inside=True,
+                          audit_stride=1024)
     out = gp.predict(d_sets[0]).cpu().numpy()
+    adm = gp.admitted()
     err = S.wrench_errors(out, Tt.cpu().numpy(), ocean)
+    err_adm = S.wrench_errors(out[adm], Tt.cpu().numpy()[adm], ocean)
     rejected = gp.rejected()
     setup_s = time.perf_counter() - t_setup
 
@@ -390,6 +441,7 @@ def surrogate_bench(args, device: int) -> dict:
         h_out.copy_(gp.predict(h_in), non_blocking=True)
     torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - t0) / e2e_steps
+    audit = gp.audit_errors()
     peak, kind = measured_tensor_peak()
     achieved = MLP_FLOP_PER_EVAL * nB / (ms_mlp / 1e3) / 1e12
     res = {
@@ -398,11 +450,25 @@ def surrogate_bench(args, device: int) -> dict:
         "exact_fp32_gpu": {"value": nB / (ms_exact / 1e3), "unit": UNIT, "ms_per_step": ms_exact,
                            "faces_per_s": nB * len(fc) / (ms_exact / 1e3)},
         "speedup_vs_exact_gpu": ms_exact / ms,
-        "error": dict(err, metric="|dF| / (rho g V), |dT| / (rho g V L/2); wrench = max of the two; "
-                                  "against exact labels (FP32 faces, FP64 cut points and sums)"),
+        "error": dict(err_adm, metric="|dF| / (rho g V), |dT| / (rho g V L/2); wrench = max of the two; "
+                                      "against exact labels (FP32 faces, FP64 cut points and sums); "
+                                      "states whose output is the network's (admitted by the gates)"),
+        "error_all_outputs": dict(err, note="every state of the step; gated and audited states carry the "
+                                            "exact step's wrench"),
+        "error_single_network": dict(single, note="one network, no gates, same states"),
+        "gate": {"rejected_frac": rejected / nB, "rules": "feature box + Mahalanobis radius; fluid position "
+                 "INSIDE; the two networks' disagreement above tau (calibrated on 65536 held-out labelled "
+                 "states for an admitted 99th percentile <= 0.01, at most 4% rejected)", "calibration": calib},
+        "audit": {"rows": int(audit.size), "stride": gp.audit_stride,
+                  "median": float(np.median(audit)) if audit.size else None,
+                  "p99": float(np.percentile(audit, 99)) if audit.size else None,
+                  "max": float(audit.max()) if audit.size else None,
+                  "note": "every predict() also runs every 1024th admitted state through the exact step "
+                          "(its output becomes exact) and records the network's error there"},
         "gate_rejected_frac": rejected / nB,
         "train": {"samples": args.sur_train, "epochs": args.sur_epochs, "batch": args.sur_batch,
-                  "lr": args.sur_lr, "label_s": t_gen, "train_s": info["seconds"],
+                  "networks": 2, "target_scaling": "force / (rho g V), torque / (rho g V L/2)",
+                  "lr": args.sur_lr, "label_s": t_gen, "train_s": info["seconds"] + info2["seconds"],
                   "train_samples_per_s": info["samples_per_s"], "final_loss": info["loss"][-1]},
         "e2e": {"value": nB / e2e_s, "unit": UNIT,
                 "h2d_bytes_per_step": int(nB * abi.BODY_DTYPE.itemsize),
@@ -456,10 +522,12 @@ def rollout_bench(args, device: int) -> dict:
     lab = S.Labeller(h64, m64, ocean, st)
     surf = RO.surface_z(h32, ocean)
     # training envelope of the floating hulls: CG within 0.6 m below to 0.5 m
-    # above the local surface, |v| components to 2 m/s, |omega| to 1 rad/s
-    F, T = S.generate(lab, args.roll_train, seed=303, depth=(-0.5, 0.6), v_range=2.0, w_range=1.0,
+    # above the local surface, |v| components to 2 m/s, |omega| to 2 rad/s
+    # (the hulls' pitch oscillation reaches rates above 1 rad/s)
+    F, T = S.generate(lab, args.roll_train, seed=303, depth=(-0.5, 0.6), v_range=2.0, w_range=2.0,
                       surface=surf)
     sur = S.Surrogate(h32, batch=args.sur_batch)
+    sur.fit_normalisation(F, T, target_scales=S.hull_scales(ocean))
     sur.fit(F, T, epochs=args.sur_epochs, lr=args.sur_lr)
     del F, T
     lab.close()
@@ -707,11 +775,10 @@ def run_gpu(args, rank: int, world: int, local_rank: int, dist):
         result["rollout"] = rollout_bench(args, local_rank)
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        cpu_s, n = cpu_baseline(sc, threads)
-        cpu1_s, n1 = cpu_baseline(sc, 1, budget_s=5.0, max_steps=3)
-        result["cpu_baseline"] = {"value": nb / cpu_s, "unit": UNIT, "cores": threads, "kind": "port",
-                                  "sample": f"median of {n} full steps of the same workload "
-                                            f"(REF32 oracle, one task per body)",
+        cpu_s, n, kind, what = cpu_baseline(sc, threads)
+        cpu1_s, n1, _, _ = cpu_baseline(sc, 1, budget_s=5.0, max_steps=3)
+        result["cpu_baseline"] = {"value": nb / cpu_s, "unit": UNIT, "cores": threads, "kind": kind,
+                                  "sample": f"median of {n} full steps of the same workload ({what})",
                                   "faces_per_s": int(per_body_faces.sum()) / cpu_s,
                                   "value_1_thread": nb / cpu1_s,
                                   "sample_1_thread": f"median of {n1} full steps on one host thread"}
@@ -726,21 +793,18 @@ def run_reference(args, rank: int):
     sc = build_workload(args.workload, args.n_bodies)
     cfg, per_body_faces = workload_config(args.workload, sc)
     threads = os.cpu_count() or 1
-    from oracle import REF32, Oracle
     from stonefish_gb300 import scenarios
-    o = Oracle()
+    run, kind, what = cpu_implementation()
     io = scenarios.new_wrenches(len(sc["bodies"]))
-    st = scenarios.settings()
     # W warm-up steps (at most 5) and up to K timed steps, stopping early once
     # 60 s of CPU time are spent so the run stays within a few minutes
     warmup = max(1, min(args.warmup, 5))
     for _ in range(warmup):
-        o.batch(REF32, threads, sc["bodies"], sc["meshes"], sc["ocean"], st, io, waves=sc.get("waves"))
+        run(threads, sc, io)
     steps = 0
     total = 0.0
     while steps < max(1, args.steps) and (steps == 0 or total < 60.0):
-        total += o.batch(REF32, threads, sc["bodies"], sc["meshes"], sc["ocean"], st, io,
-                         waves=sc.get("waves"))
+        total += run(threads, sc, io)
         steps += 1
     nb = len(sc["bodies"])
     value = nb * steps / total
@@ -750,9 +814,9 @@ def run_reference(args, rank: int):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 faces (reference arithmetic)", "data": "synthetic", "config": cfg,
             "faces_per_s": int(per_body_faces.sum()) * steps / total,
-            "cpu_baseline": {"value": value, "unit": unit, "cores": threads, "kind": "port",
+            "cpu_baseline": {"value": value, "unit": unit, "cores": threads, "kind": kind,
                              "sample": f"{steps} full steps of the workload (at most --steps, "
-                                       f"stopped after 60 s)"},
+                                       f"stopped after 60 s): {what}"},
             "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
@@ -780,7 +844,7 @@ def main():
     ap.add_argument("--roll-steps", type=int, default=1000)
     ap.add_argument("--roll-train", type=int, default=4_000_000)
     ap.add_argument("--sur-train", type=int, default=10_000_000)
-    ap.add_argument("--sur-epochs", type=int, default=6)
+    ap.add_argument("--sur-epochs", type=int, default=16)
     ap.add_argument("--sur-batch", type=int, default=1024)
     ap.add_argument("--sur-lr", type=float, default=1e-3)
     args = ap.parse_args()

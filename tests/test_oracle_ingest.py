@@ -9,6 +9,7 @@ import numpy as np
 import pytest
 
 from oracle import obj as ref_obj
+from oracle.ref import source_root
 from stonefish_gb300 import abi, meshes
 
 RHO = 1000.0
@@ -195,11 +196,16 @@ def test_oracle_sphere(oracle):
     assert math.isclose(p["surface"], meshes.mesh_area(xyz, faces), rel_tol=1e-9)
 
 
-REFERENCE_DATA = os.path.join(os.environ.get("STONEFISH_REFERENCE", "/root/reference"), "Tests", "Data")
+def _reference_data():
+    root = source_root()
+    return None if root is None else os.path.join(root, "Tests", "Data")
+
+
+REFERENCE_DATA = _reference_data()
 
 
 def _reference_objs():
-    if not os.path.isdir(REFERENCE_DATA):
+    if REFERENCE_DATA is None or not os.path.isdir(REFERENCE_DATA):
         return []
     return sorted(f for f in os.listdir(REFERENCE_DATA) if f.endswith(".obj"))
 

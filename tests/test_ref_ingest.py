@@ -204,3 +204,29 @@ def test_properties_and_approx_equal_reference_on_the_hull(oracle):
             assert a["type"] == b["type"]
             for k in APPROX_KEYS:
                 assert np.array_equal(a[k], b[k]), (trial, ap, k)
+
+
+@needs_ref
+def test_submerged_hull_volume_through_the_surface_loop(oracle):
+    """hull_hydro.obj wholly under water through the CROSSING branch's face
+    loop (ComputeHydrodynamicForcesSurface): the reference's code and the
+    oracle's REF32 give the same Vsub bit for bit, equal to the hull's volume
+    0.096699 (FluidDynamicsTestManager.cpp:207), and Fb = -rho g Vsub."""
+    from oracle import REF32
+    from tests.helpers import io_dict
+    from stonefish_gb300 import scenarios
+    ref = Reference()
+    xyz, faces, _ = ref.load_obj(os.path.join(reference_data_dir(), "hull_hydro.obj"), 1.0, 3.0)
+    mesh = (xyz, faces)
+    rng = np.random.default_rng(5)
+    oc = scenarios.flat_ocean(None)
+    for trial in range(3):
+        R = scenarios.quat_to_matrix(scenarios.random_quaternions(rng, 1))[0]
+        T = transform(R, (rng.uniform(-2, 2), rng.uniform(-2, 2), 2.0 + trial))
+        a, b = io_dict(), io_dict()
+        ref.surface_forces(scenarios.settings(), mesh, oc, T, T, np.zeros(3), np.zeros(3), a)
+        oracle.surface_forces(REF32, scenarios.settings(), mesh, oc, T, T, np.zeros(3), np.zeros(3), b)
+        for k in a:
+            assert np.array_equal(a[k], b[k]), (trial, k)
+        assert abs(a["Vsub"][0] - 0.096699) < 5e-6, a["Vsub"][0]
+        np.testing.assert_allclose(np.linalg.norm(a["Fb"]), a["Vsub"][0] * oc.density * oc.gravity, rtol=1e-6)
