@@ -522,9 +522,11 @@ def rollout_bench(args, device: int) -> dict:
     lab = S.Labeller(h64, m64, ocean, st)
     surf = RO.surface_z(h32, ocean)
     # training envelope of the floating hulls: CG within 0.6 m below to 0.5 m
-    # above the local surface, |v| components to 2 m/s, |omega| to 2 rad/s
-    # (the hulls' pitch oscillation reaches rates above 1 rad/s)
-    F, T = S.generate(lab, args.roll_train, seed=303, depth=(-0.5, 0.6), v_range=2.0, w_range=2.0,
+    # above the local surface, |v| components to 3 m/s, body-frame rates to
+    # 10 rad/s about the long axis (roll has no restoring moment and little
+    # inertia, so hulls spin up) and 2.5 rad/s about the others (the pitch
+    # oscillation reaches rates above 1 rad/s)
+    F, T = S.generate(lab, args.roll_train, seed=303, depth=(-0.5, 0.6), v_range=3.0, w_body=(10.0, 2.5, 2.5),
                       surface=surf)
     sur = S.Surrogate(h32, batch=args.sur_batch)
     sur.fit_normalisation(F, T, target_scales=S.hull_scales(ocean))
@@ -548,16 +550,30 @@ def rollout_bench(args, device: int) -> dict:
     stream = torch.cuda.current_stream()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     res = {}
+    clocks = {}
     for name, ro, k in (("exact", ex, k_ex), ("surrogate", su, k_su), ("exact_fp64_cut", e64, k_64)):
         ro.reset(init)
         torch.cuda.synchronize()
+        sampler = ClockSampler(device)
+        sampler.start()
         e0.record(stream)
         ro.replay()
         e1.record(stream)
         torch.cuda.synchronize()
+        clocks[name] = sampler.stop()
         ms = e0.elapsed_time(e1)
         res[name] = {"env_steps_per_s": n * steps / (ms / 1e3), "ms_per_step": ms / steps,
-                     "rollout_s": ms / 1e3, "gpu_launches_per_step": k / steps}
+                     "rollout_s": ms / 1e3, "gpu_launches_per_step": k / steps, "clocks": clocks[name]}
+        if name == "exact":
+            # hulls with a face loop at the last step (not out of the water),
+            # all of whose tiles the wave surface makes the kernel process
+            pos = ro.io.cpu().numpy().view(abi.WRENCH_DTYPE)["position"]
+            looping = int(np.count_nonzero((pos == abi.CROSSING_SURFACE) | (pos == abi.INSIDE)))
+            res[name]["faces_processed_last_step"] = looping * faces
+            # the whole step's time (rigid step, prep, finalize included)
+            # against the chunk kernel's instruction count: a lower bound
+            res[name]["issue_roofline"] = issue_roofline("waves", looping * faces, ms / steps / 1e3,
+                                                         clocks[name].get("sm_mhz"))
     res["surrogate"]["gate_rejected_last_step"] = gp.rejected()
     a, b, c = ex.snapshots(), su.snapshots(), e64.snapshots()
     res["divergence"] = {f"step_{(i + 1) * 100}": RO.divergence(a[i], b[i], init) for i in range(len(a))}
@@ -594,7 +610,7 @@ def section_line(args, rank: int, world: int, local_rank: int, dist):
         ms = sec["surrogate"]["ms_per_step"]
         launches = sec["surrogate"]["gpu_launches_per_step"]
         e2e = None
-        roof = None
+        roof = sec["exact"].get("issue_roofline")
         cfg = {"workload": sec["workload"]}
         dtype = "f64 rigid state, f32 faces / bf16 MLP wrench"
     if rank != 0:
@@ -842,9 +858,9 @@ def main():
     ap.add_argument("--no-rollout", action="store_true")
     ap.add_argument("--roll-envs", type=int, default=16384)
     ap.add_argument("--roll-steps", type=int, default=1000)
-    ap.add_argument("--roll-train", type=int, default=4_000_000)
+    ap.add_argument("--roll-train", type=int, default=8_000_000)
     ap.add_argument("--sur-train", type=int, default=10_000_000)
-    ap.add_argument("--sur-epochs", type=int, default=16)
+    ap.add_argument("--sur-epochs", type=int, default=32)
     ap.add_argument("--sur-batch", type=int, default=1024)
     ap.add_argument("--sur-lr", type=float, default=1e-3)
     args = ap.parse_args()

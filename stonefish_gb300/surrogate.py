@@ -64,12 +64,15 @@ def hull_scales(ocean: abi.Ocean) -> tuple[float, float]:
 
 
 def sample_states(rng: np.random.Generator, n: int, depth=(-1.0, 0.3), extent: float = 102.4,
-                  v_range: float = 1.0, w_range: float = 0.5, surface=None) -> np.ndarray:
+                  v_range: float = 1.0, w_range: float = 0.5, surface=None, w_body=None) -> np.ndarray:
     """Hull states drawn uniformly: CG x, y over the wave grid, CG z in
     ``depth`` (below the local surface when ``surface(xy) -> z`` is given,
     else absolute), uniform random orientation, v in [-v_range, v_range]^3,
     omega in [-w_range, w_range]^3 (the defaults are the single-body and
-    wave workloads' ranges).  Returns a hydro_body array with mesh id 0."""
+    wave workloads' ranges), or, with ``w_body`` = (a, b, c), omega drawn in
+    the body frame from [-a, a] x [-b, b] x [-c, c] (a free hull spins
+    about its long axis much faster than it pitches or yaws).  Returns a
+    hydro_body array with mesh id 0."""
     q = scenarios.random_quaternions(rng, n)
     R = scenarios.quat_to_matrix(q)
     pos = np.empty((n, 3))
@@ -79,7 +82,11 @@ def sample_states(rng: np.random.Generator, n: int, depth=(-1.0, 0.3), extent: f
     if surface is not None:
         pos[:, 2] += surface(pos[:, :2])
     v = rng.uniform(-v_range, v_range, (n, 3))
-    w = rng.uniform(-w_range, w_range, (n, 3))
+    if w_body is None:
+        w = rng.uniform(-w_range, w_range, (n, 3))
+    else:
+        wb = rng.uniform(-1.0, 1.0, (n, 3)) * np.asarray(w_body, dtype=np.float64)
+        w = np.einsum("nij,nj->ni", R, wb)
     half = np.tile([0.5 * HULL_LENGTH + HULL_RADIUS, HULL_RADIUS, HULL_RADIUS], (n, 1))
     return scenarios.fill_bodies(n, R, pos, v, w, half,
                                  meshes.capped_cylinder_volume(HULL_RADIUS, HULL_LENGTH),
