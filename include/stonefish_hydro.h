@@ -352,9 +352,10 @@ hydro_status hydro_batch_compute(hydro_batch* batch, const hydro_body* bodies,
 hydro_status hydro_mapped_host_ptr(const void* host, void** device);
 
 /* Autotuner (no counterpart in the reference).  Times the step on this
- * batch's own bodies for every work-chunk size in {2, 4, 8, 11, 16} tiles
- * ({896, 1792, 3584, 4928, 7168} faces) and 1 or 2 resident CTAs per SM (reps timed steps each, after
- * one warm-up step), keeps the fastest, and appends it to the context's
+ * batch's own bodies for every work-chunk size in {2, 4, 8, 11, 16, 24, 32}
+ * tiles ({896, 1792, 3584, 4928, 7168, 10752, 14336} faces) and 1 or 2
+ * resident CTAs per SM (reps timed steps each, after one warm-up step),
+ * keeps the fastest, and appends it to the context's
  * tune_cache_path (if set) under a key made of the GPU name, SM count, cut
  * precision, surface kind and the batch's face-count histogram.  A later
  * call with a cached key applies the cached choice without timing

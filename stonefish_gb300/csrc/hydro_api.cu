@@ -1894,7 +1894,7 @@ extern "C" hydro_status hydro_batch_autotune(hydro_batch* b, const hydro_body* d
         out->from_cache = 1;
         return HYDRO_OK;
     }
-    static const uint32_t kTiles[] = {2, 4, 8, 11, 16};
+    static const uint32_t kTiles[] = {2, 4, 8, 11, 16, 24, 32};
     static const uint32_t kCtas[] = {1, 2};
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     cudaEvent_t e0 = nullptr, e1 = nullptr;

@@ -78,11 +78,12 @@ __host__ __device__ __forceinline__ uint32_t tile_block_bytes(uint32_t nv, uint3
     return tile_bytes(nv, nf) + ((nf * 4u + 15u) & ~15u);
 }
 
-constexpr int kMaxTilesPerChunk = 16;
+// A chunk's tiles are described by one lane each of the producer warp.
+constexpr int kMaxTilesPerChunk = 32;
 // The active-chunk list is claimed largest chunks first, in one class per
-// tile count: the last chunks a persistent CTA takes are the short ones, so
-// the SMs run out of work at nearly the same time.
-constexpr int kClaimClasses = kMaxTilesPerChunk;
+// two tile counts: the last chunks a persistent CTA takes are the short
+// ones, so the SMs run out of work at nearly the same time.
+constexpr int kClaimClasses = kMaxTilesPerChunk / 2;
 
 // One work item: tiles [first_tile, first_tile + n_tiles) of one body.
 struct __align__(16) ChunkDesc {

@@ -30,8 +30,8 @@ struct KParams {
     int op;                  // OP_BODY / OP_SURFACE / OP_SUBMERGED
     int frame;               // HYDRO_FRAME_WORLD / HYDRO_FRAME_CENTRED (body ops)
     // The list of active chunks is kept in claim classes by tile count,
-    // largest first: class c (chunks of kMaxTilesPerChunk - c tiles) owns
-    // active[class_start[c], class_start[c + 1]).
+    // largest first: class c (chunks of kMaxTilesPerChunk - 2c or one tile
+    // fewer) owns active[class_start[c], class_start[c + 1]).
     uint32_t class_start[kClaimClasses + 1];
 };
 
@@ -40,7 +40,7 @@ struct KParams {
 __host__ __device__ inline uint32_t claim_class(uint32_t n_tiles)
 {
     const uint32_t t = n_tiles < 1u ? 1u : (n_tiles > (uint32_t)kMaxTilesPerChunk ? (uint32_t)kMaxTilesPerChunk : n_tiles);
-    return (uint32_t)kMaxTilesPerChunk - t;
+    return ((uint32_t)kMaxTilesPerChunk - t) / 2u;
 }
 
 inline void claim_class_starts(const ChunkDesc* chunks, size_t n, uint32_t* starts)

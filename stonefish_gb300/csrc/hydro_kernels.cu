@@ -673,112 +673,115 @@ struct __align__(128) ChunkSmem {
 
 size_t chunk_kernel_smem() { return sizeof(ChunkSmem); }
 
-// Tiles of a chunk to stream (bit t for tile t).  On a flat surface a tile
-// of a surface-loop body that lies wholly above the water (every vertex at
-// depth < 0, so every face is skipped, SolidEntity.cpp:1353-1354) is not
-// loaded at all.  The highest vertex of the tile is bounded by its centre's
-// height plus the smaller of two reaches along the row of T_C that gives z:
-// the bounding sphere's radius times the row's norm (2^-20 covers its FP32
-// evaluation) and the box's half extents weighted by the row's magnitudes.
-// The margin bounds the consumer's FP32 transform of each vertex far above
-// its rounding error.  A chunk keeps at least one tile, which carries its
-// (zero) partial.
-__device__ __forceinline__ uint32_t tiles_to_issue(const KParams& P, const ActiveChunk& ch, uint32_t nt)
+// Whether the tile a producer lane describes is streamed.  On a flat
+// surface a tile of a surface-loop body that lies wholly above the water
+// (every vertex at depth < 0, so every face is skipped, SolidEntity.cpp:
+// 1353-1354) is not loaded at all.  The highest vertex of the tile is bounded
+// by its centre's height plus the smaller of two reaches along the row of
+// T_C that gives z: the bounding sphere's radius times the row's norm (2^-20
+// covers its FP32 evaluation) and the box's half extents weighted by the
+// row's magnitudes.  The margin bounds the consumer's FP32 transform of each
+// vertex far above its rounding error.
+__device__ __forceinline__ bool tile_above_water(const float4 T, const TileDesc* d)
 {
-    uint32_t keep = (1u << nt) - 1u;
-    if (P.ocean.waves) return keep;
-    // the body's loop kind, its z row and the tiles' bounds are requested
-    // together (one round trip), the loop kind decides afterwards
-    const BodyParams* B = P.bparams + ch.body;
-    const int loop = B->loop;
-    const float4 T = *reinterpret_cast<const float4*>(B->TC + 8);   // row giving z
     const float ax = fabsf(T.x), ay = fabsf(T.y), az = fabsf(T.z);
     const float rn = sqrtf((T.x * T.x + T.y * T.y) + T.z * T.z) * (1.f + 0x1p-20f);
-    uint32_t drop = 0;
-#pragma unroll 4
-    for (int t = 0; t < kMaxTilesPerChunk; ++t) {
-        if ((uint32_t)t < nt) {
-            const TileDesc* d = P.tiles + ch.first_tile + t;
-            const float4 c = __ldg(&d->sphere), h = __ldg(&d->half);
-            const float zc = (T.x * c.x + T.y * c.y) + (T.z * c.z + T.w);
-            const float reach = fminf(c.w * rn, (ax * h.x + ay * h.y) + az * h.z);
-            const float margin = 1e-5f * ((ax * (fabsf(c.x) + h.x) + ay * (fabsf(c.y) + h.y)) +
-                                          (az * (fabsf(c.z) + h.z) + fabsf(T.w))) + 1e-6f;
-            if (zc + reach + margin < 0.f) drop |= 1u << t;
-        }
-    }
-    if (loop != LOOP_SURFACE) return keep;
-    keep &= ~drop;
-    return keep ? keep : 1u;
+    const float4 c = __ldg(&d->sphere), h = __ldg(&d->half);
+    const float zc = (T.x * c.x + T.y * c.y) + (T.z * c.z + T.w);
+    const float reach = fminf(c.w * rn, (ax * h.x + ay * h.y) + az * h.z);
+    const float margin = 1e-5f * ((ax * (fabsf(c.x) + h.x) + ay * (fabsf(c.y) + h.y)) +
+                                  (az * (fabsf(c.z) + h.z) + fabsf(T.w))) + 1e-6f;
+    return zc + reach + margin < 0.f;
 }
 
-// A tile as the producer needs it: where its block starts and its sizes.
-struct TileRef {
-    const float* block;
-    uint16_t nv, nf;
-};
-
+// The producer warp.  Lane 0 claims chunks and issues the copies; for each
+// chunk, lane t reads tile t's descriptor and tests it against the surface,
+// so a chunk's tiles are described in one round trip.
 __device__ __forceinline__ void producer(const KParams& P, ChunkSmem& S)
 {
+    const uint32_t lane = threadIdx.x & 31u;
+    constexpr unsigned kAll = 0xffffffffu;
     uint32_t item = 0;
     bool ok = true;
-    // Claims go class by class, largest chunks first: a producer moves to the
+    // Claims go class by class, largest chunks first: lane 0 moves to the
     // next class once its claim in the current one comes back past the
     // class's listed count.  They run one chunk ahead so that the atomic's
     // latency overlaps work; the list holds only chunks whose body runs a
     // face loop.
     uint32_t cls = 0;
     auto claim = [&]() -> uint32_t {
-        while (cls < (uint32_t)kClaimClasses) {
-            const uint32_t listed = min(P.n_listed[cls], P.class_start[cls + 1] - P.class_start[cls]);
-            if (listed != 0u) {
-                const uint32_t i = atomicAdd(P.work + cls, 1u);
-                if (i < listed) return P.class_start[cls] + i;
+        uint32_t r = 0xFFFFFFFFu;
+        if (lane == 0u) {
+            while (cls < (uint32_t)kClaimClasses) {
+                const uint32_t listed = min(P.n_listed[cls], P.class_start[cls + 1] - P.class_start[cls]);
+                if (listed != 0u) {
+                    const uint32_t i = atomicAdd(P.work + cls, 1u);
+                    if (i < listed) {
+                        r = P.class_start[cls] + i;
+                        break;
+                    }
+                }
+                ++cls;
             }
-            ++cls;
         }
-        return 0xFFFFFFFFu;
+        return __shfl_sync(kAll, r, 0);
     };
     uint32_t next = claim();
     while (ok && next != 0xFFFFFFFFu) {
         const ActiveChunk ch = P.active[next];
         next = claim();
         const uint32_t nt = ch.n_tiles < (uint32_t)kMaxTilesPerChunk ? ch.n_tiles : (uint32_t)kMaxTilesPerChunk;
-        TileRef td[kMaxTilesPerChunk];
-#pragma unroll
-        for (int t = 0; t < kMaxTilesPerChunk; ++t)
-            if ((uint32_t)t < nt) {
-                const TileDesc& d = P.tiles[ch.first_tile + t];
-                td[t] = TileRef{d.block, d.nv, d.nf};
+        // the body's loop kind and z row, and this lane's tile
+        const BodyParams* B = P.bparams + ch.body;
+        const int loop = B->loop;
+        const float4 T = *reinterpret_cast<const float4*>(B->TC + 8);   // row giving z
+        const float* block = nullptr;
+        uint32_t sizes = 0u;   // nv | nf << 16
+        bool dry = false;
+        if (lane < nt) {
+            const TileDesc* d = P.tiles + ch.first_tile + lane;
+            block = d->block;
+            sizes = (uint32_t)d->nv | ((uint32_t)d->nf << 16);
+            dry = !P.ocean.waves && tile_above_water(T, d);
+        }
+        const uint32_t all = nt >= 32u ? kAll : (1u << nt) - 1u;
+        uint32_t keep = all;
+        if (loop == LOOP_SURFACE) {
+            keep &= ~__ballot_sync(kAll, dry);
+            if (keep == 0u) keep = all & 1u;   // a chunk keeps one tile, which carries its (zero) partial
+        }
+        const uint32_t first_kept = (uint32_t)(__ffs(keep) - 1);
+        const uint32_t last_kept = 31u - (uint32_t)__clz(keep);
+        for (uint32_t rest = keep; rest != 0u; rest &= rest - 1u) {
+            const uint32_t t = (uint32_t)(__ffs(rest) - 1);
+            const uint64_t blk = __shfl_sync(kAll, (unsigned long long)reinterpret_cast<uintptr_t>(block), t);
+            const uint32_t sz = __shfl_sync(kAll, sizes, t);
+            if (lane == 0u) {
+                const int s = (int)(item % kStages);
+                if (item >= (uint32_t)kStages && !mbar_wait_sleep(&S.empty[s], ((item / kStages) - 1u) & 1u)) {
+                    atomicOr(P.err, 1u);
+                    ok = false;
+                } else {
+                    const uint32_t nv = sz & 0xFFFFu, nf = sz >> 16;
+                    const uint32_t bytes = tile_bytes(nv, nf);
+                    ItemMeta m;
+                    m.chunk = ch.chunk;
+                    m.flags = (t == first_kept ? ITEM_FIRST : 0) | (t == last_kept ? ITEM_LAST : 0);
+                    m.nv = (uint16_t)nv;
+                    m.nf = (uint16_t)nf;
+                    m.pad = 0;
+                    S.meta[s] = m;
+                    mbar_arrive_expect_tx(&S.full[s], bytes + (uint32_t)sizeof(BodyParams));
+                    tma_copy(&S.stage[s].bp, P.bparams + ch.body, (uint32_t)sizeof(BodyParams), &S.full[s]);
+                    tma_copy(S.stage[s].raw, reinterpret_cast<const float*>(blk), bytes, &S.full[s]);
+                }
             }
-        const uint32_t keep = tiles_to_issue(P, ch, nt);
-#pragma unroll 1
-        for (uint32_t t = 0; t < nt; ++t) {
-            if (!((keep >> t) & 1u)) continue;
-            const int s = (int)(item % kStages);
-            if (item >= (uint32_t)kStages && !mbar_wait_sleep(&S.empty[s], ((item / kStages) - 1u) & 1u)) {
-                atomicOr(P.err, 1u);
-                ok = false;
-                break;
-            }
-            TileRef d = td[0];
-#pragma unroll
-            for (int k = 1; k < kMaxTilesPerChunk; ++k)
-                if ((uint32_t)k == t) d = td[k];
-            const uint32_t bytes = tile_bytes(d.nv, d.nf);
-            ItemMeta m;
-            m.chunk = ch.chunk;
-            m.flags = ((keep & ((1u << t) - 1u)) == 0u ? ITEM_FIRST : 0) | ((keep >> (t + 1)) == 0u ? ITEM_LAST : 0);
-            m.nv = d.nv;
-            m.nf = d.nf;
-            m.pad = 0;
-            S.meta[s] = m;
-            mbar_arrive_expect_tx(&S.full[s], bytes + (uint32_t)sizeof(BodyParams));
-            tma_copy(&S.stage[s].bp, P.bparams + ch.body, (uint32_t)sizeof(BodyParams), &S.full[s]);
-            tma_copy(S.stage[s].raw, d.block, bytes, &S.full[s]);
+            ok = __shfl_sync(kAll, ok ? 1 : 0, 0) != 0;
+            if (!ok) break;
             ++item;
         }
     }
+    if (lane != 0u) return;
     // end of stream
     const int s = (int)(item % kStages);
     if (item >= (uint32_t)kStages && !mbar_wait_sleep(&S.empty[s], ((item / kStages) - 1u) & 1u)) {
@@ -1086,7 +1089,7 @@ __global__ void __launch_bounds__(kThreads) __maxnreg__(MINB == 2 ? 128 : 255) c
     }
     __syncthreads();
     if (tid >= kBlock) {
-        if (tid == kBlock) producer(P, S);
+        producer(P, S);
         return;
     }
     consumer<CUT64, WAVES>(P, S);

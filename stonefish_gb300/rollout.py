@@ -224,11 +224,22 @@ def divergence(a: np.ndarray, b: np.ndarray, start: np.ndarray) -> dict:
     dp = np.linalg.norm(a["p"] - b["p"], axis=1)
     dot = np.abs(np.sum(a["q"] * b["q"], axis=1)).clip(0.0, 1.0)
     ang = 2.0 * np.arccos(dot)
+    # the angle between the hulls' long (body x) axes: the attitude up to the
+    # roll about that axis, which an axisymmetric hull's hydrodynamics do not
+    # see and nothing restores
+    axis = np.arccos(np.sum(body_x_axis(a["q"]) * body_x_axis(b["q"]), axis=1).clip(-1.0, 1.0))
     travel = np.linalg.norm(a["p"] - start["p"], axis=1)
     q = lambda x, p: float(np.quantile(x, p))
     return {"pos_median_m": q(dp, 0.5), "pos_p95_m": q(dp, 0.95), "pos_max_m": float(dp.max()),
             "att_median_rad": q(ang, 0.5), "att_p95_rad": q(ang, 0.95),
+            "axis_median_rad": q(axis, 0.5), "axis_p95_rad": q(axis, 0.95),
             "travel_median_m": q(travel, 0.5), "finite_envs": int(ok.sum())}
+
+
+def body_x_axis(q: np.ndarray) -> np.ndarray:
+    """World direction of the body x axis for quaternions (w, x, y, z)."""
+    w, x, y, z = q[:, 0], q[:, 1], q[:, 2], q[:, 3]
+    return np.stack([1.0 - 2.0 * (y * y + z * z), 2.0 * (x * y + z * w), 2.0 * (x * z - y * w)], axis=1)
 
 
 def state_stats(s: np.ndarray) -> dict:

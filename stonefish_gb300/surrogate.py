@@ -227,12 +227,13 @@ class Surrogate:
     # ------------------------------------------------------ normalisation
     def fit_normalisation(self, feats: torch.Tensor, targets: torch.Tensor, sample: int = 1 << 20,
                           gate_quantile: float = 0.999, box_margin: float = 0.02,
-                          target_scales: tuple[float, float] | None = None) -> None:
+                          target_scales: tuple[float, ...] | None = None) -> None:
         """Feature/target statistics and the gate, from up to ``sample`` rows
         (host FP64 arithmetic on a copy).  Targets are centred and divided by
         their standard deviations, or, with ``target_scales`` = (force scale,
         torque scale), by those two scales: the training loss then weighs
-        each component's error as the wrench error metric does."""
+        each component's error as the wrench error metric does.  Six scales
+        (one per component) weigh the components individually."""
         f = feats[:sample].double().cpu().numpy()
         t = targets[:sample].double().cpu().numpy()
         fm, fs = f.mean(0), f.std(0)
@@ -240,7 +241,10 @@ class Surrogate:
         tm, ts = t.mean(0), t.std(0)
         ts[ts < 1e-12] = 1.0
         if target_scales is not None:
-            ts = np.array([target_scales[0]] * 3 + [target_scales[1]] * 3, dtype=np.float64)
+            if len(target_scales) == 6:
+                ts = np.array(target_scales, dtype=np.float64)
+            else:
+                ts = np.array([target_scales[0]] * 3 + [target_scales[1]] * 3, dtype=np.float64)
         f32 = dict(dtype=torch.float32, device=self.dev)
         self.f_mean = torch.tensor(fm, **f32)
         self.f_istd = torch.tensor(1.0 / fs, **f32)

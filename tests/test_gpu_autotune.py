@@ -31,9 +31,9 @@ def test_autotune_picks_a_candidate_and_caches_it(built_library, tmp_path):
     d_s = torch.zeros(len(bodies) * abi.WRENCH_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
     r = b.autotune(d_b.data_ptr(), sc["ocean"], st, d_s.data_ptr(), reps=2)
     assert not r["from_cache"]
-    assert r["chunk_faces"] in tuple(t * abi.TILE_FACES for t in (2, 4, 8, 11, 16))
+    assert r["chunk_faces"] in tuple(t * abi.TILE_FACES for t in (2, 4, 8, 11, 16, 24, 32))
     assert r["ctas_per_sm"] in (1, 2)
-    assert len(r["candidate_ms"]) == 10 and min(r["candidate_ms"]) == pytest.approx(r["ms_per_step"])
+    assert len(r["candidate_ms"]) == 14 and min(r["candidate_ms"]) == pytest.approx(r["ms_per_step"])
     after = scenarios.new_wrenches(len(bodies))
     b.compute(bodies, sc["ocean"], st, after)
     assert np.array_equal(after["position"], before["position"])

@@ -421,3 +421,111 @@ def test_fused_tensor_core_kernel_against_oracle_output(hctx):
     err = np.abs(got - ref) / scale
     assert np.all(err.max(axis=0) <= 2.0 ** -7), err.max(axis=0)
     assert np.all(np.median(err, axis=0) <= 2.0 ** -10), np.median(err, axis=0)
+
+
+def test_gate_inside_matches_fluid_position(built_library, oracle):
+    """States whose AABB lies wholly under the wavy surface (the reference's
+    INSIDE branch, SolidEntity.cpp:1239-1261) leave the network's path;
+    states already rejected stay rejected and the others keep their bit."""
+    from stonefish_gb300.hydro import HydroContext
+    rng = np.random.default_rng(41)
+    n = 2000
+    waves = scenarios.wave_grid(n=256, n_waves=16, seed=3)
+    ocean = S.wave_ocean()
+    bodies = S.sample_states(rng, n, depth=(-1.5, 1.5), extent=25.6)
+    h = HydroContext()
+    try:
+        h.set_wave_grid(waves)
+        m0 = np.ones(n, np.uint8)
+        m0[::5] = 0
+        mask = torch.from_numpy(m0.copy()).cuda()
+        d_b = torch.from_numpy(np.frombuffer(bodies.tobytes(), dtype=np.uint8).copy()).cuda()
+        _ck(h, h.lib.hydro_nn_gate_inside(h.ctx, S._ptr(d_b), n, C.byref(ocean), S._ptr(mask), None))
+        torch.cuda.synchronize()
+        got = mask.cpu().numpy()
+    finally:
+        h.close()
+    inside = np.array([oracle.fluid_position(ocean, bodies["aabb_min"][i], bodies["aabb_max"][i], waves)
+                       == abi.INSIDE for i in range(n)])
+    expect = (m0 != 0) & ~inside
+    assert np.array_equal(got != 0, expect)
+    assert inside.sum() > 50 and (~inside).sum() > 50
+
+
+def test_ensemble_mean_and_disagreement_gate(hctx):
+    """Two networks' outputs: the first becomes their mean (columns 0..5),
+    and a state whose outputs differ by more than tau in the wrench metric
+    (max of |dF| / fs and |dT| / ts) is rejected."""
+    rng = np.random.default_rng(42)
+    n, ld = 3000, 16
+    za = rng.normal(size=(n, ld)).astype(np.float32)
+    zb = (za + rng.normal(size=(n, ld)) * rng.uniform(0.0, 0.2, (n, 1))).astype(np.float32)
+    m0 = np.ones(n, np.uint8)
+    m0[::9] = 0
+    fs, ts, tau = 3.0, 5.0, 0.05
+    dza, dzb, mask = _dev(za), _dev(zb), torch.from_numpy(m0.copy()).cuda()
+    _ck(hctx, hctx.lib.hydro_nn_ensemble(hctx.ctx, S._ptr(dza), S._ptr(dzb), ld, n, fs, ts, tau, S._ptr(mask), None))
+    torch.cuda.synchronize()
+    out = dza.cpu().numpy()
+    mean = ((za + zb) * np.float32(0.5)).astype(np.float32)
+    assert np.array_equal(out[:, :6], mean[:, :6])
+    assert np.array_equal(out[:, 6:], za[:, 6:])
+    d = np.maximum(np.linalg.norm(za[:, :3].astype(np.float64) - zb[:, :3], axis=1) / fs,
+                   np.linalg.norm(za[:, 3:6].astype(np.float64) - zb[:, 3:6], axis=1) / ts)
+    clear = np.abs(d - tau) > 1e-5
+    expect = (m0 != 0) & (d <= tau)
+    got = mask.cpu().numpy() != 0
+    assert np.array_equal(got[clear], expect[clear])
+    assert (~expect & (m0 != 0)).sum() > 100 and expect.sum() > 100
+
+
+def test_audit_pick_and_error(hctx):
+    """The audit sends rows phase, phase + stride, ... that the gates
+    admitted to the exact step and measures the network's error on them
+    against the exact wrench rotated into the body frame."""
+    rng = np.random.default_rng(43)
+    n, stride, phase = 5000, 64, 17
+    k = (n + stride - 1) // stride
+    m0 = (rng.uniform(size=n) > 0.3).astype(np.uint8)
+    mask = torch.from_numpy(m0.copy()).cuda()
+    idx = torch.zeros(k, dtype=torch.int32, device="cuda")
+    _ck(hctx, hctx.lib.hydro_nn_audit_pick(hctx.ctx, S._ptr(mask), n, stride, phase, k, S._ptr(idx), None))
+    torch.cuda.synchronize()
+    rows = phase + stride * np.arange(k)
+    want = np.where((rows < n) & (m0[np.minimum(rows, n - 1)] != 0), rows, -1)
+    got_idx = idx.cpu().numpy()
+    assert np.array_equal(got_idx, want)
+    m1 = m0.copy()
+    m1[want[want >= 0]] = 0
+    assert np.array_equal(mask.cpu().numpy(), m1)
+    # errors: picked rows take slots of an exact array, one picked row is
+    # left without a slot (its error slot reads -1, as empty sample slots do)
+    bodies = S.sample_states(rng, n)
+    picked = want[want >= 0]
+    pos = np.full(n, -1, np.int32)
+    pos[picked[1:]] = np.arange(picked.size - 1)
+    ex = np.zeros(n, dtype=abi.WRENCH_DTYPE)
+    for key in ("Fb", "Tb", "Fdq", "Tdq", "Fdf", "Tdf"):
+        ex[key] = rng.normal(size=(n, 3))
+    z = rng.normal(size=(n, 16)).astype(np.float32)
+    fs, ts = 2.0, 3.0
+    err = torch.zeros(k, dtype=torch.float32, device="cuda")
+    d_b = torch.from_numpy(np.frombuffer(bodies.tobytes(), dtype=np.uint8).copy()).cuda()
+    d_ex = torch.from_numpy(np.frombuffer(ex.tobytes(), dtype=np.uint8).copy()).cuda()
+    dz, dpos = _dev(z), torch.from_numpy(pos).cuda()
+    _ck(hctx, hctx.lib.hydro_nn_audit_error(hctx.ctx, S._ptr(d_b), S._ptr(dz), 16, S._ptr(dpos), S._ptr(d_ex),
+                                            S._ptr(idx), k, fs, ts, S._ptr(err), None))
+    torch.cuda.synchronize()
+    e = err.cpu().numpy()
+    R = bodies["T_CG"]["basis"].reshape(n, 3, 3)
+    F = ex["Fb"] + ex["Fdq"] + ex["Fdf"]
+    T = ex["Tb"] + ex["Tdq"] + ex["Tdf"]
+    for j, i in enumerate(want):
+        if i < 0 or pos[i] < 0:
+            assert e[j] == -1.0
+            continue
+        Fb = R[i].T @ F[pos[i]]
+        Tb = R[i].T @ T[pos[i]]
+        x = max(np.linalg.norm(z[i, :3] - Fb) / fs, np.linalg.norm(z[i, 3:6] - Tb) / ts)
+        assert abs(e[j] - x) <= 1e-6 * x + 1e-7
+    assert (e > 0).sum() >= picked.size - 1
