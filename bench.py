@@ -869,9 +869,9 @@ def main():
     ap.add_argument("--roll-steps", type=int, default=1000)
     ap.add_argument("--roll-train", type=int, default=8_000_000)
     ap.add_argument("--sur-train", type=int, default=10_000_000)
-    ap.add_argument("--sur-epochs", type=int, default=32)
-    ap.add_argument("--sur-batch", type=int, default=1024)
-    ap.add_argument("--sur-lr", type=float, default=1e-3)
+    ap.add_argument("--sur-epochs", type=int, default=64)
+    ap.add_argument("--sur-batch", type=int, default=4096)
+    ap.add_argument("--sur-lr", type=float, default=3e-3)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
