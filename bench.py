@@ -358,7 +358,9 @@ def surrogate_bench(args, device: int) -> dict:
     pa = sur.infer_tc(Fc, zc, sur.tc_weights())[:, :6].cpu().numpy()
     pb = sur2.infer_tc(Fc, zc, sur2.tc_weights())[:, :6].cpu().numpy()
     cal_in = Wc.cpu().numpy().view(abi.WRENCH_DTYPE)["position"] != abi.INSIDE
-    calib = S.calibrate_disagreement(pa, pb, Tc.cpu().numpy(), cal_in, ocean, target_p99=0.01, max_reject=0.04)
+    # calibrated for 0.95% on the held-out states: 5% of margin below the 1%
+    # bar for the difference between two samples of 65,536 states
+    calib = S.calibrate_disagreement(pa, pb, Tc.cpu().numpy(), cal_in, ocean, target_p99=0.0095, max_reject=0.04)
     del Fc, Tc, Wc, zc
     rng = np.random.default_rng(202)
     sets, d_sets = [], []
@@ -458,7 +460,7 @@ def surrogate_bench(args, device: int) -> dict:
         "error_single_network": dict(single, note="one network, no gates, same states"),
         "gate": {"rejected_frac": rejected / nB, "rules": "feature box + Mahalanobis radius; fluid position "
                  "INSIDE; the two networks' disagreement above tau (calibrated on 65536 held-out labelled "
-                 "states for an admitted 99th percentile <= 0.01, at most 4% rejected)", "calibration": calib},
+                 "states for an admitted 99th percentile <= 0.0095, at most 4% rejected)", "calibration": calib},
         "audit": {"rows": int(audit.size), "stride": gp.audit_stride,
                   "median": float(np.median(audit)) if audit.size else None,
                   "p99": float(np.percentile(audit, 99)) if audit.size else None,

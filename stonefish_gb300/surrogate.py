@@ -452,10 +452,10 @@ class GatedPredictor:
     rejects routed to the exact step (one exact batch over n slots; slots
     past the rejected count are switched off and cost nothing)."""
 
-    # faces per work chunk of the exact fallback batch: four tiles (measured
-    # against one, two and eight: within 1% for 68 gated-out hulls of 65536,
-    # 27% faster in rollouts that gate out thousands)
-    FALLBACK_CHUNK_FACES = 4 * abi.TILE_FACES
+    # faces per work chunk of the exact fallback batch: eleven tiles (with
+    # 650 to 1,600 of 65,536 torpedo states gated out: 4-12% faster than four
+    # tiles, 1-2% faster than eight or sixteen)
+    FALLBACK_CHUNK_FACES = 11 * abi.TILE_FACES
 
     def __init__(self, sur: Surrogate, hctx_exact: HydroContext, mesh_id: int, n: int,
                  ocean: abi.Ocean, settings: abi.Settings, tensor_cores: str = "tcgen05",
