@@ -797,6 +797,58 @@ hydro_status hydro_nn_adamw(hydro_ctx* ctx, float* w, float* m, float* v, const 
                             float beta2, float eps, float weight_decay, int32_t step, void* w16,
                             void* wt16, void* stream);
 
+/* One layer of the MLP as the training loop sees it (device pointers):
+ * FP32 master weights w[k][n] and bias b[n], their AdamW moments (mw, vw,
+ * mb, vb) and gradients (gw, gb), and the bf16 copies the GEMMs read
+ * (w16 [k][n], wt16 [n][k]). */
+typedef struct hydro_nn_layer {
+    float* w;
+    float* b;
+    float* mw;
+    float* vw;
+    float* mb;
+    float* vb;
+    float* gw;
+    float* gb;
+    void* w16;
+    void* wt16;
+    int32_t k;
+    int32_t n;
+} hydro_nn_layer;
+
+/* The four-layer MLP (layers 0..2: bias + SiLU, layer 3: bias) with the work
+ * buffers of one training batch (device pointers): z[l] FP32 pre-
+ * activations [batch][n_l]; x[l] (l < 3) bf16 activations [batch][n_l];
+ * dz[l] bf16 gradients [batch][n_l]; xt[l] bf16 transposed layer inputs
+ * [k_l][batch]; targets normalised by (t - tmean) * tistd (both NULL: raw);
+ * the batch losses are added to *loss. */
+typedef struct hydro_nn_net {
+    hydro_nn_layer layer[4];
+    float* z[4];
+    void* x[3];
+    void* dz[4];
+    void* xt[4];
+    const float* tmean;
+    const float* tistd;
+    double* loss;
+    int32_t batch;
+    int32_t n_out;
+} hydro_nn_net;
+
+/* n_steps AdamW steps of the MLP, launched from native code.  Step s reads
+ * rows [rows[s], rows[s] + batch) of the bf16 network inputs X [n_rows][k_0]
+ * and of the FP32 targets T [n_rows][n_out], runs the forward and backward
+ * passes and updates every layer with learning rate lr[s] and step count
+ * step0 + s + 1 (rows and lr are host arrays of n_steps).  It launches the
+ * kernels of hydro_nn_gemm, hydro_nn_mse_grad, hydro_nn_transpose,
+ * hydro_nn_colsum and hydro_nn_adamw with the same arguments in the same
+ * order as calling those one by one, so the trained weights are the same
+ * bits; a step then costs no round trip through the caller. */
+hydro_status hydro_nn_train(hydro_ctx* ctx, const hydro_nn_net* net, const void* X, const float* T,
+                            int64_t n_rows, const int64_t* rows, const float* lr, int32_t n_steps,
+                            int32_t step0, float beta1, float beta2, float eps, float weight_decay,
+                            void* stream);
+
 /* y[rows][ld] = bf16((x - mean) * istd) of x[rows][n_in], zero in columns
  * n_in..ld-1; mean and istd both NULL for a plain conversion. */
 hydro_status hydro_nn_to_bf16(hydro_ctx* ctx, const float* x, int32_t rows, int32_t n_in, int32_t ld,

@@ -132,6 +132,18 @@ class RigidState(C.Structure):
                 ("inertial_mass", C.c_double), ("inertia", _d3), ("half_extents", _d3)]
 
 
+class NnLayer(C.Structure):
+    _fields_ = [("w", C.c_void_p), ("b", C.c_void_p), ("mw", C.c_void_p), ("vw", C.c_void_p),
+                ("mb", C.c_void_p), ("vb", C.c_void_p), ("gw", C.c_void_p), ("gb", C.c_void_p),
+                ("w16", C.c_void_p), ("wt16", C.c_void_p), ("k", C.c_int32), ("n", C.c_int32)]
+
+
+class NnNet(C.Structure):
+    _fields_ = [("layer", NnLayer * 4), ("z", C.c_void_p * 4), ("x", C.c_void_p * 3), ("dz", C.c_void_p * 4),
+                ("xt", C.c_void_p * 4), ("tmean", C.c_void_p), ("tistd", C.c_void_p), ("loss", C.c_void_p),
+                ("batch", C.c_int32), ("n_out", C.c_int32)]
+
+
 class TuneResult(C.Structure):
     _fields_ = [("chunk_faces", C.c_uint32), ("ctas_per_sm", C.c_uint32), ("ms_per_step", C.c_float),
                 ("from_cache", C.c_int32), ("n_candidates", C.c_uint32), ("candidate_ms", C.c_float * 16)]
@@ -256,6 +268,8 @@ def _declare(lib: C.CDLL) -> None:
         "hydro_nn_colsum": (i32, [vp, vp, i32, i32, vp, vp]),
         "hydro_nn_adamw": (i32, [vp, vp, vp, vp, vp, i32, i32, i32, C.c_float, C.c_float, C.c_float,
                                  C.c_float, C.c_float, i32, vp, vp, vp]),
+        "hydro_nn_train": (i32, [vp, C.POINTER(NnNet), vp, vp, C.c_int64, vp, vp, i32, i32, C.c_float, C.c_float,
+                                 C.c_float, C.c_float, vp]),
         "hydro_nn_to_bf16": (i32, [vp, vp, i32, i32, i32, vp, vp, vp, vp]),
         "hydro_nn_features": (i32, [vp, vp, u32, C.POINTER(Ocean), vp, vp]),
         "hydro_nn_gate": (i32, [vp, vp, u32, vp, vp, vp, vp, C.c_float, vp, vp]),

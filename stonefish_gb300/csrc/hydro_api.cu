@@ -61,6 +61,8 @@ struct hydro_ctx {
     hydro_batch* oneshot = nullptr;
     std::vector<hydro_mesh_id> oneshot_meshes;
     void* small_d = nullptr;   // scratch for the small entry points
+    float* nn_ws = nullptr;    // split-K partial products of the surrogate's weight-gradient GEMMs
+    size_t nn_ws_floats = 0;
     size_t small_cap = 0;
     std::string tune_path;     // autotuner cache file ("" = none)
     int frame = HYDRO_FRAME_WORLD;   // body-op frame (hydro_set_frame)
@@ -572,6 +574,7 @@ void hydro_destroy(hydro_ctx* ctx)
     cudaFree(ctx->tiles_d);
     cudaFree(ctx->wave_d);
     cudaFree(ctx->small_d);
+    cudaFree(ctx->nn_ws);
     cudaFree(ctx->cable_seg);
     cudaFree(ctx->cable_stage);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -1959,6 +1962,31 @@ extern "C" hydro_status hydro_batch_autotune(hydro_batch* b, const hydro_body* d
 
 #define NN_RET(e, what) return (e) == cudaSuccess ? HYDRO_OK : cuda_fail(ctx, (e), (what))
 
+// Room for `floats` split-K partial products in the context's workspace,
+// grown on demand; not grown while the stream captures a graph (the GEMM
+// then runs unsplit).  Returns false only when an allocation failed.
+static bool nn_workspace(hydro_ctx* ctx, size_t floats, cudaStream_t s)
+{
+    if (floats <= ctx->nn_ws_floats) return true;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+        cudaGetLastError();
+        return true;
+    }
+    float* p = nullptr;
+    if (cudaMalloc(&p, floats * sizeof(float)) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (ctx->nn_ws) {
+        cudaStreamSynchronize(s);
+        cudaFree(ctx->nn_ws);
+    }
+    ctx->nn_ws = p;
+    ctx->nn_ws_floats = floats;
+    return true;
+}
+
 extern "C" hydro_status hydro_nn_gemm(hydro_ctx* ctx, int32_t epilogue, const void* A, int32_t lda,
                                       const void* B, int32_t ldb, int32_t M, int32_t N, int32_t K,
                                       float* z, void* y, const float* bias, const float* zprev,
@@ -1973,8 +2001,12 @@ extern "C" hydro_status hydro_nn_gemm(hydro_ctx* ctx, int32_t epilogue, const vo
     if ((epilogue == 1 || epilogue == 3) && !y) return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn gemm: missing y");
     if ((epilogue == 1 || epilogue == 2) && !bias) return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn gemm: missing bias");
     if (epilogue == 3 && !zprev) return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn gemm: missing zprev");
-    cudaError_t e = launch_gemm(epilogue, A, lda, B, ldb, M, N, K, z, y, bias, zprev, ldc,
-                                static_cast<cudaStream_t>(stream));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const size_t ws = (size_t)gemm_splits(epilogue, M, N, K) * (size_t)M * (size_t)N;
+    if (ws > (size_t)M * (size_t)N && !nn_workspace(ctx, ws, st))
+        return fail(ctx, HYDRO_ERR_OOM, "nn gemm: split-K workspace");
+    cudaError_t e = launch_gemm(epilogue, A, lda, B, ldb, M, N, K, z, y, bias, zprev, ldc, st, ctx->nn_ws,
+                                ctx->nn_ws_floats);
     NN_RET(e, "nn gemm");
 }
 
@@ -2016,6 +2048,81 @@ extern "C" hydro_status hydro_nn_adamw(hydro_ctx* ctx, float* w, float* m, float
         return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn adamw");
     NN_RET(launch_adamw(w, m, v, grad, rows, cols, ldg, lr, beta1, beta2, eps, weight_decay, step, w16, wt16,
                         static_cast<cudaStream_t>(stream)), "nn adamw");
+}
+
+// The training loop: per step the forward GEMMs (bias + SiLU epilogues,
+// then bias), the MSE gradient, and per layer from the last the transposed
+// input, the weight-gradient GEMM, the bias-gradient column sums and the
+// gradient GEMM through the SiLU derivative; then AdamW on every layer's
+// weights (decayed) and bias (not decayed).  The launch sequence is the one
+// a caller makes with the single entry points, kernel for kernel.
+extern "C" hydro_status hydro_nn_train(hydro_ctx* ctx, const hydro_nn_net* net, const void* X, const float* T,
+                                       int64_t n_rows, const int64_t* rows, const float* lr, int32_t n_steps,
+                                       int32_t step0, float beta1, float beta2, float eps, float weight_decay,
+                                       void* stream)
+{
+    NN_CTX_CHECK();
+    if (!net || !X || !T || !rows || !lr || n_steps < 0 || step0 < 0 || n_rows <= 0)
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn train: missing argument");
+    const int B = net->batch;
+    if (B <= 0 || B % 64 || net->n_out <= 0 || net->n_out > net->layer[3].n || !net->loss)
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn train: batch must be a positive multiple of 64");
+    for (int l = 0; l < 4; ++l) {
+        const hydro_nn_layer& L = net->layer[l];
+        if (!L.w || !L.b || !L.mw || !L.vw || !L.mb || !L.vb || !L.gw || !L.gb || !L.w16 || !L.wt16 || !net->z[l] ||
+            !net->dz[l] || !net->xt[l] || (l < 3 && !net->x[l]) || L.k <= 0 || L.n <= 0 || L.k % 64 || L.n % 64 ||
+            (l > 0 && L.k != net->layer[l - 1].n))
+            return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn train: bad layer (k, n multiples of 64, chained)");
+    }
+    if ((!net->tmean) != (!net->tistd) || (uint64_t)B * (uint64_t)net->layer[3].n >= (1ull << 32))
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn train: bad target normalisation");
+    for (int32_t s = 0; s < n_steps; ++s)
+        if (rows[s] < 0 || rows[s] + B > n_rows || step0 + s + 1 < 1)
+            return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn train: batch rows out of range");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const hydro_nn_layer* Ls = net->layer;
+    const int k0 = Ls[0].k, n_out = net->n_out;
+    size_t ws = 0;
+    for (int l = 0; l < 4; ++l)
+        ws = std::max(ws, (size_t)gemm_splits(0, Ls[l].k, Ls[l].n, B) * (size_t)Ls[l].k * (size_t)Ls[l].n);
+    if (!nn_workspace(ctx, ws, st)) return fail(ctx, HYDRO_ERR_OOM, "nn train: split-K workspace");
+    cudaError_t e = cudaSuccess;
+#define NN_TRAIN(call)                                  \
+    do {                                                \
+        e = (call);                                     \
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "nn train: " #call); \
+    } while (0)
+    for (int32_t s = 0; s < n_steps; ++s) {
+        const void* X0 = static_cast<const unsigned char*>(X) + (size_t)rows[s] * (size_t)k0 * 2u;
+        const float* T0 = T + (size_t)rows[s] * (size_t)n_out;
+        const void* ins[4] = {X0, net->x[0], net->x[1], net->x[2]};
+        for (int l = 0; l < 3; ++l)
+            NN_TRAIN(launch_gemm(1, ins[l], Ls[l].k, Ls[l].w16, Ls[l].n, B, Ls[l].n, Ls[l].k, net->z[l], net->x[l],
+                                 Ls[l].b, nullptr, Ls[l].n, st));
+        NN_TRAIN(launch_gemm(2, ins[3], Ls[3].k, Ls[3].w16, Ls[3].n, B, Ls[3].n, Ls[3].k, net->z[3], nullptr, Ls[3].b,
+                             nullptr, Ls[3].n, st));
+        NN_TRAIN(launch_mse_grad(net->z[3], T0, B, Ls[3].n, n_out, net->tmean, net->tistd, net->dz[3], net->loss, st));
+        for (int l = 3; l >= 0; --l) {
+            const hydro_nn_layer& L = Ls[l];
+            NN_TRAIN(launch_transpose(ins[l], net->xt[l], B, L.k, st));
+            NN_TRAIN(launch_gemm(0, net->xt[l], B, net->dz[l], L.n, L.k, L.n, B, L.gw, nullptr, nullptr, nullptr,
+                                 L.n, st, ctx->nn_ws, ctx->nn_ws_floats));
+            NN_TRAIN(launch_colsum(net->dz[l], B, L.n, L.gb, st));
+            if (l > 0)
+                NN_TRAIN(launch_gemm(3, net->dz[l], L.n, L.wt16, L.k, B, L.k, L.n, nullptr, net->dz[l - 1], nullptr,
+                                     net->z[l - 1], L.k, st));
+        }
+        const int step = step0 + s + 1;
+        for (int l = 0; l < 4; ++l) {
+            const hydro_nn_layer& L = Ls[l];
+            NN_TRAIN(launch_adamw(L.w, L.mw, L.vw, L.gw, L.k, L.n, L.n, lr[s], beta1, beta2, eps, weight_decay, step,
+                                  L.w16, L.wt16, st));
+            NN_TRAIN(launch_adamw(L.b, L.mb, L.vb, L.gb, 1, L.n, L.n, lr[s], beta1, beta2, eps, 0.0f, step, nullptr,
+                                  nullptr, st));
+        }
+    }
+#undef NN_TRAIN
+    return HYDRO_OK;
 }
 
 extern "C" hydro_status hydro_nn_to_bf16(hydro_ctx* ctx, const float* x, int32_t rows, int32_t n_in, int32_t ld,

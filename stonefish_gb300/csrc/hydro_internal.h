@@ -121,9 +121,13 @@ cudaError_t launch_depth(OceanDev ocean, const float* xyz, uint32_t n, float* ou
 // C[M,N] = A[M,K] * B[K,N] (BF16 row-major, FP32 accumulate) with epilogue
 // epi: 0 z = C; 1 z = C + bias, y = bf16(silu(z)); 2 z = C + bias;
 // 3 y = bf16(C * silu'(zprev)).  M, N multiples of 64, K of 32.
+// An EPI_F32 product with few output tiles and a long K runs split along K
+// when `ws` holds gemm_splits(...) * M * N floats: each slice writes a
+// partial product there, and a second kernel sums them in slice order.
+int gemm_splits(int epi, int M, int N, int K);
 cudaError_t launch_gemm(int epi, const void* A, int lda, const void* B, int ldb, int M, int N, int K,
                         float* z, void* y, const float* bias, const float* zprev, int ldc,
-                        cudaStream_t s);
+                        cudaStream_t s, float* ws = nullptr, size_t ws_floats = 0);
 cudaError_t launch_transpose(const void* src, void* dst, int rows, int cols, cudaStream_t s);
 cudaError_t launch_mse_grad(const float* z, const float* t, int rows, int ld, int n_out, const float* tmean,
                             const float* tistd, void* dz, double* loss, cudaStream_t s);

@@ -26,6 +26,7 @@ struct EpiArgs {
     const float* bias;   // per column
     const float* zprev;  // pre-activations of the layer the gradient flows into
     int ldc;             // leading dimension of the outputs
+    size_t split_stride; // split-K (EPI_F32): floats between the partial products of consecutive K slices
 };
 
 enum : int { EPI_F32 = 0, EPI_BIAS_SILU = 1, EPI_BIAS = 2, EPI_SILU_GRAD = 3 };
@@ -66,6 +67,13 @@ __global__ void __launch_bounds__(128) gemm_kernel(const bf16* __restrict__ A, i
     __shared__ __align__(16) bf16 Bs[BK][BN + BPAD];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+    if (EPI == EPI_F32 && blockIdx.z > 0) {
+        // split-K: slice z covers K columns z K .. of A and rows of B and
+        // writes its partial product to its own plane of the workspace
+        A += (size_t)blockIdx.z * K;
+        B += (size_t)blockIdx.z * K * ldb;
+        e.z += blockIdx.z * e.split_stride;
+    }
     const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
     float acc[2][4][4];
 #pragma unroll
@@ -147,15 +155,49 @@ __global__ void __launch_bounds__(128) gemm_kernel(const bf16* __restrict__ A, i
     }
 }
 
+// out[r][c] (row stride ldc) = sum over the `splits` partial products in
+// split order (deterministic).
+__global__ void splitk_reduce_kernel(const float* __restrict__ ws, int splits, int M, int N, float* out, int ldc)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t mn = (size_t)M * N;
+    if (i >= mn) return;
+    float v = ws[i];
+    for (int z = 1; z < splits; ++z) v += ws[z * mn + i];
+    out[(i / N) * ldc + i % N] = v;
+}
+
+int gemm_splits(int epi, int M, int N, int K)
+{
+    // An EPI_F32 product with few output tiles and a long K (the weight
+    // gradients: K = batch) is split along K so that the GPU fills: slices of
+    // at least 256 columns, up to about two CTAs per SM.
+    if (epi != EPI_F32) return 1;
+    const int tiles = (M / BM) * (N / BN);
+    int s = 1;
+    while (s < 32 && K % (2 * s * BK) == 0 && K / (2 * s) >= 256 && tiles * 2 * s <= 320) s *= 2;
+    return s;
+}
+
 cudaError_t launch_gemm(int epi, const void* A, int lda, const void* B, int ldb, int M, int N, int K,
                         float* z, void* y, const float* bias, const float* zprev, int ldc,
-                        cudaStream_t s)
+                        cudaStream_t s, float* ws, size_t ws_floats)
 {
     if (M % BM || N % BN || K % BK || M <= 0 || N <= 0 || K <= 0) return cudaErrorInvalidValue;
     dim3 grid(N / BN, M / BM), block(128);
-    EpiArgs e{z, static_cast<bf16*>(y), bias, zprev, ldc};
+    EpiArgs e{z, static_cast<bf16*>(y), bias, zprev, ldc, 0};
     const bf16* a = static_cast<const bf16*>(A);
     const bf16* b = static_cast<const bf16*>(B);
+    const int splits = gemm_splits(epi, M, N, K);
+    if (splits > 1 && ws && (size_t)splits * M * N <= ws_floats) {
+        EpiArgs w{ws, nullptr, nullptr, nullptr, N, (size_t)M * N};
+        gemm_kernel<EPI_F32><<<dim3(N / BN, M / BM, splits), block, 0, s>>>(a, lda, b, ldb, K / splits, w);
+        cudaError_t err = cudaGetLastError();
+        if (err != cudaSuccess) return err;
+        const size_t mn = (size_t)M * N;
+        splitk_reduce_kernel<<<(unsigned)((mn + 255) / 256), 256, 0, s>>>(ws, splits, M, N, z, ldc);
+        return cudaGetLastError();
+    }
     switch (epi) {
     case EPI_F32: gemm_kernel<EPI_F32><<<grid, block, 0, s>>>(a, lda, b, ldb, K, e); break;
     case EPI_BIAS_SILU: gemm_kernel<EPI_BIAS_SILU><<<grid, block, 0, s>>>(a, lda, b, ldb, K, e); break;

@@ -323,33 +323,70 @@ class Surrogate:
         self.to_bf16(feats, n, N_FEAT, IN_PAD, X, self.f_mean, self.f_istd)
         return X
 
+    def _net(self) -> abi.NnNet:
+        """The network and the training buffers as hydro_nn_train reads them."""
+        bf = self._bufs()
+        net = abi.NnNet()
+        for l, L in enumerate(self.layers):
+            d = net.layer[l]
+            for f in ("w", "b", "mw", "vw", "mb", "vb", "gw", "gb", "w16", "wt16"):
+                setattr(d, f, L[f].data_ptr())
+            d.k, d.n = L["k"], L["n"]
+        for l in range(4):
+            net.z[l] = bf["z"][l].data_ptr()
+            net.dz[l] = bf["dz"][l].data_ptr()
+            net.xt[l] = bf["xt"][l].data_ptr()
+        for l in range(3):
+            net.x[l] = bf["x"][l].data_ptr()
+        net.tmean, net.tistd = self.t_mean.data_ptr(), self.t_istd.data_ptr()
+        net.loss = self.loss_d.data_ptr()
+        net.batch, net.n_out = self.B, N_OUT
+        return net
+
     def fit(self, feats: torch.Tensor, targets: torch.Tensor, epochs: int = 4, lr: float = 2e-3,
-            lr_final: float = 2e-5, warmup: int = 200, log=None, on_epoch=None) -> dict:
+            lr_final: float = 2e-5, warmup: int = 200, log=None, on_epoch=None, native: bool = True) -> dict:
         """AdamW with linear warm-up and cosine decay over ``epochs`` passes
         of consecutive batches (samples are i.i.d., so no shuffling is
-        needed; each epoch shifts the batch boundaries)."""
+        needed; each epoch shifts the batch boundaries).  With ``native``
+        each epoch is one hydro_nn_train call (the library launches every
+        step's kernels); otherwise the same kernels are called step by step
+        from here, with the same result bits."""
         if self.f_mean is None:
             self.fit_normalisation(feats, targets)
         X = self.prepare_inputs(feats)
+        T = targets.contiguous()
         n = feats.shape[0] // self.B * self.B
         per_epoch = n // self.B
         total = epochs * per_epoch
         history = []
+        net = self._net() if native else None
         torch.cuda.synchronize(self.dev)
         t0 = time.perf_counter()
         it = 0
         for e in range(epochs):
             shift = (e * 997) % (feats.shape[0] - n + 1)
             self.loss_d.zero_()
+            rows = np.empty(per_epoch, dtype=np.int64)
+            lrs = np.empty(per_epoch, dtype=np.float32)
             for i in range(per_epoch):
-                a = shift + i * self.B
-                g = it / max(total - 1, 1)
+                rows[i] = shift + i * self.B
+                g = (it + i) / max(total - 1, 1)
                 cur = lr_final + 0.5 * (lr - lr_final) * (1.0 + math.cos(math.pi * g))
-                if it < warmup:
-                    cur *= (it + 1) / warmup
-                self.forward_backward(X[a:a + self.B], targets[a:a + self.B])
-                self.optimizer_step(cur)
-                it += 1
+                if it + i < warmup:
+                    cur *= (it + i + 1) / warmup
+                lrs[i] = cur
+            if native:
+                self._ck(self.lib.hydro_nn_train(self.h.ctx, C.byref(net), _ptr(X), _ptr(T), feats.shape[0],
+                                                 rows.ctypes.data, lrs.ctypes.data, per_epoch, self.step,
+                                                 0.9, 0.999, 1e-8, 1e-5, self._s()))
+                self.step += per_epoch
+                self._infer.clear()
+            else:
+                for i in range(per_epoch):
+                    a = int(rows[i])
+                    self.forward_backward(X[a:a + self.B], T[a:a + self.B])
+                    self.optimizer_step(float(lrs[i]))
+            it += per_epoch
             mean_loss = float(self.loss_d.item()) / per_epoch
             history.append(mean_loss)
             if log:

@@ -63,6 +63,30 @@ def test_gemm_epilogues(hctx, epi):
         assert np.all(np.abs(yy - expect) <= tol + 1e-6)
 
 
+@pytest.mark.parametrize("M,N", [(256, 256), (64, 256), (256, 64)])
+def test_weight_gradient_gemm_split_along_k(hctx, M, N):
+    """The weight-gradient shapes (K = batch 4096, few output tiles) run
+    split along K: the partial products are summed in slice order, so the
+    result is within FP32 accumulation of the exact product and repeats
+    bit for bit."""
+    rng = np.random.default_rng(M + N)
+    K = 4096
+    A = mlp.bf16_round(rng.normal(size=(M, K)).astype(np.float32))
+    B = mlp.bf16_round(rng.normal(size=(K, N)).astype(np.float32))
+    dA, dB = _dev(A, torch.bfloat16), _dev(B, torch.bfloat16)
+    outs = []
+    for _ in range(2):
+        z = torch.full((M, N), float("nan"), dtype=torch.float32, device="cuda")
+        _ck(hctx, hctx.lib.hydro_nn_gemm(hctx.ctx, 0, S._ptr(dA), K, S._ptr(dB), N, M, N, K, S._ptr(z), None,
+                                         None, None, N, None))
+        torch.cuda.synchronize()
+        outs.append(z.cpu().numpy())
+    ref = A.astype(np.float64) @ B.astype(np.float64)
+    scale = np.abs(A).astype(np.float64) @ np.abs(B).astype(np.float64)
+    assert np.all(np.abs(outs[0] - ref) <= 1e-5 * scale + 1e-6)
+    assert np.array_equal(outs[0], outs[1])
+
+
 def test_gemm_rejects_unaligned_shapes(hctx):
     a = torch.zeros((64, 64), dtype=torch.bfloat16, device="cuda")
     z = torch.zeros((64, 64), dtype=torch.float32, device="cuda")
@@ -289,6 +313,41 @@ def test_surrogate_learns_and_beats_exact_step(built_library):
         o.close()
     h32.close()
     h64.close()
+
+
+def test_native_training_loop_matches_step_by_step_calls(hctx):
+    """hydro_nn_train (every step's kernels launched by the library) against
+    the same steps called one entry point at a time: the same kernels in the
+    same order, so weights, moments and bf16 copies are bit-identical."""
+    rng = np.random.default_rng(41)
+    n = 7 * 256 + 37
+    feats = _dev(rng.normal(size=(n, S.N_FEAT)) * 1.5 + 0.5)
+    targ = _dev(rng.normal(size=(n, S.N_OUT)) * 40.0 + 5.0)
+    nets = []
+    losses = []
+    for native in (True, False):
+        sur = S.Surrogate(hctx, hidden=256, seed=11, batch=256)
+        sur.fit_normalisation(feats, targ)
+        info = sur.fit(feats, targ, epochs=3, lr=3e-3, warmup=5, native=native)
+        torch.cuda.synchronize()
+        nets.append(sur)
+        losses.append(info["loss"])
+    a, b = nets
+    assert a.step == b.step == 3 * 7
+    # the epoch losses are FP64 sums of per-block atomics (their order varies)
+    np.testing.assert_allclose(losses[0], losses[1], rtol=1e-12)
+    for La, Lb in zip(a.layers, b.layers):
+        for f in ("w", "b", "mw", "vw", "mb", "vb", "w16", "wt16"):
+            assert torch.equal(La[f], Lb[f]), f
+    # a batch past the end of the inputs is rejected before anything runs
+    net = a._net()
+    X = a.prepare_inputs(feats)
+    rows = np.array([n - 255], dtype=np.int64)
+    lrs = np.array([1e-3], dtype=np.float32)
+    st = hctx.lib.hydro_nn_train(hctx.ctx, C.byref(net), S._ptr(X), S._ptr(targ), n, rows.ctypes.data,
+                                 lrs.ctypes.data, 1, 0, 0.9, 0.999, 1e-8, 1e-5, None)
+    assert st == abi.HYDRO_ERR_INVALID_ARG
+    assert torch.equal(a.layers[0]["w"], b.layers[0]["w"])
 
 
 @pytest.mark.parametrize("n", [1000, 4096])

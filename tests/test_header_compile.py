@@ -25,7 +25,7 @@ STRUCTS = {
     "hydro_cable": abi.Cable, "hydro_cable_node_forces": abi.CableNodeForces, "hydro_atmosphere": abi.Atmosphere,
     "hydro_aero_params": abi.AeroParams, "hydro_aero_wrench": abi.AeroWrench, "hydro_body": abi.Body,
     "hydro_wrench": abi.Wrench, "hydro_rigid_state": abi.RigidState, "hydro_tune_result": abi.TuneResult,
-    "hydro_config": abi.Config,
+    "hydro_config": abi.Config, "hydro_nn_layer": abi.NnLayer, "hydro_nn_net": abi.NnNet,
 }
 LIB_DIR = os.path.dirname(abi.LIB_PATH)
 WARN = ["-Wall", "-Wextra", "-Werror", "-pedantic"]
