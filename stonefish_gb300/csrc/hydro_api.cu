@@ -1979,7 +1979,7 @@ static bool nn_workspace(hydro_ctx* ctx, size_t floats, cudaStream_t s)
         return false;
     }
     if (ctx->nn_ws) {
-        cudaStreamSynchronize(s);
+        cudaDeviceSynchronize();   // a product on any stream may still read the old workspace
         cudaFree(ctx->nn_ws);
     }
     ctx->nn_ws = p;
@@ -2077,7 +2077,7 @@ extern "C" hydro_status hydro_nn_train(hydro_ctx* ctx, const hydro_nn_net* net, 
     if ((!net->tmean) != (!net->tistd) || (uint64_t)B * (uint64_t)net->layer[3].n >= (1ull << 32))
         return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn train: bad target normalisation");
     for (int32_t s = 0; s < n_steps; ++s)
-        if (rows[s] < 0 || rows[s] + B > n_rows || step0 + s + 1 < 1)
+        if (rows[s] < 0 || rows[s] > n_rows - B || (int64_t)step0 + s + 1 > (int64_t)INT32_MAX)
             return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn train: batch rows out of range");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const hydro_nn_layer* Ls = net->layer;
