@@ -765,7 +765,13 @@ hydro_status hydro_debug_fft_ocean_tables(const hydro_fft_ocean_params* params, 
 /* C[M,N] = A[M,K] (bf16, row stride lda) x B[K,N] (bf16, row stride ldb)
  * on the BF16 tensor cores with FP32 accumulation, followed by `epilogue`;
  * outputs z (FP32) and y (bf16) have row stride ldc.  M and N must be
- * multiples of 64, K a multiple of 32. */
+ * multiples of 64, K a multiple of 32.  A plain product (HYDRO_NN_EPI_F32)
+ * with few 64 x 64 output tiles and a long K (a weight gradient, K = the
+ * batch) is split along K into partial products in the context's
+ * workspace, which a second kernel sums in a fixed order (deterministic).
+ * The workspace is one per context: calls that use it (this, large-row
+ * hydro_nn_colsum, hydro_nn_train) must not run concurrently on different
+ * streams. */
 hydro_status hydro_nn_gemm(hydro_ctx* ctx, int32_t epilogue, const void* A, int32_t lda,
                            const void* B, int32_t ldb, int32_t M, int32_t N, int32_t K,
                            float* z, void* y, const float* bias, const float* zprev,
@@ -784,7 +790,9 @@ hydro_status hydro_nn_mse_grad(hydro_ctx* ctx, const float* z, const float* targ
                                int32_t ld, int32_t n_out, const float* tmean, const float* tistd,
                                void* dz, double* loss, void* stream);
 
-/* out[c] = sum over rows of the bf16 matrix g[rows][cols] (bias gradients). */
+/* out[c] = sum over rows of the bf16 matrix g[rows][cols] (bias gradients),
+ * in a fixed order; from 2048 rows on, in row slabs whose partial sums go
+ * through the context's workspace (see hydro_nn_gemm). */
 hydro_status hydro_nn_colsum(hydro_ctx* ctx, const void* g, int32_t rows, int32_t cols, float* out,
                              void* stream);
 

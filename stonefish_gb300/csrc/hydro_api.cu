@@ -2035,7 +2035,10 @@ extern "C" hydro_status hydro_nn_colsum(hydro_ctx* ctx, const void* g, int32_t r
 {
     NN_CTX_CHECK();
     if (!g || !out || rows <= 0 || cols <= 0) return fail(ctx, HYDRO_ERR_INVALID_ARG, "nn colsum");
-    NN_RET(launch_colsum(g, rows, cols, out, static_cast<cudaStream_t>(stream)), "nn colsum");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const size_t ws = (size_t)colsum_slabs(rows) * (size_t)cols;
+    if (ws > (size_t)cols && !nn_workspace(ctx, ws, st)) return fail(ctx, HYDRO_ERR_OOM, "nn colsum: workspace");
+    NN_RET(launch_colsum(g, rows, cols, out, st, ctx->nn_ws, ctx->nn_ws_floats), "nn colsum");
 }
 
 extern "C" hydro_status hydro_nn_adamw(hydro_ctx* ctx, float* w, float* m, float* v, const float* grad,
@@ -2083,8 +2086,10 @@ extern "C" hydro_status hydro_nn_train(hydro_ctx* ctx, const hydro_nn_net* net, 
     const hydro_nn_layer* Ls = net->layer;
     const int k0 = Ls[0].k, n_out = net->n_out;
     size_t ws = 0;
-    for (int l = 0; l < 4; ++l)
+    for (int l = 0; l < 4; ++l) {
         ws = std::max(ws, (size_t)gemm_splits(0, Ls[l].k, Ls[l].n, B) * (size_t)Ls[l].k * (size_t)Ls[l].n);
+        ws = std::max(ws, (size_t)colsum_slabs(B) * (size_t)Ls[l].n);
+    }
     if (!nn_workspace(ctx, ws, st)) return fail(ctx, HYDRO_ERR_OOM, "nn train: split-K workspace");
     cudaError_t e = cudaSuccess;
 #define NN_TRAIN(call)                                  \
@@ -2107,7 +2112,7 @@ extern "C" hydro_status hydro_nn_train(hydro_ctx* ctx, const hydro_nn_net* net, 
             NN_TRAIN(launch_transpose(ins[l], net->xt[l], B, L.k, st));
             NN_TRAIN(launch_gemm(0, net->xt[l], B, net->dz[l], L.n, L.k, L.n, B, L.gw, nullptr, nullptr, nullptr,
                                  L.n, st, ctx->nn_ws, ctx->nn_ws_floats));
-            NN_TRAIN(launch_colsum(net->dz[l], B, L.n, L.gb, st));
+            NN_TRAIN(launch_colsum(net->dz[l], B, L.n, L.gb, st, ctx->nn_ws, ctx->nn_ws_floats));
             if (l > 0)
                 NN_TRAIN(launch_gemm(3, net->dz[l], L.n, L.wt16, L.k, B, L.k, L.n, nullptr, net->dz[l - 1], nullptr,
                                      net->z[l - 1], L.k, st));

@@ -131,7 +131,11 @@ cudaError_t launch_gemm(int epi, const void* A, int lda, const void* B, int ldb,
 cudaError_t launch_transpose(const void* src, void* dst, int rows, int cols, cudaStream_t s);
 cudaError_t launch_mse_grad(const float* z, const float* t, int rows, int ld, int n_out, const float* tmean,
                             const float* tistd, void* dz, double* loss, cudaStream_t s);
-cudaError_t launch_colsum(const void* g, int rows, int cols, float* out, cudaStream_t s);
+// Column sums; with ws holding colsum_slabs(rows) * cols floats, in two
+// stages (row slabs, then the slabs in order).
+int colsum_slabs(int rows);
+cudaError_t launch_colsum(const void* g, int rows, int cols, float* out, cudaStream_t s, float* ws = nullptr,
+                          size_t ws_floats = 0);
 cudaError_t launch_adamw(float* w, float* m, float* v, const float* grad, int rows, int cols, int ldg,
                          float lr, float b1, float b2, float eps, float wd, int step, void* w16,
                          void* wt16, cudaStream_t s);

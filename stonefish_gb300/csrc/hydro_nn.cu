@@ -8,6 +8,7 @@
 // mma.sync m16n8k16 tiles fed by ldmatrix from shared memory; 64x64 CTA
 // tiles, four warps of 32x32.  M, N multiples of 64 and K a multiple of 32
 // (the host pads), so no tile is partial.
+#include <algorithm>
 #include <cstddef>
 #include <cstdint>
 #include <cuda_bf16.h>
@@ -63,8 +64,10 @@ __global__ void __launch_bounds__(128) gemm_kernel(const bf16* __restrict__ A, i
                                                    const bf16* __restrict__ B, int ldb, int K,
                                                    EpiArgs e)
 {
-    __shared__ __align__(16) bf16 As[BM][BK + APAD];
-    __shared__ __align__(16) bf16 Bs[BK][BN + BPAD];
+    // two stages: the next K-step's tiles are loaded into registers while
+    // the current one is multiplied, then stored into the other stage
+    __shared__ __align__(16) bf16 As[2][BM][BK + APAD];
+    __shared__ __align__(16) bf16 Bs[2][BK][BN + BPAD];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
     if (EPI == EPI_F32 && blockIdx.z > 0) {
@@ -83,30 +86,42 @@ __global__ void __launch_bounds__(128) gemm_kernel(const bf16* __restrict__ A, i
 #pragma unroll
             for (int k = 0; k < 4; ++k) acc[i][j][k] = 0.f;
 
-    for (int k0 = 0; k0 < K; k0 += BK) {
+    uint4 ra[2], rb[2];
+    auto load = [&](int k0) {
 #pragma unroll
         for (int i = 0; i < 2; ++i) {
             const int c = tid + i * 128;
-            const int r = c >> 2, col = (c & 3) * 8;
-            *reinterpret_cast<uint4*>(&As[r][col]) =
-                *reinterpret_cast<const uint4*>(A + (size_t)(m0 + r) * lda + k0 + col);
-            const int rb = c >> 3, cb = (c & 7) * 8;
-            *reinterpret_cast<uint4*>(&Bs[rb][cb]) =
-                *reinterpret_cast<const uint4*>(B + (size_t)(k0 + rb) * ldb + n0 + cb);
+            ra[i] = *reinterpret_cast<const uint4*>(A + (size_t)(m0 + (c >> 2)) * lda + k0 + (c & 3) * 8);
+            rb[i] = *reinterpret_cast<const uint4*>(B + (size_t)(k0 + (c >> 3)) * ldb + n0 + (c & 7) * 8);
         }
-        __syncthreads();
+    };
+    auto store = [&](int st) {
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            const int c = tid + i * 128;
+            *reinterpret_cast<uint4*>(&As[st][c >> 2][(c & 3) * 8]) = ra[i];
+            *reinterpret_cast<uint4*>(&Bs[st][c >> 3][(c & 7) * 8]) = rb[i];
+        }
+    };
+    load(0);
+    store(0);
+    __syncthreads();
+    int st = 0;
+    for (int k0 = 0; k0 < K; k0 += BK) {
+        const bool more = k0 + BK < K;
+        if (more) load(k0 + BK);
 #pragma unroll
         for (int kk = 0; kk < BK; kk += 16) {
             uint32_t a[2][4];
 #pragma unroll
             for (int mi = 0; mi < 2; ++mi)
-                ldsm_x4(a[mi], &As[wm + mi * 16 + (lane & 15)][kk + (lane >> 4) * 8]);
+                ldsm_x4(a[mi], &As[st][wm + mi * 16 + (lane & 15)][kk + (lane >> 4) * 8]);
             uint32_t b[4][2];
 #pragma unroll
             for (int nj = 0; nj < 2; ++nj) {
                 const int j = lane >> 3;
                 uint32_t r[4];
-                ldsm_x4_t(r, &Bs[kk + (lane & 7) + 8 * (j & 1)][wn + nj * 16 + 8 * (j >> 1)]);
+                ldsm_x4_t(r, &Bs[st][kk + (lane & 7) + 8 * (j & 1)][wn + nj * 16 + 8 * (j >> 1)]);
                 b[2 * nj][0] = r[0];
                 b[2 * nj][1] = r[1];
                 b[2 * nj + 1][0] = r[2];
@@ -117,7 +132,10 @@ __global__ void __launch_bounds__(128) gemm_kernel(const bf16* __restrict__ A, i
 #pragma unroll
                 for (int ni = 0; ni < 4; ++ni) mma_bf16(acc[mi][ni], a[mi], b[ni][0], b[ni][1]);
         }
+        // the other stage was last read before the previous barrier
+        if (more) store(st ^ 1);
         __syncthreads();
+        st ^= 1;
     }
 
 #pragma unroll
@@ -293,8 +311,52 @@ __global__ void __launch_bounds__(1024) colsum_kernel(const bf16* __restrict__ g
     }
 }
 
-cudaError_t launch_colsum(const void* g, int rows, int cols, float* out, cudaStream_t s)
+// The same sums over many rows in two stages, so that more than a handful
+// of SMs read the matrix: CTA (x, y) sums 32 columns over row slab y (the
+// single-stage order within the slab) into ws[y][c], then out[c] adds the
+// slabs' partial sums in slab order.
+__global__ void __launch_bounds__(1024) colsum_slab_kernel(const bf16* __restrict__ g, int rows, int cols,
+                                                           int slab_rows, float* __restrict__ ws)
 {
+    __shared__ float part[32][33];
+    const int c = blockIdx.x * 32 + threadIdx.x;
+    const int r0 = blockIdx.y * slab_rows, r1 = min(rows, r0 + slab_rows);
+    float s = 0.f;
+    if (c < cols)
+        for (int r = r0 + threadIdx.y; r < r1; r += 32) s += __bfloat162float(g[(size_t)r * cols + c]);
+    part[threadIdx.y][threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.y == 0 && c < cols) {
+        float t = 0.f;
+        for (int k = 0; k < 32; ++k) t += part[k][threadIdx.x];
+        ws[(size_t)blockIdx.y * cols + c] = t;
+    }
+}
+
+__global__ void colsum_slabs_kernel(const float* __restrict__ ws, int slabs, int cols, float* __restrict__ out)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= cols) return;
+    float t = 0.f;
+    for (int k = 0; k < slabs; ++k) t += ws[(size_t)k * cols + c];
+    out[c] = t;
+}
+
+int colsum_slabs(int rows) { return rows >= 2048 ? std::min(32, rows / 256) : 1; }
+
+cudaError_t launch_colsum(const void* g, int rows, int cols, float* out, cudaStream_t s, float* ws,
+                          size_t ws_floats)
+{
+    const int slabs = colsum_slabs(rows);
+    if (slabs > 1 && ws && (size_t)slabs * cols <= ws_floats) {
+        const int slab_rows = (rows + slabs - 1) / slabs;
+        colsum_slab_kernel<<<dim3((cols + 31) / 32, slabs), dim3(32, 32), 0, s>>>(static_cast<const bf16*>(g), rows,
+                                                                                   cols, slab_rows, ws);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        colsum_slabs_kernel<<<(cols + 255) / 256, 256, 0, s>>>(ws, slabs, cols, out);
+        return cudaGetLastError();
+    }
     colsum_kernel<<<(cols + 31) / 32, dim3(32, 32), 0, s>>>(static_cast<const bf16*>(g), rows, cols, out);
     return cudaGetLastError();
 }

@@ -87,6 +87,26 @@ def test_weight_gradient_gemm_split_along_k(hctx, M, N):
     assert np.array_equal(outs[0], outs[1])
 
 
+@pytest.mark.parametrize("rows,cols", [(4096, 256), (4096, 64), (3000, 192), (256, 64)])
+def test_bias_gradient_column_sums(hctx, rows, cols):
+    """hydro_nn_colsum: one stage below 2048 rows, row slabs plus an in-order
+    sum of the slabs above; FP32 sums of bf16 values within FP32 rounding of
+    the exact sums, and the same bits on a second call."""
+    rng = np.random.default_rng(rows + cols)
+    g = mlp.bf16_round(rng.normal(size=(rows, cols)).astype(np.float32))
+    dg = _dev(g, torch.bfloat16)
+    outs = []
+    for _ in range(2):
+        out = torch.full((cols,), float("nan"), dtype=torch.float32, device="cuda")
+        _ck(hctx, hctx.lib.hydro_nn_colsum(hctx.ctx, S._ptr(dg), rows, cols, S._ptr(out), None))
+        torch.cuda.synchronize()
+        outs.append(out.cpu().numpy())
+    ref = g.astype(np.float64).sum(axis=0)
+    scale = np.abs(g).astype(np.float64).sum(axis=0)
+    assert np.all(np.abs(outs[0] - ref) <= 1e-5 * scale + 1e-6)
+    assert np.array_equal(outs[0], outs[1])
+
+
 def test_gemm_rejects_unaligned_shapes(hctx):
     a = torch.zeros((64, 64), dtype=torch.bfloat16, device="cuda")
     z = torch.zeros((64, 64), dtype=torch.float32, device="cuda")
