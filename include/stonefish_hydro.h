@@ -681,6 +681,20 @@ hydro_status hydro_batch_compute_aero(hydro_batch* batch, const hydro_body* bodi
                                       hydro_aero_wrench* out);
 
 /* ------------------------------------------------------------ diagnostics */
+/* The debug geometry of the reference's surface loop: with DEBUG_HYDRO,
+ * ComputeHydrodynamicForcesSurface (SolidEntity.cpp:1390-1396 and the
+ * matching blocks of the other clip cases) records the outline of every
+ * submerged triangle or quad it evaluates, as line segments, in the
+ * `Renderable& debug` argument.  For one body (hydro_surface_forces's
+ * inputs as a body record), this writes the same points in the same order:
+ * faces in mesh order, each outline as 2 points per edge (6 for a triangle,
+ * 8 for a quad), world frame, x y z floats.  Up to `capacity` points are
+ * written; *n_points receives the total (call with capacity 0 to size the
+ * buffer). */
+hydro_status hydro_debug_surface_outline(hydro_ctx* ctx, const hydro_body* body,
+                                         const hydro_ocean* ocean, const hydro_settings* settings,
+                                         float* points, uint32_t capacity, uint32_t* n_points);
+
 /* Per-face contributions of the surface loop (ComputeHydrodynamicForcesSurface,
  * SolidEntity.cpp:1337-1687) for one body, computed by the same device code
  * as the batched kernel: out receives n_faces * 23 floats in uploaded face

@@ -33,6 +33,9 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_ref")
 LIB = os.path.join(OUT_DIR, "libstonefish_ref.so")
+# the same functions compiled with the reference's DEBUG_HYDRO switch, which
+# records the outline of every submerged face part the surface loop evaluates
+LIB_DEBUG = os.path.join(OUT_DIR, "libstonefish_ref_debug.so")
 ROOT_NOTE = os.path.join(OUT_DIR, "source_root.txt")
 DEFAULT_ROOT = "/root/reference"
 
@@ -208,15 +211,23 @@ def build_ref(force: bool = False) -> str | None:
     if root is None:
         return LIB if os.path.exists(LIB) else None
     srcs = _inputs() + [os.path.join(root, rel) for rel, _ in TYPES + FUNCTIONS]
-    if not force and os.path.exists(LIB) and all(os.path.getmtime(s) <= os.path.getmtime(LIB) for s in srcs):
+    if not force and all(os.path.exists(L) and all(os.path.getmtime(s) <= os.path.getmtime(L) for s in srcs)
+                         for L in (LIB, LIB_DEBUG)):
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
     tu = translation_unit(root)
-    cmd = [os.environ.get("CXX", "g++"), *CXXFLAGS, "-I", HERE, "-I", os.path.join(root, "3rdparty"),
-           "-I", os.path.join(os.path.dirname(HERE), "include"), "-x", "c++", "-", "-o", LIB]
-    r = subprocess.run(cmd, input=tu.encode(), stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
-    if r.returncode != 0:
-        raise RuntimeError("reference build failed:\n" + r.stdout.decode(errors="replace")[-6000:])
+    procs = []
+    for out, extra in ((LIB, []), (LIB_DEBUG, ["-DDEBUG_HYDRO"])):
+        cmd = [os.environ.get("CXX", "g++"), *CXXFLAGS, *extra, "-I", HERE, "-I", os.path.join(root, "3rdparty"),
+               "-I", os.path.join(os.path.dirname(HERE), "include"), "-x", "c++", "-", "-o", out]
+        p = subprocess.Popen(cmd, stdin=subprocess.PIPE, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+        procs.append(p)
+        p.stdin.write(tu.encode())
+        p.stdin.close()
+    for p in procs:
+        log = p.stdout.read()
+        if p.wait() != 0:
+            raise RuntimeError("reference build failed:\n" + log.decode(errors="replace")[-6000:])
     with open(ROOT_NOTE, "w") as f:
         f.write(root + "\n")
     return LIB

@@ -16,7 +16,7 @@ import numpy as np
 
 from stonefish_gb300 import abi
 
-from .build_ref import LIB, ROOT_NOTE, build_ref
+from .build_ref import LIB, LIB_DEBUG, ROOT_NOTE, build_ref
 from .oracle import Oracle, OracleMesh
 
 
@@ -141,6 +141,29 @@ class Reference:
         self.lib.ref_surface_forces(C.byref(settings), self._p(m), C.byref(ocean), self._p(w), C.byref(T_CG),
                                     C.byref(T_C), pv, pw, *ptrs)
         return io
+
+    def surface_outline(self, settings, mesh, ocean, T_CG, T_C, v, omega, waves=None) -> np.ndarray:
+        """The points the reference's DEBUG_HYDRO build records in
+        ComputeHydrodynamicForcesSurface (float32 [n, 3], two per segment)."""
+        if not hasattr(self, "dbg"):
+            self.dbg = C.CDLL(LIB_DEBUG)
+            P = C.POINTER
+            d = C.POINTER(C.c_double)
+            self.dbg.ref_surface_outline.restype = C.c_int32
+            self.dbg.ref_surface_outline.argtypes = [P(abi.Settings), C.c_void_p, P(abi.Ocean), C.c_void_p,
+                                                     P(abi.Transform), P(abi.Transform), d, d, C.c_void_p,
+                                                     C.c_uint32, P(C.c_uint32)]
+        m = None if mesh is None else self.make_mesh(*mesh)
+        w = self.make_waves(waves)
+        vv, pv = self._vec(v)
+        ww, pw = self._vec(omega)
+        n = C.c_uint32(0)
+        args = (C.byref(settings), self._p(m), C.byref(ocean), self._p(w), C.byref(T_CG), C.byref(T_C), pv, pw)
+        if self.dbg.ref_surface_outline(*args, None, 0, C.byref(n)):
+            raise ValueError("wave data not expressible as the reference's two-layer texture")
+        pts = np.zeros((n.value, 3), dtype=np.float32)
+        self.dbg.ref_surface_outline(*args, pts.ctypes.data, n.value, C.byref(n))
+        return pts
 
     def submerged_forces(self, mesh, ocean, T_CG, T_C, v, omega, io):
         m = None if mesh is None else self.make_mesh(*mesh)

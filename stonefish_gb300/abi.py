@@ -255,6 +255,8 @@ def _declare(lib: C.CDLL) -> None:
         "hydro_correct_forces": (i32, [vp, C.POINTER(Ocean), d, d, d, d, d, d, d]),
         "hydro_fluid_position": (i32, [vp, C.POINTER(Ocean), d, d, C.POINTER(i32)]),
         "hydro_debug_division_check": (i32, [vp, C.c_uint64, C.c_uint64, vp]),
+        "hydro_debug_surface_outline": (i32, [vp, vp, C.POINTER(Ocean), C.POINTER(Settings), vp, u32,
+                                              C.POINTER(u32)]),
         "hydro_debug_tile_order": (i32, [vp, u32, u32, vp, vp, u32, C.POINTER(u32)]),
         "hydro_mapped_host_ptr": (i32, [vp, C.POINTER(vp)]),
         "hydro_compute_wrenches": (i32, [vp, vp, u32, vp, vp, vp, vp, vp]),

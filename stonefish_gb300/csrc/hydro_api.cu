@@ -1715,6 +1715,50 @@ hydro_status hydro_fluid_position(hydro_ctx* ctx, const hydro_ocean* ocean, cons
 }
 
 // Per-face surface-loop terms of one body (n_faces * 23 floats, host).
+hydro_status hydro_debug_surface_outline(hydro_ctx* ctx, const hydro_body* body, const hydro_ocean* ocean,
+                                         const hydro_settings* settings, float* points, uint32_t capacity,
+                                         uint32_t* n_points)
+{
+    if (!ctx) return HYDRO_ERR_INVALID_ARG;
+    std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+    if (!body || !valid_ocean(ocean) || !settings || !n_points || (capacity && !points) ||
+        body->mesh >= ctx->meshes.size())
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "surface outline: bad arguments");
+    if (ocean->waves && !ctx->wave_d) return fail(ctx, HYDRO_ERR_INVALID_ARG, "no wave grid");
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return fail(ctx, HYDRO_ERR_DEVICE, "cudaSetDevice");
+    hydro_status st = sync_tiles(ctx);
+    if (st != HYDRO_OK) return st;
+    const MeshRec& m = ctx->meshes[body->mesh];
+    const size_t bytes = (size_t)m.n_faces * 13 * sizeof(float);
+    st = ensure_small(ctx, bytes + sizeof(hydro_body) + 256);
+    if (st != HYDRO_OK) return st;
+    char* base = static_cast<char*>(ctx->small_d);
+    hydro_body* db = reinterpret_cast<hydro_body*>(base);
+    float* dout = reinterpret_cast<float*>(base + 256 * ((sizeof(hydro_body) + 255) / 256));
+    CK(ctx, cudaMemcpyAsync(db, body, sizeof(hydro_body), cudaMemcpyHostToDevice, ctx->stream));
+    SettingsDev sd{settings->damping_forces ? 1 : 0, settings->realistic_buoyancy ? 1 : 0};
+    cudaError_t e = launch_outline(ctx->tiles_d, m.first_tile, m.n_tiles, db, make_ocean(ctx, ocean), sd,
+                                   ctx->cfg.cut_precision == HYDRO_CUT_FP64, dout, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "outline kernel");
+    std::vector<float> rec((size_t)m.n_faces * 13);
+    CK(ctx, cudaMemcpyAsync(rec.data(), dout, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(ctx, cudaStreamSynchronize(ctx->stream));
+    // segments in the reference's order: faces in mesh order, each outline
+    // as (c0, c1), (c1, c2), ..., (c_last, c0)
+    uint32_t n = 0;
+    for (size_t f = 0; f < m.n_faces; ++f) {
+        const float* r = &rec[f * 13];
+        const int k = (int)r[0];
+        for (int i = 0; i < k; ++i) {
+            const float* c[2] = {r + 1 + 3 * i, r + 1 + 3 * ((i + 1) % k)};
+            for (int j = 0; j < 2; ++j, ++n)
+                if (n < capacity) std::memcpy(points + 3 * (size_t)n, c[j], 3 * sizeof(float));
+        }
+    }
+    *n_points = n;
+    return HYDRO_OK;
+}
+
 hydro_status hydro_debug_face_terms(hydro_ctx* ctx, const hydro_body* body, const hydro_ocean* ocean,
                                     const hydro_settings* settings, int32_t packed, float* out)
 {

@@ -505,9 +505,22 @@ __device__ __forceinline__ void face_forces(const OceanDev& o, const BodyParams&
 }
 
 // One face straddling the surface: the six mixed clip cases (:1360-1617).
-template <bool CUT64, bool WAVES>
+// The outline of an evaluated submerged part (the points the reference's
+// DEBUG_HYDRO build records, SolidEntity.cpp:1390-1396 and the matching
+// blocks of the other cases): ol[0] = corner count (3 or 4), then the
+// corners in outline order.  OUTLINE = false compiles it away.
+__device__ __forceinline__ void put_outline(float* ol, int n, v3 a, v3 b, v3 c, v3 d)
+{
+    ol[0] = (float)n;
+    ol[1] = a.x; ol[2] = a.y; ol[3] = a.z;
+    ol[4] = b.x; ol[5] = b.y; ol[6] = b.z;
+    ol[7] = c.x; ol[8] = c.y; ol[9] = c.z;
+    ol[10] = d.x; ol[11] = d.y; ol[12] = d.z;
+}
+
+template <bool CUT64, bool WAVES, bool OUTLINE = false>
 __device__ __forceinline__ void face_cut(const OceanDev& o, const BodyParams& B, Acc& a,
-                                      v3 p1, v3 p2, v3 p3, float d0, float d1, float d2)
+                                      v3 p1, v3 p2, v3 p3, float d0, float d1, float d2, float* ol = nullptr)
 {
     v3 p4 = mk(0.f, 0.f, 0.f);
     bool quad = false;
@@ -546,6 +559,7 @@ __device__ __forceinline__ void face_cut(const OceanDev& o, const BodyParams& B,
     float A;
     if (!quad) {
         if (!tri_props(p1, p2, p3, fc, fn1, A)) return;
+        if (OUTLINE) put_outline(ol, 3, p1, p2, p3, p3);
     } else {
         v3 p04 = sub(p4, B.p0);
         v3 fv1 = sub(p2, p1);
@@ -563,6 +577,10 @@ __device__ __forceinline__ void face_cut(const OceanDev& o, const BodyParams& B,
         v3 fn = cross(fv1, fv2);
         float len = dot(fn, fn);
         if (len < 1e-12f) return;
+        if (OUTLINE) {
+            if (kind == 0) put_outline(ol, 4, p1, p2, p3, p4);
+            else put_outline(ol, 4, p1, p2, p4, p3);
+        }
         len = sqrtf(len);
         fn1 = dvs_rcp(fn, len);
         v3 c2 = cross(fv3, fv4);
@@ -573,15 +591,16 @@ __device__ __forceinline__ void face_cut(const OceanDev& o, const BodyParams& B,
 
 // A surface-loop face whose three corners are all under water
 // (:1618-1647, then :1650-1686).
-template <bool WAVES>
+template <bool WAVES, bool OUTLINE = false>
 __device__ __forceinline__ void face_full(const OceanDev& o, const BodyParams& B, Acc& a,
-                                          float4 q1, float4 q2, float4 q3)
+                                          float4 q1, float4 q2, float4 q3, float* ol = nullptr)
 {
     v3 p1 = mk(q1.x, q1.y, q1.z), p2 = mk(q2.x, q2.y, q2.z), p3 = mk(q3.x, q3.y, q3.z);
     tetra(a, sub(p1, B.p0), sub(p2, B.p0), sub(p3, B.p0));
     v3 fc, fn1;
     float A;
     if (!tri_props(p1, p2, p3, fc, fn1, A)) return;
+    if (OUTLINE) put_outline(ol, 3, p1, p2, p3, p3);
     face_forces<WAVES>(o, B, a, fc, fn1, A);
 }
 
@@ -596,18 +615,18 @@ __device__ __forceinline__ int face_class(float d0, float d1, float d2)
 
 // One face of the surface loop (:1337-1687) given transformed vertices
 // (x, y, z, depth).
-template <bool CUT64, bool WAVES>
+template <bool CUT64, bool WAVES, bool OUTLINE = false>
 __device__ __forceinline__ void face_surface(const OceanDev& o, const BodyParams& B, Acc& a,
-                                             float4 q1, float4 q2, float4 q3)
+                                             float4 q1, float4 q2, float4 q3, float* ol = nullptr)
 {
     const int cls = face_class(q1.w, q2.w, q3.w);
     if (cls == 0) return;
     if (cls == 2) {
-        face_cut<CUT64, WAVES>(o, B, a, mk(q1.x, q1.y, q1.z), mk(q2.x, q2.y, q2.z),
-                               mk(q3.x, q3.y, q3.z), q1.w, q2.w, q3.w);
+        face_cut<CUT64, WAVES, OUTLINE>(o, B, a, mk(q1.x, q1.y, q1.z), mk(q2.x, q2.y, q2.z),
+                                        mk(q3.x, q3.y, q3.z), q1.w, q2.w, q3.w, ol);
         return;
     }
-    face_full<WAVES>(o, B, a, q1, q2, q3);
+    face_full<WAVES, OUTLINE>(o, B, a, q1, q2, q3, ol);
 }
 
 // One face of the submerged loop (:1748-1789)

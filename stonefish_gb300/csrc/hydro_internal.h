@@ -95,6 +95,12 @@ cudaError_t launch_face_terms(const TileDesc* tiles, uint32_t first_tile, uint32
                              const hydro_body* body, OceanDev ocean, SettingsDev st, int frame,
                              int cut64, int packed, float* out, cudaStream_t s);
 
+// Outlines of the submerged face parts of one body's surface loop (the
+// reference's DEBUG_HYDRO points): out holds n_faces * 13 floats in uploaded
+// face order (count 0, 3 or 4, then four corners x, y, z), world frame.
+cudaError_t launch_outline(const TileDesc* tiles, uint32_t first_tile, uint32_t n_tiles, const hydro_body* body,
+                           OceanDev ocean, SettingsDev st, int cut64, float* out, cudaStream_t s);
+
 // CorrectHydrodynamicForces on 4 vectors (io: Fdq, Tdq, Fdf, Tdf), one thread.
 cudaError_t launch_correct(double density, double* io12, const double* Cd, const double* Cf,
                            const double* R_O, cudaStream_t s);

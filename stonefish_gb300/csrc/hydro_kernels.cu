@@ -1497,6 +1497,56 @@ __global__ void __launch_bounds__(kBlock) face_terms_kernel(const TileDesc* tile
     }
 }
 
+// The outlines the reference's DEBUG_HYDRO build records for one body in
+// the surface loop: one thread per face on the scalar path, in the world
+// frame like the reference; out receives 13 floats per face in uploaded
+// face order (corner count 0, 3 or 4, then four corners).
+template <bool CUT64>
+__global__ void __launch_bounds__(kBlock) outline_kernel(const TileDesc* tiles, uint32_t first_tile,
+                                                         const hydro_body* body, OceanDev ocean, SettingsDev st,
+                                                         float* out)
+{
+    __shared__ float4 verts[kTileVerts];
+    __shared__ BodyParams Bs;
+    const int tid = threadIdx.x;
+    const TileDesc td = tiles[first_tile + blockIdx.x];
+    if (tid == 0) body_prologue(body, body->mesh, OP_SURFACE, ocean, st, HYDRO_FRAME_WORLD, Bs);
+    __syncthreads();
+    const BodyParams B = Bs;
+    const int nv = td.nv, nvp = (nv + 3) & ~3;
+    for (int v = tid; v < nv; v += kBlock) {
+        v3 p = xform(B.TC, td.block[v], td.block[nvp + v], td.block[2 * nvp + v]);
+        verts[v] = make_float4(p.x, p.y, p.z, depth_at_b(ocean, B, p.x, p.y, p.z));
+    }
+    __syncthreads();
+    const uint32_t* idx = reinterpret_cast<const uint32_t*>(td.block + 3 * nvp);
+    const uint32_t* face_id = reinterpret_cast<const uint32_t*>(reinterpret_cast<const char*>(td.block) +
+                                                                tile_bytes(td.nv, td.nf));
+    for (int f = tid; f < td.nf; f += kBlock) {
+        const uint32_t w = idx[f];
+        const float4 q1 = verts[w & 511u], q2 = verts[(w >> 9) & 511u], q3 = verts[w >> 18];
+        float* o = out + (size_t)face_id[f] * 13;
+        o[0] = 0.f;
+        Acc a;
+        for (int k = 0; k < kQ; ++k) a.q[k] = 0.f;
+        if (ocean.waves)
+            face_surface<CUT64, true, true>(ocean, B, a, q1, q2, q3, o);
+        else
+            face_surface<CUT64, false, true>(ocean, B, a, q1, q2, q3, o);
+    }
+}
+
+cudaError_t launch_outline(const TileDesc* tiles, uint32_t first_tile, uint32_t n_tiles, const hydro_body* body,
+                           OceanDev ocean, SettingsDev st, int cut64, float* out, cudaStream_t s)
+{
+    if (n_tiles == 0) return cudaSuccess;
+    if (cut64)
+        outline_kernel<true><<<n_tiles, kBlock, 0, s>>>(tiles, first_tile, body, ocean, st, out);
+    else
+        outline_kernel<false><<<n_tiles, kBlock, 0, s>>>(tiles, first_tile, body, ocean, st, out);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_face_terms(const TileDesc* tiles, uint32_t first_tile, uint32_t n_tiles,
                               const hydro_body* body, OceanDev ocean, SettingsDev st, int frame,
                               int cut64, int packed, float* out, cudaStream_t s)

@@ -231,6 +231,18 @@ class HydroContext:
                                                  C.byref(settings), int(packed), out.ctypes.data))
         return out
 
+    def surface_outline(self, body: np.ndarray, ocean, settings) -> np.ndarray:
+        """hydro_debug_surface_outline: the reference's DEBUG_HYDRO points of
+        one body's surface loop, float32 (n, 3), two per outline segment."""
+        n = C.c_uint32(0)
+        self._ck(self.lib.hydro_debug_surface_outline(self.ctx, body.ctypes.data, C.byref(ocean), C.byref(settings),
+                                                      None, 0, C.byref(n)))
+        pts = np.zeros((n.value, 3), dtype=np.float32)
+        if n.value:
+            self._ck(self.lib.hydro_debug_surface_outline(self.ctx, body.ctypes.data, C.byref(ocean),
+                                                          C.byref(settings), pts.ctypes.data, n.value, C.byref(n)))
+        return pts
+
     def division_check(self, n_pairs: int = 1 << 26, seed: int = 1) -> list[int]:
         """Mismatch counts of the kernels' FMA-corrected division against IEEE
         division (x/3 over all floats, two sets of random pairs)."""

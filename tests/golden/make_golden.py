@@ -84,6 +84,7 @@ def main():
     save("currents_jet_pipe", sc)
     save_face_patterns()
     save_ingest()
+    save_outlines()
 
 
 def ingest_meshes():
@@ -191,6 +192,45 @@ def save_face_patterns():
                         wave_data=waves["data"], wave_layers=np.array(waves["layers"], dtype=np.float64),
                         reference=out)
     print("ref_face_patterns", len(xyz))
+
+
+def save_outlines():
+    """The points the reference's DEBUG_HYDRO build records in
+    ComputeHydrodynamicForcesSurface (outlines of the evaluated submerged
+    parts) for bodies of three fixtures: the 227 single-face cases of
+    ref_face_patterns.npz, the first four crossing bodies of
+    sphere_crossing.npz and the first four of waves_small.npz."""
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from tests import golden_io
+    from tests.helpers import body_transform
+    ref = Reference()
+    st = scenarios.settings()
+    arrays = {}
+
+    def outline(body, mesh, ocean, waves):
+        return ref.surface_outline(st, mesh, ocean, body_transform(body, "T_CG"), body_transform(body, "T_C"),
+                                   body["v"][0], body["omega"][0], waves=waves)
+
+    fp = golden_io.load_face_patterns()
+    faces = np.array([[0, 1, 2]], dtype=np.uint32)
+    pts = []
+    for i in range(len(fp["xyz"])):
+        oc = scenarios.flat_ocean(tuple(fp["current"][i]))
+        oc.waves = int(fp["waves_on"][i])
+        pts.append(outline(fp["bodies"][i:i + 1], (fp["xyz"][i], faces), oc,
+                           fp["waves"] if fp["waves_on"][i] else None))
+    arrays["face_patterns_count"] = np.array([len(q) for q in pts], np.int64)
+    arrays["face_patterns_points"] = np.concatenate(pts)
+    for name in ("sphere_crossing", "waves_small"):
+        g = golden_io.load(name)
+        b = g["bodies"]
+        sel = [i for i in range(len(b)) if g["out"]["reference"]["position"][i] == abi.CROSSING_SURFACE][:4]
+        pts = [outline(b[i:i + 1], g["meshes"][int(b["mesh"][i])], g["ocean"], g["waves"]) for i in sel]
+        arrays[name + "_bodies"] = np.array(sel, np.int64)
+        arrays[name + "_count"] = np.array([len(q) for q in pts], np.int64)
+        arrays[name + "_points"] = np.concatenate(pts)
+    np.savez_compressed(os.path.join(HERE, "ref_outline.npz"), **arrays)
+    print("ref_outline", {k: v.shape for k, v in arrays.items()})
 
 
 if __name__ == "__main__":

@@ -76,3 +76,48 @@ def test_gpu_face_terms_equal_reference_single_faces(hctx, packed):
                 assert np.array_equal((t[3:6] * k).astype(np.float64), r[3:6]), (i, "Tb")
         else:
             assert r[19] == 0.0 and np.all(r[0:6] == 0.0), (i, "stale outputs")
+
+
+def _outline_fixture():
+    import os
+    from tests.golden_io import GOLDEN
+    return np.load(os.path.join(GOLDEN, "ref_outline.npz"))
+
+
+def _split(points, counts):
+    return np.split(points, np.cumsum(counts)[:-1])
+
+
+def test_gpu_surface_outline_equals_reference_debug_points(hctx):
+    """hydro_debug_surface_outline against the points the reference's
+    DEBUG_HYDRO build records in ComputeHydrodynamicForcesSurface
+    (tests/golden/ref_outline.npz): the outline of every evaluated submerged
+    triangle or quad, faces in mesh order, bit for bit -- the 227 single-face
+    cases (every clip case, flat and wavy surfaces, slivers) and whole
+    meshes (an icosphere on a flat surface, torpedo hulls on waves)."""
+    z = _outline_fixture()
+    st = scenarios.settings()
+    fp = load_face_patterns()
+    hctx.set_wave_grid(fp["waves"])
+    faces = np.array([[0, 1, 2]], dtype=np.uint32)
+    for i, want in enumerate(_split(z["face_patterns_points"], z["face_patterns_count"])):
+        oc = scenarios.flat_ocean(tuple(fp["current"][i]))
+        oc.waves = int(fp["waves_on"][i])
+        body = fp["bodies"][i:i + 1].copy()
+        body["mesh"] = hctx.upload_mesh(fp["xyz"][i], faces)
+        got = hctx.surface_outline(body, oc, st)
+        assert np.array_equal(got, want), i
+    for name in ("sphere_crossing", "waves_small"):
+        g = load(name)
+        if g["waves"] is not None:
+            hctx.set_wave_grid(g["waves"])
+        ids = [hctx.upload_mesh(x, f) for x, f in g["meshes"]]
+        wants = _split(z[name + "_points"], z[name + "_count"])
+        assert len(z[name + "_points"]) > 0
+        for j, want in zip(z[name + "_bodies"], wants):
+            # (a crossing body whose box dips under the surface but none of
+            # whose faces does records no points, in the reference too)
+            body = g["bodies"][j:j + 1].copy()
+            body["mesh"] = ids[int(body["mesh"][0])]
+            got = hctx.surface_outline(body, g["ocean"], st)
+            assert np.array_equal(got, want), (name, int(j))
