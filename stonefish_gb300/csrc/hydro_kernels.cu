@@ -24,6 +24,7 @@
 //             CorrectHydrodynamicForces (:1263-1287).
 // No result depends on scheduling: every sum has a fixed order.
 #include <algorithm>
+#include <atomic>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -1181,14 +1182,43 @@ static void* chunk_kernel_for(int cut64, int waves, int ctas_per_sm)
     return ctas_per_sm >= 2 ? kernel_ptr<2>(cut64, waves) : kernel_ptr<1>(cut64, waves);
 }
 
+// The dynamic shared-memory attribute and the resident-CTA count of each
+// chunk-kernel variant, set and queried once per device: both are host API
+// calls that would otherwise sit in front of every step's first launch.
+// Index: device (first 16), cut64, waves, 1 or 2 CTAs per SM; occupancy is
+// stored plus one (0 = not yet known).
+constexpr int kDevCache = 16;
+static std::atomic<int> g_chunk_occ[kDevCache][2][2][2];
+static std::atomic<bool> g_chunk_attr[kDevCache][2][2][2];
+
+static cudaError_t chunk_kernel_attr(int cut64, int waves, int ctas_per_sm)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::atomic<bool>* flag = dev < kDevCache ? &g_chunk_attr[dev][cut64 != 0][waves != 0][ctas_per_sm >= 2] : nullptr;
+    if (flag && flag->load(std::memory_order_acquire)) return cudaSuccess;
+    e = cudaFuncSetAttribute(chunk_kernel_for(cut64, waves, ctas_per_sm), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sizeof(ChunkSmem));
+    if (e == cudaSuccess && flag) flag->store(true, std::memory_order_release);
+    return e;
+}
+
 int chunk_kernel_occupancy(int cut64, int waves, int ctas_per_sm)
 {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    std::atomic<int>* slot = dev < kDevCache ? &g_chunk_occ[dev][cut64 != 0][waves != 0][ctas_per_sm >= 2] : nullptr;
+    if (slot) {
+        const int known = slot->load(std::memory_order_acquire);
+        if (known > 0) return known - 1;
+    }
     int n = 0;
     const void* k = chunk_kernel_for(cut64, waves, ctas_per_sm);
-    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ChunkSmem)) != cudaSuccess)
-        return 0;
+    if (chunk_kernel_attr(cut64, waves, ctas_per_sm) != cudaSuccess) return 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, kThreads, sizeof(ChunkSmem)) != cudaSuccess)
         return 0;
+    if (slot) slot->store(n + 1, std::memory_order_release);
     return n;
 }
 
@@ -1209,8 +1239,7 @@ cudaError_t launch_step(const KParams& P, LaunchShape shape, int cut64, cudaStre
     if (grid > (int)P.n_chunks) grid = (int)P.n_chunks;
     if (grid < 1) grid = 1;
     const void* k = chunk_kernel_for(cut64, P.ocean.waves != 0, shape.ctas_per_sm);
-    if ((e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ChunkSmem))))
-        return e;
+    if ((e = chunk_kernel_attr(cut64, P.ocean.waves != 0, shape.ctas_per_sm))) return e;
     void* args[] = {const_cast<KParams*>(&P)};
     if ((e = cudaLaunchKernel(k, dim3(grid), dim3(kThreads), args, sizeof(ChunkSmem), s))) return e;
     if (ev && (e = cudaEventRecord(ev[2], s))) return e;
@@ -1420,7 +1449,7 @@ cudaError_t launch_compound_step(const KParams& P, const CompoundParams& C, Laun
         if (grid > (int)P.n_chunks) grid = (int)P.n_chunks;
         if (grid < 1) grid = 1;
         const void* k = chunk_kernel_for(cut64, P.ocean.waves != 0, shape.ctas_per_sm);
-        if ((e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ChunkSmem))))
+        if ((e = chunk_kernel_attr(cut64, P.ocean.waves != 0, shape.ctas_per_sm)))
             return e;
         void* args[] = {const_cast<KParams*>(&P)};
         if ((e = cudaLaunchKernel(k, dim3(grid), dim3(kThreads), args, sizeof(ChunkSmem), s))) return e;
