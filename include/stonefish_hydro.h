@@ -276,7 +276,8 @@ hydro_status hydro_mesh_info(hydro_ctx* ctx, hydro_mesh_id id,
  * data is an N x N grid of `channels` interleaved floats (row j, column i at
  * (j*N+i)*channels); each of the n_layers layers reads channel
  * layer_channel[l] over a square of layer_grid_size[l] metres, and
- * wave height = -sum_l bilinear(layer l) (periodic, texel-centred). */
+ * wave height = -sum_l bilinear(layer l) (periodic, texel-centred).
+ * N * N * channels must be below 2^32 (HYDRO_ERR_INVALID_ARG otherwise). */
 hydro_status hydro_wave_grid_set(hydro_ctx* ctx, const float* data,
                                  uint32_t size, uint32_t channels,
                                  uint32_t n_layers,

@@ -269,7 +269,6 @@ OceanDev make_ocean(const hydro_ctx* ctx, const hydro_ocean* o)
     d.wave_n = ctx->wave_n;
     d.wave_channels = ctx->wave_channels;
     d.wave_layers = ctx->wave_layers;
-    d.wave_idx32 = (uint64_t)ctx->wave_n * ctx->wave_n * ctx->wave_channels < (uint64_t(1) << 32) ? 1 : 0;
     d.wave_half = ctx->wave_n ? 0.5f / (float)ctx->wave_n : 0.f;
     for (int l = 0; l < HYDRO_MAX_WAVE_LAYERS; ++l) {
         d.wave_channel[l] = ctx->wave_channel[l];
@@ -425,7 +424,8 @@ hydro_status batch_launch(hydro_batch* b, const hydro_body* d_bodies, const hydr
     const int cut64 = ctx->cfg.cut_precision == HYDRO_CUT_FP64;
     LaunchShape shape{};
     const int want = b->ctas_per_sm ? (int)b->ctas_per_sm : ctx->cfg.ctas_per_sm ? (int)ctx->cfg.ctas_per_sm : 2;
-    shape.ctas_per_sm = std::max(1, std::min(want, chunk_kernel_occupancy(cut64, P.ocean.waves, want)));
+    shape.ctas_per_sm = std::max(1, std::min(want, chunk_kernel_occupancy(cut64, P.ocean.waves, want,
+                                                                            op == OP_AERO || op == OP_AERO_BODY)));
     shape.grid = ctx->sm_count * shape.ctas_per_sm;
     uint32_t launches = 0;
     // kernel timing events (hydro_batch_profile) outside stream capture only
@@ -823,6 +823,8 @@ hydro_status hydro_wave_grid_set(hydro_ctx* ctx, const float* data, uint32_t siz
     if (!data || size == 0 || channels == 0 || n_layers == 0 || n_layers > HYDRO_MAX_WAVE_LAYERS ||
         !layer_channel || !layer_grid_size || size > 65536)
         return fail(ctx, HYDRO_ERR_INVALID_ARG, "wave grid: bad arguments");
+    if ((uint64_t)size * size * channels >= (uint64_t(1) << 32))
+        return fail(ctx, HYDRO_ERR_INVALID_ARG, "wave grid: N * N * channels must be below 2^32");
     for (uint32_t l = 0; l < n_layers; ++l) {
         if (layer_channel[l] >= channels || !(layer_grid_size[l] > 0.f))
             return fail(ctx, HYDRO_ERR_INVALID_ARG, "wave grid: bad layer %u", l);
@@ -1259,7 +1261,7 @@ hydro_status compound_launch(hydro_compound_batch* cb, const hydro_body* d_compo
     const int cut64 = ctx->cfg.cut_precision == HYDRO_CUT_FP64;
     LaunchShape shape{};
     const int want = (b && b->ctas_per_sm) ? (int)b->ctas_per_sm : ctx->cfg.ctas_per_sm ? (int)ctx->cfg.ctas_per_sm : 2;
-    shape.ctas_per_sm = std::max(1, std::min(want, chunk_kernel_occupancy(cut64, P.ocean.waves, want)));
+    shape.ctas_per_sm = std::max(1, std::min(want, chunk_kernel_occupancy(cut64, P.ocean.waves, want, 0)));
     shape.grid = ctx->sm_count * shape.ctas_per_sm;
     uint32_t launches = 0;
     cudaError_t e = launch_compound_step(P, C, shape, cut64, s, &launches);
@@ -2471,7 +2473,7 @@ extern "C" hydro_status hydro_compute_wrenches_static(hydro_ctx* ctx, const hydr
     const int cut64 = ctx->cfg.cut_precision == HYDRO_CUT_FP64;
     LaunchShape shape{};
     const int want = ctx->cfg.ctas_per_sm ? (int)ctx->cfg.ctas_per_sm : 2;
-    shape.ctas_per_sm = std::max(1, std::min(want, chunk_kernel_occupancy(cut64, P.ocean.waves, want)));
+    shape.ctas_per_sm = std::max(1, std::min(want, chunk_kernel_occupancy(cut64, P.ocean.waves, want, 0)));
     shape.grid = ctx->sm_count * shape.ctas_per_sm;
     uint32_t launches = 0;
     cudaError_t e = launch_step(P, shape, cut64, s, &launches);

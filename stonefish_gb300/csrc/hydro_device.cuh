@@ -130,7 +130,6 @@ struct OceanDev {
     float wave_grid[HYDRO_MAX_WAVE_LAYERS];
     float wave_inv_grid[HYDRO_MAX_WAVE_LAYERS];   // RN(1 / wave_grid[l])
     float wave_half;             // 0.5f / (float)wave_n, the texel-centre offset
-    int wave_idx32;              // N * N * channels < 2^32: texel offsets fit 32 bits
     hydro_current currents[HYDRO_MAX_CURRENTS];
 };
 
@@ -229,13 +228,13 @@ __device__ __forceinline__ v3 xform(const float* M, float x, float y, float z)
 __device__ __forceinline__ float fracf_(float x) { return x - truncf(x); }
 
 // Texel offset j * N + i of the four bilinear taps, wrapped modulo N * N,
-// times the channel count plus the channel; U is 32-bit when every offset
-// fits (the result is the same integer either way).
-template <class U>
-__device__ __forceinline__ U texel_offset(uint32_t N, int j, int i, uint32_t C, uint32_t ch)
+// times the channel count plus the channel.  The grid holds fewer than 2^32
+// values (hydro_wave_grid_set), so 32 bits hold every offset, also the
+// j * N + i of a tap one texel past the last row before it wraps.
+__device__ __forceinline__ uint32_t texel_offset(uint32_t N, int j, int i, uint32_t C, uint32_t ch)
 {
-    const U NN = (U)N * N;
-    U l = (U)j * N + (U)i;
+    const uint32_t NN = N * N;
+    uint32_t l = (uint32_t)j * N + (uint32_t)i;
     if (l >= NN) l -= NN;
     return l * C + ch;
 }
@@ -264,18 +263,13 @@ __device__ __forceinline__ float wave_interp(const OceanDev& o, float x, float y
     float beta = fracf_(j0f * Nf);
     const float* d = o.wave_data;
     const uint32_t C = o.wave_channels;
-    float t0, t1, t2, t3;
-    if (o.wave_idx32) {
-        t0 = __ldg(d + texel_offset<uint32_t>(N, j0, i0, C, ch));
-        t1 = __ldg(d + texel_offset<uint32_t>(N, j0, i1, C, ch));
-        t2 = __ldg(d + texel_offset<uint32_t>(N, j1, i0, C, ch));
-        t3 = __ldg(d + texel_offset<uint32_t>(N, j1, i1, C, ch));
-    } else {
-        t0 = __ldg(d + texel_offset<uint64_t>(N, j0, i0, C, ch));
-        t1 = __ldg(d + texel_offset<uint64_t>(N, j0, i1, C, ch));
-        t2 = __ldg(d + texel_offset<uint64_t>(N, j1, i0, C, ch));
-        t3 = __ldg(d + texel_offset<uint64_t>(N, j1, i1, C, ch));
-    }
+    // 32-bit offsets: hydro_wave_grid_set keeps N * N * channels below 2^32
+    // (one code path at every inlined lookup keeps the kernels' instruction
+    // footprint small)
+    const float t0 = __ldg(d + texel_offset(N, j0, i0, C, ch));
+    const float t1 = __ldg(d + texel_offset(N, j0, i1, C, ch));
+    const float t2 = __ldg(d + texel_offset(N, j1, i0, C, ch));
+    const float t3 = __ldg(d + texel_offset(N, j1, i1, C, ch));
     return (1.f - alpha) * (1.f - beta) * t0 + alpha * (1.f - beta) * t1
          + (1.f - alpha) * beta * t2 + alpha * beta * t3;
 }

@@ -842,7 +842,7 @@ struct PairQueue {
 // all 32 lanes (64 paired faces, 32 straddling faces) or when `drain` (the
 // chunk's last tile).  Returns the number of faces each lane added at most
 // (a pair pass counts two, a clipping pass one).
-template <bool CUT64, bool WAVES>
+template <bool CUT64, bool WAVES, bool AERO>
 __device__ __forceinline__ int tile_faces(const KParams& P, const StageBuf& st, const ItemMeta& m,
                                           const float4* verts, const uint32_t* flags, PairQueue& pq,
                                           CutQueue& cq, bool drain, Acc& acc)
@@ -868,8 +868,9 @@ __device__ __forceinline__ int tile_faces(const KParams& P, const StageBuf& st, 
     }
     const int nf = m.nf, nvp = (m.nv + 3) & ~3;
     const uint32_t* idx = reinterpret_cast<const uint32_t*>(reinterpret_cast<const float*>(st.raw) + 3 * nvp);
-    if (Bl.loop == LOOP_AERO) {
-        // every face, one per lane, on the scalar path (no clipping)
+    if (AERO) {
+        // every face, one per lane, on the scalar path (no clipping); an
+        // aerodynamic launch lists only bodies of the aerodynamic loop
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
             const int f = (k * 32 + lane) * kWarps + warp;
@@ -1001,7 +1002,7 @@ __device__ __forceinline__ int tile_faces(const KParams& P, const StageBuf& st, 
 // the vertices of tile i + 1 into the other vertex buffer; one barrier (which
 // also checks that every thread's wait for tile i + 1 succeeded) separates
 // iterations, so a warp that finishes its faces early starts transforming.
-template <bool CUT64, bool WAVES>
+template <bool CUT64, bool WAVES, bool AERO>
 __device__ __forceinline__ void consumer(const KParams& P, ChunkSmem& S)
 {
     const int tid = threadIdx.x;
@@ -1031,7 +1032,7 @@ __device__ __forceinline__ void consumer(const KParams& P, ChunkSmem& S)
     for (uint32_t item = 0; !(m.flags & ITEM_END); ++item) {
         const int s = (int)(item % kStages);
         const bool last = (m.flags & ITEM_LAST) != 0;
-        run += tile_faces<CUT64, WAVES>(P, S.stage[s], m, S.verts[item & 1u], S.tflags[item & 1u], pq, cq, last,
+        run += tile_faces<CUT64, WAVES, AERO>(P, S.stage[s], m, S.verts[item & 1u], S.tflags[item & 1u], pq, cq, last,
                                         acc);
         // next tile: wait, read its metadata, transform its vertices
         const uint32_t nx = item + 1u;
@@ -1074,7 +1075,11 @@ __device__ __forceinline__ void consumer(const KParams& P, ChunkSmem& S)
 // sub-partition, whose 16K registers then allow 128 per thread.  The cap is
 // given as a register limit rather than a minimum block count, with which
 // ptxas allocates the flat-surface variants without spills.
-template <bool CUT64, bool WAVES, int MINB>
+// AERO: an aerodynamic launch (every listed body in the aerodynamic loop);
+// the hydrodynamic variants carry no aerodynamic code and the aerodynamic
+// one no clipping or wave code, which keeps each one's instruction
+// footprint small.
+template <bool CUT64, bool WAVES, bool AERO, int MINB>
 __global__ void __launch_bounds__(kThreads) __maxnreg__(MINB == 2 ? 128 : 255) chunk_kernel(const KParams P)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -1093,7 +1098,7 @@ __global__ void __launch_bounds__(kThreads) __maxnreg__(MINB == 2 ? 128 : 255) c
         producer(P, S);
         return;
     }
-    consumer<CUT64, WAVES>(P, S);
+    consumer<CUT64, WAVES, AERO>(P, S);
 }
 
 // ----------------------------------------------------------- finalise kernel
@@ -1170,52 +1175,56 @@ __global__ void __launch_bounds__(kBodyThreads) finalize_kernel(const KParams P)
 }
 
 template <int MINB>
-static void* kernel_ptr(int cut64, int waves)
+static void* kernel_ptr(int cut64, int waves, int aero)
 {
-    if (cut64) return waves ? (void*)chunk_kernel<true, true, MINB> : (void*)chunk_kernel<true, false, MINB>;
-    return waves ? (void*)chunk_kernel<false, true, MINB> : (void*)chunk_kernel<false, false, MINB>;
+    if (aero) return (void*)chunk_kernel<false, false, true, MINB>;
+    if (cut64)
+        return waves ? (void*)chunk_kernel<true, true, false, MINB> : (void*)chunk_kernel<true, false, false, MINB>;
+    return waves ? (void*)chunk_kernel<false, true, false, MINB> : (void*)chunk_kernel<false, false, false, MINB>;
 }
 
 // The kernel variant compiled for `ctas_per_sm` resident CTAs (1 or 2).
-static void* chunk_kernel_for(int cut64, int waves, int ctas_per_sm)
+static void* chunk_kernel_for(int cut64, int waves, int ctas_per_sm, int aero)
 {
-    return ctas_per_sm >= 2 ? kernel_ptr<2>(cut64, waves) : kernel_ptr<1>(cut64, waves);
+    return ctas_per_sm >= 2 ? kernel_ptr<2>(cut64, waves, aero) : kernel_ptr<1>(cut64, waves, aero);
 }
 
 // The dynamic shared-memory attribute and the resident-CTA count of each
 // chunk-kernel variant, set and queried once per device: both are host API
 // calls that would otherwise sit in front of every step's first launch.
-// Index: device (first 16), cut64, waves, 1 or 2 CTAs per SM; occupancy is
-// stored plus one (0 = not yet known).
+// Index: device (first 16), cut64, waves, aerodynamic, 1 or 2 CTAs per SM;
+// occupancy is stored plus one (0 = not yet known).
 constexpr int kDevCache = 16;
-static std::atomic<int> g_chunk_occ[kDevCache][2][2][2];
-static std::atomic<bool> g_chunk_attr[kDevCache][2][2][2];
+static std::atomic<int> g_chunk_occ[kDevCache][2][2][2][2];
+static std::atomic<bool> g_chunk_attr[kDevCache][2][2][2][2];
 
-static cudaError_t chunk_kernel_attr(int cut64, int waves, int ctas_per_sm)
+static cudaError_t chunk_kernel_attr(int cut64, int waves, int ctas_per_sm, int aero)
 {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
-    std::atomic<bool>* flag = dev < kDevCache ? &g_chunk_attr[dev][cut64 != 0][waves != 0][ctas_per_sm >= 2] : nullptr;
+    std::atomic<bool>* flag =
+        dev < kDevCache ? &g_chunk_attr[dev][cut64 != 0][waves != 0][aero != 0][ctas_per_sm >= 2] : nullptr;
     if (flag && flag->load(std::memory_order_acquire)) return cudaSuccess;
-    e = cudaFuncSetAttribute(chunk_kernel_for(cut64, waves, ctas_per_sm), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)sizeof(ChunkSmem));
+    e = cudaFuncSetAttribute(chunk_kernel_for(cut64, waves, ctas_per_sm, aero),
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ChunkSmem));
     if (e == cudaSuccess && flag) flag->store(true, std::memory_order_release);
     return e;
 }
 
-int chunk_kernel_occupancy(int cut64, int waves, int ctas_per_sm)
+int chunk_kernel_occupancy(int cut64, int waves, int ctas_per_sm, int aero)
 {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
-    std::atomic<int>* slot = dev < kDevCache ? &g_chunk_occ[dev][cut64 != 0][waves != 0][ctas_per_sm >= 2] : nullptr;
+    std::atomic<int>* slot =
+        dev < kDevCache ? &g_chunk_occ[dev][cut64 != 0][waves != 0][aero != 0][ctas_per_sm >= 2] : nullptr;
     if (slot) {
         const int known = slot->load(std::memory_order_acquire);
         if (known > 0) return known - 1;
     }
     int n = 0;
-    const void* k = chunk_kernel_for(cut64, waves, ctas_per_sm);
-    if (chunk_kernel_attr(cut64, waves, ctas_per_sm) != cudaSuccess) return 0;
+    const void* k = chunk_kernel_for(cut64, waves, ctas_per_sm, aero);
+    if (chunk_kernel_attr(cut64, waves, ctas_per_sm, aero) != cudaSuccess) return 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, kThreads, sizeof(ChunkSmem)) != cudaSuccess)
         return 0;
     if (slot) slot->store(n + 1, std::memory_order_release);
@@ -1238,8 +1247,9 @@ cudaError_t launch_step(const KParams& P, LaunchShape shape, int cut64, cudaStre
     int grid = shape.grid;
     if (grid > (int)P.n_chunks) grid = (int)P.n_chunks;
     if (grid < 1) grid = 1;
-    const void* k = chunk_kernel_for(cut64, P.ocean.waves != 0, shape.ctas_per_sm);
-    if ((e = chunk_kernel_attr(cut64, P.ocean.waves != 0, shape.ctas_per_sm))) return e;
+    const int aero = (P.op == OP_AERO || P.op == OP_AERO_BODY) ? 1 : 0;
+    const void* k = chunk_kernel_for(cut64, P.ocean.waves != 0, shape.ctas_per_sm, aero);
+    if ((e = chunk_kernel_attr(cut64, P.ocean.waves != 0, shape.ctas_per_sm, aero))) return e;
     void* args[] = {const_cast<KParams*>(&P)};
     if ((e = cudaLaunchKernel(k, dim3(grid), dim3(kThreads), args, sizeof(ChunkSmem), s))) return e;
     if (ev && (e = cudaEventRecord(ev[2], s))) return e;
@@ -1448,8 +1458,8 @@ cudaError_t launch_compound_step(const KParams& P, const CompoundParams& C, Laun
         int grid = shape.grid;
         if (grid > (int)P.n_chunks) grid = (int)P.n_chunks;
         if (grid < 1) grid = 1;
-        const void* k = chunk_kernel_for(cut64, P.ocean.waves != 0, shape.ctas_per_sm);
-        if ((e = chunk_kernel_attr(cut64, P.ocean.waves != 0, shape.ctas_per_sm)))
+        const void* k = chunk_kernel_for(cut64, P.ocean.waves != 0, shape.ctas_per_sm, 0);
+        if ((e = chunk_kernel_attr(cut64, P.ocean.waves != 0, shape.ctas_per_sm, 0)))
             return e;
         void* args[] = {const_cast<KParams*>(&P)};
         if ((e = cudaLaunchKernel(k, dim3(grid), dim3(kThreads), args, sizeof(ChunkSmem), s))) return e;

@@ -364,6 +364,25 @@ def test_prefix_entry_and_chunk_size(hctx, chunk_faces):
     b0.close()
 
 
+def test_wave_grid_limit(built_library):
+    """A grid of 2^32 or more values is rejected before anything is read or
+    allocated (the lookups use 32-bit texel offsets); the context stays
+    usable."""
+    import ctypes as C
+    from stonefish_gb300.hydro import HydroContext
+    h = HydroContext()
+    try:
+        tiny = np.zeros(4, dtype=np.float32)
+        ch = (C.c_uint32 * 1)(0)
+        gs = (C.c_float * 1)(102.4)
+        for n, c in ((65536, 1), (32768, 4)):
+            st = h.lib.hydro_wave_grid_set(h.ctx, tiny.ctypes.data, n, c, 1, ch, gs)
+            assert st == abi.HYDRO_ERR_INVALID_ARG, (n, c)
+        h.set_wave_grid(scenarios.wave_grid(n=64, n_waves=4, seed=9))
+    finally:
+        h.close()
+
+
 @pytest.mark.parametrize("cut", ["fp64", "fp32"])
 def test_waves_batch(oracle, hctx, hctx64, cut):
     h = hctx64 if cut == "fp64" else hctx
