@@ -425,7 +425,8 @@ hydro_status batch_launch(hydro_batch* b, const hydro_body* d_bodies, const hydr
     LaunchShape shape{};
     const int want = b->ctas_per_sm ? (int)b->ctas_per_sm : ctx->cfg.ctas_per_sm ? (int)ctx->cfg.ctas_per_sm : 2;
     shape.ctas_per_sm = std::max(1, std::min(want, chunk_kernel_occupancy(cut64, P.ocean.waves, want,
-                                                                            op == OP_AERO || op == OP_AERO_BODY)));
+                                                                            op == OP_AERO || op == OP_AERO_BODY,
+                                                                            P.ocean.field_currents)));
     shape.grid = ctx->sm_count * shape.ctas_per_sm;
     uint32_t launches = 0;
     // kernel timing events (hydro_batch_profile) outside stream capture only
@@ -1261,7 +1262,8 @@ hydro_status compound_launch(hydro_compound_batch* cb, const hydro_body* d_compo
     const int cut64 = ctx->cfg.cut_precision == HYDRO_CUT_FP64;
     LaunchShape shape{};
     const int want = (b && b->ctas_per_sm) ? (int)b->ctas_per_sm : ctx->cfg.ctas_per_sm ? (int)ctx->cfg.ctas_per_sm : 2;
-    shape.ctas_per_sm = std::max(1, std::min(want, chunk_kernel_occupancy(cut64, P.ocean.waves, want, 0)));
+    shape.ctas_per_sm = std::max(
+        1, std::min(want, chunk_kernel_occupancy(cut64, P.ocean.waves, want, 0, P.ocean.field_currents)));
     shape.grid = ctx->sm_count * shape.ctas_per_sm;
     uint32_t launches = 0;
     cudaError_t e = launch_compound_step(P, C, shape, cut64, s, &launches);
@@ -2473,7 +2475,8 @@ extern "C" hydro_status hydro_compute_wrenches_static(hydro_ctx* ctx, const hydr
     const int cut64 = ctx->cfg.cut_precision == HYDRO_CUT_FP64;
     LaunchShape shape{};
     const int want = ctx->cfg.ctas_per_sm ? (int)ctx->cfg.ctas_per_sm : 2;
-    shape.ctas_per_sm = std::max(1, std::min(want, chunk_kernel_occupancy(cut64, P.ocean.waves, want, 0)));
+    shape.ctas_per_sm = std::max(
+        1, std::min(want, chunk_kernel_occupancy(cut64, P.ocean.waves, want, 0, P.ocean.field_currents)));
     shape.grid = ctx->sm_count * shape.ctas_per_sm;
     uint32_t launches = 0;
     cudaError_t e = launch_step(P, shape, cut64, s, &launches);

@@ -368,9 +368,12 @@ __device__ __forceinline__ float depth_at_b(const OceanDev& o, const BodyParams&
     return z - wave_height(o, x, y);
 }
 
+// FIELD = false: compiled for launches without jet or pipe currents (the
+// field-current code then takes no room in the kernel).
+template <bool FIELD = true>
 __device__ __forceinline__ v3 fluid_velocity_b(const OceanDev& o, const BodyParams& B, v3 pt)
 {
-    if (!o.field_currents) return mk(o.U[0], o.U[1], o.U[2]);
+    if (!FIELD || !o.field_currents) return mk(o.U[0], o.U[1], o.U[2]);
     if (!B.centred) return fluid_velocity(o, pt);
     double p[3] = {(double)pt.x + (double)B.off[0], (double)pt.y + (double)B.off[1], (double)pt.z};
     double fv[3] = {0.0, 0.0, 0.0};
@@ -423,11 +426,12 @@ __device__ __forceinline__ void tetra(Acc& a, v3 x, v3 y, v3 z)
 }
 
 // Damping of one face (:1661-1683 and :1778-1789)
+template <bool FIELD = true>
 __device__ __forceinline__ void damping(const OceanDev& o, const BodyParams& B, Acc& a,
                                         v3 fc, v3 fn1, float A)
 {
     v3 r = sub(fc, B.p);
-    v3 vc = sub(fluid_velocity_b(o, B, fc), add(B.v, cross(B.omega, r)));
+    v3 vc = sub(fluid_velocity_b<FIELD>(o, B, fc), add(B.v, cross(B.omega, r)));
     float vc_n = dot(vc, fn1);
     v3 vn = mk(vc_n * fn1.x, vc_n * fn1.y, vc_n * fn1.z);
     v3 vt = sub(vc, vn);
@@ -465,13 +469,14 @@ __device__ __forceinline__ bool tri_props(v3 p1, v3 p2, v3 p3, v3& fc, v3& fn1, 
 // centroid, its normal part vn, and for faces it flows into the term
 // vn * vn.length() * A, where glm's vec3::length() is the component count 3.
 // Force and torque go to the Q_FDQ / Q_TDQ accumulators.
+template <bool FIELD = true>
 __device__ __forceinline__ void face_aero(const OceanDev& o, const BodyParams& B, Acc& a, v3 p1, v3 p2, v3 p3)
 {
     v3 fc, fn1;
     float A;
     if (!tri_props(p1, p2, p3, fc, fn1, A)) return;
     const v3 r = sub(fc, B.p);
-    const v3 vc = sub(fluid_velocity_b(o, B, fc), add(B.v, cross(B.omega, r)));
+    const v3 vc = sub(fluid_velocity_b<FIELD>(o, B, fc), add(B.v, cross(B.omega, r)));
     const float s = dot(vc, fn1);
     const v3 vn = mk(s * fn1.x, s * fn1.y, s * fn1.z);
     if (dot(fn1, vn) < -1e-12f) {
@@ -484,7 +489,7 @@ __device__ __forceinline__ void face_aero(const OceanDev& o, const BodyParams& B
 // The part of a surface-loop face after its polygon is known (:1650-1686).
 // WAVES is Ocean::hasWaves(): the pressure buoyancy is summed per face only
 // with waves.
-template <bool WAVES>
+template <bool WAVES, bool FIELD = true>
 __device__ __forceinline__ void face_forces(const OceanDev& o, const BodyParams& B, Acc& a,
                                             v3 fc, v3 fn1, float A)
 {
@@ -494,7 +499,7 @@ __device__ __forceinline__ void face_forces(const OceanDev& o, const BodyParams&
         acc_add3(a, Q_FB, Fbi);
         acc_add3(a, Q_TB, cross(sub(fc, B.p), Fbi));
     }
-    if (B.damping) damping(o, B, a, fc, fn1, A);
+    if (B.damping) damping<FIELD>(o, B, a, fc, fn1, A);
     a.q[Q_SWET] += A;
 }
 
@@ -512,7 +517,7 @@ __device__ __forceinline__ void put_outline(float* ol, int n, v3 a, v3 b, v3 c, 
     ol[10] = d.x; ol[11] = d.y; ol[12] = d.z;
 }
 
-template <bool CUT64, bool WAVES, bool OUTLINE = false>
+template <bool CUT64, bool WAVES, bool OUTLINE = false, bool FIELD = true>
 __device__ __forceinline__ void face_cut(const OceanDev& o, const BodyParams& B, Acc& a,
                                       v3 p1, v3 p2, v3 p3, float d0, float d1, float d2, float* ol = nullptr)
 {
@@ -580,7 +585,7 @@ __device__ __forceinline__ void face_cut(const OceanDev& o, const BodyParams& B,
         v3 c2 = cross(fv3, fv4);
         A = (len + sqrtf(dot(c2, c2))) * 0.5f;
     }
-    face_forces<WAVES>(o, B, a, fc, fn1, A);
+    face_forces<WAVES, FIELD>(o, B, a, fc, fn1, A);
 }
 
 // A surface-loop face whose three corners are all under water

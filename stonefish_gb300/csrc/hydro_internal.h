@@ -77,8 +77,8 @@ size_t chunk_kernel_smem();
 
 // Resident CTAs per SM that the chunk-kernel variant compiled for
 // `ctas_per_sm` (1 or 2) reaches (0 on error); aero selects the variant of
-// the aerodynamic launches.
-int chunk_kernel_occupancy(int cut64, int waves, int ctas_per_sm, int aero);
+// the aerodynamic launches, field the one with jet or pipe currents.
+int chunk_kernel_occupancy(int cut64, int waves, int ctas_per_sm, int aero, int field);
 
 // The batched wrench step: prep (per body), persistent chunk kernel with a
 // TMA-fed tile pipeline, finalise (per body).  `cut64` selects FP64 cut

@@ -842,7 +842,7 @@ struct PairQueue {
 // all 32 lanes (64 paired faces, 32 straddling faces) or when `drain` (the
 // chunk's last tile).  Returns the number of faces each lane added at most
 // (a pair pass counts two, a clipping pass one).
-template <bool CUT64, bool WAVES, bool AERO>
+template <bool CUT64, bool WAVES, bool AERO, bool FIELD>
 __device__ __forceinline__ int tile_faces(const KParams& P, const StageBuf& st, const ItemMeta& m,
                                           const float4* verts, const uint32_t* flags, PairQueue& pq,
                                           CutQueue& cq, bool drain, Acc& acc)
@@ -860,7 +860,7 @@ __device__ __forceinline__ int tile_faces(const KParams& P, const StageBuf& st, 
     Bl.omega = mk(q2.y, q2.z, q2.w);
     Bl.loop = fl.x; Bl.buoyancy = fl.y; Bl.damping = fl.z;
     Bl.centred = 0;
-    if (WAVES || P.ocean.field_currents) {      // the frame offset, bytes 112..127
+    if (WAVES || FIELD) {      // the frame offset, bytes 112..127
         const float4 q3 = bq[4];
         Bl.off[0] = q3.y;
         Bl.off[1] = q3.z;
@@ -879,7 +879,8 @@ __device__ __forceinline__ int tile_faces(const KParams& P, const StageBuf& st, 
                 const float4 q1 = verts[w & 511u];
                 const float4 q2 = verts[(w >> 9) & 511u];
                 const float4 q3 = verts[w >> 18];
-                face_aero(P.ocean, Bl, acc, mk(q1.x, q1.y, q1.z), mk(q2.x, q2.y, q2.z), mk(q3.x, q3.y, q3.z));
+                face_aero<FIELD>(P.ocean, Bl, acc, mk(q1.x, q1.y, q1.z), mk(q2.x, q2.y, q2.z),
+                                 mk(q3.x, q3.y, q3.z));
             }
         }
         return 2;
@@ -972,8 +973,8 @@ __device__ __forceinline__ int tile_faces(const KParams& P, const StageBuf& st, 
                 p3 = pk(f2(a[6], b[6]), f2(a[7], b[7]), f2(a[8], b[8]));
             }
             const BodyPair Bp = body_pair(Bl, P.ocean);
-            if (Bl.loop == LOOP_SURFACE) face_full2<WAVES>(P.ocean, Bl, Bp, acc, p1, p2, p3, hasB);
-            else face_submerged2(P.ocean, Bl, Bp, acc, p1, p2, p3, hasB);
+            if (Bl.loop == LOOP_SURFACE) face_full2<WAVES, FIELD>(P.ocean, Bl, Bp, acc, p1, p2, p3, hasB);
+            else face_submerged2<FIELD>(P.ocean, Bl, Bp, acc, p1, p2, p3, hasB);
         }
         if (from_queue) {
             pq.head = wrap_pair_queue(pq.head + n);
@@ -987,7 +988,7 @@ __device__ __forceinline__ int tile_faces(const KParams& P, const StageBuf& st, 
         if (lane < n) {
             const float4* e = cq.q[wrap_queue(cq.head + lane)];
             const float4 q1 = e[0], q2 = e[1], q3 = e[2];
-            face_cut<CUT64, WAVES>(P.ocean, Bl, acc, mk(q1.x, q1.y, q1.z), mk(q2.x, q2.y, q2.z),
+            face_cut<CUT64, WAVES, false, FIELD>(P.ocean, Bl, acc, mk(q1.x, q1.y, q1.z), mk(q2.x, q2.y, q2.z),
                                    mk(q3.x, q3.y, q3.z), q1.w, q2.w, q3.w);
         }
         cq.head = wrap_queue(cq.head + n);
@@ -1002,7 +1003,7 @@ __device__ __forceinline__ int tile_faces(const KParams& P, const StageBuf& st, 
 // the vertices of tile i + 1 into the other vertex buffer; one barrier (which
 // also checks that every thread's wait for tile i + 1 succeeded) separates
 // iterations, so a warp that finishes its faces early starts transforming.
-template <bool CUT64, bool WAVES, bool AERO>
+template <bool CUT64, bool WAVES, bool AERO, bool FIELD>
 __device__ __forceinline__ void consumer(const KParams& P, ChunkSmem& S)
 {
     const int tid = threadIdx.x;
@@ -1032,7 +1033,8 @@ __device__ __forceinline__ void consumer(const KParams& P, ChunkSmem& S)
     for (uint32_t item = 0; !(m.flags & ITEM_END); ++item) {
         const int s = (int)(item % kStages);
         const bool last = (m.flags & ITEM_LAST) != 0;
-        run += tile_faces<CUT64, WAVES, AERO>(P, S.stage[s], m, S.verts[item & 1u], S.tflags[item & 1u], pq, cq, last,
+        run += tile_faces<CUT64, WAVES, AERO, FIELD>(P, S.stage[s], m, S.verts[item & 1u], S.tflags[item & 1u], pq, cq,
+                                                     last,
                                         acc);
         // next tile: wait, read its metadata, transform its vertices
         const uint32_t nx = item + 1u;
@@ -1076,10 +1078,11 @@ __device__ __forceinline__ void consumer(const KParams& P, ChunkSmem& S)
 // given as a register limit rather than a minimum block count, with which
 // ptxas allocates the flat-surface variants without spills.
 // AERO: an aerodynamic launch (every listed body in the aerodynamic loop);
-// the hydrodynamic variants carry no aerodynamic code and the aerodynamic
-// one no clipping or wave code, which keeps each one's instruction
-// footprint small.
-template <bool CUT64, bool WAVES, bool AERO, int MINB>
+// FIELD: jet or pipe currents are enabled.  The hydrodynamic variants carry
+// no aerodynamic code, the aerodynamic ones no clipping or wave code, and
+// those without field currents no FP64 current code, which keeps each
+// one's instruction footprint small.
+template <bool CUT64, bool WAVES, bool AERO, bool FIELD, int MINB>
 __global__ void __launch_bounds__(kThreads) __maxnreg__(MINB == 2 ? 128 : 255) chunk_kernel(const KParams P)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -1098,7 +1101,7 @@ __global__ void __launch_bounds__(kThreads) __maxnreg__(MINB == 2 ? 128 : 255) c
         producer(P, S);
         return;
     }
-    consumer<CUT64, WAVES, AERO>(P, S);
+    consumer<CUT64, WAVES, AERO, FIELD>(P, S);
 }
 
 // ----------------------------------------------------------- finalise kernel
@@ -1174,57 +1177,65 @@ __global__ void __launch_bounds__(kBodyThreads) finalize_kernel(const KParams P)
     }
 }
 
-template <int MINB>
-static void* kernel_ptr(int cut64, int waves, int aero)
+template <int MINB, bool FIELD>
+static void* kernel_ptr_f(int cut64, int waves, int aero)
 {
-    if (aero) return (void*)chunk_kernel<false, false, true, MINB>;
+    if (aero) return (void*)chunk_kernel<false, false, true, FIELD, MINB>;
     if (cut64)
-        return waves ? (void*)chunk_kernel<true, true, false, MINB> : (void*)chunk_kernel<true, false, false, MINB>;
-    return waves ? (void*)chunk_kernel<false, true, false, MINB> : (void*)chunk_kernel<false, false, false, MINB>;
+        return waves ? (void*)chunk_kernel<true, true, false, FIELD, MINB>
+                     : (void*)chunk_kernel<true, false, false, FIELD, MINB>;
+    return waves ? (void*)chunk_kernel<false, true, false, FIELD, MINB>
+                 : (void*)chunk_kernel<false, false, false, FIELD, MINB>;
+}
+
+template <int MINB>
+static void* kernel_ptr(int cut64, int waves, int aero, int field)
+{
+    return field ? kernel_ptr_f<MINB, true>(cut64, waves, aero) : kernel_ptr_f<MINB, false>(cut64, waves, aero);
 }
 
 // The kernel variant compiled for `ctas_per_sm` resident CTAs (1 or 2).
-static void* chunk_kernel_for(int cut64, int waves, int ctas_per_sm, int aero)
+static void* chunk_kernel_for(int cut64, int waves, int ctas_per_sm, int aero, int field)
 {
-    return ctas_per_sm >= 2 ? kernel_ptr<2>(cut64, waves, aero) : kernel_ptr<1>(cut64, waves, aero);
+    return ctas_per_sm >= 2 ? kernel_ptr<2>(cut64, waves, aero, field) : kernel_ptr<1>(cut64, waves, aero, field);
 }
 
 // The dynamic shared-memory attribute and the resident-CTA count of each
 // chunk-kernel variant, set and queried once per device: both are host API
 // calls that would otherwise sit in front of every step's first launch.
-// Index: device (first 16), cut64, waves, aerodynamic, 1 or 2 CTAs per SM;
-// occupancy is stored plus one (0 = not yet known).
+// Index: device (first 16), cut64, waves, aerodynamic, field currents, 1 or
+// 2 CTAs per SM; occupancy is stored plus one (0 = not yet known).
 constexpr int kDevCache = 16;
-static std::atomic<int> g_chunk_occ[kDevCache][2][2][2][2];
-static std::atomic<bool> g_chunk_attr[kDevCache][2][2][2][2];
+static std::atomic<int> g_chunk_occ[kDevCache][2][2][2][2][2];
+static std::atomic<bool> g_chunk_attr[kDevCache][2][2][2][2][2];
 
-static cudaError_t chunk_kernel_attr(int cut64, int waves, int ctas_per_sm, int aero)
+static cudaError_t chunk_kernel_attr(int cut64, int waves, int ctas_per_sm, int aero, int field)
 {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
-    std::atomic<bool>* flag =
-        dev < kDevCache ? &g_chunk_attr[dev][cut64 != 0][waves != 0][aero != 0][ctas_per_sm >= 2] : nullptr;
+    std::atomic<bool>* flag = dev < kDevCache
+        ? &g_chunk_attr[dev][cut64 != 0][waves != 0][aero != 0][field != 0][ctas_per_sm >= 2] : nullptr;
     if (flag && flag->load(std::memory_order_acquire)) return cudaSuccess;
-    e = cudaFuncSetAttribute(chunk_kernel_for(cut64, waves, ctas_per_sm, aero),
+    e = cudaFuncSetAttribute(chunk_kernel_for(cut64, waves, ctas_per_sm, aero, field),
                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ChunkSmem));
     if (e == cudaSuccess && flag) flag->store(true, std::memory_order_release);
     return e;
 }
 
-int chunk_kernel_occupancy(int cut64, int waves, int ctas_per_sm, int aero)
+int chunk_kernel_occupancy(int cut64, int waves, int ctas_per_sm, int aero, int field)
 {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
-    std::atomic<int>* slot =
-        dev < kDevCache ? &g_chunk_occ[dev][cut64 != 0][waves != 0][aero != 0][ctas_per_sm >= 2] : nullptr;
+    std::atomic<int>* slot = dev < kDevCache
+        ? &g_chunk_occ[dev][cut64 != 0][waves != 0][aero != 0][field != 0][ctas_per_sm >= 2] : nullptr;
     if (slot) {
         const int known = slot->load(std::memory_order_acquire);
         if (known > 0) return known - 1;
     }
     int n = 0;
-    const void* k = chunk_kernel_for(cut64, waves, ctas_per_sm, aero);
-    if (chunk_kernel_attr(cut64, waves, ctas_per_sm, aero) != cudaSuccess) return 0;
+    const void* k = chunk_kernel_for(cut64, waves, ctas_per_sm, aero, field);
+    if (chunk_kernel_attr(cut64, waves, ctas_per_sm, aero, field) != cudaSuccess) return 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, kThreads, sizeof(ChunkSmem)) != cudaSuccess)
         return 0;
     if (slot) slot->store(n + 1, std::memory_order_release);
@@ -1248,8 +1259,9 @@ cudaError_t launch_step(const KParams& P, LaunchShape shape, int cut64, cudaStre
     if (grid > (int)P.n_chunks) grid = (int)P.n_chunks;
     if (grid < 1) grid = 1;
     const int aero = (P.op == OP_AERO || P.op == OP_AERO_BODY) ? 1 : 0;
-    const void* k = chunk_kernel_for(cut64, P.ocean.waves != 0, shape.ctas_per_sm, aero);
-    if ((e = chunk_kernel_attr(cut64, P.ocean.waves != 0, shape.ctas_per_sm, aero))) return e;
+    const int field = P.ocean.field_currents ? 1 : 0;
+    const void* k = chunk_kernel_for(cut64, P.ocean.waves != 0, shape.ctas_per_sm, aero, field);
+    if ((e = chunk_kernel_attr(cut64, P.ocean.waves != 0, shape.ctas_per_sm, aero, field))) return e;
     void* args[] = {const_cast<KParams*>(&P)};
     if ((e = cudaLaunchKernel(k, dim3(grid), dim3(kThreads), args, sizeof(ChunkSmem), s))) return e;
     if (ev && (e = cudaEventRecord(ev[2], s))) return e;
@@ -1458,8 +1470,9 @@ cudaError_t launch_compound_step(const KParams& P, const CompoundParams& C, Laun
         int grid = shape.grid;
         if (grid > (int)P.n_chunks) grid = (int)P.n_chunks;
         if (grid < 1) grid = 1;
-        const void* k = chunk_kernel_for(cut64, P.ocean.waves != 0, shape.ctas_per_sm, 0);
-        if ((e = chunk_kernel_attr(cut64, P.ocean.waves != 0, shape.ctas_per_sm, 0)))
+        const int field = P.ocean.field_currents ? 1 : 0;
+        const void* k = chunk_kernel_for(cut64, P.ocean.waves != 0, shape.ctas_per_sm, 0, field);
+        if ((e = chunk_kernel_attr(cut64, P.ocean.waves != 0, shape.ctas_per_sm, 0, field)))
             return e;
         void* args[] = {const_cast<KParams*>(&P)};
         if ((e = cudaLaunchKernel(k, dim3(grid), dim3(kThreads), args, sizeof(ChunkSmem), s))) return e;

@@ -159,11 +159,12 @@ __device__ __forceinline__ BodyPair body_pair(const BodyParams& B, const OceanDe
 }
 
 // Fluid velocity at both centroids (Ocean::GetFluidVelocity).
+template <bool FIELD = true>
 __device__ __forceinline__ P3 fluid_velocity2(const OceanDev& o, const BodyParams& B, const BodyPair& Bp, P3 fc)
 {
-    if (!o.field_currents) return Bp.U;
-    v3 a = fluid_velocity_b(o, B, mk(fc.x.x, fc.y.x, fc.z.x));
-    v3 b = fluid_velocity_b(o, B, mk(fc.x.y, fc.y.y, fc.z.y));
+    if (!FIELD || !o.field_currents) return Bp.U;
+    v3 a = fluid_velocity_b<FIELD>(o, B, mk(fc.x.x, fc.y.x, fc.z.x));
+    v3 b = fluid_velocity_b<FIELD>(o, B, mk(fc.x.y, fc.y.y, fc.z.y));
     return pk(f2(a.x, b.x), f2(a.y, b.y), f2(a.z, b.z));
 }
 
@@ -188,11 +189,12 @@ __device__ __forceinline__ void tri_props2(P3 p1, P3 p2, P3 p3, P3& fc, P3& fn1,
 
 // Damping of two faces (:1661-1683).  Drag and skin friction of a face
 // that does not get them are computed with a zero area.
+template <bool FIELD = true>
 __device__ __forceinline__ void damping2(const OceanDev& o, const BodyParams& B, const BodyPair& Bp, Acc& a,
                                          P3 fc, P3 fn1, float2 A)
 {
     P3 r = psub(fc, Bp.p);
-    P3 vc = psub(fluid_velocity2(o, B, Bp, fc), padd(Bp.v, pcross(Bp.omega, r)));
+    P3 vc = psub(fluid_velocity2<FIELD>(o, B, Bp, fc), padd(Bp.v, pcross(Bp.omega, r)));
     float2 vc_n = pdot(vc, fn1);
     P3 vn = pk(mul2(vc_n, fn1.x), mul2(vc_n, fn1.y), mul2(vc_n, fn1.z));
     P3 vt = psub(vc, vn);
@@ -212,7 +214,7 @@ __device__ __forceinline__ void damping2(const OceanDev& o, const BodyParams& B,
 
 // Two fully submerged faces of the surface loop (:1618-1647, :1650-1686).
 // validB false: the B half is padding and contributes nothing.
-template <bool WAVES>
+template <bool WAVES, bool FIELD = true>
 __device__ __forceinline__ void face_full2(const OceanDev& o, const BodyParams& B, const BodyPair& Bp,
                                            Acc& a, P3 p1, P3 p2, P3 p3, bool validB)
 {
@@ -232,18 +234,19 @@ __device__ __forceinline__ void face_full2(const OceanDev& o, const BodyParams& 
         acc_add3p(a, Q_FB, Fbi);
         acc_add3p(a, Q_TB, pcross(psub(fc, Bp.p), Fbi));
     }
-    if (B.damping) damping2(o, B, Bp, a, fc, fn1, A);
+    if (B.damping) damping2<FIELD>(o, B, Bp, a, fc, fn1, A);
     acc_add2(a.q[Q_SWET], A);
 }
 
 // Two faces of the submerged loop (:1748-1789).
+template <bool FIELD = true>
 __device__ __forceinline__ void face_submerged2(const OceanDev& o, const BodyParams& B, const BodyPair& Bp, Acc& a,
                                                 P3 p1, P3 p2, P3 p3, bool validB)
 {
     P3 fc, fn1;
     float2 A;
     tri_props2(p1, p2, p3, fc, fn1, A, validB);
-    damping2(o, B, Bp, a, fc, fn1, A);
+    damping2<FIELD>(o, B, Bp, a, fc, fn1, A);
 }
 
 }  // namespace sfh
