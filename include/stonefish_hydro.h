@@ -402,14 +402,17 @@ hydro_status hydro_batch_kernel_ms(hydro_batch* batch, float* prep_ms, float* ch
  * most HYDRO_STATIC_MAX_BODIES bodies and a work list that fits the array
  * (about 16000 chunks of up to 8 tiles); larger requests return
  * HYDRO_ERR_INVALID_ARG and launch nothing.  The first call on a device
- * looks up the array's device address, so make it before any stream
- * capture; meshes uploaded afterwards are accepted as long as the device
- * tile table does not need to grow (otherwise HYDRO_ERR_INVALID_ARG).  Each
- * call builds its work list on the host in static (pageable) arrays and
- * uploads it with cudaMemcpyAsync, which may make the host wait while the
- * driver stages the copy; it clears the array's control words on `stream`
- * before its kernels.  All calls share the array and it keeps the last
- * call's contents: calls whose work overlaps on the GPU race. */
+ * looks up the array's device address; meshes uploaded afterwards are
+ * accepted as long as the device tile table does not need to grow
+ * (otherwise HYDRO_ERR_INVALID_ARG).  Each call builds its work list on the
+ * host in static (pageable) arrays and uploads it with cudaMemcpyAsync,
+ * which may make the host wait while the driver stages the copy; it clears
+ * the array's control words on `stream` before its kernels.  The call is
+ * therefore not graph-capturable: do not issue it inside a stream capture
+ * (a captured graph would replay whatever work list a later call left in
+ * the host arrays); for a captured step use hydro_batch_compute_device.
+ * All calls share the array and it keeps the last call's contents: calls
+ * whose work overlaps on the GPU race. */
 #define HYDRO_STATIC_SCRATCH_BYTES (4u << 20)
 #define HYDRO_STATIC_MAX_BODIES 4096u
 hydro_status hydro_compute_wrenches_static(hydro_ctx* ctx, const hydro_mesh_id* mesh_of_body,
