@@ -14,9 +14,11 @@ with the inputs resident in HBM (``value``), and through the host-buffer C ABI
 call with the host<->device copies inside the timed region (``e2e``).  The
 mesh data (~0.5 GB) is larger than L2, so no flush is needed between steps.
 
-``--impl reference`` times the CPU restatement of the reference's routine
-(the oracle's REF32 variant: FP32 glm-order face arithmetic, one task per
-body on all host threads) on the same workload.
+``--impl reference`` times the reference's own routine on the host cores
+on the same workload: its hydrodynamics functions compiled from its sources
+(oracle/_ref) where they were built on this machine, else the oracle's REF32
+restatement (FP32 glm-order face arithmetic); one task per body on all host
+threads either way.
 """
 from __future__ import annotations
 
@@ -858,7 +860,7 @@ def run_reference(args, rank: int):
             "dtype": "f32 faces (reference arithmetic)", "data": "synthetic", "config": cfg,
             "faces_per_s": int(per_body_faces.sum()) * steps / total,
             "cpu_baseline": {"value": value, "unit": unit, "cores": threads, "kind": kind,
-                             "sample": f"{steps} full steps of the workload (at most --steps, "
+                             "sample": f"{steps} full step{'s' if steps != 1 else ''} of the workload (at most --steps, "
                                        f"stopped after 60 s): {what}"},
             "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
