@@ -299,7 +299,7 @@ hydro_status hydro_batch_create(hydro_ctx* ctx, const hydro_mesh_id* mesh_of_bod
                                 uint32_t n_bodies, hydro_batch** out);
 
 /* As hydro_batch_create, with the work-chunk size of this batch in faces
- * (rounded up to whole tiles of HYDRO_TILE_FACES faces, at most 16 tiles;
+ * (rounded up to whole tiles of HYDRO_TILE_FACES faces, at most 32 tiles;
  * 0 = the context's setting).  Small chunks suit batches of which only a few bodies are
  * active at a time (no counterpart in the reference). */
 hydro_status hydro_batch_create_ex(hydro_ctx* ctx, const hydro_mesh_id* mesh_of_body,
