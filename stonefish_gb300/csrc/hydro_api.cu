@@ -1718,7 +1718,9 @@ hydro_status hydro_fluid_position(hydro_ctx* ctx, const hydro_ocean* ocean, cons
     return HYDRO_OK;
 }
 
-// Per-face surface-loop terms of one body (n_faces * 23 floats, host).
+// The DEBUG_HYDRO outline of one body: the kernel writes per face a record
+// of 13 floats (corner count, up to four corners of the evaluated submerged
+// part), expanded here into line segments on the host.
 hydro_status hydro_debug_surface_outline(hydro_ctx* ctx, const hydro_body* body, const hydro_ocean* ocean,
                                          const hydro_settings* settings, float* points, uint32_t capacity,
                                          uint32_t* n_points)
@@ -1752,7 +1754,7 @@ hydro_status hydro_debug_surface_outline(hydro_ctx* ctx, const hydro_body* body,
     uint32_t n = 0;
     for (size_t f = 0; f < m.n_faces; ++f) {
         const float* r = &rec[f * 13];
-        const int k = (int)r[0];
+        const int k = std::min(std::max((int)r[0], 0), 4);   // a record holds at most four corners
         for (int i = 0; i < k; ++i) {
             const float* c[2] = {r + 1 + 3 * i, r + 1 + 3 * ((i + 1) % k)};
             for (int j = 0; j < 2; ++j, ++n)
