@@ -97,6 +97,29 @@ def test_null_context_is_rejected_without_device(built_library):
     lib.hydro_batch_destroy(None)
 
 
+def test_every_entry_point_rejects_null_arguments(built_library):
+    """Each status-returning entry point declared in the header, called with
+    null handles and pointers and zero counts, returns HYDRO_ERR_INVALID_ARG
+    without touching the device and without aborting the process."""
+    lib = abi.load_library(built_library)
+    checked = 0
+    for name in abi.exported_symbols_from_header():
+        fn = getattr(lib, name)
+        if fn.restype is not C.c_int32 or not fn.argtypes:
+            continue
+        args = []
+        for t in fn.argtypes:
+            if t in (C.c_float, C.c_double):
+                args.append(0.0)
+            elif t in (C.c_int32, C.c_uint32, C.c_int64, C.c_uint64, C.c_size_t, C.c_int):
+                args.append(0)
+            else:
+                args.append(None)
+        assert fn(*args) == abi.HYDRO_ERR_INVALID_ARG, name
+        checked += 1
+    assert checked >= 60
+
+
 def test_create_reports_device_error_without_gpu(built_library):
     try:
         import torch
