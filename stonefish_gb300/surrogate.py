@@ -356,6 +356,8 @@ class Surrogate:
         X = self.prepare_inputs(feats)
         T = targets.contiguous()
         n = feats.shape[0] // self.B * self.B
+        if n == 0:
+            raise ValueError(f"fit needs at least one batch of {self.B} rows, got {feats.shape[0]}")
         per_epoch = n // self.B
         total = epochs * per_epoch
         history = []
